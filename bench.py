@@ -1,0 +1,371 @@
+"""Benchmark of the hot path: the symmetry-reduced Hamiltonian action H.v and the
+Lanczos ground-state solve that consumes it, on one GPU per process.
+
+Default workload: Heisenberg J1-J2 chain L=32, nup=16, kblock=0, pblock=+1,
+zblock=+1 (N = 4,707,969 representatives), J1=1.0, J2=0.5, FP64.
+
+A step is one matvec y = H x over the whole sector.  `value` is the H.v
+throughput in GB/s of algorithmic traffic (bytes per row defined below) with x, y
+resident in HBM; `e2e` is the same metric through the C ABI with host buffers
+(host->device copy of x and device->host copy of y inside every timed step).
+Lanczos solves/s (eigsh k=1 :SA, tol 1e-10) and the FP32 form are reported
+beside it.  Synthetic data only (seeded N(0,1) vectors; the Hamiltonian is the
+model itself).  N > 1 runs independent replicas (the path is not sharded).
+
+`--impl reference` times the CPU restatement of the reference's algorithm
+(oracle/, representative-space port, all host threads) on a bounded sample of
+rows of the same workload and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "quspin.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "H·v GB/s (% HBM peak), Lanczos solves/s, p50/p99 latency; FP32 vs FP64 form"
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def j1j2_spec(L, J1=1.0, J2=0.5):
+    b1 = [(i, i % L + 1) for i in range(1, L + 1)]
+    b2 = [(i, (i + 1) % L + 1) for i in range(1, L + 1)]
+    return [("+-", [(J1 / 2, a, b) for a, b in b1] + [(J2 / 2, a, b) for a, b in b2]),
+            ("-+", [(J1 / 2, a, b) for a, b in b1] + [(J2 / 2, a, b) for a, b in b2]),
+            ("zz", [(J1, a, b) for a, b in b1] + [(J2, a, b) for a, b in b2])]
+
+
+WORKLOADS = {
+    "j1j2_L32_k0_p1_z1": dict(L=32, nup=16, sym=dict(kblock=0, pblock=1, zblock=1), J2=0.5,
+                              desc="Heisenberg J1-J2 chain L=32, nup=16, kblock=0, pblock=+1, zblock=+1, "
+                                   "J1=1.0, J2=0.5"),
+    "j1j2_L24_k0_p1_z1": dict(L=24, nup=12, sym=dict(kblock=0, pblock=1, zblock=1), J2=0.5,
+                              desc="Heisenberg J1-J2 chain L=24, nup=12, kblock=0, pblock=+1, zblock=+1 (small case)"),
+}
+
+
+def alive_transitions(states, L, J2):
+    """Average number of off-diagonal transitions that survive per row: one per
+    bond whose two spins differ (the +- / -+ pair), J1 and J2 bonds."""
+    s = states.astype(np.uint64)
+    tot = np.zeros(s.size)
+    for d in (1, 2) if J2 else (1,):
+        for i in range(L):
+            j = (i + d) % L
+            tot += (((s >> np.uint64(i)) ^ (s >> np.uint64(j))) & np.uint64(1)).astype(np.float64)
+    return float(tot.mean())
+
+
+def bytes_per_row(nbar, vec_bytes, state_bytes=4):
+    """Algorithmic HBM bytes per output row of the symmetric matvec: the row's
+    representative (state_bytes) and stabiliser code (2), its diagonal entry,
+    x[r], y[r] write, and one x gather per surviving transition."""
+    return state_bytes + 2 + vec_bytes + vec_bytes + vec_bytes + nbar * vec_bytes
+
+
+class ClockSampler:
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0]
+        if dev:
+            cmd += ["-i", dev]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+
+        def rd():
+            for line in self.proc.stdout:
+                self.rows.append([x.strip() for x in line.split(",")])
+        self.thread = threading.Thread(target=rd, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, name in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("QS_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v, device=None):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_port_sample(wl, nthreads, target_s=10.0, seed=20261203):
+    """Times the oracle's representative-space port on contiguous row samples
+    until ~target_s of CPU work; returns (seconds per row, rows timed, nbar, N)."""
+    import oracle
+    L, nup = wl["L"], wl["nup"]
+    rb = oracle.RepBasis(L, nup=nup, pauli=False, nthreads=nthreads, **wl["sym"])
+    spec = j1j2_spec(L, 1.0, wl["J2"])
+    pk = oracle.pack_terms(spec)
+    n = rb.Ns
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(n).astype(np.complex128)
+    d = rb.diagonal(spec)
+    rows_done, t_total = 0, 0.0
+    block = max(1024, n // 256)
+    start = n // 3
+    while t_total < target_s and rows_done < n:
+        r0 = (start + rows_done) % n
+        r1 = min(n, r0 + block)
+        t = time.perf_counter()
+        rb.matvec(spec, x, diag=d, rows=(r0, r1), packed=pk)
+        t_total += time.perf_counter() - t
+        rows_done += r1 - r0
+        block = min(n, block * 2)
+    nbar = alive_transitions(rb.states[n // 3: n // 3 + 100000], L, wl["J2"])
+    return t_total / rows_done, rows_done, nbar, n, t_total
+
+
+def run_reference(args, wl, world, rank):
+    if rank != 0:
+        return
+    import oracle
+    oracle.lib()
+    nthreads = os.cpu_count() or 1
+    sec_per_row, rows, nbar, n, tt = cpu_port_sample(wl, nthreads, target_s=max(3.0, 1.5 * args.steps))
+    # the port computes in complex128; the metric counts the FP64 real form's bytes
+    bpr = bytes_per_row(nbar, 8)
+    gbs = bpr / sec_per_row / 1e9
+    line = {
+        "metric": METRIC, "value": gbs, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_row * n * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl["desc"], "N": n, "step": "one H.v over the sector (extrapolated from a row sample)"},
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{rows} contiguous rows of {n} ({tt:.1f} s), representative-space "
+                                   "restatement of the reference matvec (the reference's own projector "
+                                   "algorithm needs the 601M-state parent sector)"},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    import qsgpu as qs
+    from qsgpu import _lib
+    from qsgpu import build as qbuild
+    qbuild.build()
+    lib = _lib.load()
+    dev = torch.device("cuda", local)
+    L, nup = wl["L"], wl["nup"]
+    spec = j1j2_spec(L, 1.0, wl["J2"])
+    t0 = time.perf_counter()
+    basis = qs.SpinBasis1D(L, nup=nup, pauli=False, **wl["sym"])
+    t_basis = time.perf_counter() - t0
+    op = qs.QuantumLinearOperator(basis, [qs.OperatorTerm(o, c) for o, c in spec])
+    n = basis.Ns
+    stream = torch.cuda.current_stream(dev)
+    _lib.check(lib.qs_op_set_stream(op._h, ctypes.c_void_p(stream.cuda_stream)))
+    g = torch.Generator(device="cpu").manual_seed(20261203 + rank)
+    xh = torch.randn(n, generator=g, dtype=torch.float64)
+    x = xh.to(dev)
+    y = torch.empty_like(x)
+    x32 = x.float()
+    y32 = torch.empty_like(x32)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2
+    one = np.array([1.0, 0.0])
+    zero = np.array([0.0, 0.0])
+
+    def mv(xt, yt, code):
+        _lib.check(lib.qs_op_matvec(op._h, 0, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()), code, _lib.ptr(zero),
+                                    ctypes.c_void_p(yt.data_ptr()), code, 1, _lib.QS_MEM_DEVICE))
+
+    def timed(xt, yt, code, steps, warmup):
+        for _ in range(warmup):
+            mv(xt, yt, code)
+        torch.cuda.synchronize()
+        barrier(world)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        l0 = lib.qs_launch_count()
+        for s, e in ev:
+            flush.zero_()
+            s.record(stream)
+            mv(xt, yt, code)
+            e.record(stream)
+        torch.cuda.synchronize()
+        launches = lib.qs_launch_count() - l0
+        ms = [s.elapsed_time(e) for s, e in ev]
+        return ms, launches
+
+    # nbar from a sample of representatives (exact count of alive programs)
+    reps = basis.orbit_minima()
+    nbar = alive_transitions(reps[n // 3: n // 3 + 200000], L, wl["J2"])
+    del reps
+    bpr64 = bytes_per_row(nbar, 8)
+    bpr32 = bytes_per_row(nbar, 4)
+    clocks = ClockSampler()
+    clocks.start()
+    ms64, launches = timed(x, y, _lib.QS_F64, args.steps, args.warmup)
+    ms32, _ = timed(x32, y32, _lib.QS_F32, args.steps, args.warmup)
+    # e2e through the C ABI with host buffers (pinned), copies inside the step
+    xp = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    xp.copy_(xh)
+    yp = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    e2e_t = []
+    for it in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        _lib.check(lib.qs_op_matvec(op._h, 0, _lib.ptr(one), ctypes.c_void_p(xp.data_ptr()), _lib.QS_F64,
+                                    _lib.ptr(zero), ctypes.c_void_p(yp.data_ptr()), _lib.QS_F64, 1,
+                                    _lib.QS_MEM_HOST))
+        if it >= args.warmup:
+            e2e_t.append(time.perf_counter() - t)
+    # Lanczos ground state, FP64 and FP32 + FP64 polish (device-resident v0)
+    solves = {}
+    for prec in ("fp64", "fp32"):
+        info = {}
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        vals = qs.eigsh(op, k=1, which="SA", tol=1e-10, v0=xh.numpy(), return_eigenvectors=False,
+                        precision=prec, info=info)
+        dt = time.perf_counter() - t
+        solves[prec] = dict(seconds=dt, e0=float(vals[0]), matvecs=info.get("matvecs"),
+                            restarts=info.get("restarts"))
+    clk = clocks.stop()
+
+    t_step = float(np.mean(ms64)) / 1e3
+    t_step = max_over_ranks(world, t_step, dev)
+    value = world * bpr64 * n / t_step / 1e9
+    peak, peak_kind = load_peaks()
+    achieved = bpr64 * n / (float(np.mean(ms64)) / 1e3) / 1e9
+    gbs32 = bpr32 * n / (float(np.mean(ms32)) / 1e3) / 1e9
+    e2e_mean = float(np.mean(e2e_t))
+    e2e_mean = max_over_ranks(world, e2e_mean, dev)
+    e2e_val = world * bpr64 * n / e2e_mean / 1e9
+    rel_e0 = abs(solves["fp32"]["e0"] - solves["fp64"]["e0"]) / abs(solves["fp64"]["e0"])
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            import oracle
+            oracle.lib()
+            nthreads = os.cpu_count() or 1
+            spr, rows, _, _, tt = cpu_port_sample(wl, nthreads, target_s=10.0)
+            cpu = {"value": bpr64 / spr / 1e9, "unit": "GB/s", "cores": nthreads, "kind": "port",
+                   "sample": f"{rows} contiguous rows of {n} ({tt:.1f} s of matvec), representative-space "
+                             "restatement of the reference matvec on all host cores"}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {exc}"}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl["desc"], "N": n, "step": "one H.v over the sector, x/y resident in HBM",
+                   "l2": "256 MB buffer written between timed steps", "nbar": round(nbar, 3),
+                   "bytes_per_row": round(bpr64, 2), "basis_build_s": round(t_basis, 3),
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind},
+        "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "fp32_form": {"value": gbs32, "unit": "GB/s", "ms_per_step": float(np.mean(ms32)),
+                      "speedup_vs_fp64": float(np.mean(ms64)) / float(np.mean(ms32))},
+        "lanczos": {"solves_per_s_fp64": 1.0 / solves["fp64"]["seconds"],
+                    "solves_per_s_fp32_polished": 1.0 / solves["fp32"]["seconds"],
+                    "e0": solves["fp64"]["e0"], "fp32_polished_rel_err": rel_e0,
+                    "matvecs_fp64": solves["fp64"]["matvecs"], "matvecs_fp32": solves["fp32"]["matvecs"],
+                    "tol": 1e-10},
+        "latency_ms": {"p50": float(np.percentile(ms64, 50)), "p99": float(np.percentile(ms64, 99))},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="j1j2_L32_k0_p1_z1", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    wl = WORKLOADS[args.workload]
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, wl, world, rank)
+    else:
+        run_ours(args, wl, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,217 @@
+/*
+ * qsgpu.h -- C ABI of the GB300 (sm_103a) engine for QuSpin.jl's matrix-free
+ * Hamiltonian action on symmetry-reduced spin-1/2 bases and the Krylov solvers
+ * that consume it.
+ *
+ * Every entry point takes plain pointers and sizes.  Functions return a
+ * qs_status (0 = success); on failure qs_last_error() returns a message that
+ * the Julia shim raises as the exception named beside each status code.  The
+ * library owns device memory behind opaque handles; host arrays passed in are
+ * borrowed for the duration of the call, outputs are caller-allocated (Julia
+ * mul! semantics).  Calls on distinct handles may run from different threads;
+ * calls on one handle must be serialised by the caller.
+ *
+ * Complex vectors are interleaved (re, im) doubles, the memory layout of
+ * Julia's Vector{ComplexF64}.  Indices are 0-based here; the Julia shim adds 1.
+ *
+ * Reference citations are paths inside QuSpin.jl.
+ */
+#ifndef QSGPU_H
+#define QSGPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define QS_API __attribute__((visibility("default")))
+#else
+#define QS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    QS_OK = 0,
+    QS_ERR_ARGUMENT = 1,        /* ArgumentError */
+    QS_ERR_DIMENSION = 2,       /* DimensionMismatch */
+    QS_ERR_CUDA = 3,            /* ErrorException: device failure */
+    QS_ERR_NOMEM = 4,           /* OutOfMemoryError */
+    QS_ERR_NOT_CONVERGED = 5,   /* ErrorException: Krylov / Lanczos did not converge */
+    QS_ERR_UNSUPPORTED = 6,     /* ArgumentError: outside what this engine implements */
+    QS_ERR_TIMEOUT = 7          /* ErrorException: a bounded device wait ran out */
+} qs_status;
+
+typedef enum { QS_F64 = 0, QS_C128 = 1, QS_F32 = 2, QS_C64 = 3 } qs_dtype;
+typedef enum { QS_MEM_HOST = 0, QS_MEM_DEVICE = 1 } qs_mem;
+
+typedef struct qs_basis qs_basis;
+typedef struct qs_op qs_op;
+
+/* ------------------------------------------------------------------ basis */
+
+/* Keyword arguments of SpinBasis1D(L; nup, pauli, a, kblock, pblock, zblock,
+ * pzblock, zAblock, zBblock), src/basis.jl:622-637.  nup = -1 means "not
+ * given"; a block of 0 means "not given", otherwise +1 / -1. */
+typedef struct {
+    int32_t L;
+    int32_t nup;
+    int32_t pauli;
+    int32_t a;
+    int32_t has_kblock;
+    int32_t kblock;
+    int32_t pblock;
+    int32_t zblock;
+    int32_t pzblock;
+    int32_t zAblock;
+    int32_t zBblock;
+} qs_basis_spec;
+
+/* Replaces SpinBasis1D(L; ...) (src/basis.jl:622-777): enumerates the sector on
+ * the device, keeps one representative per symmetric orbit and orders columns
+ * as the reference's projector does (ascending orbit minimum). */
+QS_API int qs_basis_create(const qs_basis_spec *spec, qs_basis **out);
+QS_API void qs_basis_destroy(qs_basis *basis);
+
+/* length(basis) / basis.Ns (src/basis.jl:779, 786-799). */
+QS_API int64_t qs_basis_size(const qs_basis *basis);
+
+/* 1 if the sector needs a complex projector (src/symmetry_basis.jl:622-629,
+ * _basis_requires_complex). */
+QS_API int qs_basis_requires_complex(const qs_basis *basis);
+
+/* Order of the symmetry group the sector is reduced by (1 without symmetry). */
+QS_API int32_t qs_basis_group_order(const qs_basis *basis);
+
+/* states(basis) / basis.states (src/basis.jl:785): the reference's
+ * representative of every column, in column order. */
+QS_API int qs_basis_states(const qs_basis *basis, uint64_t *out, int64_t n);
+
+/* Ascending orbit minima of the columns (the device's canonical key). */
+QS_API int qs_basis_orbit_minima(const qs_basis *basis, uint64_t *out, int64_t n);
+
+/* state_index(basis, s) (src/basis.jl:1016-1022) for n states at once;
+ * out[i] = column or -1 when the state is not represented (the shim raises
+ * ArgumentError "state ... is not represented by this basis"). */
+QS_API int qs_basis_state_index(const qs_basis *basis, const uint64_t *states, int64_t n, int64_t *out);
+
+/* representative / normalization / get_amp (src/discrete_basis.jl:2386-2422)
+ * for n parent states.  status[i] = 0 ok, 1 outside the parent sector,
+ * 2 zero weight in this sector.  amps is 2n doubles (complex). */
+QS_API int qs_basis_representative(const qs_basis *basis, const uint64_t *states, int64_t n,
+                            uint64_t *reps, double *norms, double *amps, int32_t *status);
+
+/* --------------------------------------------------------------- operator */
+
+/* One OperatorTerm (src/operators.jl:42-63): op string over {I,z,+,-,x,y},
+ * n_couplings couplings, coefficient c (2 doubles, complex) and one-based
+ * sites (strlen(op) ints) each. */
+typedef struct {
+    const char *op;
+    int32_t n_couplings;
+    const double *coeffs;   /* 2 * n_couplings */
+    const int32_t *sites;   /* strlen(op) * n_couplings, one-based */
+    int32_t complex_coeffs; /* 1 if the Julia coefficient type is complex */
+} qs_term;
+
+enum {
+    QS_CHECK_SYMM = 1,
+    QS_CHECK_HERM = 2,
+    QS_CHECK_PCON = 4,
+    QS_DIAG_COMPLEX = 8     /* the user diagonal has a complex eltype */
+};
+
+/* QuantumLinearOperator(basis, static_list; diagonal, check_symm, check_herm,
+ * check_pcon), src/operators.jl:2492-2552.  diagonal: NULL or 2*Ns doubles
+ * (complex, user diagonal).  check_symm is structural (every generator maps
+ * the consolidated term set onto itself) instead of the reference's dense
+ * parent-space residual, which does not fit in memory at these sizes. */
+QS_API int qs_op_create(qs_basis *basis, const qs_term *terms, int32_t nterms, const double *diagonal,
+                 int32_t checks, qs_op **out);
+QS_API void qs_op_destroy(qs_op *op);
+
+/* eltype(op): QS_F64 or QS_C128 (src/operators.jl:2523-2529). */
+QS_API int qs_op_dtype(const qs_op *op);
+/* ishermitian(op) (src/operators.jl:3269). */
+QS_API int qs_op_hermitian(const qs_op *op);
+/* Launch this operator's kernels (matvec and solvers) on the caller's CUDA
+ * stream (a cudaStream_t); NULL returns to the library's own stream.  No
+ * reference counterpart: it lets a host runtime that owns streams (CUDA.jl,
+ * PyTorch) order the engine's work with its own. */
+QS_API int qs_op_set_stream(qs_op *op, void *stream);
+/* set_diagonal!(op, d) (src/operators.jl:3298-3307); d is 2*Ns doubles. */
+QS_API int qs_op_set_diagonal(qs_op *op, const double *diagonal);
+
+enum { QS_TRANSPOSE = 1, QS_CONJUGATE = 2 };
+
+/* mul!(Y, op, X, alpha, beta) (src/operators.jl:3147-3208) for nrhs column-
+ * major right-hand sides with leading dimension Ns:
+ *   Y = alpha * op(A) * X + beta * Y,  op() from flags (transpose(op),
+ *   conj(op), adjoint(op), src/operators.jl:3283-3295).
+ * x_dtype / y_dtype: QS_F64 or QS_C128 (y must be complex if A or x is), or
+ * QS_F32 / QS_C64 for the single-precision form (x, y both single, FP32
+ * accumulation).  alpha, beta: complex (2 doubles).  mem: where X and Y live;
+ * with QS_MEM_DEVICE the call only enqueues work on the operator's stream
+ * (qs_op_set_stream) and returns, with QS_MEM_HOST it returns when Y is
+ * written back. */
+QS_API int qs_op_matvec(qs_op *op, int32_t flags, const double *alpha, const void *x, int32_t x_dtype,
+                 const double *beta, void *y, int32_t y_dtype, int64_t nrhs, int32_t mem);
+
+/* ----------------------------------------------------------------- solvers */
+
+typedef struct {
+    int32_t k;            /* number of eigenpairs */
+    int32_t which;        /* 0 = SA (smallest algebraic), 1 = LA */
+    double tol;           /* relative Ritz tolerance, 0 = machine epsilon (ARPACK default) */
+    int32_t ncv;          /* Lanczos basis size, 0 = max(20, 2k+1) (Arpack.jl default) */
+    int32_t maxiter;      /* restarts, 0 = 300 */
+    int32_t precision;    /* 0 = FP64, 1 = FP32 matvec and vectors + FP64 polish */
+    int32_t want_vectors;
+    const double *v0;     /* NULL or starting vector, dtype of op */
+    int32_t mem;          /* QS_MEM_HOST or QS_MEM_DEVICE for v0 and vectors */
+} qs_eigsh_opts;
+
+typedef struct {
+    int32_t nconv;
+    int32_t restarts;
+    int64_t matvecs;
+    double max_rel_residual;
+    double seconds;
+} qs_eigsh_info;
+
+/* eigsh(op; k, which=:SA, v0, tol, ncv, maxiter) (src/operators.jl:3367-3408):
+ * values ascending (k doubles); vectors Ns x k column-major in the op dtype
+ * (host).  A thick-restart Lanczos with full reorthogonalisation replaces the
+ * ARPACK implicitly restarted Lanczos; convergence is ARPACK's test
+ * ||r_i|| <= tol * max(eps^(2/3), |theta_i|). */
+QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *vectors, qs_eigsh_info *info);
+
+/* apply(ExpmMultiplyParallel(A, a), v; tol) (tools.jl:1662-1708) and the
+ * Krylov exponential action _krylov_expmv_vector (src/operators.jl:1758-1803):
+ * out = exp(a * A) v with complex a.  v, out: Ns complex (host). */
+QS_API int qs_expm_multiply(qs_op *op, const double *a, const double *v, double *out, double tol,
+                     int32_t krylov_dim, int32_t precision);
+
+/* evolve(H, v0, t0, times; eom=:SE, imag_time, tol, krylov_dim) for a static
+ * Hamiltonian (src/operators.jl:2073-2164 via _krylov_expmv_times
+ * 1805-1893): out is Ns x nt column-major complex (host). */
+QS_API int qs_evolve(qs_op *op, const double *v0, double t0, const double *times, int32_t nt, int32_t imag_time,
+              double tol, int32_t krylov_dim, int32_t precision, double *out);
+
+/* ----------------------------------------------------------------- errors */
+
+/* Message of the last failure on the calling thread (empty if none). */
+QS_API const char *qs_last_error(void);
+
+/* Number of kernels this library has launched in the process so far (all
+ * handles).  No reference counterpart: instrumentation for benchmarks. */
+QS_API int64_t qs_launch_count(void);
+
+/* Library version string. */
+QS_API const char *qs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QSGPU_H */

@@ -1,0 +1,433 @@
+"""CPU oracle for the QuSpin.jl spin-1/2 hot path.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` as the checker.  The shipped library never
+imports it.
+
+Two restatements of the reference, see ``qs_oracle.c``:
+
+* :class:`RefBasis` -- the reference algorithm (explicit projector, argmax
+  representatives, lift/scatter/project matvec), IEEE-exact.
+* :class:`RepBasis` -- representative-space restatement for large sectors.
+
+The Krylov routines below restate ``src/operators.jl:1655-1893`` in numpy; eigsh
+uses SciPy's ARPACK (the reference calls ARPACK through Arpack.jl 0.5,
+``src/operators.jl:3367-3408``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build() -> str:
+    """Compile the oracle shared library (gcc, no GPU needed)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return os.path.join(_HERE, "_build", "libqs_oracle.so")
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "_build", "libqs_oracle.so")
+        src = os.path.join(_HERE, "qs_oracle.c")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        i64 = ctypes.c_int64
+        L.ora_basis_create.argtypes = [ctypes.c_int] * 11 + [ctypes.POINTER(P), ctypes.c_char_p, ctypes.c_int]
+        L.ora_basis_create.restype = ctypes.c_int
+        L.ora_basis_free.argtypes = [P]
+        for name in ("ora_basis_size", "ora_basis_parent_size", "ora_basis_projector_nnz"):
+            getattr(L, name).argtypes = [P]
+            getattr(L, name).restype = i64
+        L.ora_basis_reduced.argtypes = [P]
+        L.ora_basis_states.argtypes = [P, P]
+        L.ora_basis_parent_states.argtypes = [P, P]
+        L.ora_basis_projector.argtypes = [P, P, P, P]
+        L.ora_state_index.argtypes = [P, ctypes.c_uint64]
+        L.ora_state_index.restype = i64
+        L.ora_representative.argtypes = [P, ctypes.c_uint64, P, P, P]
+        L.ora_representative.restype = ctypes.c_int
+        L.ora_extract_diagonal.argtypes = [P, ctypes.c_int, P, P, P, P, P, P]
+        L.ora_extract_diagonal.restype = ctypes.c_int
+        L.ora_qlo_matvec.argtypes = [P, ctypes.c_int, P, P, P, P, P, ctypes.c_int, P, ctypes.c_int,
+                                     ctypes.c_int, P, P, P, P]
+        L.ora_qlo_matvec.restype = ctypes.c_int
+        L.ora_rbasis_create.argtypes = [ctypes.c_int] * 12 + [ctypes.POINTER(P), ctypes.c_char_p, ctypes.c_int]
+        L.ora_rbasis_create.restype = ctypes.c_int
+        L.ora_rbasis_free.argtypes = [P]
+        L.ora_rbasis_size.argtypes = [P]
+        L.ora_rbasis_size.restype = i64
+        L.ora_rbasis_group_order.argtypes = [P]
+        L.ora_rbasis_states.argtypes = [P, P, P]
+        L.ora_rbasis_matvec.argtypes = [P, ctypes.c_int, P, P, P, P, P, P, P, P, P, P, i64, i64, ctypes.c_int]
+        L.ora_rbasis_matvec.restype = ctypes.c_int
+        L.ora_rbasis_diagonal.argtypes = [P, ctypes.c_int, P, P, P, P, P, P]
+        L.ora_rbasis_diagonal.restype = ctypes.c_int
+        L.ora_num_threads.restype = ctypes.c_int
+        _LIB = L
+    return _LIB
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _sym_args(L, nup, pauli, a, kblock, pblock, zblock, pzblock, zAblock, zBblock):
+    return [int(L), -1 if nup is None else int(nup), int(bool(pauli)), int(a),
+            int(kblock is not None), int(kblock or 0), int(pblock or 0), int(zblock or 0),
+            int(pzblock or 0), int(zAblock or 0), int(zBblock or 0)]
+
+
+class OracleError(ValueError):
+    pass
+
+
+# ----------------------------------------------------------------- terms
+def consolidate_terms(terms):
+    """Restates ``_consolidate_terms`` (src/operators.jl:214-263): sums duplicate
+    (op, sites) couplings in first-seen order and drops zero coefficients."""
+    coeffs = {}
+    order = []
+    for op, couplings in terms:
+        for c in couplings:
+            key = (op, tuple(int(s) for s in c[1:]))
+            if key not in coeffs:
+                order.append(key)
+                coeffs[key] = 0
+            coeffs[key] = coeffs[key] + c[0]
+    grouped = {}
+    op_order = []
+    for key in order:
+        co = coeffs[key]
+        if co == 0:
+            continue
+        op, sites = key
+        if op not in grouped:
+            grouped[op] = []
+            op_order.append(op)
+        grouped[op].append((co,) + sites)
+    return [(op, grouped[op]) for op in op_order]
+
+
+@dataclass
+class PackedTerms:
+    nterms: int
+    ops: np.ndarray
+    oplen: np.ndarray
+    coup_off: np.ndarray
+    coef: np.ndarray
+    sites: np.ndarray
+
+    def args(self):
+        return [self.nterms, _ptr(self.ops), _ptr(self.oplen), _ptr(self.coup_off), _ptr(self.coef),
+                _ptr(self.sites)]
+
+
+def pack_terms(terms) -> PackedTerms:
+    nt = len(terms)
+    ops = np.zeros(8 * max(nt, 1), dtype=np.uint8)
+    oplen = np.zeros(max(nt, 1), dtype=np.int32)
+    off = np.zeros(nt + 1, dtype=np.int64)
+    coefs, sites = [], []
+    for t, (op, couplings) in enumerate(terms):
+        if len(op) > 8:
+            raise OracleError("operator strings longer than 8 characters are not supported")
+        ops[8 * t:8 * t + len(op)] = np.frombuffer(op.encode(), dtype=np.uint8)
+        oplen[t] = len(op)
+        off[t + 1] = off[t] + len(couplings)
+        for c in couplings:
+            if len(c) != len(op) + 1:
+                raise OracleError("operator arity and coupling sites differ")
+            v = complex(c[0])
+            coefs.extend([v.real, v.imag])
+            s = [int(x) for x in c[1:]] + [0] * (8 - len(op))
+            sites.extend(s)
+    coef = np.array(coefs if coefs else [0.0, 0.0], dtype=np.float64)
+    site_arr = np.array(sites if sites else [0] * 8, dtype=np.int32)
+    return PackedTerms(nt, ops, oplen, off, coef, site_arr)
+
+
+def is_diag_op(op):
+    return all(ch in "Izn|" for ch in op)
+
+
+# ----------------------------------------------------------------- bases
+class RefBasis:
+    """SpinBasis1D built with the reference algorithm (explicit projector)."""
+
+    def __init__(self, L, nup=None, pauli=True, a=1, kblock=None, pblock=None, zblock=None,
+                 pzblock=None, zAblock=None, zBblock=None):
+        lb = lib()
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(256)
+        rc = lb.ora_basis_create(*_sym_args(L, nup, pauli, a, kblock, pblock, zblock, pzblock, zAblock,
+                                            zBblock), ctypes.byref(h), err, 256)
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        self._h = h
+        self.L, self.nup, self.pauli = L, nup, pauli
+        self.Ns = int(lb.ora_basis_size(h))
+        self.n_parent = int(lb.ora_basis_parent_size(h))
+        self.reduced = bool(lb.ora_basis_reduced(h))
+        self.states = np.zeros(self.Ns, dtype=np.uint64)
+        lb.ora_basis_states(h, _ptr(self.states))
+        self.parent_states = np.zeros(self.n_parent, dtype=np.uint64)
+        lb.ora_basis_parent_states(h, _ptr(self.parent_states))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().ora_basis_free(self._h)
+            self._h = None
+
+    def projector(self):
+        import scipy.sparse as sp
+        if not self.reduced:
+            return sp.identity(self.n_parent, dtype=np.complex128, format="csc")
+        lb = lib()
+        nnz = int(lb.ora_basis_projector_nnz(self._h))
+        colptr = np.zeros(self.Ns + 1, dtype=np.int64)
+        rowval = np.zeros(nnz, dtype=np.int64)
+        vals = np.zeros(nnz, dtype=np.complex128)
+        lb.ora_basis_projector(self._h, _ptr(colptr), _ptr(rowval), _ptr(vals))
+        return sp.csc_matrix((vals, rowval, colptr), shape=(self.n_parent, self.Ns))
+
+    def state_index(self, s):
+        i = int(lib().ora_state_index(self._h, int(s)))
+        if i < 0:
+            raise OracleError(f"state {s} is not represented by this basis")
+        return i
+
+    def representative(self, s):
+        rep = ctypes.c_uint64()
+        norm = ctypes.c_double()
+        amp = np.zeros(2)
+        rc = lib().ora_representative(self._h, int(s), ctypes.byref(rep), ctypes.byref(norm), _ptr(amp))
+        if rc == -1:
+            raise OracleError("state is outside the parent particle sector")
+        if rc == -2:
+            raise OracleError("state has zero weight in this symmetry sector")
+        return int(rep.value), float(norm.value), complex(amp[0], amp[1])
+
+    def extract_diagonal(self, terms):
+        pk = pack_terms(terms)
+        out = np.zeros(self.Ns, dtype=np.complex128)
+        rc = lib().ora_extract_diagonal(self._h, *pk.args(), _ptr(out))
+        if rc:
+            raise OracleError("unsupported spin operator")
+        return out
+
+    def qlo_matvec(self, terms, x, alpha=1.0, beta=0.0, y=None, diag=None, extract=True,
+                   transposed=False, conjugated=False):
+        """mul!(y, QuantumLinearOperator(basis, terms; diagonal=diag), x, alpha, beta)."""
+        pk = pack_terms(terms)
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.zeros(self.Ns, dtype=np.complex128) if y is None else np.array(y, dtype=np.complex128)
+        d = np.zeros(self.Ns, dtype=np.complex128)
+        if extract:
+            d += self.extract_diagonal(terms)
+        if diag is not None:
+            d += np.asarray(diag, dtype=np.complex128)
+        a = np.array([complex(alpha).real, complex(alpha).imag])
+        b = np.array([complex(beta).real, complex(beta).imag])
+        rc = lib().ora_qlo_matvec(self._h, *pk.args(), int(extract), _ptr(d), int(transposed), int(conjugated),
+                                  _ptr(a), _ptr(b), _ptr(x), _ptr(y))
+        if rc:
+            raise OracleError("unsupported spin operator")
+        return y
+
+    def dense(self, terms, diag=None, extract=True):
+        n = self.Ns
+        out = np.zeros((n, n), dtype=np.complex128)
+        e = np.zeros(n, dtype=np.complex128)
+        for j in range(n):
+            e[:] = 0
+            e[j] = 1
+            out[:, j] = self.qlo_matvec(terms, e, diag=diag, extract=extract)
+        return out
+
+
+class RepBasis:
+    """Representative-space restatement (orbit minima, group by closure)."""
+
+    def __init__(self, L, nup=None, pauli=True, a=1, kblock=None, pblock=None, zblock=None,
+                 pzblock=None, zAblock=None, zBblock=None, nthreads=0):
+        lb = lib()
+        h = ctypes.c_void_p()
+        err = ctypes.create_string_buffer(256)
+        args = _sym_args(L, nup, pauli, a, kblock, pblock, zblock, pzblock, zAblock, zBblock) + [int(nthreads)]
+        rc = lb.ora_rbasis_create(*args, ctypes.byref(h), err, 256)
+        if rc != 0:
+            raise OracleError(err.value.decode())
+        self._h = h
+        self.L, self.nup, self.pauli = L, nup, pauli
+        self.Ns = int(lb.ora_rbasis_size(h))
+        self.group_order = int(lb.ora_rbasis_group_order(h))
+        self.states = np.zeros(self.Ns, dtype=np.uint64)
+        self.orbit = np.zeros(self.Ns, dtype=np.int32)
+        lb.ora_rbasis_states(h, _ptr(self.states), _ptr(self.orbit))
+        self.nthreads = nthreads
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().ora_rbasis_free(self._h)
+            self._h = None
+
+    def diagonal(self, terms):
+        pk = pack_terms(terms)
+        out = np.zeros(self.Ns, dtype=np.complex128)
+        if lib().ora_rbasis_diagonal(self._h, *pk.args(), _ptr(out)):
+            raise OracleError("unsupported spin operator")
+        return out
+
+    def matvec(self, terms, x, alpha=1.0, beta=0.0, y=None, diag=None, rows=None, packed=None):
+        pk = packed or pack_terms(terms)
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.zeros(self.Ns, dtype=np.complex128) if y is None else np.ascontiguousarray(y, dtype=np.complex128)
+        d = self.diagonal(terms) if diag is None else np.ascontiguousarray(diag, dtype=np.complex128)
+        a = np.array([complex(alpha).real, complex(alpha).imag])
+        b = np.array([complex(beta).real, complex(beta).imag])
+        r0, r1 = (0, self.Ns) if rows is None else rows
+        rc = lib().ora_rbasis_matvec(self._h, *pk.args(), _ptr(d), _ptr(a), _ptr(b), _ptr(x), _ptr(y),
+                                     int(r0), int(r1), int(self.nthreads))
+        if rc:
+            raise OracleError("unsupported spin operator")
+        return y
+
+
+# ----------------------------------------------------------------- Krylov
+def krylov_factorization(matvec, v, hermitian, krylov_dim=30, dtype=np.complex128):
+    """Restates ``_krylov_factorization`` (src/operators.jl:1655-1731)."""
+    initial = np.array(v, dtype=dtype)
+    beta = np.linalg.norm(initial)
+    n = initial.size
+    steps = min(int(krylov_dim), n)
+    V = np.zeros((n, steps + 1), dtype=dtype)
+    Hm = np.zeros((steps + 1, steps), dtype=dtype)
+    V[:, 0] = initial / beta
+    completed = steps
+    terminal = 0.0
+    if hermitian:
+        prev = 0.0
+        for col in range(steps):
+            r = np.array(matvec(V[:, col]), dtype=dtype)
+            if col > 0:
+                r -= prev * V[:, col - 1]
+            a = np.vdot(V[:, col], r)
+            Hm[col, col] = a
+            r -= a * V[:, col]
+            terminal = np.linalg.norm(r)
+            Hm[col + 1, col] = terminal
+            if col < steps - 1:
+                Hm[col, col + 1] = terminal
+            if terminal <= 100 * np.finfo(float).eps * max(1.0, np.linalg.norm(Hm)):
+                completed = col + 1
+                break
+            elif col < steps - 1:
+                V[:, col + 1] = r / terminal
+            prev = terminal
+    else:
+        for col in range(steps):
+            r = np.array(matvec(V[:, col]), dtype=dtype)
+            for row in range(col + 1):
+                c = np.vdot(V[:, row], r)
+                Hm[row, col] = c
+                r -= c * V[:, row]
+            for row in range(col + 1):
+                c = np.vdot(V[:, row], r)
+                Hm[row, col] += c
+                r -= c * V[:, row]
+            terminal = np.linalg.norm(r)
+            Hm[col + 1, col] = terminal
+            if terminal <= 100 * np.finfo(float).eps * max(1.0, np.linalg.norm(Hm)):
+                completed = col + 1
+                break
+            elif col < steps - 1:
+                V[:, col + 1] = r / terminal
+    return dict(initial=initial, beta=beta, basis=V, hessenberg=Hm, completed=completed, terminal_norm=terminal,
+                dimension=n, steps=steps, hermitian=hermitian)
+
+
+def krylov_project(f, scale):
+    """Restates ``_krylov_project`` (src/operators.jl:1733-1756)."""
+    import scipy.linalg as sla
+    m = f["completed"]
+    E = sla.expm(scale * f["hessenberg"][:m, :m])
+    result = f["basis"][:, :m] @ E[:, 0] * f["beta"]
+    est = (abs(scale) * f["terminal_norm"] * f["beta"] * abs(E[-1, 0])
+           if (m == f["steps"] and m < f["dimension"]) else 0.0)
+    return result, est
+
+
+def krylov_expmv_vector(matvec, v, scale, hermitian, tol=1e-12, krylov_dim=30, depth=0):
+    """Restates ``_krylov_expmv_vector`` (src/operators.jl:1758-1803)."""
+    initial = np.array(v, dtype=np.complex128)
+    if scale == 0 or np.linalg.norm(initial) == 0:
+        return initial
+    f = krylov_factorization(matvec, initial, hermitian, krylov_dim)
+    res, est = krylov_project(f, scale)
+    if est > tol * max(1.0, np.linalg.norm(res)):
+        if depth >= 14:
+            raise RuntimeError("Krylov exponential action did not converge; increase krylov_dim")
+        mid = krylov_expmv_vector(matvec, initial, scale / 2, hermitian, tol / 2, krylov_dim, depth + 1)
+        return krylov_expmv_vector(matvec, mid, scale / 2, hermitian, tol / 2, krylov_dim, depth + 1)
+    return res
+
+
+def krylov_expmv_times(matvec, v, scales, hermitian, tol=1e-12, krylov_dim=30):
+    """Restates ``_krylov_expmv_times`` (src/operators.jl:1805-1893)."""
+    initial = np.array(v, dtype=np.complex128)
+    out = np.zeros((initial.size, len(scales)), dtype=np.complex128)
+    if len(scales) == 0:
+        return out
+    if np.linalg.norm(initial) == 0 or all(s == 0 for s in scales):
+        out[:] = initial[:, None]
+        return out
+    f = krylov_factorization(matvec, initial, hermitian, krylov_dim)
+    m = f["completed"]
+    if hermitian:
+        T = f["hessenberg"][:m, :m]
+        Th = np.triu(T) + np.triu(T, 1).conj().T
+        Th[np.diag_indices(m)] = np.real(np.diag(T))
+        w, U = np.linalg.eigh(Th)
+        first = U.conj().T[:, 0]
+        for j, s in enumerate(scales):
+            if s == 0:
+                out[:, j] = initial
+                continue
+            c = U @ (np.exp(s * w) * first)
+            state = f["beta"] * (f["basis"][:, :m] @ c)
+            est = (abs(s) * f["terminal_norm"] * f["beta"] * abs(c[-1])
+                   if (m == f["steps"] and m < f["dimension"]) else 0.0)
+            if est > tol * max(1.0, np.linalg.norm(state)):
+                state = krylov_expmv_vector(matvec, initial, s, hermitian, tol, krylov_dim)
+            out[:, j] = state
+    else:
+        for j, s in enumerate(scales):
+            if s == 0:
+                out[:, j] = initial
+                continue
+            state, est = krylov_project(f, s)
+            if est > tol * max(1.0, np.linalg.norm(state)):
+                state = krylov_expmv_vector(matvec, initial, s, hermitian, tol, krylov_dim)
+            out[:, j] = state
+    return out
+
+
+def eigsh_arpack(matvec, n, k, dtype, v0=None, tol=0.0, ncv=None, maxiter=None):
+    """k smallest-algebraic eigenpairs through SciPy's ARPACK, sorted ascending
+    (src/operators.jl:3367-3408 semantics)."""
+    import scipy.sparse.linalg as spla
+    op = spla.LinearOperator((n, n), matvec=matvec, dtype=dtype)
+    vals, vecs = spla.eigsh(op, k=k, which="SA", v0=v0, tol=tol, ncv=ncv, maxiter=maxiter)
+    order = np.argsort(vals)
+    return vals[order], vecs[:, order]

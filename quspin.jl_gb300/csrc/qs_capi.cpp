@@ -1,0 +1,250 @@
+// qs_capi.cpp -- the C ABI (include/qsgpu.h): status codes, last-error text,
+// host/device buffer staging.  Every entry point catches exceptions and turns
+// them into a qs_status; nothing throws across the boundary.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/qsgpu.h"
+#include "qs_internal.h"
+#include "qs_krylov.h"
+
+struct qs_basis {
+    qs::Basis b;
+};
+struct qs_op {
+    qs::Op* op;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F>
+int guard(F&& f) {
+    try {
+        g_last_error.clear();
+        f();
+        return QS_OK;
+    } catch (const qs::Error& e) {
+        g_last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return QS_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return QS_ERR_CUDA;
+    }
+}
+
+bool is_complex(int dt) { return dt == QS_C128 || dt == QS_C64; }
+bool is_single(int dt) { return dt == QS_F32 || dt == QS_C64; }
+size_t dt_bytes(int dt) {
+    switch (dt) {
+        case QS_F64: return 8;
+        case QS_C128: return 16;
+        case QS_F32: return 4;
+        case QS_C64: return 8;
+        default: throw qs::Error(QS_ERR_ARGUMENT, "unknown dtype");
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* qs_last_error(void) { return g_last_error.c_str(); }
+const char* qs_version(void) { return "qsgpu 0.1.0 (sm_103a)"; }
+
+int qs_basis_create(const qs_basis_spec* spec, qs_basis** out) {
+    return guard([&] {
+        if (!spec || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        *out = nullptr;
+        qs_basis* h = new qs_basis();
+        h->b.spec = *spec;
+        try {
+            qs::basis_build(h->b);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+void qs_basis_destroy(qs_basis* basis) { delete basis; }
+
+int64_t qs_basis_size(const qs_basis* basis) { return basis ? basis->b.n : -1; }
+
+int qs_basis_requires_complex(const qs_basis* basis) { return basis && basis->b.complex_chars ? 1 : 0; }
+
+int32_t qs_basis_group_order(const qs_basis* basis) { return basis ? basis->b.group.ng : 0; }
+
+int qs_basis_orbit_minima(const qs_basis* basis, uint64_t* out, int64_t n) {
+    return guard([&] {
+        const qs::Basis& b = basis->b;
+        if (n != b.n) throw qs::Error(QS_ERR_DIMENSION, "output length must equal Ns");
+        if (!b.symmetric) {
+            if (b.nup < 0) {
+                for (int64_t i = 0; i < n; ++i) out[i] = (uint64_t)i;
+                return;
+            }
+            // Gosper order (src/basis.jl:229-250)
+            if (b.nup == 0) { out[0] = 0; return; }
+            uint64_t s = (b.nup >= 64) ? ~0ull : ((1ull << b.nup) - 1ull);
+            for (int64_t i = 0; i < n; ++i) {
+                out[i] = s;
+                if (i == n - 1) break;
+                uint64_t lowest = s & (~s + 1ull);
+                uint64_t next = s + lowest;
+                s = next | (((next ^ s) >> 2) >> __builtin_ctzll(lowest));
+            }
+            return;
+        }
+        if (b.wide) {
+            QS_CUDA(cudaMemcpy(out, b.d_reps.p, n * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<uint32_t> tmp(n);
+            QS_CUDA(cudaMemcpy(tmp.data(), b.d_reps.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            for (int64_t i = 0; i < n; ++i) out[i] = tmp[i];
+        }
+    });
+}
+
+int qs_basis_states(const qs_basis* basis, uint64_t* out, int64_t n) {
+    if (!basis) return QS_ERR_ARGUMENT;
+    if (!basis->b.symmetric) return qs_basis_orbit_minima(basis, out, n);
+    return guard([&] {
+        qs::Basis& b = const_cast<qs::Basis&>(basis->b);
+        if (n != b.n) throw qs::Error(QS_ERR_DIMENSION, "output length must equal Ns");
+        qs::basis_compute_refrep(b);
+        std::memcpy(out, b.h_refrep.data(), n * sizeof(uint64_t));
+    });
+}
+
+int qs_basis_state_index(const qs_basis* basis, const uint64_t* states, int64_t n, int64_t* out) {
+    return guard([&] { qs::basis_index_of(const_cast<qs::Basis&>(basis->b), states, n, out); });
+}
+
+int qs_basis_representative(const qs_basis* basis, const uint64_t* states, int64_t n, uint64_t* reps, double* norms,
+                            double* amps, int32_t* status) {
+    return guard([&] {
+        qs::basis_representative(const_cast<qs::Basis&>(basis->b), states, n, reps, norms, amps, status);
+    });
+}
+
+int qs_op_create(qs_basis* basis, const qs_term* terms, int32_t nterms, const double* diagonal, int32_t checks,
+                 qs_op** out) {
+    return guard([&] {
+        if (!basis || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        *out = nullptr;
+        qs::Op* op = qs::op_create(&basis->b, terms, nterms, diagonal, checks);
+        *out = new qs_op{op};
+    });
+}
+
+void qs_op_destroy(qs_op* op) {
+    if (!op) return;
+    delete op->op;
+    delete op;
+}
+
+int qs_op_set_stream(qs_op* op, void* stream) {
+    return guard([&] {
+        qs::Op& o = *op->op;
+        QS_CUDA(cudaStreamSynchronize(o.stream));
+        o.stream = stream ? (cudaStream_t)stream : o.own_stream;
+    });
+}
+
+int64_t qs_launch_count(void) { return qs::launches(); }
+
+int qs_op_dtype(const qs_op* op) { return op->op->complex_mat ? QS_C128 : QS_F64; }
+int qs_op_hermitian(const qs_op* op) { return op->op->hermitian ? 1 : 0; }
+
+int qs_op_set_diagonal(qs_op* op, const double* diagonal) {
+    return guard([&] {
+        qs::Op& o = *op->op;
+        o.user_diag.resize(o.basis->n);
+        for (int64_t i = 0; i < o.basis->n; ++i) o.user_diag[i] = {diagonal[2 * i], diagonal[2 * i + 1]};
+        qs::op_prepare_device(o);
+    });
+}
+
+int qs_op_matvec(qs_op* op, int32_t flags, const double* alpha, const void* x, int32_t x_dtype, const double* beta,
+                 void* y, int32_t y_dtype, int64_t nrhs, int32_t mem) {
+    return guard([&] {
+        qs::Op& o = *op->op;
+        const int64_t n = o.basis->n;
+        if (is_single(x_dtype) != is_single(y_dtype))
+            throw qs::Error(QS_ERR_ARGUMENT, "input and output must share a precision");
+        if (!is_complex(y_dtype) && (is_complex(x_dtype) || o.complex_mat))
+            throw qs::Error(QS_ERR_ARGUMENT, "the output must be complex for a complex operator or input");
+        if (nrhs < 0) throw qs::Error(QS_ERR_DIMENSION, "nrhs must be nonnegative");
+        const bool single = is_single(y_dtype);
+        const bool ycx = is_complex(y_dtype);
+        const size_t yb = dt_bytes(y_dtype), xb = dt_bytes(x_dtype);
+        qs::MatvecCall c;
+        c.flags = flags;
+        c.alpha = qs::cx(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
+        c.beta = qs::cx(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
+        c.single = single;
+        c.x_complex = ycx;
+        c.y_complex = ycx;
+        const bool beta_zero = c.beta.re == 0.0 && c.beta.im == 0.0;
+        if (mem == QS_MEM_DEVICE) {
+            if (is_complex(x_dtype) != ycx)
+                throw qs::Error(QS_ERR_UNSUPPORTED, "device buffers must share the output dtype");
+            for (int64_t j = 0; j < nrhs; ++j) {
+                c.x = (const char*)x + (size_t)j * n * xb;
+                c.y = (char*)y + (size_t)j * n * yb;
+                qs::op_matvec_device(o, c, o.stream);
+            }
+            return;  // asynchronous on the operator's stream
+        }
+        if (!o.d_x.p || o.d_x.bytes < n * yb) o.d_x.alloc(n * yb);
+        if (!o.d_y.p || o.d_y.bytes < n * yb) o.d_y.alloc(n * yb);
+        std::vector<char> widen;
+        for (int64_t j = 0; j < nrhs; ++j) {
+            const char* xs = (const char*)x + (size_t)j * n * xb;
+            if (is_complex(x_dtype) == ycx) {
+                QS_CUDA(cudaMemcpyAsync(o.d_x.p, xs, n * yb, cudaMemcpyHostToDevice, o.stream));
+            } else {
+                // real input, complex output: widen on the host
+                widen.assign(n * yb, 0);
+                for (int64_t i = 0; i < n; ++i) {
+                    if (single) ((float*)widen.data())[2 * i] = ((const float*)xs)[i];
+                    else ((double*)widen.data())[2 * i] = ((const double*)xs)[i];
+                }
+                QS_CUDA(cudaMemcpyAsync(o.d_x.p, widen.data(), n * yb, cudaMemcpyHostToDevice, o.stream));
+            }
+            char* ys = (char*)y + (size_t)j * n * yb;
+            if (!beta_zero) QS_CUDA(cudaMemcpyAsync(o.d_y.p, ys, n * yb, cudaMemcpyHostToDevice, o.stream));
+            c.x = o.d_x.p;
+            c.y = o.d_y.p;
+            qs::op_matvec_device(o, c, o.stream);
+            QS_CUDA(cudaMemcpyAsync(ys, o.d_y.p, n * yb, cudaMemcpyDeviceToHost, o.stream));
+            QS_CUDA(cudaStreamSynchronize(o.stream));
+        }
+    });
+}
+
+int qs_eigsh(qs_op* op, const qs_eigsh_opts* opts, double* values, void* vectors, qs_eigsh_info* info) {
+    return guard([&] { qs::eigsh(*op->op, *opts, values, vectors, info); });
+}
+
+int qs_expm_multiply(qs_op* op, const double* a, const double* v, double* out, double tol, int32_t krylov_dim,
+                     int32_t precision) {
+    return guard([&] {
+        qs::expm_multiply(*op->op, std::complex<double>(a[0], a[1]), v, out, tol, krylov_dim, precision);
+    });
+}
+
+int qs_evolve(qs_op* op, const double* v0, double t0, const double* times, int32_t nt, int32_t imag_time, double tol,
+              int32_t krylov_dim, int32_t precision, double* out) {
+    return guard(
+        [&] { qs::evolve(*op->op, v0, t0, times, nt, imag_time, tol, krylov_dim, precision, out); });
+}
+
+}  // extern "C"

@@ -1,0 +1,142 @@
+// qs_internal.h -- host-side structures of libqsgpu (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/qsgpu.h"
+#include "qs_common.h"
+
+namespace qs {
+
+// Exception carrying a qs_status; converted to a status code at the C ABI.
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define QS_CUDA(call)                                                                        \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            int st_ = (e_ == cudaErrorMemoryAllocation) ? QS_ERR_NOMEM : QS_ERR_CUDA;        \
+            throw ::qs::Error(st_, std::string("CUDA error: ") + cudaGetErrorString(e_) +    \
+                                       " at " + __FILE__ + ":" + std::to_string(__LINE__));  \
+        }                                                                                    \
+    } while (0)
+
+// Owning device buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t n) { alloc(n); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t n) {
+        release();
+        if (n) QS_CUDA(cudaMalloc(&p, n));
+        bytes = n;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Symmetry generator in the reference's order (src/basis.jl:691-735).
+enum GenKind { GEN_T = 0, GEN_P, GEN_Z, GEN_PZ, GEN_ZA, GEN_ZB };
+struct Generator {
+    int kind;
+    int shift, refl;
+    uint64_t mask;
+    cplx eig;       // eigenvalue exactly as the reference computes it
+    int order;      // cyclic order of the map (L/a for T, 2 otherwise)
+};
+
+struct Basis {
+    qs_basis_spec spec{};
+    int L = 0;
+    int nup = -1;
+    bool symmetric = false;
+    bool wide = false;               // states need 64 bits (L > 32)
+    bool complex_chars = false;
+    int64_t n = 0;
+    int64_t n_parent = 0;
+    std::vector<Generator> gens;
+    GroupDesc group{};               // host copy
+    DevBuf d_group;                  // GroupDesc on device
+    DevBuf d_reps;                   // ascending orbit minima (uint32 or uint64)
+    DevBuf d_stab;                   // uint16 stabiliser order per representative
+    DevBuf d_split;                  // search splitters (same type as reps)
+    int64_t nsplit = 0, split_stride = 1;
+    DevBuf d_binom;                  // uint64 C(b, p) table for combinadic ranks
+    std::vector<uint64_t> h_refrep;  // reference (argmax) representatives
+    bool refrep_ready = false;
+    // per-level subgroup element lists and the level-0 coefficient table used
+    // to replay the reference's projector arithmetic
+    std::vector<GroupDesc> level_groups;
+    std::vector<cplx> level0_table;  // [len * 64 + j]
+    DevBuf d_level_groups, d_level0;
+    cudaStream_t stream = nullptr;
+    ~Basis();
+};
+
+struct Op {
+    Basis* basis = nullptr;
+    bool complex_mat = false;       // eltype ComplexF64
+    bool hermitian = true;
+    bool commuting = true;          // terms commute with the group (fast pull form)
+    bool extracted = true;          // diagonal terms folded into the diagonal
+    std::vector<TermProg> progs;    // off-diagonal transition programs
+    std::vector<TermProg> diag_progs;
+    std::vector<std::complex<double>> user_diag;
+    DevBuf d_progs;
+    DevBuf d_diag;                  // complex diagonal (user + extracted), 2*n doubles
+    DevBuf d_diag32;                // single-precision copy
+    DevBuf d_x, d_y;                // staging for host vectors
+    DevBuf d_x32, d_y32;
+    cudaStream_t stream = nullptr;      // stream in use
+    cudaStream_t own_stream = nullptr;  // created by the library
+    ~Op();
+};
+
+// qs_basis.cu
+void basis_build(Basis& b);
+void basis_index_of(Basis& b, const uint64_t* states, int64_t n, int64_t* out);
+void basis_compute_refrep(Basis& b);
+void basis_representative(Basis& b, const uint64_t* states, int64_t n, uint64_t* reps, double* norms,
+                          double* amps, int32_t* status);
+
+// qs_op.cpp
+Op* op_create(Basis* basis, const qs_term* terms, int nterms, const double* diagonal, int checks);
+
+// qs_matvec.cu
+struct MatvecCall {
+    int flags = 0;
+    cplx alpha{1, 0}, beta{0, 0};
+    const void* x = nullptr;
+    void* y = nullptr;
+    bool x_complex = false, y_complex = false;
+    bool single = false;            // FP32 vectors and accumulation
+};
+void op_prepare_device(Op& op);
+// kernel launch accounting (qs_launch_count)
+void note_launches(int64_t n);
+int64_t launches();
+void op_matvec_device(Op& op, const MatvecCall& c, cudaStream_t s);
+
+}  // namespace qs

@@ -1,0 +1,19 @@
+"""qsgpu -- GB300-native engine for QuSpin.jl's matrix-free Hamiltonian action on
+symmetry-reduced spin-1/2 bases and its Krylov solvers.
+
+This package is the host-side mirror of the reference's Julia interface over the
+C ABI of libqsgpu (include/qsgpu.h).  Every compute call runs on the GPU; there
+is no CPU fallback.
+"""
+from .basis import (SpinBasis1D, get_amp, int_to_state, normalization, representative, state_at, state_index,
+                    state_to_int, states)
+from .errors import ArgumentError, DimensionMismatch, ErrorException, UnsupportedError
+from .operators import (ExpmMultiplyParallel, Hamiltonian, OperatorTerm, QuantumLinearOperator, apply, eigsh,
+                        evolve, expm_multiply_parallel, isquantum_LinearOperator, set_a)
+
+__all__ = [
+    "SpinBasis1D", "states", "state_index", "state_at", "representative", "normalization", "get_amp",
+    "int_to_state", "state_to_int", "OperatorTerm", "QuantumLinearOperator", "Hamiltonian", "eigsh", "evolve",
+    "ExpmMultiplyParallel", "expm_multiply_parallel", "apply", "set_a", "isquantum_LinearOperator",
+    "ArgumentError", "DimensionMismatch", "ErrorException", "UnsupportedError",
+]

@@ -1,0 +1,103 @@
+"""ctypes binding of libqsgpu (include/qsgpu.h).
+
+There is no CPU fallback: if the shared library is missing or cannot be loaded
+the import fails with the loader's message.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .errors import raise_status
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqsgpu.so")
+
+P = ctypes.c_void_p
+i32 = ctypes.c_int32
+i64 = ctypes.c_int64
+f64 = ctypes.c_double
+
+
+class BasisSpec(ctypes.Structure):
+    _fields_ = [(name, i32) for name in (
+        "L", "nup", "pauli", "a", "has_kblock", "kblock", "pblock", "zblock", "pzblock", "zAblock", "zBblock")]
+
+
+class Term(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_char_p), ("n_couplings", i32), ("coeffs", P), ("sites", P),
+                ("complex_coeffs", i32)]
+
+
+class EigshOpts(ctypes.Structure):
+    _fields_ = [("k", i32), ("which", i32), ("tol", f64), ("ncv", i32), ("maxiter", i32), ("precision", i32),
+                ("want_vectors", i32), ("v0", P), ("mem", i32)]
+
+
+class EigshInfo(ctypes.Structure):
+    _fields_ = [("nconv", i32), ("restarts", i32), ("matvecs", i64), ("max_rel_residual", f64), ("seconds", f64)]
+
+
+QS_F64, QS_C128, QS_F32, QS_C64 = 0, 1, 2, 3
+QS_MEM_HOST, QS_MEM_DEVICE = 0, 1
+QS_CHECK_SYMM, QS_CHECK_HERM, QS_CHECK_PCON, QS_DIAG_COMPLEX = 1, 2, 4, 8
+QS_TRANSPOSE, QS_CONJUGATE = 1, 2
+
+# every symbol declared in include/qsgpu.h
+EXPORTS = (
+    "qs_basis_create", "qs_basis_destroy", "qs_basis_size", "qs_basis_requires_complex", "qs_basis_group_order",
+    "qs_basis_states", "qs_basis_orbit_minima", "qs_basis_state_index", "qs_basis_representative",
+    "qs_op_create", "qs_op_destroy", "qs_op_dtype", "qs_op_hermitian", "qs_op_set_diagonal", "qs_op_matvec",
+    "qs_eigsh", "qs_expm_multiply", "qs_evolve", "qs_last_error", "qs_version", "qs_op_set_stream",
+    "qs_launch_count",
+)
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libqsgpu.so is not built ({LIB_PATH}); run qsgpu.build.build() first")
+    L = ctypes.CDLL(LIB_PATH)
+    L.qs_basis_create.argtypes = [ctypes.POINTER(BasisSpec), ctypes.POINTER(P)]
+    L.qs_basis_destroy.argtypes = [P]
+    L.qs_basis_destroy.restype = None
+    L.qs_basis_size.argtypes = [P]
+    L.qs_basis_size.restype = i64
+    L.qs_basis_requires_complex.argtypes = [P]
+    L.qs_basis_group_order.argtypes = [P]
+    L.qs_basis_group_order.restype = i32
+    L.qs_basis_states.argtypes = [P, P, i64]
+    L.qs_basis_orbit_minima.argtypes = [P, P, i64]
+    L.qs_basis_state_index.argtypes = [P, P, i64, P]
+    L.qs_basis_representative.argtypes = [P, P, i64, P, P, P, P]
+    L.qs_op_create.argtypes = [P, ctypes.POINTER(Term), i32, P, i32, ctypes.POINTER(P)]
+    L.qs_op_destroy.argtypes = [P]
+    L.qs_op_destroy.restype = None
+    L.qs_op_dtype.argtypes = [P]
+    L.qs_op_hermitian.argtypes = [P]
+    L.qs_op_set_diagonal.argtypes = [P, P]
+    L.qs_op_matvec.argtypes = [P, i32, P, P, i32, P, P, i32, i64, i32]
+    L.qs_eigsh.argtypes = [P, ctypes.POINTER(EigshOpts), P, P, ctypes.POINTER(EigshInfo)]
+    L.qs_expm_multiply.argtypes = [P, P, P, P, f64, i32, i32]
+    L.qs_evolve.argtypes = [P, P, f64, P, i32, i32, f64, i32, i32, P]
+    L.qs_op_set_stream.argtypes = [P, P]
+    L.qs_launch_count.restype = i64
+    L.qs_last_error.restype = ctypes.c_char_p
+    L.qs_version.restype = ctypes.c_char_p
+    for name in EXPORTS:
+        getattr(L, name)
+    _lib = L
+    return L
+
+
+def check(status: int):
+    if status != 0:
+        raise_status(status, load().qs_last_error().decode(errors="replace"))
+
+
+def ptr(a):
+    return a.ctypes.data_as(P)

@@ -1,0 +1,167 @@
+"""SpinBasis1D on the device (mirror of src/basis.jl:206-213, 622-799, 1016-1057).
+
+Indices follow the reference's Julia convention: ``state_index`` returns and
+``state_at`` takes one-based column numbers.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .errors import ArgumentError
+
+
+class SpinBasis1D:
+    """SpinBasis1D(L; nup, pauli, a, kblock, pblock, zblock, pzblock, zAblock, zBblock)."""
+
+    def __init__(self, L, nup=None, Nup=None, m=None, S="1/2", pauli=True, a=1, kblock=None, pblock=None,
+                 zblock=None, pzblock=None, zAblock=None, zBblock=None):
+        if str(S) not in ("1/2", "0.5"):
+            raise ArgumentError("only spin-1/2 bases run on this engine")
+        if not (1 <= int(L) <= 63):
+            raise ArgumentError("L must be between 1 and 63")
+        if nup is not None and Nup is not None:
+            raise ArgumentError("specify only one of nup and Nup")
+        sel = Nup if nup is None else nup
+        if m is not None:
+            if sel is not None:
+                raise ArgumentError("m cannot be combined with nup or Nup")
+            sel = int(round((float(m) + 0.5) * L))
+        if sel is not None and not (0 <= int(sel) <= L):
+            raise ArgumentError("nup must lie between 0 and L")
+        lib = _lib.load()
+        spec = _lib.BasisSpec(int(L), -1 if sel is None else int(sel), int(bool(pauli)), int(a),
+                              int(kblock is not None), int(kblock or 0), int(pblock or 0), int(zblock or 0),
+                              int(pzblock or 0), int(zAblock or 0), int(zBblock or 0))
+        h = ctypes.c_void_p()
+        _lib.check(lib.qs_basis_create(ctypes.byref(spec), ctypes.byref(h)))
+        self._h = h
+        self.L = int(L)
+        self.nup = None if sel is None else int(sel)
+        self.pauli = bool(pauli)
+        self.Ns = int(lib.qs_basis_size(h))
+        self.group_order = int(lib.qs_basis_group_order(h))
+        self.requires_complex = bool(lib.qs_basis_requires_complex(h))
+        blocks = {"nup": self.nup, "pauli": self.pauli}
+        order = self.L // int(a) if self.L % int(a) == 0 else None
+        if kblock is not None:
+            blocks["a"] = int(a)
+            blocks["kblock"] = int(kblock) % order
+        for name, v in (("pblock", pblock), ("zblock", zblock), ("pzblock", pzblock), ("zAblock", zAblock),
+                        ("zBblock", zBblock)):
+            if v is not None:
+                blocks[name] = int(v)
+        self.blocks = blocks
+        self.symmetric = any(k in blocks for k in ("kblock", "pblock", "zblock", "pzblock", "zAblock", "zBblock"))
+        self._states = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.load().qs_basis_destroy(h)
+            self._h = None
+
+    def __len__(self):
+        return self.Ns
+
+    N = property(lambda self: self.L)
+    sps = 2
+    dtype = np.uint64
+    operators = ("I", "z", "+", "-", "x", "y")
+    description = "spin-1/2 chain basis"
+
+    @property
+    def states(self):
+        if self._states is None:
+            out = np.zeros(self.Ns, dtype=np.uint64)
+            _lib.check(_lib.load().qs_basis_states(self._h, _lib.ptr(out), self.Ns))
+            self._states = out
+        return self._states.copy()
+
+    def orbit_minima(self):
+        out = np.zeros(self.Ns, dtype=np.uint64)
+        _lib.check(_lib.load().qs_basis_orbit_minima(self._h, _lib.ptr(out), self.Ns))
+        return out
+
+    def index_array(self, states):
+        """0-based columns of many states at once (-1 where not represented)."""
+        q = np.ascontiguousarray(states, dtype=np.uint64)
+        out = np.zeros(q.size, dtype=np.int64)
+        _lib.check(_lib.load().qs_basis_state_index(self._h, _lib.ptr(q), q.size, _lib.ptr(out)))
+        return out
+
+    def representative_array(self, states):
+        q = np.ascontiguousarray(states, dtype=np.uint64)
+        n = q.size
+        reps = np.zeros(n, dtype=np.uint64)
+        norms = np.zeros(n)
+        amps = np.zeros(n, dtype=np.complex128)
+        status = np.zeros(n, dtype=np.int32)
+        _lib.check(_lib.load().qs_basis_representative(self._h, _lib.ptr(q), n, _lib.ptr(reps), _lib.ptr(norms),
+                                                       _lib.ptr(amps), _lib.ptr(status)))
+        return reps, norms, amps, status
+
+
+def states(basis):
+    return basis.states
+
+
+def state_index(basis, state):
+    """One-based column of a representative (src/basis.jl:1016-1022)."""
+    if state < 0:
+        raise ArgumentError("state must be nonnegative")
+    i = int(basis.index_array([state])[0])
+    if i < 0:
+        raise ArgumentError(f"state {state} is not represented by this basis")
+    return i + 1
+
+
+def state_at(basis, index):
+    if not (1 <= index <= basis.Ns):
+        raise IndexError(f"index {index} out of bounds for a basis of length {basis.Ns}")
+    return basis.states[index - 1]
+
+
+def _rep_query(basis, state):
+    reps, norms, amps, status = basis.representative_array([state])
+    if status[0] == 1:
+        raise ArgumentError("state is outside the parent particle sector")
+    if status[0] == 2:
+        raise ArgumentError("state has zero weight in this symmetry sector")
+    return int(reps[0]), float(norms[0]), complex(amps[0])
+
+
+def representative(basis, state):
+    if not basis.symmetric:
+        return state
+    return _rep_query(basis, state)[0]
+
+
+def normalization(basis, state):
+    if not basis.symmetric:
+        return 1.0
+    return _rep_query(basis, state)[1]
+
+
+def get_amp(basis, state):
+    if not basis.symmetric:
+        return 1.0
+    return _rep_query(basis, state)[2]
+
+
+def int_to_state(basis, state, bracket_notation=True):
+    if not (0 <= state < (1 << basis.L)):
+        raise ArgumentError("state must fit in L bits")
+    bits = format(int(state), "b").zfill(basis.L)
+    return "|" + " ".join(bits) + ">" if bracket_notation else bits
+
+
+def state_to_int(basis, state):
+    compact = state.strip("|>").replace(" ", "")
+    if len(compact) != basis.L:
+        raise ArgumentError(f"state must contain exactly {basis.L} binary digits")
+    if any(ch not in "01" for ch in compact):
+        raise ArgumentError("state must be binary")
+    return int(compact, 2)

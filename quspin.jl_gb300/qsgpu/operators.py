@@ -1,0 +1,328 @@
+"""Operators and Krylov solvers over libqsgpu (mirror of src/operators.jl).
+
+QuantumLinearOperator (2331-2552, 3133-3365), eigsh (3367-3408), the static
+Hamiltonian's matvec (754-766) and evolve (2073-2164); the matvec, Lanczos and
+Krylov exponential all run on the device.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .errors import ArgumentError, DimensionMismatch
+
+
+class OperatorTerm:
+    """OperatorTerm(op, couplings): couplings are (coefficient, site, ...) with one-based sites."""
+
+    def __init__(self, op, couplings):
+        if not op:
+            raise ArgumentError("operator string cannot be empty")
+        arity = sum(1 for ch in op if ch != "|")
+        norm = []
+        for c in couplings:
+            c = tuple(c)
+            if len(c) != arity + 1:
+                raise ArgumentError("operator arity and coupling sites differ")
+            if not all(isinstance(s, (int, np.integer)) for s in c[1:]):
+                raise ArgumentError("all sites must be integers")
+            norm.append(c)
+        self.op = str(op)
+        self.couplings = norm
+
+    def __eq__(self, other):
+        return isinstance(other, OperatorTerm) and self.op == other.op and self.couplings == other.couplings
+
+    def __repr__(self):
+        return f"OperatorTerm({self.op!r}, {self.couplings!r})"
+
+
+def _pack_terms(terms):
+    keep = []
+    arr = (_lib.Term * max(1, len(terms)))()
+    for i, t in enumerate(terms):
+        n = len(t.couplings)
+        arity = sum(1 for ch in t.op if ch != "|")
+        coeffs = np.zeros(2 * max(n, 1))
+        sites = np.zeros(max(arity * n, 1), dtype=np.int32)
+        cplx = False
+        for j, c in enumerate(t.couplings):
+            v = c[0]
+            if isinstance(v, (complex, np.complexfloating)):
+                cplx = True
+            v = complex(v)
+            coeffs[2 * j], coeffs[2 * j + 1] = v.real, v.imag
+            sites[j * arity:(j + 1) * arity] = [int(s) for s in c[1:]]
+        opb = t.op.encode()
+        keep += [coeffs, sites, opb]
+        arr[i] = _lib.Term(opb, n, _lib.ptr(coeffs), _lib.ptr(sites), int(cplx))
+    return arr, keep
+
+
+class QuantumLinearOperator:
+    """QuantumLinearOperator(basis, static_list; diagonal, check_symm, check_herm, check_pcon)."""
+
+    def __init__(self, basis, static_list, diagonal=None, check_symm=True, check_herm=True, check_pcon=True,
+                 _flags=0, _shared=None):
+        self.basis = basis
+        self.static_list = list(static_list)
+        self._flags = _flags
+        if _shared is not None:
+            self._h, self._owner = _shared
+        else:
+            lib = _lib.load()
+            arr, keep = _pack_terms(self.static_list)
+            checks = (_lib.QS_CHECK_SYMM if check_symm else 0) | (_lib.QS_CHECK_HERM if check_herm else 0) | (
+                _lib.QS_CHECK_PCON if check_pcon else 0)
+            dptr = None
+            d = None
+            if diagonal is not None:
+                dv = np.asarray(diagonal)
+                if dv.shape != (basis.Ns,):
+                    raise DimensionMismatch("diagonal must have length Ns")
+                if np.iscomplexobj(dv):
+                    checks |= _lib.QS_DIAG_COMPLEX
+                d = np.ascontiguousarray(dv, dtype=np.complex128)
+                dptr = _lib.ptr(d)
+            h = ctypes.c_void_p()
+            _lib.check(lib.qs_op_create(basis._h, arr, len(self.static_list), dptr, checks, ctypes.byref(h)))
+            self._h = h
+            self._owner = _Owner(h)
+            self._diag = np.zeros(basis.Ns) if d is None else (d if np.iscomplexobj(diagonal) else d.real.copy())
+        lib = _lib.load()
+        self.dtype = np.complex128 if lib.qs_op_dtype(self._h) == _lib.QS_C128 else np.float64
+        self.hermitian = bool(lib.qs_op_hermitian(self._h))
+        self.Ns = basis.Ns
+        self.shape = (basis.Ns, basis.Ns)
+        self.ndim = 2
+
+    @property
+    def diagonal(self):
+        return self._diag
+
+    @property
+    def get_shape(self):
+        return self.shape
+
+    def _with_flags(self, toggle):
+        op = QuantumLinearOperator(self.basis, self.static_list, _flags=self._flags ^ toggle,
+                                   _shared=(self._h, self._owner))
+        op._diag = self._diag
+        return op
+
+    def transpose(self):
+        return self._with_flags(_lib.QS_TRANSPOSE)
+
+    def conj(self):
+        return self._with_flags(_lib.QS_CONJUGATE)
+
+    def adjoint(self):
+        return self._with_flags(_lib.QS_TRANSPOSE | _lib.QS_CONJUGATE)
+
+    T = property(transpose)
+    H = property(adjoint)
+
+    def set_diagonal(self, diagonal):
+        d = np.ascontiguousarray(diagonal, dtype=np.complex128)
+        if d.shape != (self.Ns,):
+            raise DimensionMismatch("diagonal must have length Ns")
+        _lib.check(_lib.load().qs_op_set_diagonal(self._h, _lib.ptr(d)))
+        self._diag = np.asarray(diagonal).copy()
+        return self
+
+    # mul!(out, op, x, alpha, beta)
+    def mul(self, out, x, alpha=1.0, beta=0.0, precision="fp64"):
+        x = np.asarray(x)
+        if out.shape[0] != self.Ns:
+            raise DimensionMismatch("output and operator dimensions do not match")
+        if x.shape[0] != self.Ns:
+            raise DimensionMismatch("operator and value dimensions do not match")
+        if x.ndim != out.ndim or (x.ndim == 2 and x.shape[1] != out.shape[1]):
+            raise DimensionMismatch("output has the wrong dimensions")
+        single = precision == "fp32"
+        nrhs = 1 if x.ndim == 1 else x.shape[1]
+        ycx = np.iscomplexobj(out)
+        if (np.iscomplexobj(x) or self.dtype == np.complex128 or complex(alpha).imag or complex(beta).imag) and not ycx:
+            raise ArgumentError("a complex result cannot be stored in a real output")
+        if single:
+            xdt = np.complex64 if np.iscomplexobj(x) else np.float32
+            ydt = np.complex64 if ycx else np.float32
+        else:
+            xdt = np.complex128 if np.iscomplexobj(x) else np.float64
+            ydt = np.complex128 if ycx else np.float64
+        xs = np.asfortranarray(x, dtype=xdt)
+        ys = np.asfortranarray(out, dtype=ydt) if out.dtype != ydt or not out.flags.f_contiguous else out
+        if xs is ys or np.shares_memory(xs, ys):
+            xs = xs.copy(order="F")
+        code = {np.float64: 0, np.complex128: 1, np.float32: 2, np.complex64: 3}
+        a = np.array([complex(alpha).real, complex(alpha).imag])
+        b = np.array([complex(beta).real, complex(beta).imag])
+        _lib.check(_lib.load().qs_op_matvec(self._h, self._flags, _lib.ptr(a), _lib.ptr(xs), code[xdt], _lib.ptr(b),
+                                            _lib.ptr(ys), code[ydt], nrhs, _lib.QS_MEM_HOST))
+        if ys is not out:
+            out[...] = ys
+        return out
+
+    def dot(self, x, precision="fp64"):
+        x = np.asarray(x)
+        if x.shape[0] != self.Ns:
+            raise DimensionMismatch("operator and value dimensions do not match")
+        cpx = np.iscomplexobj(x) or self.dtype == np.complex128
+        out = np.zeros(x.shape, dtype=np.complex128 if cpx else np.float64, order="F")
+        return self.mul(out, x, precision=precision)
+
+    __matmul__ = dot
+
+    def __mul__(self, x):
+        return self.dot(x)
+
+    def toarray(self):
+        """Matrix(op): dense materialisation (small Ns only)."""
+        return self.dot(np.eye(self.Ns, dtype=self.dtype))
+
+
+class _Owner:
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        if self.h:
+            _lib.load().qs_op_destroy(self.h)
+            self.h = None
+
+
+def isquantum_LinearOperator(value):
+    return isinstance(value, QuantumLinearOperator)
+
+
+def apply(op, value, out=None, a=1.0):
+    if isinstance(op, ExpmMultiplyParallel):
+        return op.apply(value)
+    if out is None:
+        cpx = np.iscomplexobj(value) or op.dtype == np.complex128 or isinstance(a, complex)
+        out = np.zeros(np.shape(value), dtype=np.complex128 if cpx else np.float64, order="F")
+    return op.mul(out, value, a, 0.0)
+
+
+class Hamiltonian(QuantumLinearOperator):
+    """Static Hamiltonian(basis, terms): H * v and mul! (src/operators.jl:754-766)
+    on the device.  The assembled CSC field H.data is not materialised."""
+
+    def __init__(self, basis, terms, static_fmt=None, check_symm=True, check_herm=True, check_pcon=True):
+        super().__init__(basis, terms, check_symm=check_symm, check_herm=check_herm, check_pcon=check_pcon)
+
+
+def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, ncv=None, maxiter=None,
+          precision="fp64", info=None):
+    """eigsh(op; k, which=:SA, v0, tol, ncv, maxiter): k extremal eigenpairs."""
+    n = op.Ns
+    k = min(6, n) if k is None else int(k)
+    if not (1 <= k <= n):
+        raise ArgumentError("k must lie in 1:Ns")
+    w = str(which).upper()
+    if w not in ("SA", "LA", "SM", "LM", "BE"):
+        raise ArgumentError("which must be SA, LA, SM, LM, or BE")
+    if w not in ("SA", "LA"):
+        raise ArgumentError(f"which={w} is not implemented on this engine")
+    vv = None
+    if v0 is not None:
+        vv = np.ascontiguousarray(v0, dtype=op.dtype)
+        if vv.shape != (n,):
+            raise DimensionMismatch("v0 must have length Ns")
+    opts = _lib.EigshOpts(k, 0 if w == "SA" else 1, float(tol), int(ncv or 0), int(maxiter or 0),
+                          1 if precision == "fp32" else 0, int(bool(return_eigenvectors)),
+                          _lib.ptr(vv) if vv is not None else None, _lib.QS_MEM_HOST)
+    vals = np.zeros(k)
+    vecs = np.zeros((n, k), dtype=op.dtype, order="F") if return_eigenvectors else None
+    inf = _lib.EigshInfo()
+    _lib.check(_lib.load().qs_eigsh(op._h, ctypes.byref(opts), _lib.ptr(vals),
+                                    _lib.ptr(vecs) if vecs is not None else None, ctypes.byref(inf)))
+    if info is not None:
+        info.update(nconv=inf.nconv, restarts=inf.restarts, matvecs=inf.matvecs,
+                    max_rel_residual=inf.max_rel_residual, seconds=inf.seconds)
+    return (vals, vecs) if return_eigenvectors else vals
+
+
+def evolve(H, v0, t0, times, eom="SE", iterate=False, imag_time=False, tol=1e-12, krylov_dim=30, precision="fp64"):
+    """evolve(H, v0, t0, times; eom=:SE) for a static Hamiltonian (src/operators.jl:2073-2164)."""
+    if str(eom) not in ("SE", "LvNE"):
+        raise ArgumentError("eom must be :SE or :LvNE")
+    if str(eom) == "LvNE":
+        raise ArgumentError("LvNE evolution is not implemented on this engine")
+    scalar = np.isscalar(times)
+    ts = np.atleast_1d(np.asarray(times, dtype=np.float64))
+    v = np.ascontiguousarray(v0, dtype=np.complex128)
+    if v.shape != (H.Ns,):
+        raise DimensionMismatch("operator and vector dimensions do not match")
+    out = np.zeros((H.Ns, ts.size), dtype=np.complex128, order="F")
+    _lib.check(_lib.load().qs_evolve(H._h, _lib.ptr(v), float(t0), _lib.ptr(ts), ts.size, int(bool(imag_time)),
+                                     float(tol), int(krylov_dim), 1 if precision == "fp32" else 0, _lib.ptr(out)))
+    if iterate:
+        return (out[:, i].copy() for i in range(ts.size))
+    if scalar:
+        return out[:, 0].copy()
+    return out
+
+
+class ExpmMultiplyParallel:
+    """ExpmMultiplyParallel(A, a; dtype) with apply(v; work_array, overwrite_v, tol) (tools.jl:1605-1708)."""
+
+    def __init__(self, A, a=1.0, dtype=None, copy=False):
+        if not isinstance(A, QuantumLinearOperator):
+            raise ArgumentError("A must be a device operator of this engine")
+        if A.shape[0] != A.shape[1]:
+            raise ArgumentError("A must be a square matrix")
+        self.A = A
+        self.a = complex(a)
+        self.dtype = np.complex128
+
+    def set_a(self, a, dtype=None):
+        if dtype is not None and np.dtype(dtype) not in (np.dtype(np.complex128), np.dtype(np.float64)):
+            raise ArgumentError("changing the exponential dtype requires constructing a new operator")
+        self.a = complex(a)
+        return self
+
+    def apply(self, v, work_array=None, overwrite_v=False, tol=None, precision="fp64"):
+        v_in = np.asarray(v)
+        if v_in.shape[0] != self.A.shape[1]:
+            raise DimensionMismatch("A and v dimensions do not match")
+        if work_array is not None:
+            if work_array.size != 2 * v_in.size:
+                raise DimensionMismatch("work_array must contain twice as many elements as v")
+            if work_array.dtype != np.complex128:
+                raise ArgumentError("work_array must have element type ComplexF64")
+        tol = 1e-12 if tol is None else float(tol)
+        cols = v_in.reshape(v_in.shape[0], -1)
+        res = np.zeros(cols.shape, dtype=np.complex128)
+        a = np.array([self.a.real, self.a.imag])
+        for j in range(cols.shape[1]):
+            x = np.ascontiguousarray(cols[:, j], dtype=np.complex128)
+            o = np.zeros_like(x)
+            _lib.check(_lib.load().qs_expm_multiply(self.A._h, _lib.ptr(a), _lib.ptr(x), _lib.ptr(o), tol, 30,
+                                                    1 if precision == "fp32" else 0))
+            res[:, j] = o
+        res = res.reshape(v_in.shape)
+        if work_array is not None:
+            work_array[:v_in.size] = v_in.reshape(-1)
+            work_array[v_in.size:] = res.reshape(-1)
+            res = work_array[v_in.size:].reshape(v_in.shape)
+        if overwrite_v:
+            if not np.iscomplexobj(v):
+                raise ArgumentError("overwrite_v requires an input with the output dtype")
+            v[...] = res
+            return v
+        return res
+
+    def __mul__(self, v):
+        return self.apply(v)
+
+    __matmul__ = __mul__
+
+
+expm_multiply_parallel = ExpmMultiplyParallel
+
+
+def set_a(op, a, dtype=None):
+    return op.set_a(a, dtype)

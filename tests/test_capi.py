@@ -1,0 +1,52 @@
+"""The C-ABI library loads, exports every symbol of include/qsgpu.h, and turns
+invalid arguments into the reference's errors before touching the device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "qsgpu.h")) as f:
+        src = f.read()
+    return sorted(set(re.findall(r"QS_API[^;(]*?\b(qs_\w+)\s*\(", src)))
+
+
+def test_header_lists_entry_points():
+    syms = declared_symbols()
+    assert "qs_op_matvec" in syms and "qs_eigsh" in syms and "qs_evolve" in syms
+    assert len(syms) >= 20
+
+
+def test_library_exports_every_declared_symbol(qs):
+    from qsgpu import _lib
+    lib = _lib.load()
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+    assert set(declared_symbols()) == set(_lib.EXPORTS)
+    assert lib.qs_version().decode().startswith("qsgpu")
+
+
+@pytest.mark.parametrize("kwargs,msg", [
+    (dict(L=0), "L must be between 1 and 63"),
+    (dict(L=64), "L must be between 1 and 63"),
+    (dict(L=4, nup=5), "nup must lie between 0 and L"),
+    (dict(L=6, nup=3, kblock=1, pblock=1), "pblock can be combined with kblock only at k=0 or pi"),
+    (dict(L=6, nup=2, zblock=1), "symmetry transformation leaves the selected particle sector"),
+    (dict(L=6, nup=3, zAblock=1), "symmetry transformation leaves the selected particle sector"),
+    (dict(L=6, nup=3, a=4, kblock=0), "a must be a positive divisor of L"),
+    (dict(L=6, nup=3, pblock=2), "pblock must be +1 or -1"),
+    (dict(L=6, nup=3, kblock=0, pblock=1, zblock=1, pzblock=-1), "the requested symmetry sector is empty"),
+])
+def test_basis_argument_errors(qs, kwargs, msg):
+    with pytest.raises(qs.ArgumentError, match=re.escape(msg)):
+        qs.SpinBasis1D(**kwargs)
+
+
+def test_unsupported_symmetry_combination(qs):
+    # zA after a one-site translation needs the reference's dense nullspace path
+    with pytest.raises(qs.ArgumentError):
+        qs.SpinBasis1D(6, kblock=0, zAblock=1)

@@ -1,0 +1,182 @@
+"""Device matvec and Krylov solvers vs the oracle (reference algorithm)."""
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+import models
+
+pytestmark = pytest.mark.gpu
+
+MV_CASES = [
+    # (L, nup, pauli, sym, model)
+    (10, 5, False, dict(), "xxz"),
+    (10, None, True, dict(), "tfim"),
+    (12, 6, False, dict(kblock=0, pblock=1, zblock=1), "j1j2"),
+    (12, 6, False, dict(kblock=0, pblock=-1), "j1j2"),
+    (12, 6, False, dict(kblock=6, pblock=1, zblock=-1), "xxz"),
+    (12, 6, False, dict(kblock=1), "j1j2"),
+    (12, 6, False, dict(kblock=5, zblock=1), "j1j2"),
+    (12, None, True, dict(kblock=0, pblock=1), "tfim"),
+    (12, None, True, dict(kblock=3), "tfim"),
+    (10, None, False, dict(kblock=2), "xyz"),
+    (12, None, False, dict(kblock=0, pblock=1, zblock=1), "xyz_z"),
+]
+
+
+def spec(model, L):
+    if model == "xxz":
+        return models.xxz(L, 1.0, 0.5)
+    if model == "j1j2":
+        return models.j1j2(L, 1.0, 0.5)
+    if model == "tfim":
+        return models.tfim(L, 1.0, 0.7)
+    if model == "xyz":
+        return models.xyz_field(L)
+    if model == "xyz_z":
+        return [t for t in models.xyz_field(L) if t[0] not in ("y", "z")]
+    raise ValueError(model)
+
+
+@pytest.mark.parametrize("L,nup,pauli,sym,model", MV_CASES)
+def test_matvec_matches_oracle(qs, ora, L, nup, pauli, sym, model):
+    sp = spec(model, L)
+    ref = ora.RefBasis(L, nup=nup, pauli=pauli, **sym)
+    b = qs.SpinBasis1D(L, nup=nup, pauli=pauli, **sym)
+    op = qs.QuantumLinearOperator(b, models.to_terms(qs, sp))
+    n = b.Ns
+    x = models.seeded(n, complex_=True)
+    y0 = models.seeded(n, seed=7, complex_=True)
+    cterms = ora.consolidate_terms(sp)
+    for flags, (T, C) in ((0, (False, False)), ("T", (True, False)), ("C", (False, True)), ("H", (True, True))):
+        o = {0: op, "T": op.T, "C": op.conj(), "H": op.H}[flags]
+        want = ref.qlo_matvec(cterms, x, alpha=1.25 - 0.5j, beta=-0.5, y=y0, transposed=T, conjugated=C)
+        got = o.mul(y0.copy(), x, alpha=1.25 - 0.5j, beta=-0.5)
+        scale = max(1.0, np.abs(want).max())
+        assert np.max(np.abs(got - want)) <= 1e-13 * scale, flags
+    if op.dtype == np.float64:
+        xr = models.seeded(n)
+        want = ref.qlo_matvec(cterms, xr).real
+        got = op.dot(xr)
+        assert got.dtype == np.float64
+        assert np.max(np.abs(got - want)) <= 1e-13 * max(1.0, np.abs(want).max())
+    # repeated calls are bit-identical (fixed per-row summation order)
+    assert np.array_equal(op.dot(x), op.dot(x))
+
+
+def test_qlo_protocol_kat(qs, ora, kats):
+    k = kats["qlo_protocol_L3"]
+    b = qs.SpinBasis1D(k["L"], nup=k["nup"], pauli=k["pauli"])
+    terms = [qs.OperatorTerm(op, [tuple(c) for c in cs]) for op, cs in k["terms"]]
+    diag = np.array(k["diagonal"])
+    op = qs.QuantumLinearOperator(b, terms, diagonal=diag)
+    ref = ora.RefBasis(k["L"], nup=k["nup"], pauli=k["pauli"])
+    M = ref.dense(ora.consolidate_terms([(t.op, t.couplings) for t in terms]), diag=diag)
+    assert op.Ns == 3 and op.shape == (3, 3) and op.dtype == np.float64
+    assert np.array_equal(op.toarray(), M.real)
+    assert np.array_equal(op.H.toarray(), M.conj().T.real)
+    assert np.array_equal(op.T.toarray(), M.T.real)
+    v = np.array([complex(*c) for c in k["vector_unnormalized"]])
+    v /= np.linalg.norm(v)
+    assert np.allclose(op.dot(v), M @ v, atol=k["atol"])
+    dest = np.array([complex(*c) for c in k["destination"]])
+    out = op.mul(dest.copy(), v, k["alpha"], k["beta"])
+    assert np.allclose(out, k["alpha"] * (M @ v) + k["beta"] * dest, atol=k["atol"])
+    vals, vecs = qs.eigsh(op, k=k["eigsh_k"], which="SA")
+    assert np.allclose(M.real @ vecs, vecs * vals, atol=k["eigsh_atol"])
+    op.set_diagonal(np.zeros(3))
+    assert np.allclose(op.toarray(), ref.dense(ora.consolidate_terms([(t.op, t.couplings) for t in terms])).real,
+                       atol=0)
+
+
+def test_unchecked_nonsymmetric_qlo(qs, ora, kats):
+    k = kats["unchecked_symmetric_qlo"]
+    terms = [(op, [tuple(c) for c in cs]) for op, cs in k["terms"]]
+    b = qs.SpinBasis1D(k["L"], nup=k["nup"], pauli=False, kblock=0)
+    with pytest.raises(qs.ArgumentError):
+        qs.QuantumLinearOperator(b, models.to_terms(qs, terms))
+    op = qs.QuantumLinearOperator(b, models.to_terms(qs, terms), check_symm=False)
+    ref = ora.RefBasis(k["L"], nup=k["nup"], pauli=False, kblock=0)
+    v = models.seeded(b.Ns, complex_=True)
+    assert np.allclose(op.dot(v), ref.qlo_matvec(terms, v, extract=False), atol=k["atol"])
+
+
+def test_operator_errors(qs):
+    b = qs.SpinBasis1D(6, nup=3, pauli=False)
+    with pytest.raises(qs.ArgumentError, match="not Hermitian"):
+        qs.QuantumLinearOperator(b, [qs.OperatorTerm("+-", [(1.0, 1, 2)])])
+    with pytest.raises(qs.ArgumentError, match="particle sector"):
+        qs.QuantumLinearOperator(b, [qs.OperatorTerm("x", [(1.0, 1)])])
+    with pytest.raises(qs.ArgumentError, match="outside"):
+        qs.QuantumLinearOperator(b, [qs.OperatorTerm("z", [(1.0, 7)])])
+    op = qs.QuantumLinearOperator(b, [qs.OperatorTerm("zz", [(1.0, 1, 2)])])
+    with pytest.raises(qs.DimensionMismatch):
+        op.dot(np.ones(b.Ns + 1))
+    with pytest.raises(qs.ArgumentError, match="k must lie"):
+        qs.eigsh(op, k=0)
+
+
+@pytest.mark.parametrize("sym,model,L,nup,pauli", [
+    (dict(), "xxz", 12, 6, False),
+    (dict(kblock=0, pblock=1, zblock=1), "j1j2", 16, 8, False),
+    (dict(kblock=1), "j1j2", 14, 7, False),
+    (dict(kblock=0, pblock=1), "tfim", 14, None, True),
+])
+def test_eigsh_matches_dense(qs, ora, sym, model, L, nup, pauli):
+    sp = spec(model, L)
+    b = qs.SpinBasis1D(L, nup=nup, pauli=pauli, **sym)
+    op = qs.QuantumLinearOperator(b, models.to_terms(qs, sp))
+    rep = ora.RepBasis(L, nup=nup, pauli=pauli, **sym)
+    n = b.Ns
+    H = np.zeros((n, n), dtype=np.complex128)
+    e = np.zeros(n, dtype=np.complex128)
+    for j in range(n):
+        e[:] = 0
+        e[j] = 1
+        H[:, j] = rep.matvec(sp, e)
+    w = np.linalg.eigvalsh(H)
+    info = {}
+    vals, vecs = qs.eigsh(op, k=4, which="SA", tol=1e-12, info=info)
+    assert np.allclose(vals, w[:4], rtol=1e-10, atol=1e-10 * np.abs(w).max())
+    res = op.dot(vecs) - vecs * vals
+    assert np.abs(res).max() < 1e-8 * max(1, np.abs(w).max())
+    # single-precision Lanczos with FP64 polish reaches the same eigenvalue
+    v32 = qs.eigsh(op, k=1, which="SA", tol=1e-10, precision="fp32", return_eigenvectors=False)
+    assert abs(v32[0] - w[0]) <= 1e-10 * abs(w[0])
+
+
+def test_evolve_and_expm_match_oracle(qs, ora, kats):
+    k = kats["matrix_free_krylov_L8"]
+    L = k["L"]
+    bonds = [(i, i % L + 1) for i in range(1, L + 1)]
+    sp = [(op, [(c, a, bb) for a, bb in bonds]) for op, c in k["terms"]]
+    b = qs.SpinBasis1D(L, nup=4, pauli=False)
+    H = qs.Hamiltonian(b, models.to_terms(qs, sp))
+    M = ora.RefBasis(L, nup=4, pauli=False).dense(sp)
+    n = b.Ns
+    idx = np.arange(1, n + 1)
+    v = np.sin(idx) + 1j * np.cos(2 * idx)
+    v /= np.linalg.norm(v)
+    assert np.allclose(H.dot(v), M @ v, atol=k["matvec_atol"])
+    ev = qs.evolve(H, v, 0.0, k["times"])
+    assert np.allclose(ev[:, -1], sla.expm(-1j * k["times"][-1] * M) @ v, atol=k["evolve_atol"])
+    assert all(abs(np.linalg.norm(ev[:, j]) - 1) < k["norm_atol"] for j in range(ev.shape[1]))
+    a = complex(*k["expm_a"])
+    E = qs.ExpmMultiplyParallel(H, a)
+    assert np.allclose(E.apply(v), sla.expm(a * M) @ v, atol=k["evolve_atol"])
+    vals, vecs = qs.eigsh(H, k=2, which="SA")
+    assert np.allclose(M @ vecs, vecs * vals, atol=k["eigsh_atol"])
+
+
+def test_evolve_symmetric_sector_vs_oracle(qs, ora):
+    L = 14
+    sp = models.tfim(L, 1.0, 0.7)
+    sym = dict(kblock=0, pblock=1)
+    b = qs.SpinBasis1D(L, pauli=True, **sym)
+    H = qs.Hamiltonian(b, models.to_terms(qs, sp))
+    rep = ora.RepBasis(L, pauli=True, **sym)
+    v = models.seeded(b.Ns, complex_=True)
+    v /= np.linalg.norm(v)
+    times = np.linspace(0.1, 2.0, 5)
+    got = qs.evolve(H, v, 0.0, times, tol=1e-9)
+    want = ora.krylov_expmv_times(lambda x: rep.matvec(sp, x), v, [-1j * t for t in times], hermitian=True, tol=1e-9)
+    assert np.max(np.linalg.norm(got - want, axis=0)) < 1e-9
