@@ -75,11 +75,12 @@ def alive_transitions(states, L, J2):
     return float(tot.mean())
 
 
-def bytes_per_row(nbar, vec_bytes, state_bytes=4):
-    """Algorithmic HBM bytes per output row of the symmetric matvec: the row's
-    representative (state_bytes) and stabiliser code (2), its diagonal entry,
-    x[r], y[r] write, and one x gather per surviving transition."""
-    return state_bytes + 2 + vec_bytes + vec_bytes + vec_bytes + nbar * vec_bytes
+def asm_bytes_per_row(nbar, vec_bytes=8):
+    """Compulsory HBM bytes per row of one product with the assembled operator:
+    4 bytes per stored transition (packed column + value code), the row pointer
+    (8), the stabiliser code (2), the diagonal, x[r] and the y[r] write.  The x
+    gathers of the transitions hit L2 when x fits in it and are not counted."""
+    return 4 * nbar + 8 + 2 + 3 * vec_bytes
 
 
 class ClockSampler:
@@ -193,7 +194,7 @@ def run_reference(args, wl, world, rank):
     nthreads = os.cpu_count() or 1
     sec_per_row, rows, nbar, n, tt = cpu_port_sample(wl, nthreads, target_s=max(3.0, 1.5 * args.steps))
     # the port computes in complex128; the metric counts the FP64 real form's bytes
-    bpr = bytes_per_row(nbar, 8)
+    bpr = asm_bytes_per_row(nbar, 8)
     gbs = bpr / sec_per_row / 1e9
     line = {
         "metric": METRIC, "value": gbs, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
@@ -220,13 +221,23 @@ def run_ours(args, wl, world, rank, local):
     dev = torch.device("cuda", local)
     L, nup = wl["L"], wl["nup"]
     spec = j1j2_spec(L, 1.0, wl["J2"])
+    terms = [qs.OperatorTerm(o, c) for o, c in spec]
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     basis = qs.SpinBasis1D(L, nup=nup, pauli=False, **wl["sym"])
     t_basis = time.perf_counter() - t0
-    op = qs.QuantumLinearOperator(basis, [qs.OperatorTerm(o, c) for o, c in spec])
+    t0 = time.perf_counter()
+    H = qs.Hamiltonian(basis, terms)          # assembled on the device (the reference's H.data)
+    t_asm = time.perf_counter() - t0
+    op = qs.QuantumLinearOperator(basis, terms)  # matrix-free
     n = basis.Ns
-    stream = torch.cuda.current_stream(dev)
-    _lib.check(lib.qs_op_set_stream(op._h, ctypes.c_void_p(stream.cuda_stream)))
+    nnz = H.nnz
+    # a dedicated stream: the engine launches on it and the CUDA events below
+    # are recorded on it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    for o in (H, op):
+        _lib.check(lib.qs_op_set_stream(o._h, ctypes.c_void_p(stream.cuda_stream)))
     g = torch.Generator(device="cpu").manual_seed(20261203 + rank)
     xh = torch.randn(n, generator=g, dtype=torch.float64)
     x = xh.to(dev)
@@ -237,13 +248,13 @@ def run_ours(args, wl, world, rank, local):
     one = np.array([1.0, 0.0])
     zero = np.array([0.0, 0.0])
 
-    def mv(xt, yt, code):
-        _lib.check(lib.qs_op_matvec(op._h, 0, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()), code, _lib.ptr(zero),
+    def mv(o, xt, yt, code):
+        _lib.check(lib.qs_op_matvec(o._h, 0, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()), code, _lib.ptr(zero),
                                     ctypes.c_void_p(yt.data_ptr()), code, 1, _lib.QS_MEM_DEVICE))
 
-    def timed(xt, yt, code, steps, warmup):
+    def timed(o, xt, yt, code, steps, warmup):
         for _ in range(warmup):
-            mv(xt, yt, code)
+            mv(o, xt, yt, code)
         torch.cuda.synchronize()
         barrier(world)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -251,23 +262,22 @@ def run_ours(args, wl, world, rank, local):
         for s, e in ev:
             flush.zero_()
             s.record(stream)
-            mv(xt, yt, code)
+            mv(o, xt, yt, code)
             e.record(stream)
         torch.cuda.synchronize()
         launches = lib.qs_launch_count() - l0
-        ms = [s.elapsed_time(e) for s, e in ev]
-        return ms, launches
+        return [s.elapsed_time(e) for s, e in ev], launches
 
-    # nbar from a sample of representatives (exact count of alive programs)
-    reps = basis.orbit_minima()
-    nbar = alive_transitions(reps[n // 3: n // 3 + 200000], L, wl["J2"])
-    del reps
-    bpr64 = bytes_per_row(nbar, 8)
-    bpr32 = bytes_per_row(nbar, 4)
+    # algorithmic (compulsory) HBM bytes of one product
+    asm_bytes64 = 4 * nnz + 8 * (n + 1) + 2 * n + 8 * n + 8 * n + 8 * n
+    asm_bytes32 = 4 * nnz + 8 * (n + 1) + 2 * n + 4 * n + 4 * n + 4 * n
+    mf_bytes64 = n * (4 + 2 + 8 + 8 + 8)
     clocks = ClockSampler()
     clocks.start()
-    ms64, launches = timed(x, y, _lib.QS_F64, args.steps, args.warmup)
-    ms32, _ = timed(x32, y32, _lib.QS_F32, args.steps, args.warmup)
+    ms64, launches = timed(H, x, y, _lib.QS_F64, args.steps, args.warmup)
+    ms32, _ = timed(H, x32, y32, _lib.QS_F32, args.steps, args.warmup)
+    mf_steps = max(3, min(args.steps, 10))
+    ms_mf, _ = timed(op, x, y, _lib.QS_F64, mf_steps, 2)
     # e2e through the C ABI with host buffers (pinned), copies inside the step
     xp = torch.empty(n, dtype=torch.float64, pin_memory=True)
     xp.copy_(xh)
@@ -276,33 +286,30 @@ def run_ours(args, wl, world, rank, local):
     for it in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        _lib.check(lib.qs_op_matvec(op._h, 0, _lib.ptr(one), ctypes.c_void_p(xp.data_ptr()), _lib.QS_F64,
+        _lib.check(lib.qs_op_matvec(H._h, 0, _lib.ptr(one), ctypes.c_void_p(xp.data_ptr()), _lib.QS_F64,
                                     _lib.ptr(zero), ctypes.c_void_p(yp.data_ptr()), _lib.QS_F64, 1,
                                     _lib.QS_MEM_HOST))
         if it >= args.warmup:
             e2e_t.append(time.perf_counter() - t)
-    # Lanczos ground state, FP64 and FP32 + FP64 polish (device-resident v0)
+    # Lanczos ground state on the assembled operator, FP64 and FP32 + FP64 polish
     solves = {}
     for prec in ("fp64", "fp32"):
         info = {}
         torch.cuda.synchronize()
         t = time.perf_counter()
-        vals = qs.eigsh(op, k=1, which="SA", tol=1e-10, v0=xh.numpy(), return_eigenvectors=False,
+        vals = qs.eigsh(H, k=1, which="SA", tol=1e-10, v0=xh.numpy(), return_eigenvectors=False,
                         precision=prec, info=info)
         dt = time.perf_counter() - t
         solves[prec] = dict(seconds=dt, e0=float(vals[0]), matvecs=info.get("matvecs"),
                             restarts=info.get("restarts"))
     clk = clocks.stop()
 
-    t_step = float(np.mean(ms64)) / 1e3
-    t_step = max_over_ranks(world, t_step, dev)
-    value = world * bpr64 * n / t_step / 1e9
+    t_step = max_over_ranks(world, float(np.mean(ms64)) / 1e3, dev)
+    value = world * asm_bytes64 / t_step / 1e9
     peak, peak_kind = load_peaks()
-    achieved = bpr64 * n / (float(np.mean(ms64)) / 1e3) / 1e9
-    gbs32 = bpr32 * n / (float(np.mean(ms32)) / 1e3) / 1e9
-    e2e_mean = float(np.mean(e2e_t))
-    e2e_mean = max_over_ranks(world, e2e_mean, dev)
-    e2e_val = world * bpr64 * n / e2e_mean / 1e9
+    achieved = asm_bytes64 / (float(np.mean(ms64)) / 1e3) / 1e9
+    e2e_mean = max_over_ranks(world, float(np.mean(e2e_t)), dev)
+    e2e_val = world * asm_bytes64 / e2e_mean / 1e9
     rel_e0 = abs(solves["fp32"]["e0"] - solves["fp64"]["e0"]) / abs(solves["fp64"]["e0"])
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -311,7 +318,7 @@ def run_ours(args, wl, world, rank, local):
             oracle.lib()
             nthreads = os.cpu_count() or 1
             spr, rows, _, _, tt = cpu_port_sample(wl, nthreads, target_s=10.0)
-            cpu = {"value": bpr64 / spr / 1e9, "unit": "GB/s", "cores": nthreads, "kind": "port",
+            cpu = {"value": asm_bytes64 / n / spr / 1e9, "unit": "GB/s", "cores": nthreads, "kind": "port",
                    "sample": f"{rows} contiguous rows of {n} ({tt:.1f} s of matvec), representative-space "
                              "restatement of the reference matvec on all host cores"}
         except Exception as exc:  # the baseline is reported, never required
@@ -323,17 +330,22 @@ def run_ours(args, wl, world, rank, local):
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wl["desc"], "N": n, "step": "one H.v over the sector, x/y resident in HBM",
-                   "l2": "256 MB buffer written between timed steps", "nbar": round(nbar, 3),
-                   "bytes_per_row": round(bpr64, 2), "basis_build_s": round(t_basis, 3),
+        "config": {"workload": wl["desc"], "N": n, "nnz": nnz,
+                   "step": "one H.v of the assembled Hamiltonian over the sector, x/y resident in HBM",
+                   "bytes_per_step": asm_bytes64, "l2": "256 MB buffer written between timed steps",
+                   "basis_build_s": round(t_basis, 3), "assemble_s": round(t_asm, 3),
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind},
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "spmv_kernel (assembled H.v)"},
         "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": int(launches),
         "clocks": clk,
-        "fp32_form": {"value": gbs32, "unit": "GB/s", "ms_per_step": float(np.mean(ms32)),
+        "fp32_form": {"value": asm_bytes32 / (float(np.mean(ms32)) / 1e3) / 1e9, "unit": "GB/s",
+                      "ms_per_step": float(np.mean(ms32)),
                       "speedup_vs_fp64": float(np.mean(ms64)) / float(np.mean(ms32))},
+        "matrix_free": {"ms_per_step": float(np.mean(ms_mf)), "unit": "GB/s",
+                        "value": mf_bytes64 / (float(np.mean(ms_mf)) / 1e3) / 1e9,
+                        "note": "QuantumLinearOperator path: transitions regenerated every product"},
         "lanczos": {"solves_per_s_fp64": 1.0 / solves["fp64"]["seconds"],
                     "solves_per_s_fp32_polished": 1.0 / solves["fp32"]["seconds"],
                     "e0": solves["fp64"]["e0"], "fp32_polished_rel_err": rel_e0,

@@ -139,6 +139,15 @@ QS_API int qs_op_hermitian(const qs_op *op);
  * reference counterpart: it lets a host runtime that owns streams (CUDA.jl,
  * PyTorch) order the engine's work with its own. */
 QS_API int qs_op_set_stream(qs_op *op, void *stream);
+/* Assemble the operator on the device, as Hamiltonian(basis, terms) assembles
+ * H.data (src/operators.jl:461-614): every surviving transition is recorded
+ * once as a packed (column, value-code) word, and later products with this
+ * operator (qs_op_matvec and the solvers) stream it instead of regenerating
+ * the transitions.  QS_ERR_UNSUPPORTED when the operator cannot be assembled
+ * (non-commuting, or a site acted on twice); it then stays matrix-free. */
+QS_API int qs_op_assemble(qs_op *op);
+/* Stored nonzeros of the assembled form (off-diagonal), -1 if not assembled. */
+QS_API int64_t qs_op_nnz(const qs_op *op);
 /* set_diagonal!(op, d) (src/operators.jl:3298-3307); d is 2*Ns doubles. */
 QS_API int qs_op_set_diagonal(qs_op *op, const double *diagonal);
 

@@ -1,0 +1,455 @@
+// qs_assembled.cu -- the assembled (compiled-transition) form of an operator.
+//
+// The reference's static Hamiltonian assembles H.data as a CSC matrix at
+// construction (_assemble, src/operators.jl:461-576) and its matvec is a
+// SparseArrays SpMV (754-766).  Here the assembled form is built on the device
+// by one pass of the fused row kernel that records, for every surviving
+// transition, its column and a small value code, packed into one 32-bit word
+// (column in the high bits, code in the low bits).  Every matrix element is a
+// product  A_class * (+-1) * chi_class * sqrt(stab_col) / sqrt(stab_row),  so a
+// table of a few hundred values replaces the 8-16 bytes of a stored element and
+// the SpMV streams 4 bytes per nonzero.  Rows are sub-warp owned; no atomics.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "qs_device.cuh"
+#include "qs_internal.h"
+
+namespace qs {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxSplit = 2048;
+
+struct BuildArgs {
+    const void* reps;
+    const uint16_t* stab;
+    const void* split;
+    int64_t n, nsplit, stride;
+    const GroupDesc* group;
+    const uint64_t* binom;
+    const int32_t* index;
+    int L, nup, mode;      // mode: 0 full space, 1 combinadic, 2 search, 3 direct index
+    const TermProg* progs;
+    int nprog;
+    const uint16_t* prog_code;   // (aclass * 2 + sign) per program
+    const uint16_t* elem_code;   // (cclass * 2 + sign) per group element
+    const uint8_t* stab_class;   // dclass per stabiliser order
+    int nC, nD, code_bits;
+    int32_t* counts;             // pass 1
+    const int64_t* rowptr;       // pass 2
+    uint32_t* words;
+    uint16_t* codes;             // unpacked layout: code per nonzero
+    int32_t* cols;               // unpacked layout: column per nonzero
+    int packed;
+};
+
+template <typename U>
+__device__ __forceinline__ U build_row_state(const BuildArgs& a, int64_t r) {
+    if (a.mode >= 2) return ((const U*)a.reps)[r];
+    if (a.mode == 0) return (U)r;
+    U s = 0;
+    int b = a.L - 1;
+    int64_t rem = r;
+    for (int p = a.nup; p >= 1; --p) {
+        while ((int64_t)__ldg(a.binom + b * 65 + p) > rem) --b;
+        s |= (U)1 << b;
+        rem -= (int64_t)__ldg(a.binom + b * 65 + p);
+        --b;
+    }
+    return s;
+}
+
+template <typename U, bool kWrite>
+__global__ void __launch_bounds__(kThreads) build_kernel(BuildArgs a) {
+    __shared__ GroupSmem g;
+    __shared__ U spl[kMaxSplit];
+    if (a.mode >= 2) {
+        load_group_smem(g, a.group);
+        if (a.mode == 2)
+            for (int i = threadIdx.x; i < a.nsplit; i += blockDim.x) spl[i] = ((const U*)a.split)[i];
+        __syncthreads();
+    }
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.n; r += (int64_t)gridDim.x * blockDim.x) {
+        const U s = build_row_state<U>(a, r);
+        int64_t out = kWrite ? a.rowptr[r] : 0;
+        int32_t cnt = 0;
+        for (int k = 0; k < a.nprog; ++k) {
+            const TermProg& p = a.progs[k];
+            if ((s & (U)p.need1) != (U)p.need1 || (s & (U)p.need0) != (U)0) continue;
+            U t = s ^ (U)p.flip;
+            int sign = (__popcll((unsigned long long)(~s & (U)p.zmask)) + __popcll((unsigned long long)(s & (U)p.ymask))) & 1;
+            int64_t idx;
+            int cclass = 0, dclass = 0;
+            if (a.mode >= 2) {
+                U m;
+                int bi, st;
+                orbit_min<U>(g, t, m, bi, st);
+                if (a.mode == 3) {
+                    int64_t rk = a.nup >= 0 ? combinadic_rank<U>(m, a.binom, 65) : (int64_t)m;
+                    idx = __ldg(a.index + rk);
+                } else {
+                    idx = rank_search<U>((const U*)a.reps, a.n, spl, (int)a.nsplit, a.stride, m);
+                }
+                if (idx < 0) continue;
+                int ec = a.elem_code[bi];
+                cclass = ec >> 1;
+                sign ^= ec & 1;
+                dclass = a.stab_class[st];
+            } else if (a.mode == 1) {
+                if (__popcll((unsigned long long)t) != a.nup) continue;
+                idx = combinadic_rank<U>(t, a.binom, 65);
+            } else {
+                idx = (int64_t)t;
+            }
+            if (kWrite) {
+                int pc = a.prog_code[k];
+                sign ^= pc & 1;
+                uint32_t code = (uint32_t)((((pc >> 1) * a.nC + cclass) * a.nD + dclass) * 2 + sign);
+                if (a.packed) a.words[out] = ((uint32_t)idx << a.code_bits) | code;
+                else {
+                    a.cols[out] = (int32_t)idx;
+                    a.codes[out] = (uint16_t)code;
+                }
+                ++out;
+            } else {
+                ++cnt;
+            }
+        }
+        if (!kWrite) a.counts[r] = cnt;
+    }
+}
+
+__global__ void counts_to_i64(const int32_t* c, int64_t* o, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        o[i] = c[i];
+}
+
+template <typename T> struct V2;
+template <> struct V2<double> { using t = double2; };
+template <> struct V2<float> { using t = float2; };
+
+struct SpmvArgs {
+    const int64_t* rowptr;
+    const uint32_t* words;
+    const int32_t* cols;
+    const uint16_t* codes;
+    int packed;
+    uint32_t code_mask;
+    int code_bits;
+    const void* table;       // value per code (T or complex T)
+    int ncodes;
+    const uint16_t* stab;    // row stabiliser order (null: 1)
+    const void* diag;        // complex T per row
+    int64_t n;
+    double ar, ai, br, bi;
+    int beta_zero;
+    int conj;                // use the conjugated value table and diagonal
+    const void* x;
+    void* y;
+};
+
+// y = beta*y + alpha*( d.*x + (1/sqrt(stab_r)) * sum_j table[code_j] x[col_j] ),
+// kG lanes per row.
+template <int kG, bool kCM, bool kCV, typename T>
+__global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvArgs a) {
+    using T2 = typename V2<T>::t;
+    __shared__ T2 tab[1024];
+    __shared__ T rsq[kMaxGroup + 1];
+    const bool smem_tab = a.ncodes <= 1024;
+    if (smem_tab)
+        for (int i = threadIdx.x; i < a.ncodes; i += blockDim.x) {
+            T2 v = ((const T2*)a.table)[i];
+            if (a.conj) v.y = -v.y;
+            tab[i] = v;
+        }
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) rsq[i] = i ? (T)(1.0 / sqrt((double)i)) : (T)0;
+    __syncthreads();
+    const int lane = threadIdx.x % kG;
+    constexpr int kRowsPerWarp = 32 / kG;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) / 32;
+    const int sub = (threadIdx.x % 32) / kG;
+    // every lane of a warp runs the same number of iterations (shuffles below)
+    for (int64_t base = warp0 * kRowsPerWarp; base < a.n; base += nwarps * kRowsPerWarp) {
+        const int64_t r = base + sub;
+        const bool live = r < a.n;
+        const int64_t j0 = live ? a.rowptr[r] : 0, j1 = live ? a.rowptr[r + 1] : 0;
+        T acc_r = 0, acc_i = 0;
+        for (int64_t j = j0 + lane; j < j1; j += kG) {
+            uint32_t col, code;
+            if (a.packed) {
+                uint32_t w = __ldg(a.words + j);
+                col = w >> a.code_bits;
+                code = w & a.code_mask;
+            } else {
+                col = (uint32_t)__ldg(a.cols + j);
+                code = __ldg(a.codes + j);
+            }
+            T2 v;
+            if (smem_tab) v = tab[code];
+            else {
+                v = ((const T2*)a.table)[code];
+                if (a.conj) v.y = -v.y;
+            }
+            if (kCV) {
+                T2 xv = ((const T2*)a.x)[col];
+                if (kCM) {
+                    acc_r += v.x * xv.x - v.y * xv.y;
+                    acc_i += v.x * xv.y + v.y * xv.x;
+                } else {
+                    acc_r += v.x * xv.x;
+                    acc_i += v.x * xv.y;
+                }
+            } else {
+                acc_r += v.x * ((const T*)a.x)[col];
+            }
+        }
+#pragma unroll
+        for (int o = kG / 2; o > 0; o >>= 1) {
+            acc_r += __shfl_xor_sync(0xffffffffu, acc_r, o, kG);
+            if (kCV) acc_i += __shfl_xor_sync(0xffffffffu, acc_i, o, kG);
+        }
+        if (lane == 0 && live) {
+            T sc = a.stab ? rsq[a.stab[r]] : (T)1;
+            acc_r *= sc;
+            acc_i *= sc;
+            T2 d = ((const T2*)a.diag)[r];
+            T dr = d.x, di = a.conj ? -d.y : d.y;
+            if (kCV) {
+                T2 xv = ((const T2*)a.x)[r];
+                acc_r += dr * xv.x - di * xv.y;
+                acc_i += dr * xv.y + di * xv.x;
+                T2* y = (T2*)a.y;
+                T yr = 0, yi = 0;
+                if (!a.beta_zero) {
+                    T2 yo = y[r];
+                    yr = (T)a.br * yo.x - (T)a.bi * yo.y;
+                    yi = (T)a.br * yo.y + (T)a.bi * yo.x;
+                }
+                T2 o;
+                o.x = yr + (T)a.ar * acc_r - (T)a.ai * acc_i;
+                o.y = yi + (T)a.ar * acc_i + (T)a.ai * acc_r;
+                y[r] = o;
+            } else {
+                acc_r += dr * ((const T*)a.x)[r];
+                T* y = (T*)a.y;
+                T yr = a.beta_zero ? (T)0 : (T)a.br * y[r];
+                y[r] = yr + (T)a.ar * acc_r;
+            }
+        }
+    }
+}
+
+int grid_rows(int64_t threads_needed) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int64_t blocks = (threads_needed + kThreads - 1) / kThreads;
+    int64_t cap = (int64_t)sms * 8;
+    return (int)std::max<int64_t>(1, std::min(blocks, cap));
+}
+
+}  // namespace
+
+void op_assemble(Op& op) {
+    Basis& b = *op.basis;
+    if (op.assembled) return;
+    if (!op.commuting) throw Error(QS_ERR_UNSUPPORTED, "only symmetry-commuting operators are assembled");
+    const size_t nfwd = op.progs.size() / 2;
+    std::vector<TermProg> fwd(op.progs.begin(), op.progs.begin() + nfwd);
+    for (const TermProg& p : fwd)
+        if (!p.distinct) throw Error(QS_ERR_UNSUPPORTED, "operators acting twice on one site are not assembled");
+    // value classes
+    using cd = std::complex<double>;
+    auto canon = [](cd v, int& sign) {
+        sign = 0;
+        if (v.real() < 0 || (v.real() == 0 && v.imag() < 0)) { v = -v; sign = 1; }
+        return v;
+    };
+    std::vector<cd> A, C;
+    std::vector<uint16_t> prog_code(std::max<size_t>(1, nfwd));
+    for (size_t k = 0; k < nfwd; ++k) {
+        int sg;
+        cd v = canon(cd(fwd[k].amp0_re, fwd[k].amp0_im), sg);
+        size_t c = 0;
+        while (c < A.size() && A[c] != v) ++c;
+        if (c == A.size()) A.push_back(v);
+        prog_code[k] = (uint16_t)(c * 2 + sg);
+    }
+    if (A.empty()) A.push_back(cd(0, 0));
+    const GroupDesc& G = b.group;
+    std::vector<uint16_t> elem_code(kMaxGroup, 0);
+    std::vector<uint8_t> stab_class(kMaxGroup + 1, 0);
+    std::vector<double> D;
+    if (b.symmetric) {
+        for (int e = 0; e < G.ng; ++e) {
+            int sg;
+            cd v = canon(cd(G.chi_re[e], G.chi_im[e]), sg);
+            size_t c = 0;
+            while (c < C.size() && std::abs(C[c] - v) > 1e-14) ++c;
+            if (c == C.size()) C.push_back(v);
+            elem_code[e] = (uint16_t)(c * 2 + sg);
+        }
+        for (int st = 1; st <= G.ng; ++st)
+            if (G.ng % st == 0) {
+                stab_class[st] = (uint8_t)D.size();
+                D.push_back(std::sqrt((double)st));
+            }
+    } else {
+        C.push_back(cd(1, 0));
+        D.push_back(1.0);
+    }
+    const int nA = (int)A.size(), nC = (int)C.size(), nD = (int)D.size();
+    const int64_t ncodes = (int64_t)nA * nC * nD * 2;
+    if (ncodes > 65536) throw Error(QS_ERR_UNSUPPORTED, "too many distinct matrix elements to assemble");
+    int col_bits = 1;
+    while (((int64_t)1 << col_bits) < b.n) ++col_bits;
+    int code_bits = 1;
+    while (((int64_t)1 << code_bits) < ncodes) ++code_bits;
+    const bool packed = col_bits + code_bits <= 32;
+    if (packed) code_bits = 32 - col_bits;
+    std::vector<cd> table(ncodes);
+    for (int a = 0; a < nA; ++a)
+        for (int c = 0; c < nC; ++c)
+            for (int d = 0; d < nD; ++d)
+                for (int sg = 0; sg < 2; ++sg) {
+                    cd v = A[a] * C[c] * D[d];
+                    table[(((int64_t)a * nC + c) * nD + d) * 2 + sg] = sg ? -v : v;
+                }
+    Assembled& M = op.asm_;
+    M.ncodes = (int)ncodes;
+    M.code_bits = code_bits;
+    M.packed = packed;
+    M.table64.alloc(ncodes * sizeof(cd));
+    QS_CUDA(cudaMemcpy(M.table64.p, table.data(), ncodes * sizeof(cd), cudaMemcpyHostToDevice));
+    std::vector<std::complex<float>> t32(ncodes);
+    for (int64_t i = 0; i < ncodes; ++i) t32[i] = std::complex<float>((float)table[i].real(), (float)table[i].imag());
+    M.table32.alloc(ncodes * sizeof(std::complex<float>));
+    QS_CUDA(cudaMemcpy(M.table32.p, t32.data(), ncodes * sizeof(std::complex<float>), cudaMemcpyHostToDevice));
+
+    cudaStream_t s = op.stream;
+    DevBuf d_prog(fwd.size() * sizeof(TermProg) + 1), d_pc(prog_code.size() * 2), d_ec(kMaxGroup * 2),
+        d_sc(kMaxGroup + 1);
+    if (!fwd.empty())
+        QS_CUDA(cudaMemcpy(d_prog.p, fwd.data(), fwd.size() * sizeof(TermProg), cudaMemcpyHostToDevice));
+    QS_CUDA(cudaMemcpy(d_pc.p, prog_code.data(), prog_code.size() * 2, cudaMemcpyHostToDevice));
+    QS_CUDA(cudaMemcpy(d_ec.p, elem_code.data(), kMaxGroup * 2, cudaMemcpyHostToDevice));
+    QS_CUDA(cudaMemcpy(d_sc.p, stab_class.data(), kMaxGroup + 1, cudaMemcpyHostToDevice));
+    BuildArgs a{};
+    a.reps = b.d_reps.p;
+    a.stab = b.d_stab.as<uint16_t>();
+    a.split = b.d_split.p;
+    a.n = b.n;
+    a.nsplit = b.nsplit;
+    a.stride = b.split_stride;
+    a.group = b.d_group.as<GroupDesc>();
+    a.binom = b.d_binom.as<uint64_t>();
+    a.index = b.has_index ? b.d_index.as<int32_t>() : nullptr;
+    a.L = b.L;
+    a.nup = b.nup;
+    a.mode = b.symmetric ? (b.has_index ? 3 : 2) : (b.nup >= 0 ? 1 : 0);
+    a.progs = d_prog.as<TermProg>();
+    a.nprog = (int)fwd.size();
+    a.prog_code = d_pc.as<uint16_t>();
+    a.elem_code = d_ec.as<uint16_t>();
+    a.stab_class = d_sc.as<uint8_t>();
+    a.nC = nC;
+    a.nD = nD;
+    a.code_bits = code_bits;
+    a.packed = packed;
+    DevBuf cnt32(b.n * sizeof(int32_t)), cnt64(b.n * sizeof(int64_t));
+    M.rowptr.alloc((b.n + 1) * sizeof(int64_t));
+    a.counts = cnt32.as<int32_t>();
+    int grid = grid_rows(b.n);
+    const bool wide = b.symmetric ? b.wide : true;
+    if (wide) build_kernel<uint64_t, false><<<grid, kThreads, 0, s>>>(a);
+    else build_kernel<uint32_t, false><<<grid, kThreads, 0, s>>>(a);
+    QS_CUDA(cudaGetLastError());
+    counts_to_i64<<<grid, kThreads, 0, s>>>(cnt32.as<int32_t>(), cnt64.as<int64_t>(), b.n);
+    QS_CUDA(cudaGetLastError());
+    scan_i64(cnt64.as<int64_t>(), M.rowptr.as<int64_t>(), b.n, s);
+    int64_t last = 0, lastc = 0;
+    QS_CUDA(cudaMemcpyAsync(&last, M.rowptr.as<int64_t>() + b.n - 1, 8, cudaMemcpyDeviceToHost, s));
+    QS_CUDA(cudaMemcpyAsync(&lastc, cnt64.as<int64_t>() + b.n - 1, 8, cudaMemcpyDeviceToHost, s));
+    QS_CUDA(cudaStreamSynchronize(s));
+    M.nnz = last + lastc;
+    QS_CUDA(cudaMemcpy(M.rowptr.as<int64_t>() + b.n, &M.nnz, 8, cudaMemcpyHostToDevice));
+    if (packed) {
+        M.words.alloc(std::max<int64_t>(1, M.nnz) * sizeof(uint32_t));
+        a.words = M.words.as<uint32_t>();
+    } else {
+        M.cols.alloc(std::max<int64_t>(1, M.nnz) * sizeof(int32_t));
+        M.codes.alloc(std::max<int64_t>(1, M.nnz) * sizeof(uint16_t));
+        a.cols = M.cols.as<int32_t>();
+        a.codes = M.codes.as<uint16_t>();
+    }
+    a.rowptr = M.rowptr.as<int64_t>();
+    if (wide) build_kernel<uint64_t, true><<<grid, kThreads, 0, s>>>(a);
+    else build_kernel<uint32_t, true><<<grid, kThreads, 0, s>>>(a);
+    QS_CUDA(cudaGetLastError());
+    QS_CUDA(cudaStreamSynchronize(s));
+    note_launches(4);
+    // lanes per row: the power of two nearest a quarter of the mean row length
+    double mean = b.n ? (double)M.nnz / (double)b.n : 0.0;
+    M.lanes = mean > 48 ? 16 : (mean > 12 ? 8 : 4);
+    op.assembled = true;
+}
+
+void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
+    const Basis& b = *op.basis;
+    const Assembled& M = op.asm_;
+    SpmvArgs a{};
+    a.rowptr = M.rowptr.as<int64_t>();
+    a.words = M.words.as<uint32_t>();
+    a.cols = M.cols.as<int32_t>();
+    a.codes = M.codes.as<uint16_t>();
+    a.packed = M.packed;
+    a.code_bits = M.code_bits;
+    a.code_mask = M.code_bits >= 32 ? 0xffffffffu : ((1u << M.code_bits) - 1u);
+    a.ncodes = M.ncodes;
+    a.stab = b.symmetric ? b.d_stab.as<uint16_t>() : nullptr;
+    a.n = b.n;
+    a.ar = c.alpha.re;
+    a.ai = c.alpha.im;
+    a.br = c.beta.re;
+    a.bi = c.beta.im;
+    a.beta_zero = (c.beta.re == 0.0 && c.beta.im == 0.0);
+    const bool T = (c.flags & QS_TRANSPOSE) != 0, C = (c.flags & QS_CONJUGATE) != 0;
+    // transpose of a Hermitian operator is its conjugate
+    a.conj = T != C;
+    a.x = c.x;
+    a.y = c.y;
+    const bool cm = op.complex_mat, cv = c.y_complex;
+    const int64_t thr = b.n * M.lanes;
+    const int grid = grid_rows(thr);
+#define QS_SPMV(G, T_)                                                                          \
+    do {                                                                                        \
+        if (cm) spmv_kernel<G, true, true, T_><<<grid, kThreads, 0, s>>>(a);                    \
+        else if (cv) spmv_kernel<G, false, true, T_><<<grid, kThreads, 0, s>>>(a);              \
+        else spmv_kernel<G, false, false, T_><<<grid, kThreads, 0, s>>>(a);                     \
+    } while (0)
+    if (c.single) {
+        a.table = M.table32.p;
+        a.diag = op.d_diag32.p;
+        if (M.lanes == 16) QS_SPMV(16, float);
+        else if (M.lanes == 8) QS_SPMV(8, float);
+        else QS_SPMV(4, float);
+    } else {
+        a.table = M.table64.p;
+        a.diag = op.d_diag.p;
+        if (M.lanes == 16) QS_SPMV(16, double);
+        else if (M.lanes == 8) QS_SPMV(8, double);
+        else QS_SPMV(4, double);
+    }
+#undef QS_SPMV
+    QS_CUDA(cudaGetLastError());
+    note_launches(1);
+}
+
+}  // namespace qs

@@ -293,6 +293,17 @@ __global__ void splitter_kernel(const U* reps, U* spl, int64_t nsplit, int64_t s
     if (i < nsplit) spl[i] = reps[i * stride];
 }
 
+// Direct index: column of every representative at its parent-sector rank
+// (combinadic rank for a fixed-weight sector, the state itself otherwise).
+template <typename U>
+__global__ void index_fill_kernel(const U* reps, int64_t n, const uint64_t* binom, int nup, int32_t* index) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        U s = reps[i];
+        int64_t rk = nup >= 0 ? combinadic_rank<U>(s, binom, 65) : (int64_t)s;
+        index[rk] = (int32_t)i;
+    }
+}
+
 int grid_for(int64_t work, int threads) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -345,10 +356,25 @@ void enumerate_sector(Basis& b, DevBuf& d_chi_one) {
     splitter_kernel<U><<<(unsigned)((b.nsplit + 255) / 256), 256, 0, s>>>(b.d_reps.as<U>(), b.d_split.as<U>(),
                                                                           b.nsplit, b.split_stride);
     QS_CUDA(cudaGetLastError());
+    // Direct rank -> column table when it fits in a quarter of free memory and
+    // every column fits an int32: one HBM load replaces the search.
+    size_t free_b = 0, total_b = 0;
+    QS_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    size_t need = (size_t)b.n_parent * sizeof(int32_t);
+    if (b.n < INT32_MAX && need <= free_b / 4) {
+        b.d_index.alloc(need);
+        QS_CUDA(cudaMemsetAsync(b.d_index.p, 0xFF, need, s));
+        index_fill_kernel<U><<<grid_for(b.n, 256), 256, 0, s>>>(b.d_reps.as<U>(), b.n, b.d_binom.as<uint64_t>(),
+                                                                 b.nup, b.d_index.as<int32_t>());
+        QS_CUDA(cudaGetLastError());
+        b.has_index = true;
+    }
     QS_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace
+
+void scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t s) { exclusive_scan(in, out, n, s); }
 
 // ----------------------------------------------------------- basis_build
 void basis_build(Basis& b) {

@@ -160,6 +160,12 @@ int qs_op_set_stream(qs_op* op, void* stream) {
 
 int64_t qs_launch_count(void) { return qs::launches(); }
 
+int qs_op_assemble(qs_op* op) {
+    return guard([&] { qs::op_assemble(*op->op); });
+}
+
+int64_t qs_op_nnz(const qs_op* op) { return op->op->assembled ? op->op->asm_.nnz : -1; }
+
 int qs_op_dtype(const qs_op* op) { return op->op->complex_mat ? QS_C128 : QS_F64; }
 int qs_op_hermitian(const qs_op* op) { return op->op->hermitian ? 1 : 0; }
 

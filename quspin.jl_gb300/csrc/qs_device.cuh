@@ -104,4 +104,18 @@ __device__ __forceinline__ int64_t combinadic_rank(U s, const uint64_t* binom, i
     return r;
 }
 
+// Combinadic rank of a state of at most 32 sites with the C(bit, p) table in
+// shared memory (32 x 33 uint32 entries).
+__device__ __forceinline__ int64_t combinadic_rank32(uint32_t s, const uint32_t* binom32) {
+    uint32_t r = 0;
+    int particle = 1;
+    while (s) {
+        int bit = __ffs((int)s) - 1;
+        r += binom32[bit * 33 + particle];
+        ++particle;
+        s &= s - 1;
+    }
+    return (int64_t)r;
+}
+
 }  // namespace qs

@@ -84,6 +84,8 @@ struct Basis {
     DevBuf d_split;                  // search splitters (same type as reps)
     int64_t nsplit = 0, split_stride = 1;
     DevBuf d_binom;                  // uint64 C(b, p) table for combinadic ranks
+    DevBuf d_index;                  // int32 column of each parent-sector rank (-1: none)
+    bool has_index = false;          // direct rank -> column table built
     std::vector<uint64_t> h_refrep;  // reference (argmax) representatives
     bool refrep_ready = false;
     // per-level subgroup element lists and the level-0 coefficient table used
@@ -94,6 +96,10 @@ struct Basis {
     cudaStream_t stream = nullptr;
     ~Basis();
 };
+
+}  // namespace qs
+#include "qs_assembled.h"
+namespace qs {
 
 struct Op {
     Basis* basis = nullptr;
@@ -111,6 +117,8 @@ struct Op {
     DevBuf d_x32, d_y32;
     cudaStream_t stream = nullptr;      // stream in use
     cudaStream_t own_stream = nullptr;  // created by the library
+    Assembled asm_;                     // assembled (compiled-transition) form
+    bool assembled = false;
     ~Op();
 };
 
@@ -134,6 +142,11 @@ struct MatvecCall {
     bool single = false;            // FP32 vectors and accumulation
 };
 void op_prepare_device(Op& op);
+// qs_assembled.cu
+void op_assemble(Op& op);
+void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s);
+// device-wide exclusive scan of int64 (qs_basis.cu)
+void scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t s);
 // kernel launch accounting (qs_launch_count)
 void note_launches(int64_t n);
 int64_t launches();

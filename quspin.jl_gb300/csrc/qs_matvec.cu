@@ -33,7 +33,7 @@ namespace {
 
 constexpr int kMvThreads = 256;
 constexpr int kMaxSplit = 2048;
-constexpr int kSmemProgs = 256;
+constexpr int kSmemProgs = 160;
 
 template <typename T> struct V2;
 template <> struct V2<double> { using t = double2; };
@@ -49,6 +49,7 @@ struct MvArgs {
     int L, nup, pauli;
     const TermProg* progs;
     int nprog;
+    const int32_t* index;    // direct rank -> column table (mode 3)
     const void* diag;        // complex, precision of the call
     int conj_amp, conj_chi;
     double ar, ai, br, bi;
@@ -156,13 +157,19 @@ __device__ __forceinline__ void load_x(const MvArgs& a, int64_t i, T& xr, T& xi)
 
 template <typename U, int kMode, bool kCM, bool kCV, typename T>
 __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
+    constexpr bool kSym = kMode >= 2;
     __shared__ GroupSmem g;
     __shared__ U spl[kMode == 2 ? kMaxSplit : 1];
+    __shared__ uint32_t binom32[kMode == 3 && sizeof(U) == 4 ? 32 * 33 : 1];
     __shared__ TermProg progs[kSmemProgs];
     __shared__ double sqrt_stab[kMaxGroup + 1];
-    if (kMode == 2) {
+    if (kSym) {
         load_group_smem(g, a.group);
-        for (int i = threadIdx.x; i < a.nsplit; i += blockDim.x) spl[i] = ((const U*)a.split)[i];
+        if (kMode == 2)
+            for (int i = threadIdx.x; i < a.nsplit; i += blockDim.x) spl[i] = ((const U*)a.split)[i];
+        if (kMode == 3 && sizeof(U) == 4)
+            for (int i = threadIdx.x; i < 32 * 33; i += blockDim.x)
+                binom32[i] = (uint32_t)a.binom[(i / 33) * 65 + (i % 33)];
         for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) sqrt_stab[i] = sqrt((double)i);
     }
     const int np_smem = a.nprog < kSmemProgs ? a.nprog : kSmemProgs;
@@ -172,9 +179,9 @@ __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
     const double* chi_im = a.group->chi_im;
 
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.n; r += (int64_t)gridDim.x * blockDim.x) {
-        const U s = row_state<U>(a, kMode, r);
+        const U s = row_state<U>(a, kSym ? 2 : kMode, r);
         T inv_sr = 1;
-        if (kMode == 2) inv_sr = (T)1 / (T)sqrt_stab[a.stab[r]];
+        if (kSym) inv_sr = (T)1 / (T)sqrt_stab[a.stab[r]];
         T acc_r = 0, acc_i = 0;
         for (int k = 0; k < a.nprog; ++k) {
             const TermProg& p = (k < kSmemProgs) ? progs[k] : a.progs[k];
@@ -183,11 +190,19 @@ __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
             if (!run_prog<U, T>(p, a.pauli, s, t, wr, wi)) continue;
             int64_t idx;
             if (a.conj_amp) wi = -wi;
-            if (kMode == 2) {
+            if (kSym) {
                 U m;
                 int bi, st;
                 orbit_min<U>(g, t, m, bi, st);
-                idx = rank_search<U>((const U*)a.reps, a.n, spl, (int)a.nsplit, a.stride, m);
+                if (kMode == 3) {
+                    int64_t rk;
+                    if (a.nup < 0) rk = (int64_t)m;
+                    else if (sizeof(U) == 4) rk = combinadic_rank32((uint32_t)m, binom32);
+                    else rk = combinadic_rank<U>(m, a.binom, 65);
+                    idx = __ldg(a.index + rk);
+                } else {
+                    idx = rank_search<U>((const U*)a.reps, a.n, spl, (int)a.nsplit, a.stride, m);
+                }
                 if (idx < 0) continue;
                 const T f = (T)sqrt_stab[st] * inv_sr;
                 if (kCM) {
@@ -341,7 +356,9 @@ __global__ void diag_kernel(MvArgs a, const double* user, double* out) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.n; r += (int64_t)gridDim.x * blockDim.x) {
         int mode = a.reps ? 2 : (a.nup >= 0 ? 1 : 0);
         U s = row_state<U>(a, mode, r);
-        double dr = user ? user[2 * r] : 0.0, di = user ? user[2 * r + 1] : 0.0;
+        // extracted diagonal summed from zero in term order, then added to the
+        // user diagonal (diagonal + extracted_diagonal, src/operators.jl:3103-3106)
+        double dr = 0.0, di = 0.0;
         for (int k = 0; k < a.nprog; ++k) {
             U t;
             double are, aim;
@@ -349,8 +366,8 @@ __global__ void diag_kernel(MvArgs a, const double* user, double* out) {
             dr += are;
             di += aim;
         }
-        out[2 * r] = dr;
-        out[2 * r + 1] = di;
+        out[2 * r] = (user ? user[2 * r] : 0.0) + dr;
+        out[2 * r + 1] = (user ? user[2 * r + 1] : 0.0) + di;
     }
 }
 
@@ -382,6 +399,7 @@ MvArgs base_args(const Op& op) {
     a.L = b.L;
     a.nup = b.nup;
     a.pauli = b.spec.pauli;
+    a.index = b.has_index ? b.d_index.as<int32_t>() : nullptr;
     return a;
 }
 
@@ -395,7 +413,10 @@ void launch_mode(const MvArgs& a, bool cm, bool cv, cudaStream_t s) {
 
 template <typename T>
 void launch_matvec(const Basis& b, const MvArgs& a, bool cm, bool cv, cudaStream_t s) {
-    if (b.symmetric) {
+    if (b.symmetric && b.has_index) {
+        if (b.wide) launch_mode<uint64_t, 3, T>(a, cm, cv, s);
+        else launch_mode<uint32_t, 3, T>(a, cm, cv, s);
+    } else if (b.symmetric) {
         if (b.wide) launch_mode<uint64_t, 2, T>(a, cm, cv, s);
         else launch_mode<uint32_t, 2, T>(a, cm, cv, s);
     } else if (b.nup >= 0) {
@@ -491,6 +512,10 @@ void op_matvec_device(Op& op, const MatvecCall& c, cudaStream_t s) {
         }
         QS_CUDA(cudaGetLastError());
         note_launches(1);
+        return;
+    }
+    if (op.assembled && (!T || op.hermitian)) {
+        op_spmv_device(op, c, s);
         return;
     }
     if (c.single) {

@@ -21,6 +21,7 @@ SOURCES = [
     "qs_matvec.cu",
     "qs_blas.cu",
     "qs_krylov.cu",
+    "qs_assembled.cu",
     "qs_dense.cpp",
     "qs_op.cpp",
     "qs_capi.cpp",

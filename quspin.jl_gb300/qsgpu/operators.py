@@ -210,8 +210,20 @@ class Hamiltonian(QuantumLinearOperator):
     """Static Hamiltonian(basis, terms): H * v and mul! (src/operators.jl:754-766)
     on the device.  The assembled CSC field H.data is not materialised."""
 
-    def __init__(self, basis, terms, static_fmt=None, check_symm=True, check_herm=True, check_pcon=True):
+    def __init__(self, basis, terms, static_fmt=None, check_symm=True, check_herm=True, check_pcon=True,
+                 assemble=True):
         super().__init__(basis, terms, check_symm=check_symm, check_herm=check_herm, check_pcon=check_pcon)
+        self.assembled = False
+        if assemble:
+            st = _lib.load().qs_op_assemble(self._h)
+            if st == 0:
+                self.assembled = True
+            elif st != 6:  # 6: not assemblable, stays matrix-free
+                _lib.check(st)
+
+    @property
+    def nnz(self):
+        return int(_lib.load().qs_op_nnz(self._h))
 
 
 def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, ncv=None, maxiter=None,

@@ -47,10 +47,16 @@ def test_matvec_matches_oracle(qs, ora, L, nup, pauli, sym, model):
     x = models.seeded(n, complex_=True)
     y0 = models.seeded(n, seed=7, complex_=True)
     cterms = ora.consolidate_terms(sp)
+    alpha, beta = 1.25 - 0.5j, -0.5
     for flags, (T, C) in ((0, (False, False)), ("T", (True, False)), ("C", (False, True)), ("H", (True, True))):
         o = {0: op, "T": op.T, "C": op.conj(), "H": op.H}[flags]
-        want = ref.qlo_matvec(cterms, x, alpha=1.25 - 0.5j, beta=-0.5, y=y0, transposed=T, conjugated=C)
-        got = o.mul(y0.copy(), x, alpha=1.25 - 0.5j, beta=-0.5)
+        # mul! semantics: alpha * op(A) x + beta * y
+        want = alpha * ref.qlo_matvec(cterms, x, transposed=T, conjugated=C) + beta * y0
+        if b.symmetric or not C:
+            # the reference computes exactly this (symmetric path applies alpha after projecting)
+            assert np.allclose(want, ref.qlo_matvec(cterms, x, alpha=alpha, beta=beta, y=y0, transposed=T,
+                                                    conjugated=C), atol=1e-12 * max(1, np.abs(want).max()))
+        got = o.mul(y0.copy(), x, alpha=alpha, beta=beta)
         scale = max(1.0, np.abs(want).max())
         assert np.max(np.abs(got - want)) <= 1e-13 * scale, flags
     if op.dtype == np.float64:
@@ -180,3 +186,49 @@ def test_evolve_symmetric_sector_vs_oracle(qs, ora):
     got = qs.evolve(H, v, 0.0, times, tol=1e-9)
     want = ora.krylov_expmv_times(lambda x: rep.matvec(sp, x), v, [-1j * t for t in times], hermitian=True, tol=1e-9)
     assert np.max(np.linalg.norm(got - want, axis=0)) < 1e-9
+
+
+def test_conjugated_complex_alpha_on_unreduced_basis(qs, ora):
+    """The reference conjugates a complex alpha together with the term amplitudes
+    when conjugated=true on an unreduced basis (src/operators.jl:2565, 2582) but
+    not in its diagonal or symmetric paths.  The engine applies alpha as mul!
+    defines it; the oracle records the reference's behaviour."""
+    L = 8
+    sp = models.xxz(L, 1.0, 0.5)
+    ref = ora.RefBasis(L, nup=4, pauli=False)
+    b = qs.SpinBasis1D(L, nup=4, pauli=False)
+    op = qs.QuantumLinearOperator(b, models.to_terms(qs, sp)).conj()
+    cterms = ora.consolidate_terms(sp)
+    x = models.seeded(b.Ns, complex_=True)
+    alpha = 0.3 + 0.7j
+    d = ref.extract_diagonal(cterms)
+    offdiag = ref.qlo_matvec(cterms, x, conjugated=True) - np.conj(d) * x
+    quirk = ref.qlo_matvec(cterms, x, alpha=alpha, conjugated=True)
+    assert np.allclose(quirk, np.conj(alpha) * offdiag + alpha * np.conj(d) * x, atol=1e-13)
+    got = op.mul(np.zeros(b.Ns, dtype=complex), x, alpha=alpha)
+    assert np.allclose(got, alpha * (offdiag + np.conj(d) * x), atol=1e-13)
+
+
+@pytest.mark.parametrize("L,nup,pauli,sym,model", MV_CASES)
+def test_assembled_matches_matrix_free(qs, ora, L, nup, pauli, sym, model):
+    """Hamiltonian (assembled on the device, as the reference assembles H.data)
+    against the matrix-free operator and the oracle, FP64 and FP32."""
+    sp = spec(model, L)
+    b = qs.SpinBasis1D(L, nup=nup, pauli=pauli, **sym)
+    terms = models.to_terms(qs, sp)
+    op = qs.QuantumLinearOperator(b, terms)
+    H = qs.Hamiltonian(b, terms)
+    assert H.assembled and H.nnz > 0
+    ref = ora.RefBasis(L, nup=nup, pauli=pauli, **sym)
+    x = models.seeded(b.Ns, complex_=True)
+    want = ref.qlo_matvec(ora.consolidate_terms(sp), x)
+    scale = max(1.0, np.abs(want).max())
+    for o_h, o_q in ((H, op), (H.H, op.H), (H.conj(), op.conj()), (H.T, op.T)):
+        a = o_h.dot(x)
+        assert np.max(np.abs(a - o_q.dot(x))) <= 1e-13 * scale
+    assert np.max(np.abs(H.dot(x) - want)) <= 1e-13 * scale
+    y32 = H.dot(x, precision="fp32")
+    assert np.max(np.abs(y32 - want)) <= 2e-5 * scale
+    if H.dtype == np.float64:
+        xr = models.seeded(b.Ns)
+        assert np.max(np.abs(H.dot(xr) - op.dot(xr))) <= 1e-13 * scale
