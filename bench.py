@@ -248,13 +248,13 @@ def run_ours(args, wl, world, rank, local):
     one = np.array([1.0, 0.0])
     zero = np.array([0.0, 0.0])
 
-    def mv(o, xt, yt, code):
-        _lib.check(lib.qs_op_matvec(o._h, 0, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()), code, _lib.ptr(zero),
+    def mv(o, xt, yt, code, flags=0):
+        _lib.check(lib.qs_op_matvec(o._h, flags, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()), code, _lib.ptr(zero),
                                     ctypes.c_void_p(yt.data_ptr()), code, 1, _lib.QS_MEM_DEVICE))
 
-    def timed(o, xt, yt, code, steps, warmup):
+    def timed(o, xt, yt, code, steps, warmup, flags=0):
         for _ in range(warmup):
-            mv(o, xt, yt, code)
+            mv(o, xt, yt, code, flags)
         torch.cuda.synchronize()
         barrier(world)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -262,7 +262,7 @@ def run_ours(args, wl, world, rank, local):
         for s, e in ev:
             flush.zero_()
             s.record(stream)
-            mv(o, xt, yt, code)
+            mv(o, xt, yt, code, flags)
             e.record(stream)
         torch.cuda.synchronize()
         launches = lib.qs_launch_count() - l0
@@ -275,6 +275,10 @@ def run_ours(args, wl, world, rank, local):
     clocks = ClockSampler()
     clocks.start()
     ms64, launches = timed(H, x, y, _lib.QS_F64, args.steps, args.warmup)
+    y_native = y.clone()
+    ydf = torch.empty_like(x)
+    msdf, _ = timed(H, x, ydf, _lib.QS_F64, args.steps, args.warmup, _lib.QS_DOUBLE_FLOAT)
+    df_err = float((ydf - y_native).norm() / y_native.norm())
     ms32, _ = timed(H, x32, y32, _lib.QS_F32, args.steps, args.warmup)
     mf_steps = max(3, min(args.steps, 10))
     ms_mf, _ = timed(op, x, y, _lib.QS_F64, mf_steps, 2)
@@ -293,7 +297,7 @@ def run_ours(args, wl, world, rank, local):
             e2e_t.append(time.perf_counter() - t)
     # Lanczos ground state on the assembled operator, FP64 and FP32 + FP64 polish
     solves = {}
-    for prec in ("fp64", "fp32"):
+    for prec in ("fp64", "fp32", "fp64df"):
         info = {}
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -343,11 +347,18 @@ def run_ours(args, wl, world, rank, local):
         "fp32_form": {"value": asm_bytes32 / (float(np.mean(ms32)) / 1e3) / 1e9, "unit": "GB/s",
                       "ms_per_step": float(np.mean(ms32)),
                       "speedup_vs_fp64": float(np.mean(ms64)) / float(np.mean(ms32))},
+        "fp64_double_float_form": {"value": asm_bytes64 / (float(np.mean(msdf)) / 1e3) / 1e9, "unit": "GB/s",
+                                   "ms_per_step": float(np.mean(msdf)),
+                                   "frac_of_peak": asm_bytes64 / (float(np.mean(msdf)) / 1e3) / 1e9 / peak,
+                                   "rel_err_vs_native_fp64": df_err,
+                                   "speedup_vs_fp64": float(np.mean(ms64)) / float(np.mean(msdf))},
         "matrix_free": {"ms_per_step": float(np.mean(ms_mf)), "unit": "GB/s",
                         "value": mf_bytes64 / (float(np.mean(ms_mf)) / 1e3) / 1e9,
                         "note": "QuantumLinearOperator path: transitions regenerated every product"},
         "lanczos": {"solves_per_s_fp64": 1.0 / solves["fp64"]["seconds"],
                     "solves_per_s_fp32_polished": 1.0 / solves["fp32"]["seconds"],
+                    "solves_per_s_fp64_double_float": 1.0 / solves["fp64df"]["seconds"],
+                    "fp64df_rel_err": abs(solves["fp64df"]["e0"] - solves["fp64"]["e0"]) / abs(solves["fp64"]["e0"]),
                     "e0": solves["fp64"]["e0"], "fp32_polished_rel_err": rel_e0,
                     "matvecs_fp64": solves["fp64"]["matvecs"], "matvecs_fp32": solves["fp32"]["matvecs"],
                     "tol": 1e-10},

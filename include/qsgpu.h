@@ -151,7 +151,14 @@ QS_API int64_t qs_op_nnz(const qs_op *op);
 /* set_diagonal!(op, d) (src/operators.jl:3298-3307); d is 2*Ns doubles. */
 QS_API int qs_op_set_diagonal(qs_op *op, const double *diagonal);
 
-enum { QS_TRANSPOSE = 1, QS_CONJUGATE = 2 };
+enum {
+    QS_TRANSPOSE = 1,
+    QS_CONJUGATE = 2,
+    /* FP64 vectors, products of an assembled operator carried in double-float
+     * (pairs of FP32, ~48-bit significand) to stay off GB300's slow FP64 pipe;
+     * ignored for single precision and for matrix-free operators. */
+    QS_DOUBLE_FLOAT = 4
+};
 
 /* mul!(Y, op, X, alpha, beta) (src/operators.jl:3147-3208) for nrhs column-
  * major right-hand sides with leading dimension Ns:
@@ -174,7 +181,8 @@ typedef struct {
     double tol;           /* relative Ritz tolerance, 0 = machine epsilon (ARPACK default) */
     int32_t ncv;          /* Lanczos basis size, 0 = max(20, 2k+1) (Arpack.jl default) */
     int32_t maxiter;      /* restarts, 0 = 300 */
-    int32_t precision;    /* 0 = FP64, 1 = FP32 matvec and vectors + FP64 polish */
+    int32_t precision;    /* 0 = FP64, 1 = FP32 matvec and vectors + FP64 polish,
+                             2 = FP64 vectors with double-float products (assembled operators) */
     int32_t want_vectors;
     const double *v0;     /* NULL or starting vector, dtype of op */
     int32_t mem;          /* QS_MEM_HOST or QS_MEM_DEVICE for v0 and vectors */

@@ -40,6 +40,8 @@ struct BuildArgs {
     const uint16_t* prog_code;   // (aclass * 2 + sign) per program
     const uint16_t* elem_code;   // (cclass * 2 + sign) per group element
     const uint8_t* stab_class;   // dclass per stabiliser order
+    FastGroup fast;              // zero-run orbit search when enabled
+    const uint16_t* fast_code;   // (cclass * 2 + sign) per fast element code
     int nC, nD, code_bits;
     int32_t* counts;             // pass 1
     const int64_t* rowptr;       // pass 2
@@ -89,7 +91,14 @@ __global__ void __launch_bounds__(kThreads) build_kernel(BuildArgs a) {
             if (a.mode >= 2) {
                 U m;
                 int bi, st;
-                orbit_min<U>(g, t, m, bi, st);
+                int ec;
+                if (a.fast.enabled) {
+                    orbit_min_fast<U>(a.fast, t, m, bi, st);
+                    ec = a.fast_code[bi];
+                } else {
+                    orbit_min<U>(g, t, m, bi, st);
+                    ec = a.elem_code[bi];
+                }
                 if (a.mode == 3) {
                     int64_t rk = a.nup >= 0 ? combinadic_rank<U>(m, a.binom, 65) : (int64_t)m;
                     idx = __ldg(a.index + rk);
@@ -97,7 +106,6 @@ __global__ void __launch_bounds__(kThreads) build_kernel(BuildArgs a) {
                     idx = rank_search<U>((const U*)a.reps, a.n, spl, (int)a.nsplit, a.stride, m);
                 }
                 if (idx < 0) continue;
-                int ec = a.elem_code[bi];
                 cclass = ec >> 1;
                 sign ^= ec & 1;
                 dclass = a.stab_class[st];
@@ -246,6 +254,159 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvArgs a) {
     }
 }
 
+// ---------------------------------------------------------- double-float form
+// GB300's FP64 pipe, not HBM, bounds the FP64 product above (one DFMA per
+// nonzero).  This form keeps every per-nonzero operation on the FP32 pipe:
+// x is split once per row into hi + lo floats, the value table holds hi + lo
+// pairs, and products and sums are carried as unevaluated float pairs with
+// the error-free transformations TwoProd (via fma) and TwoSum (Knuth), i.e.
+// about 48 significand bits.  Only the per-row combination runs in FP64.
+
+struct DF {
+    float h, l;
+};
+
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return DF{s, e};
+}
+
+// acc += t * x  (t, x double-float)
+__device__ __forceinline__ void df_mac(DF& acc, float th, float tl, float xh, float xl) {
+    float p = th * xh;
+    float pe = fmaf(th, xh, -p);
+    pe = fmaf(th, xl, pe);
+    pe = fmaf(tl, xh, pe);
+    DF s = df_two_sum(acc.h, p);
+    acc.h = s.h;
+    acc.l = acc.l + (s.l + pe);
+}
+
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    DF s = df_two_sum(a.h, b.h);
+    s.l += a.l + b.l;
+    return df_two_sum(s.h, s.l);
+}
+
+__device__ __forceinline__ double df_to_double(DF a) { return (double)a.h + (double)a.l; }
+
+__device__ __forceinline__ float2 df_split(double v) {
+    float h = __double2float_rn(v);
+    float l = __double2float_rn(v - (double)h);
+    return make_float2(h, l);
+}
+
+// x (double, or double2 when complex) -> (hi, lo) float pairs per component
+template <bool kCV>
+__global__ void split_kernel(const void* x, float4* out_c, float2* out_r, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (kCV) {
+            double2 v = ((const double2*)x)[i];
+            float2 a = df_split(v.x), b = df_split(v.y);
+            out_c[i] = make_float4(a.x, a.y, b.x, b.y);
+        } else {
+            out_r[i] = df_split(((const double*)x)[i]);
+        }
+    }
+}
+
+struct SpmvDFArgs {
+    SpmvArgs s;
+    const float4* tab_df;    // per code: re(hi, lo), im(hi, lo)
+    const void* xs;          // split x: float2 (real) or float4 (complex)
+};
+
+template <int kG, bool kCM, bool kCV>
+__global__ void __launch_bounds__(kThreads) spmv_df_kernel(SpmvDFArgs da) {
+    const SpmvArgs& a = da.s;
+    __shared__ float4 tab[1024];
+    __shared__ double rsq[kMaxGroup + 1];
+    const bool smem_tab = a.ncodes <= 1024;
+    if (smem_tab)
+        for (int i = threadIdx.x; i < a.ncodes; i += blockDim.x) {
+            float4 v = da.tab_df[i];
+            if (a.conj) { v.z = -v.z; v.w = -v.w; }
+            tab[i] = v;
+        }
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) rsq[i] = i ? 1.0 / sqrt((double)i) : 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x % kG;
+    constexpr int kRowsPerWarp = 32 / kG;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) / 32;
+    const int sub = (threadIdx.x % 32) / kG;
+    for (int64_t base = warp0 * kRowsPerWarp; base < a.n; base += nwarps * kRowsPerWarp) {
+        const int64_t r = base + sub;
+        const bool live = r < a.n;
+        const int64_t j0 = live ? a.rowptr[r] : 0, j1 = live ? a.rowptr[r + 1] : 0;
+        DF ar{0.f, 0.f}, ai{0.f, 0.f};
+        for (int64_t j = j0 + lane; j < j1; j += kG) {
+            uint32_t col, code;
+            if (a.packed) {
+                uint32_t w = __ldg(a.words + j);
+                col = w >> a.code_bits;
+                code = w & a.code_mask;
+            } else {
+                col = (uint32_t)__ldg(a.cols + j);
+                code = __ldg(a.codes + j);
+            }
+            float4 v;
+            if (smem_tab) v = tab[code];
+            else {
+                v = da.tab_df[code];
+                if (a.conj) { v.z = -v.z; v.w = -v.w; }
+            }
+            if (kCV) {
+                float4 xv = ((const float4*)da.xs)[col];
+                df_mac(ar, v.x, v.y, xv.x, xv.y);
+                df_mac(ai, v.x, v.y, xv.z, xv.w);
+                if (kCM) {
+                    df_mac(ar, -v.z, -v.w, xv.z, xv.w);
+                    df_mac(ai, v.z, v.w, xv.x, xv.y);
+                }
+            } else {
+                float2 xv = ((const float2*)da.xs)[col];
+                df_mac(ar, v.x, v.y, xv.x, xv.y);
+            }
+        }
+#pragma unroll
+        for (int o = kG / 2; o > 0; o >>= 1) {
+            DF br{__shfl_xor_sync(0xffffffffu, ar.h, o, kG), __shfl_xor_sync(0xffffffffu, ar.l, o, kG)};
+            ar = df_add(ar, br);
+            if (kCV) {
+                DF bi{__shfl_xor_sync(0xffffffffu, ai.h, o, kG), __shfl_xor_sync(0xffffffffu, ai.l, o, kG)};
+                ai = df_add(ai, bi);
+            }
+        }
+        if (lane == 0 && live) {
+            double sc = a.stab ? rsq[a.stab[r]] : 1.0;
+            double acc_r = df_to_double(ar) * sc, acc_i = kCV ? df_to_double(ai) * sc : 0.0;
+            double2 d = ((const double2*)a.diag)[r];
+            double dr = d.x, di = a.conj ? -d.y : d.y;
+            if (kCV) {
+                double2 xv = ((const double2*)a.x)[r];
+                acc_r += dr * xv.x - di * xv.y;
+                acc_i += dr * xv.y + di * xv.x;
+                double2* y = (double2*)a.y;
+                double yr = 0, yi = 0;
+                if (!a.beta_zero) {
+                    double2 yo = y[r];
+                    yr = a.br * yo.x - a.bi * yo.y;
+                    yi = a.br * yo.y + a.bi * yo.x;
+                }
+                y[r] = make_double2(yr + a.ar * acc_r - a.ai * acc_i, yi + a.ar * acc_i + a.ai * acc_r);
+            } else {
+                acc_r += dr * ((const double*)a.x)[r];
+                double* y = (double*)a.y;
+                double yr = a.beta_zero ? 0.0 : a.br * y[r];
+                y[r] = yr + a.ar * acc_r;
+            }
+        }
+    }
+}
+
 int grid_rows(int64_t threads_needed) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -332,10 +493,25 @@ void op_assemble(Op& op) {
     for (int64_t i = 0; i < ncodes; ++i) t32[i] = std::complex<float>((float)table[i].real(), (float)table[i].imag());
     M.table32.alloc(ncodes * sizeof(std::complex<float>));
     QS_CUDA(cudaMemcpy(M.table32.p, t32.data(), ncodes * sizeof(std::complex<float>), cudaMemcpyHostToDevice));
+    std::vector<float> tdf(4 * ncodes);
+    for (int64_t i = 0; i < ncodes; ++i) {
+        double re = table[i].real(), im = table[i].imag();
+        float rh = (float)re, ih = (float)im;
+        tdf[4 * i] = rh;
+        tdf[4 * i + 1] = (float)(re - (double)rh);
+        tdf[4 * i + 2] = ih;
+        tdf[4 * i + 3] = (float)(im - (double)ih);
+    }
+    M.table_df.alloc(ncodes * 4 * sizeof(float));
+    QS_CUDA(cudaMemcpy(M.table_df.p, tdf.data(), ncodes * 4 * sizeof(float), cudaMemcpyHostToDevice));
+    M.xsplit.alloc((size_t)b.n * 4 * sizeof(float));
 
     cudaStream_t s = op.stream;
+    std::vector<uint16_t> fast_code(std::max<size_t>(1, b.fast_to_elem.size()), 0);
+    for (size_t i = 0; i < b.fast_to_elem.size(); ++i) fast_code[i] = elem_code[b.fast_to_elem[i]];
     DevBuf d_prog(fwd.size() * sizeof(TermProg) + 1), d_pc(prog_code.size() * 2), d_ec(kMaxGroup * 2),
-        d_sc(kMaxGroup + 1);
+        d_sc(kMaxGroup + 1), d_fc(fast_code.size() * 2);
+    QS_CUDA(cudaMemcpy(d_fc.p, fast_code.data(), fast_code.size() * 2, cudaMemcpyHostToDevice));
     if (!fwd.empty())
         QS_CUDA(cudaMemcpy(d_prog.p, fwd.data(), fwd.size() * sizeof(TermProg), cudaMemcpyHostToDevice));
     QS_CUDA(cudaMemcpy(d_pc.p, prog_code.data(), prog_code.size() * 2, cudaMemcpyHostToDevice));
@@ -359,6 +535,8 @@ void op_assemble(Op& op) {
     a.prog_code = d_pc.as<uint16_t>();
     a.elem_code = d_ec.as<uint16_t>();
     a.stab_class = d_sc.as<uint8_t>();
+    a.fast = b.fast;
+    a.fast_code = d_fc.as<uint16_t>();
     a.nC = nC;
     a.nD = nD;
     a.code_bits = code_bits;
@@ -434,6 +612,30 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
         else if (cv) spmv_kernel<G, false, true, T_><<<grid, kThreads, 0, s>>>(a);              \
         else spmv_kernel<G, false, false, T_><<<grid, kThreads, 0, s>>>(a);                     \
     } while (0)
+    if (c.df && !c.single) {
+        a.diag = op.d_diag.p;
+        SpmvDFArgs da{};
+        da.s = a;
+        da.tab_df = M.table_df.as<float4>();
+        da.xs = M.xsplit.p;
+        const int sg = grid_rows(b.n);
+        if (cv) split_kernel<true><<<sg, kThreads, 0, s>>>(c.x, M.xsplit.as<float4>(), nullptr, b.n);
+        else split_kernel<false><<<sg, kThreads, 0, s>>>(c.x, nullptr, M.xsplit.as<float2>(), b.n);
+        QS_CUDA(cudaGetLastError());
+#define QS_SPMV_DF(G)                                                                           \
+        do {                                                                                    \
+            if (cm) spmv_df_kernel<G, true, true><<<grid, kThreads, 0, s>>>(da);                \
+            else if (cv) spmv_df_kernel<G, false, true><<<grid, kThreads, 0, s>>>(da);          \
+            else spmv_df_kernel<G, false, false><<<grid, kThreads, 0, s>>>(da);                 \
+        } while (0)
+        if (M.lanes == 16) QS_SPMV_DF(16);
+        else if (M.lanes == 8) QS_SPMV_DF(8);
+        else QS_SPMV_DF(4);
+#undef QS_SPMV_DF
+        QS_CUDA(cudaGetLastError());
+        note_launches(2);
+        return;
+    }
     if (c.single) {
         a.table = M.table32.p;
         a.diag = op.d_diag32.p;

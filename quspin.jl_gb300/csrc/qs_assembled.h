@@ -12,6 +12,8 @@ struct Assembled {
     DevBuf codes;      // uint16 code per nonzero, when not packed
     DevBuf table64;    // complex double value per code
     DevBuf table32;    // complex float value per code
+    DevBuf table_df;   // per code: re hi, re lo, im hi, im lo (float)
+    DevBuf xsplit;     // x split into float pairs for the double-float product
     int64_t nnz = 0;
     int ncodes = 0;
     int code_bits = 0;

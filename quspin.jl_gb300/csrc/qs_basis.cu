@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <vector>
 
 #include "qs_device.cuh"
@@ -376,6 +377,69 @@ void enumerate_sector(Basis& b, DevBuf& d_chi_one) {
 
 void scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t s) { exclusive_scan(in, out, n, s); }
 
+namespace {
+
+// Recognises G = translations by multiples of a x {1, parity} x {1, full flip}
+// (every combination present and distinct) and builds the per-element tables
+// the zero-run orbit search (qs_orbit.cuh) needs.
+void detect_fast_group(Basis& b, const Closure& C, int kmom, int nT) {
+    b.fast = FastGroup{};
+    b.fast_chi.clear();
+    b.fast_to_elem.clear();
+    if (!b.symmetric) return;
+    const int L = b.L;
+    const uint64_t lm = low_mask(L);
+    std::map<std::tuple<int, int, uint64_t>, int> where;
+    for (size_t i = 0; i < C.elems.size(); ++i) {
+        const Elem& e = C.elems[i];
+        if (e.mask != 0 && e.mask != lm) return;
+        where[std::make_tuple(e.refl, e.shift, e.mask)] = (int)i;
+    }
+    int a = L;
+    for (const Elem& e : C.elems)
+        if (!e.refl && !e.mask && e.shift > 0) a = std::min(a, e.shift);
+    if (L % a) return;
+    const int nt = L / a;
+    const int has_refl = where.count(std::make_tuple(1, 0, (uint64_t)0)) ? 1 : 0;
+    const int has_flip = where.count(std::make_tuple(0, 0, lm)) ? 1 : 0;
+    if ((size_t)nt * (1 + has_refl) * (1 + has_flip) != C.elems.size()) return;
+    // map fast codes to generic elements (the group order of fill_desc)
+    std::vector<int> gidx(C.elems.size());
+    {
+        std::vector<int> order(C.elems.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            if (C.elems[x].refl != C.elems[y].refl) return C.elems[x].refl < C.elems[y].refl;
+            return C.elems[x].shift < C.elems[y].shift;
+        });
+        for (size_t k = 0; k < order.size(); ++k) gidx[order[k]] = (int)k;
+    }
+    b.fast_chi.assign(4 * nt, cx(0, 0));
+    b.fast_to_elem.assign(4 * nt, 0);
+    for (int r = 0; r <= has_refl; ++r)
+        for (int f = 0; f <= has_flip; ++f)
+            for (int j = 0; j < nt; ++j) {
+                auto it = where.find(std::make_tuple(r, (a * j) % L, f ? lm : (uint64_t)0));
+                if (it == where.end()) return;
+                int code = (r * 2 + f) * nt + j;
+                b.fast_chi[code] = char_value(C.elems[it->second], kmom, nT);
+                b.fast_to_elem[code] = gidx[it->second];
+            }
+    b.fast.enabled = 1;
+    b.fast.L = L;
+    b.fast.a = a;
+    b.fast.nT = nt;
+    b.fast.has_refl = has_refl;
+    b.fast.has_flip = has_flip;
+    b.fast.lmask = lm;
+    uint64_t allowed = 0;
+    for (int p = 0; p < L; ++p)
+        if (((L - 1 - p) % a) == 0) allowed |= 1ull << p;
+    b.fast.allowed = allowed;
+}
+
+}  // namespace
+
 // ----------------------------------------------------------- basis_build
 void basis_build(Basis& b) {
     const qs_basis_spec& sp = b.spec;
@@ -497,6 +561,11 @@ void basis_build(Basis& b) {
     QS_CUDA(cudaMemcpy(b.d_binom.p, binom.data(), binom.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
     b.d_group.alloc(sizeof(GroupDesc));
     QS_CUDA(cudaMemcpy(b.d_group.p, &b.group, sizeof(GroupDesc), cudaMemcpyHostToDevice));
+    detect_fast_group(b, C, kmom, nT);
+    if (b.fast.enabled) {
+        b.d_fast_chi.alloc(b.fast_chi.size() * sizeof(cplx));
+        QS_CUDA(cudaMemcpy(b.d_fast_chi.p, b.fast_chi.data(), b.fast_chi.size() * sizeof(cplx), cudaMemcpyHostToDevice));
+    }
 
     if (!b.symmetric) {
         b.n = b.n_parent;

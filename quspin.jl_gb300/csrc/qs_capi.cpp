@@ -192,7 +192,8 @@ int qs_op_matvec(qs_op* op, int32_t flags, const double* alpha, const void* x, i
         const bool ycx = is_complex(y_dtype);
         const size_t yb = dt_bytes(y_dtype), xb = dt_bytes(x_dtype);
         qs::MatvecCall c;
-        c.flags = flags;
+        c.flags = flags & (QS_TRANSPOSE | QS_CONJUGATE);
+        c.df = (flags & QS_DOUBLE_FLOAT) != 0;
         c.alpha = qs::cx(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
         c.beta = qs::cx(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
         c.single = single;

@@ -11,6 +11,7 @@
 
 #include "../../include/qsgpu.h"
 #include "qs_common.h"
+#include "qs_orbit.cuh"
 
 namespace qs {
 
@@ -85,6 +86,10 @@ struct Basis {
     int64_t nsplit = 0, split_stride = 1;
     DevBuf d_binom;                  // uint64 C(b, p) table for combinadic ranks
     DevBuf d_index;                  // int32 column of each parent-sector rank (-1: none)
+    FastGroup fast{};                // translation x parity x flip structure, when present
+    std::vector<cplx> fast_chi;      // character per fast element code
+    std::vector<int> fast_to_elem;   // generic element index per fast element code
+    DevBuf d_fast_chi;               // complex double, 4 * nT
     bool has_index = false;          // direct rank -> column table built
     std::vector<uint64_t> h_refrep;  // reference (argmax) representatives
     bool refrep_ready = false;
@@ -140,6 +145,7 @@ struct MatvecCall {
     void* y = nullptr;
     bool x_complex = false, y_complex = false;
     bool single = false;            // FP32 vectors and accumulation
+    bool df = false;                // FP64 vectors, double-float products (assembled form)
 };
 void op_prepare_device(Op& op);
 // qs_assembled.cu

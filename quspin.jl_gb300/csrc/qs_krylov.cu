@@ -37,7 +37,9 @@ struct Ctx {
     cudaStream_t s;
     Blas blas;
     int64_t matvecs = 0;
-    Ctx(Op& o, VKind k) : op(o), n(o.basis->n), vk(k), s(o.stream), blas(k, o.basis->n, o.stream) {}
+    bool df = false;   // double-float products of an assembled operator
+    Ctx(Op& o, VKind k, bool df_ = false)
+        : op(o), n(o.basis->n), vk(k), s(o.stream), blas(k, o.basis->n, o.stream), df(df_) {}
     void* col(DevBuf& V, int j) const { return (char*)V.p + (size_t)j * n * vk_bytes(vk); }
     void matvec(const void* x, void* y) {
         MatvecCall c;
@@ -45,6 +47,7 @@ struct Ctx {
         c.y = y;
         c.x_complex = c.y_complex = vk_complex(vk);
         c.single = vk_single(vk);
+        c.df = df && !c.single;
         op_matvec_device(op, c, s);
         ++matvecs;
     }
@@ -294,7 +297,7 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
     int maxiter = o.maxiter > 0 ? o.maxiter : 300;
     const bool single = o.precision == 1;
     const VKind vk = single ? (cpx ? VKind::C64 : VKind::F32) : k64;
-    Ctx c(op, vk);
+    Ctx c(op, vk, o.precision == 2);
     DevBuf v0((size_t)n * vk_bytes(vk));
     const bool dev = o.mem == QS_MEM_DEVICE;
     if (o.v0) {

@@ -50,6 +50,8 @@ struct MvArgs {
     const TermProg* progs;
     int nprog;
     const int32_t* index;    // direct rank -> column table (mode 3)
+    FastGroup fast;          // zero-run orbit search when enabled
+    const double* fast_chi;  // complex character per fast element code
     const void* diag;        // complex, precision of the call
     int conj_amp, conj_chi;
     double ar, ai, br, bi;
@@ -193,7 +195,17 @@ __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
             if (kSym) {
                 U m;
                 int bi, st;
-                orbit_min<U>(g, t, m, bi, st);
+                const double* chr = chi_re;
+                const double* chi = chi_im;
+                int cstride = 1;
+                if (a.fast.enabled) {
+                    orbit_min_fast<U>(a.fast, t, m, bi, st);
+                    chr = a.fast_chi;
+                    chi = a.fast_chi + 1;
+                    cstride = 2;
+                } else {
+                    orbit_min<U>(g, t, m, bi, st);
+                }
                 if (kMode == 3) {
                     int64_t rk;
                     if (a.nup < 0) rk = (int64_t)m;
@@ -206,13 +218,13 @@ __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
                 if (idx < 0) continue;
                 const T f = (T)sqrt_stab[st] * inv_sr;
                 if (kCM) {
-                    T cr = (T)__ldg(chi_re + bi), ci = (T)__ldg(chi_im + bi);
+                    T cr = (T)__ldg(chr + bi * cstride), ci = (T)__ldg(chi + bi * cstride);
                     if (a.conj_chi) ci = -ci;
                     T nr = wr * cr - wi * ci, ni = wr * ci + wi * cr;
                     wr = nr * f;
                     wi = ni * f;
                 } else {
-                    wr *= (T)__ldg(chi_re + bi) * f;
+                    wr *= (T)__ldg(chr + bi * cstride) * f;
                 }
             } else if (kMode == 1) {
                 if (__popcll((unsigned long long)t) != a.nup) continue;
@@ -400,6 +412,8 @@ MvArgs base_args(const Op& op) {
     a.nup = b.nup;
     a.pauli = b.spec.pauli;
     a.index = b.has_index ? b.d_index.as<int32_t>() : nullptr;
+    a.fast = b.fast;
+    a.fast_chi = b.fast.enabled ? b.d_fast_chi.as<double>() : nullptr;
     return a;
 }
 

@@ -41,7 +41,7 @@ class EigshInfo(ctypes.Structure):
 QS_F64, QS_C128, QS_F32, QS_C64 = 0, 1, 2, 3
 QS_MEM_HOST, QS_MEM_DEVICE = 0, 1
 QS_CHECK_SYMM, QS_CHECK_HERM, QS_CHECK_PCON, QS_DIAG_COMPLEX = 1, 2, 4, 8
-QS_TRANSPOSE, QS_CONJUGATE = 1, 2
+QS_TRANSPOSE, QS_CONJUGATE, QS_DOUBLE_FLOAT = 1, 2, 4
 
 # every symbol declared in include/qsgpu.h
 EXPORTS = (

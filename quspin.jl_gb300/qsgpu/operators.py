@@ -141,7 +141,10 @@ class QuantumLinearOperator:
             raise DimensionMismatch("operator and value dimensions do not match")
         if x.ndim != out.ndim or (x.ndim == 2 and x.shape[1] != out.shape[1]):
             raise DimensionMismatch("output has the wrong dimensions")
+        if precision not in ("fp64", "fp32", "fp64df"):
+            raise ArgumentError("precision must be fp64, fp32 or fp64df")
         single = precision == "fp32"
+        flags = self._flags | (_lib.QS_DOUBLE_FLOAT if precision == "fp64df" else 0)
         nrhs = 1 if x.ndim == 1 else x.shape[1]
         ycx = np.iscomplexobj(out)
         if (np.iscomplexobj(x) or self.dtype == np.complex128 or complex(alpha).imag or complex(beta).imag) and not ycx:
@@ -159,7 +162,7 @@ class QuantumLinearOperator:
         code = {np.float64: 0, np.complex128: 1, np.float32: 2, np.complex64: 3}
         a = np.array([complex(alpha).real, complex(alpha).imag])
         b = np.array([complex(beta).real, complex(beta).imag])
-        _lib.check(_lib.load().qs_op_matvec(self._h, self._flags, _lib.ptr(a), _lib.ptr(xs), code[xdt], _lib.ptr(b),
+        _lib.check(_lib.load().qs_op_matvec(self._h, flags, _lib.ptr(a), _lib.ptr(xs), code[xdt], _lib.ptr(b),
                                             _lib.ptr(ys), code[ydt], nrhs, _lib.QS_MEM_HOST))
         if ys is not out:
             out[...] = ys
@@ -243,8 +246,10 @@ def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, nc
         vv = np.ascontiguousarray(v0, dtype=op.dtype)
         if vv.shape != (n,):
             raise DimensionMismatch("v0 must have length Ns")
+    if precision not in ("fp64", "fp32", "fp64df"):
+        raise ArgumentError("precision must be fp64, fp32 or fp64df")
     opts = _lib.EigshOpts(k, 0 if w == "SA" else 1, float(tol), int(ncv or 0), int(maxiter or 0),
-                          1 if precision == "fp32" else 0, int(bool(return_eigenvectors)),
+                          {"fp64": 0, "fp32": 1, "fp64df": 2}[precision], int(bool(return_eigenvectors)),
                           _lib.ptr(vv) if vv is not None else None, _lib.QS_MEM_HOST)
     vals = np.zeros(k)
     vecs = np.zeros((n, k), dtype=op.dtype, order="F") if return_eigenvectors else None

@@ -148,6 +148,10 @@ def test_eigsh_matches_dense(qs, ora, sym, model, L, nup, pauli):
     # single-precision Lanczos with FP64 polish reaches the same eigenvalue
     v32 = qs.eigsh(op, k=1, which="SA", tol=1e-10, precision="fp32", return_eigenvectors=False)
     assert abs(v32[0] - w[0]) <= 1e-10 * abs(w[0])
+    H = qs.Hamiltonian(b, models.to_terms(qs, sp))
+    for prec in ("fp64", "fp32", "fp64df"):
+        vh = qs.eigsh(H, k=2, which="SA", tol=1e-12, precision=prec, return_eigenvectors=False)
+        assert np.allclose(vh, w[:2], rtol=1e-10, atol=1e-10 * np.abs(w).max()), prec
 
 
 def test_evolve_and_expm_match_oracle(qs, ora, kats):
@@ -229,6 +233,11 @@ def test_assembled_matches_matrix_free(qs, ora, L, nup, pauli, sym, model):
     assert np.max(np.abs(H.dot(x) - want)) <= 1e-13 * scale
     y32 = H.dot(x, precision="fp32")
     assert np.max(np.abs(y32 - want)) <= 2e-5 * scale
+    # double-float products: FP64-class accuracy on the FP32 pipe
+    ydf = H.dot(x, precision="fp64df")
+    assert np.max(np.abs(ydf - want)) <= 1e-13 * scale
+    ydf_h = H.H.dot(x, precision="fp64df")
+    assert np.max(np.abs(ydf_h - op.H.dot(x))) <= 1e-13 * scale
     if H.dtype == np.float64:
         xr = models.seeded(b.Ns)
         assert np.max(np.abs(H.dot(xr) - op.dot(xr))) <= 1e-13 * scale
