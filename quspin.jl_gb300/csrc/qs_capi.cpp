@@ -237,6 +237,14 @@ int qs_op_matvec(qs_op* op, int32_t flags, const double* alpha, const void* x, i
     });
 }
 
+int qs_op_matvec_noalloc(qs_op* op, int32_t flags, const double* alpha, const void* x, int32_t x_dtype,
+                         const double* beta, void* y, int32_t y_dtype, int64_t nrhs) {
+    return guard([&] {
+        qs::op_matvec_noalloc(*op->op, flags, qs::cx(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0), x, x_dtype,
+                              qs::cx(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0), y, y_dtype, nrhs);
+    });
+}
+
 int qs_eigsh(qs_op* op, const qs_eigsh_opts* opts, double* values, void* vectors, qs_eigsh_info* info) {
     return guard([&] { qs::eigsh(*op->op, *opts, values, vectors, info); });
 }

@@ -148,6 +148,10 @@ struct MatvecCall {
     bool df = false;                // FP64 vectors, double-float products (assembled form)
 };
 void op_prepare_device(Op& op);
+// qs_noalloc.cu
+size_t noalloc_vector_bytes();
+void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype, cplx beta, void* y, int y_dtype,
+                       int64_t nrhs);
 // qs_assembled.cu
 void op_assemble(Op& op);
 void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s);

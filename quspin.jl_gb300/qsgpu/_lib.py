@@ -49,7 +49,7 @@ EXPORTS = (
     "qs_basis_states", "qs_basis_orbit_minima", "qs_basis_state_index", "qs_basis_representative",
     "qs_op_create", "qs_op_destroy", "qs_op_dtype", "qs_op_hermitian", "qs_op_set_diagonal", "qs_op_matvec",
     "qs_eigsh", "qs_expm_multiply", "qs_evolve", "qs_last_error", "qs_version", "qs_op_set_stream",
-    "qs_launch_count", "qs_op_assemble", "qs_op_nnz",
+    "qs_launch_count", "qs_op_assemble", "qs_op_nnz", "qs_op_matvec_noalloc",
 )
 
 _lib = None
@@ -85,6 +85,7 @@ def load():
     L.qs_expm_multiply.argtypes = [P, P, P, P, f64, i32, i32]
     L.qs_evolve.argtypes = [P, P, f64, P, i32, i32, f64, i32, i32, P]
     L.qs_op_set_stream.argtypes = [P, P]
+    L.qs_op_matvec_noalloc.argtypes = [P, i32, P, P, i32, P, P, i32, i64]
     L.qs_op_assemble.argtypes = [P]
     L.qs_op_nnz.argtypes = [P]
     L.qs_op_nnz.restype = i64

@@ -22,6 +22,7 @@ SOURCES = [
     "qs_blas.cu",
     "qs_krylov.cu",
     "qs_assembled.cu",
+    "qs_noalloc.cu",
     "qs_dense.cpp",
     "qs_op.cpp",
     "qs_capi.cpp",
