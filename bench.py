@@ -77,10 +77,11 @@ def alive_transitions(states, L, J2):
 
 def asm_bytes_per_row(nbar, vec_bytes=8):
     """Compulsory HBM bytes per row of one product with the assembled operator:
-    4 bytes per stored transition (packed column + value code), the row pointer
-    (8), the stabiliser code (2), the diagonal, x[r] and the y[r] write.  The x
-    gathers of the transitions hit L2 when x fits in it and are not counted."""
-    return 4 * nbar + 8 + 2 + 3 * vec_bytes
+    4 bytes per stored transition (packed column + value code), a 2-byte row
+    length, the 2-byte stabiliser code, the diagonal, x[r] and the y[r] write.
+    The x gathers of the transitions hit L2 when x fits in it and are not
+    counted."""
+    return 4 * nbar + 2 + 2 + 3 * vec_bytes
 
 
 class ClockSampler:
@@ -210,6 +211,123 @@ def run_reference(args, wl, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def xxz_spec(L, J=1.0, delta=0.5):
+    bonds = [(i, i % L + 1) for i in range(1, L + 1)]
+    return [("+-", [(J / 2, a, b) for a, b in bonds]), ("-+", [(J / 2, a, b) for a, b in bonds]),
+            ("zz", [(J * delta, a, b) for a, b in bonds])]
+
+
+def tfim_spec(L, J=1.0, h=0.7):
+    bonds = [(i, i % L + 1) for i in range(1, L + 1)]
+    return [("zz", [(J, a, b) for a, b in bonds]), ("x", [(h, i) for i in range(1, L + 1)])]
+
+
+def section_c1(qs, torch, timed_events):
+    """Periodic XXZ L=16, nup=8 (12,870 states), no spatial symmetry, FP64:
+    one QuantumLinearOperator matvec and eigsh k=4 :SA (tol 1e-10, v0 = ones),
+    against the oracle's restatement of the reference algorithm (serial scatter
+    with per-state lookups, 1 thread) and SciPy's ARPACK over it."""
+    import oracle
+    L = 16
+    spec = xxz_spec(L)
+    b = qs.SpinBasis1D(L, nup=8, pauli=False)
+    op = qs.QuantumLinearOperator(b, [qs.OperatorTerm(o, c) for o, c in spec])
+    n = b.Ns
+    x = np.random.default_rng(20261203).standard_normal(n)
+    us = timed_events(op, x, 200) * 1e3
+    v0 = np.ones(n) / np.sqrt(n)
+    t = time.perf_counter()
+    vals = qs.eigsh(op, k=4, which="SA", tol=1e-10, v0=v0, return_eigenvectors=False)
+    t_gpu = time.perf_counter() - t
+    ref = oracle.RefBasis(L, nup=8, pauli=False)
+    ct = oracle.consolidate_terms(spec)
+    d = ref.extract_diagonal(ct)
+    pk = oracle.pack_terms(ct)
+    t = time.perf_counter()
+    reps = 20
+    for _ in range(reps):
+        ref.qlo_matvec(ct, x, total_diag=d, packed=pk)
+    cpu_mv = (time.perf_counter() - t) / reps
+    t = time.perf_counter()
+    cvals, _ = oracle.eigsh_arpack(lambda v: ref.qlo_matvec(ct, v, total_diag=d, packed=pk).real, n, 4,
+                                   np.float64, v0=v0, tol=1e-10)
+    t_cpu = time.perf_counter() - t
+    return {"workload": "periodic XXZ L=16, nup=8, J=1, Delta=0.5, pauli=false, N=12870",
+            "matvec_us_gpu": us, "matvec_us_cpu_reference_algorithm": cpu_mv * 1e6,
+            "eigsh_k4_s_gpu": t_gpu, "eigsh_k4_s_cpu_arpack_reference_algorithm": t_cpu,
+            "eigenvalues": [float(v) for v in vals],
+            "max_abs_diff_vs_cpu": float(np.max(np.abs(np.sort(vals) - np.sort(cvals)))),
+            "cpu_cores": 1}
+
+
+def section_c3(qs, torch):
+    """TFIM L=30 periodic, J=1, h=0.7 (pauli), k=0, p=+1, no U(1) (N=17,920,860):
+    evolve ComplexF64 from the homogeneous product state at the first 5 of the
+    50 times range(0.1, 5.0) (krylov_dim 30, tol 1e-9), FP64 and FP32."""
+    L = 30
+    b = qs.SpinBasis1D(L, pauli=True, kblock=0, pblock=1)
+    t = time.perf_counter()
+    H = qs.Hamiltonian(b, [qs.OperatorTerm(o, c) for o, c in tfim_spec(L)])
+    t_asm = time.perf_counter() - t
+    rng = np.random.default_rng(20261203)
+    th, ph = rng.uniform(0, np.pi), rng.uniform(0, 2 * np.pi)
+    reps = b.orbit_minima()
+    pop = np.zeros(reps.size, dtype=np.int64)
+    for i in range(L):
+        pop += ((reps >> np.uint64(i)) & np.uint64(1)).astype(np.int64)
+    orb = b.group_order / b.stabilizers().astype(np.float64)
+    up, dn = np.exp(1j * ph) * np.sin(th), np.cos(th)
+    v0 = (up ** pop) * (dn ** (L - pop)) * np.sqrt(orb)
+    v0 /= np.linalg.norm(v0)
+    times = np.linspace(0.1, 5.0, 50)[:5]
+    out = {"workload": "TFIM L=30, J=1, h=0.7, k=0, p=+1, N=%d, nnz=%d" % (b.Ns, H.nnz), "times": times.tolist(),
+           "assemble_s": t_asm}
+    res = {}
+    for prec in ("fp64", "fp32"):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        st = qs.evolve(H, v0, 0.0, times, tol=1e-9, krylov_dim=30, precision=prec)
+        out[f"evolve_5_times_s_{prec}"] = time.perf_counter() - t
+        res[prec] = st
+        out[f"norm_drift_{prec}"] = float(np.max(np.abs(np.linalg.norm(st, axis=0) - 1)))
+    out["fp32_vs_fp64_state_err"] = float(np.max(np.linalg.norm(res["fp32"] - res["fp64"], axis=0)))
+    return out
+
+
+def section_c4(qs, torch):
+    """All momentum sectors (p=+-1 at k=0, 13) of the J1-J2 chain L=26, nup=13,
+    J2=0.3: ground state of every sector, batched (one launch per Lanczos step
+    for all 28 sectors) against sector-by-sector eigsh."""
+    L = 26
+    spec = j1j2_spec(L, 1.0, 0.3)
+    terms = [qs.OperatorTerm(o, c) for o, c in spec]
+    syms = []
+    for k in range(L):
+        if k in (0, L // 2):
+            syms += [dict(kblock=k, pblock=1), dict(kblock=k, pblock=-1)]
+        else:
+            syms.append(dict(kblock=k))
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    ops = [qs.Hamiltonian(qs.SpinBasis1D(L, nup=13, pauli=False, **sy), terms) for sy in syms]
+    t_build = time.perf_counter() - t
+    sizes = [o.Ns for o in ops]
+    qs.eigsh_batch(ops[:2], k=1, tol=1e-10)   # warm-up
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    vb = qs.eigsh_batch(ops, k=1, tol=1e-10)
+    t_batch = time.perf_counter() - t
+    t = time.perf_counter()
+    vs = [qs.eigsh(o, k=1, which="SA", tol=1e-10, return_eigenvectors=False)[0] for o in ops]
+    t_seq = time.perf_counter() - t
+    return {"workload": "J1-J2 L=26, nup=13, J2=0.3, %d sectors, %d states" % (len(ops), sum(sizes)),
+            "sector_sizes": [min(sizes), max(sizes)], "build_s": t_build,
+            "batched_solves_per_s": len(ops) / t_batch, "sequential_solves_per_s": len(ops) / t_seq,
+            "batched_speedup": t_seq / t_batch,
+            "max_abs_diff_batched_vs_sequential": float(np.max(np.abs(vb[:, 0] - np.array(vs)))),
+            "ground_energy": float(np.min(vb[:, 0]))}
+
+
 def run_ours(args, wl, world, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -268,9 +386,11 @@ def run_ours(args, wl, world, rank, local):
         launches = lib.qs_launch_count() - l0
         return [s.elapsed_time(e) for s, e in ev], launches
 
-    # algorithmic (compulsory) HBM bytes of one product
-    asm_bytes64 = 4 * nnz + 8 * (n + 1) + 2 * n + 8 * n + 8 * n + 8 * n
-    asm_bytes32 = 4 * nnz + 8 * (n + 1) + 2 * n + 4 * n + 4 * n + 4 * n
+    # algorithmic (compulsory) HBM bytes of one product: 4 per stored
+    # transition, a 2-byte row length, the 2-byte stabiliser code, the
+    # diagonal, x[r] and y[r]
+    asm_bytes64 = 4 * nnz + n * (2 + 2 + 3 * 8)
+    asm_bytes32 = 4 * nnz + n * (2 + 2 + 3 * 4)
     mf_bytes64 = n * (4 + 2 + 8 + 8 + 8)
     clocks = ClockSampler()
     clocks.start()
@@ -328,6 +448,29 @@ def run_ours(args, wl, world, rank, local):
         except Exception as exc:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {exc}"}
+    sections = {}
+    if rank == 0 and not args.no_sections:
+        def timed_events(o, xh_np, reps):
+            xt = torch.from_numpy(np.ascontiguousarray(xh_np)).to(dev)
+            yt = torch.empty_like(xt)
+            _lib.check(lib.qs_op_set_stream(o._h, ctypes.c_void_p(stream.cuda_stream)))
+            for _ in range(5):
+                mv(o, xt, yt, _lib.QS_F64)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                mv(o, xt, yt, _lib.QS_F64)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+        for name, fn in (("c1_xxz_L16", lambda: section_c1(qs, torch, timed_events)),
+                         ("c4_batched_sectors_L26", lambda: section_c4(qs, torch)),
+                         ("c3_tfim_L30_evolve", lambda: section_c3(qs, torch))):
+            try:
+                sections[name] = fn()
+            except Exception as exc:  # a failing side workload must not hide the headline
+                sections[name] = {"error": f"{type(exc).__name__}: {exc}"}
     if rank != 0:
         return
     line = {
@@ -340,7 +483,7 @@ def run_ours(args, wl, world, rank, local):
                    "basis_build_s": round(t_basis, 3), "assemble_s": round(t_asm, 3),
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "spmv_kernel (assembled H.v)"},
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "sell_kernel (assembled H.v, sliced ELL)"},
         "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": int(launches),
         "clocks": clk,
@@ -364,6 +507,7 @@ def run_ours(args, wl, world, rank, local):
                     "tol": 1e-10},
         "latency_ms": {"p50": float(np.percentile(ms64, 50)), "p99": float(np.percentile(ms64, 99))},
         "cpu_baseline": cpu,
+        "workloads": sections,
     }
     print(json.dumps(line), flush=True)
 
@@ -376,6 +520,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="j1j2_L32_k0_p1_z1", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sections", action="store_true", help="skip the side workloads (XXZ L=16, batched sectors, TFIM evolve)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

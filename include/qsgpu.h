@@ -90,6 +90,11 @@ QS_API int qs_basis_states(const qs_basis *basis, uint64_t *out, int64_t n);
 /* Ascending orbit minima of the columns (the device's canonical key). */
 QS_API int qs_basis_orbit_minima(const qs_basis *basis, uint64_t *out, int64_t n);
 
+/* Order of the stabiliser of every column's orbit minimum (1 without
+ * symmetry); the orbit holds group_order / stab states, and the reference's
+ * normalization(basis, s) is that count up to rounding. */
+QS_API int qs_basis_stabilizers(const qs_basis *basis, uint16_t *out, int64_t n);
+
 /* state_index(basis, s) (src/basis.jl:1016-1022) for n states at once;
  * out[i] = column or -1 when the state is not represented (the shim raises
  * ArgumentError "state ... is not represented by this basis"). */
@@ -215,6 +220,18 @@ typedef struct {
  * ARPACK implicitly restarted Lanczos; convergence is ARPACK's test
  * ||r_i|| <= tol * max(eps^(2/3), |theta_i|). */
 QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *vectors, qs_eigsh_info *info);
+
+/* eigsh on nops Hermitian operators at once (e.g. every momentum / parity
+ * sector of one model): the Lanczos iterations of all operators run in
+ * lockstep, each step being one multi-sector launch per kernel over the
+ * assembled operators (assembled here if needed); operators that converge
+ * drop out.  Replaces the per-sector loop of block_diag_hamiltonian /
+ * BlockOps (tools.jl:2213-2420) followed by eigsh on each block.  values:
+ * nops * k, ascending per operator; vectors: NULL or nops pointers (each NULL
+ * or Ns_i x k in the operator's dtype, host); infos: NULL or nops entries.
+ * opts->v0 and opts->precision are ignored (seeded start vectors, FP64). */
+QS_API int qs_eigsh_batch(qs_op *const *ops, int32_t nops, const qs_eigsh_opts *opts, double *values, void **vectors,
+                          qs_eigsh_info *infos);
 
 /* apply(ExpmMultiplyParallel(A, a), v; tol) (tools.jl:1662-1708) and the
  * Krylov exponential action _krylov_expmv_vector (src/operators.jl:1758-1803):

@@ -227,16 +227,21 @@ class RefBasis:
         return out
 
     def qlo_matvec(self, terms, x, alpha=1.0, beta=0.0, y=None, diag=None, extract=True,
-                   transposed=False, conjugated=False):
-        """mul!(y, QuantumLinearOperator(basis, terms; diagonal=diag), x, alpha, beta)."""
-        pk = pack_terms(terms)
+                   transposed=False, conjugated=False, total_diag=None, packed=None):
+        """mul!(y, QuantumLinearOperator(basis, terms; diagonal=diag), x, alpha, beta).
+        total_diag: the operator's stored diagonal (user + extracted), as the
+        reference keeps it from construction; skips re-extracting it."""
+        pk = packed or pack_terms(terms)
         x = np.ascontiguousarray(x, dtype=np.complex128)
         y = np.zeros(self.Ns, dtype=np.complex128) if y is None else np.array(y, dtype=np.complex128)
-        d = np.zeros(self.Ns, dtype=np.complex128)
-        if extract:
-            d += self.extract_diagonal(terms)
-        if diag is not None:
-            d += np.asarray(diag, dtype=np.complex128)
+        if total_diag is not None:
+            d = np.ascontiguousarray(total_diag, dtype=np.complex128)
+        else:
+            d = np.zeros(self.Ns, dtype=np.complex128)
+            if extract:
+                d += self.extract_diagonal(terms)
+            if diag is not None:
+                d += np.asarray(diag, dtype=np.complex128)
         a = np.array([complex(alpha).real, complex(alpha).imag])
         b = np.array([complex(beta).real, complex(beta).imag])
         rc = lib().ora_qlo_matvec(self._h, *pk.args(), int(extract), _ptr(d), int(transposed), int(conjugated),

@@ -407,6 +407,225 @@ __global__ void __launch_bounds__(kThreads) spmv_df_kernel(SpmvDFArgs da) {
     }
 }
 
+// ----------------------------------------------------------- sliced ELL
+constexpr int kSlice = 32;
+
+__global__ void sell_fill_kernel(const int64_t* rowptr, const uint32_t* words, const int32_t* cols,
+                                 const uint16_t* codes, int packed, const int32_t* perm, const int64_t* sptr,
+                                 int64_t npos, uint32_t* swords, int32_t* scols, uint16_t* scodes) {
+    for (int64_t pos = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pos < npos; pos += (int64_t)gridDim.x * blockDim.x) {
+        const int r = perm[pos];
+        if (r < 0) continue;
+        const int64_t s = pos / kSlice, l = pos % kSlice;
+        const int64_t j0 = rowptr[r], j1 = rowptr[r + 1];
+        const int64_t base = sptr[s] + l;
+        for (int64_t j = j0; j < j1; ++j) {
+            const int64_t o = base + (j - j0) * kSlice;
+            if (packed) swords[o] = words[j];
+            else {
+                scols[o] = cols[j];
+                scodes[o] = codes[j];
+            }
+        }
+    }
+}
+
+struct SellArgs {
+    const int64_t* sptr;
+    const int32_t* perm;
+    const uint16_t* len;
+    const uint32_t* words;
+    const int32_t* cols;
+    const uint16_t* codes;
+    int packed;
+    uint32_t code_mask;
+    int code_bits;
+    const void* table;
+    int ncodes;
+    const uint16_t* stab;
+    const void* diag;
+    const void* diag_re;     // real diagonal (real operators)
+    int64_t nslices, n;
+    double ar, ai, br, bi;
+    int beta_zero;
+    int conj;
+    const void* x;
+    void* y;
+};
+
+template <typename T>
+__device__ __forceinline__ void sell_word(const SellArgs& a, int64_t o, uint32_t& col, uint32_t& code) {
+    if (a.packed) {
+        const uint32_t w = __ldg(a.words + o);
+        col = w >> a.code_bits;
+        code = w & a.code_mask;
+    } else {
+        col = (uint32_t)__ldg(a.cols + o);
+        code = __ldg(a.codes + o);
+    }
+}
+
+// One thread per row: y[r] = beta y[r] + alpha (d[r] x[r] + rs(stab[r]) sum_j T[code_j] x[col_j])
+template <bool kCM, bool kCV, typename T>
+__global__ void __launch_bounds__(kThreads, 8) sell_kernel(SellArgs a) {
+    using T2 = typename V2<T>::t;
+    __shared__ T2 tab[1024];
+    __shared__ T rsq[kMaxGroup + 1];
+    const bool smem_tab = a.ncodes <= 1024;
+    if (smem_tab)
+        for (int i = threadIdx.x; i < a.ncodes; i += blockDim.x) {
+            T2 v = ((const T2*)a.table)[i];
+            if (a.conj) v.y = -v.y;
+            tab[i] = v;
+        }
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) rsq[i] = i ? (T)(1.0 / sqrt((double)i)) : (T)0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp0; s < a.nslices; s += nwarps) {
+        const int64_t r = s * kSlice + lane;
+        if (r >= a.n) continue;
+        const int len = a.len[r];
+        const int64_t base = a.sptr[s] + lane;
+        T acc_r = 0, acc_i = 0;
+#pragma unroll 4
+        for (int j = 0; j < len; ++j) {
+            uint32_t col, code;
+            sell_word<T>(a, base + (int64_t)j * kSlice, col, code);
+            T2 v;
+            if (smem_tab) v = tab[code];
+            else {
+                v = ((const T2*)a.table)[code];
+                if (a.conj) v.y = -v.y;
+            }
+            if (kCV) {
+                const T2 xv = __ldg((const T2*)a.x + col);
+                if (kCM) {
+                    acc_r += v.x * xv.x - v.y * xv.y;
+                    acc_i += v.x * xv.y + v.y * xv.x;
+                } else {
+                    acc_r += v.x * xv.x;
+                    acc_i += v.x * xv.y;
+                }
+            } else {
+                acc_r += v.x * __ldg((const T*)a.x + col);
+            }
+        }
+        const T sc = a.stab ? rsq[a.stab[r]] : (T)1;
+        acc_r *= sc;
+        acc_i *= sc;
+        T dr, di = 0;
+        if (kCM) {
+            const T2 d = ((const T2*)a.diag)[r];
+            dr = d.x;
+            di = a.conj ? -d.y : d.y;
+        } else {
+            dr = ((const T*)a.diag_re)[r];
+        }
+        if (kCV) {
+            const T2 xv = ((const T2*)a.x)[r];
+            acc_r += dr * xv.x - di * xv.y;
+            acc_i += dr * xv.y + di * xv.x;
+            T2* y = (T2*)a.y;
+            T yr = 0, yi = 0;
+            if (!a.beta_zero) {
+                const T2 yo = y[r];
+                yr = (T)a.br * yo.x - (T)a.bi * yo.y;
+                yi = (T)a.br * yo.y + (T)a.bi * yo.x;
+            }
+            T2 o;
+            o.x = yr + (T)a.ar * acc_r - (T)a.ai * acc_i;
+            o.y = yi + (T)a.ar * acc_i + (T)a.ai * acc_r;
+            y[r] = o;
+        } else {
+            acc_r += dr * ((const T*)a.x)[r];
+            T* y = (T*)a.y;
+            const T yr = a.beta_zero ? (T)0 : (T)a.br * y[r];
+            y[r] = yr + (T)a.ar * acc_r;
+        }
+    }
+}
+
+// Double-float products, one thread per row; FP64 only in the per-row tail,
+// where all 32 lanes of a warp work on 32 rows.
+template <bool kCM, bool kCV>
+__global__ void __launch_bounds__(kThreads, 8) sell_df_kernel(SellArgs a, const float4* __restrict__ tab_df,
+                                                           const void* __restrict__ xs) {
+    __shared__ float4 tab[1024];
+    __shared__ double rsq[kMaxGroup + 1];
+    const bool smem_tab = a.ncodes <= 1024;
+    if (smem_tab)
+        for (int i = threadIdx.x; i < a.ncodes; i += blockDim.x) {
+            float4 v = tab_df[i];
+            if (a.conj) { v.z = -v.z; v.w = -v.w; }
+            tab[i] = v;
+        }
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) rsq[i] = i ? 1.0 / sqrt((double)i) : 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp0; s < a.nslices; s += nwarps) {
+        const int64_t r = s * kSlice + lane;
+        if (r >= a.n) continue;
+        const int len = a.len[r];
+        const int64_t base = a.sptr[s] + lane;
+        DF ar{0.f, 0.f}, ai{0.f, 0.f};
+#pragma unroll 4
+        for (int j = 0; j < len; ++j) {
+            uint32_t col, code;
+            sell_word<float>(a, base + (int64_t)j * kSlice, col, code);
+            float4 v;
+            if (smem_tab) v = tab[code];
+            else {
+                v = tab_df[code];
+                if (a.conj) { v.z = -v.z; v.w = -v.w; }
+            }
+            if (kCV) {
+                const float4 xv = __ldg((const float4*)xs + col);
+                df_mac(ar, v.x, v.y, xv.x, xv.y);
+                df_mac(ai, v.x, v.y, xv.z, xv.w);
+                if (kCM) {
+                    df_mac(ar, -v.z, -v.w, xv.z, xv.w);
+                    df_mac(ai, v.z, v.w, xv.x, xv.y);
+                }
+            } else {
+                const float2 xv = __ldg((const float2*)xs + col);
+                df_mac(ar, v.x, v.y, xv.x, xv.y);
+            }
+        }
+        const double sc = a.stab ? rsq[a.stab[r]] : 1.0;
+        double acc_r = df_to_double(ar) * sc, acc_i = kCV ? df_to_double(ai) * sc : 0.0;
+        double dr, di = 0;
+        if (kCM) {
+            const double2 d = ((const double2*)a.diag)[r];
+            dr = d.x;
+            di = a.conj ? -d.y : d.y;
+        } else {
+            dr = ((const double*)a.diag_re)[r];
+        }
+        if (kCV) {
+            const double2 xv = ((const double2*)a.x)[r];
+            acc_r += dr * xv.x - di * xv.y;
+            acc_i += dr * xv.y + di * xv.x;
+            double2* y = (double2*)a.y;
+            double yr = 0, yi = 0;
+            if (!a.beta_zero) {
+                const double2 yo = y[r];
+                yr = a.br * yo.x - a.bi * yo.y;
+                yi = a.br * yo.y + a.bi * yo.x;
+            }
+            y[r] = make_double2(yr + a.ar * acc_r - a.ai * acc_i, yi + a.ar * acc_i + a.ai * acc_r);
+        } else {
+            acc_r += dr * ((const double*)a.x)[r];
+            double* y = (double*)a.y;
+            const double yr = a.beta_zero ? 0.0 : a.br * y[r];
+            y[r] = yr + a.ar * acc_r;
+        }
+    }
+}
+
 int grid_rows(int64_t threads_needed) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -417,6 +636,57 @@ int grid_rows(int64_t threads_needed) {
 }
 
 }  // namespace
+
+// Sliced-ELL copy of the CSR words: slices of kSlice consecutive rows, words
+// column-major inside a slice; every row keeps its own length, so the padding
+// of a slice is allocated but never read.
+void build_sell(const Basis& b, Assembled& M, cudaStream_t s) {
+    const int64_t n = b.n;
+    std::vector<int64_t> rp(n + 1);
+    QS_CUDA(cudaMemcpy(rp.data(), M.rowptr.p, (n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    for (int64_t r = 0; r < n; ++r)
+        if (rp[r + 1] - rp[r] > 65535) return;  // keep the CSR path
+    M.nslices = (n + kSlice - 1) / kSlice;
+    const int64_t npos = M.nslices * kSlice;
+    std::vector<int32_t> perm(npos, -1);
+    std::vector<uint16_t> len(npos, 0);
+    // Rows stay in their natural order: each thread loops over its own row
+    // only, so a slice's padding is never read, while the natural order keeps
+    // y, the diagonal and x[r] coalesced and the x gathers of neighbouring
+    // rows close together (sorting by length inside windows measured slower).
+    for (int64_t r = 0; r < n; ++r) {
+        perm[r] = (int32_t)r;
+        len[r] = (uint16_t)(rp[r + 1] - rp[r]);
+    }
+    std::vector<int64_t> sptr(M.nslices + 1, 0);
+    for (int64_t sl = 0; sl < M.nslices; ++sl) {
+        int mx = 0;
+        for (int l = 0; l < kSlice; ++l) mx = std::max<int>(mx, len[sl * kSlice + l]);
+        sptr[sl + 1] = sptr[sl] + (int64_t)mx * kSlice;
+    }
+    const int64_t total = std::max<int64_t>(1, sptr[M.nslices]);
+    M.sell_ptr.alloc((M.nslices + 1) * sizeof(int64_t));
+    M.sell_perm.alloc(npos * sizeof(int32_t));
+    M.sell_len.alloc(npos * sizeof(uint16_t));
+    QS_CUDA(cudaMemcpy(M.sell_ptr.p, sptr.data(), (M.nslices + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    QS_CUDA(cudaMemcpy(M.sell_perm.p, perm.data(), npos * sizeof(int32_t), cudaMemcpyHostToDevice));
+    QS_CUDA(cudaMemcpy(M.sell_len.p, len.data(), npos * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    if (M.packed) {
+        M.sell_words.alloc(total * sizeof(uint32_t));
+    } else {
+        M.sell_cols.alloc(total * sizeof(int32_t));
+        M.sell_codes.alloc(total * sizeof(uint16_t));
+    }
+    sell_fill_kernel<<<grid_rows(npos), kThreads, 0, s>>>(M.rowptr.as<int64_t>(), M.words.as<uint32_t>(),
+                                                         M.cols.as<int32_t>(), M.codes.as<uint16_t>(), M.packed,
+                                                         M.sell_perm.as<int32_t>(), M.sell_ptr.as<int64_t>(), npos,
+                                                         M.sell_words.as<uint32_t>(), M.sell_cols.as<int32_t>(),
+                                                         M.sell_codes.as<uint16_t>());
+    QS_CUDA(cudaGetLastError());
+    QS_CUDA(cudaStreamSynchronize(s));
+    note_launches(1);
+    M.has_sell = true;
+}
 
 void op_assemble(Op& op) {
     Basis& b = *op.basis;
@@ -576,12 +846,74 @@ void op_assemble(Op& op) {
     // lanes per row: the power of two nearest a quarter of the mean row length
     double mean = b.n ? (double)M.nnz / (double)b.n : 0.0;
     M.lanes = mean > 48 ? 16 : (mean > 12 ? 8 : 4);
+    build_sell(b, M, s);
     op.assembled = true;
 }
 
 void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
     const Basis& b = *op.basis;
     const Assembled& M = op.asm_;
+    if (M.has_sell) {
+        SellArgs a{};
+        a.sptr = M.sell_ptr.as<int64_t>();
+        a.perm = M.sell_perm.as<int32_t>();
+        a.len = M.sell_len.as<uint16_t>();
+        a.words = M.sell_words.as<uint32_t>();
+        a.cols = M.sell_cols.as<int32_t>();
+        a.codes = M.sell_codes.as<uint16_t>();
+        a.packed = M.packed;
+        a.code_bits = M.code_bits;
+        a.code_mask = M.code_bits >= 32 ? 0xffffffffu : ((1u << M.code_bits) - 1u);
+        a.ncodes = M.ncodes;
+        a.stab = b.symmetric ? b.d_stab.as<uint16_t>() : nullptr;
+        a.nslices = M.nslices;
+        a.n = b.n;
+        a.ar = c.alpha.re;
+        a.ai = c.alpha.im;
+        a.br = c.beta.re;
+        a.bi = c.beta.im;
+        a.beta_zero = (c.beta.re == 0.0 && c.beta.im == 0.0);
+        const bool T = (c.flags & QS_TRANSPOSE) != 0, C = (c.flags & QS_CONJUGATE) != 0;
+        a.conj = T != C;
+        a.x = c.x;
+        a.y = c.y;
+        const bool cm = op.complex_mat, cv = c.y_complex;
+        const int grid = grid_rows(M.nslices * kSlice);
+        if (c.df && !c.single) {
+            a.table = M.table64.p;
+            a.diag = op.d_diag.p;
+            a.diag_re = op.d_diag_re.p;
+            const int sg = grid_rows(b.n);
+            if (cv) split_kernel<true><<<sg, kThreads, 0, s>>>(c.x, M.xsplit.as<float4>(), nullptr, b.n);
+            else split_kernel<false><<<sg, kThreads, 0, s>>>(c.x, nullptr, M.xsplit.as<float2>(), b.n);
+            QS_CUDA(cudaGetLastError());
+            const float4* td = M.table_df.as<float4>();
+            if (cm) sell_df_kernel<true, true><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);
+            else if (cv) sell_df_kernel<false, true><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);
+            else sell_df_kernel<false, false><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);
+            QS_CUDA(cudaGetLastError());
+            note_launches(2);
+            return;
+        }
+        if (c.single) {
+            a.table = M.table32.p;
+            a.diag = op.d_diag32.p;
+            a.diag_re = op.d_diag32_re.p;
+            if (cm) sell_kernel<true, true, float><<<grid, kThreads, 0, s>>>(a);
+            else if (cv) sell_kernel<false, true, float><<<grid, kThreads, 0, s>>>(a);
+            else sell_kernel<false, false, float><<<grid, kThreads, 0, s>>>(a);
+        } else {
+            a.table = M.table64.p;
+            a.diag = op.d_diag.p;
+            a.diag_re = op.d_diag_re.p;
+            if (cm) sell_kernel<true, true, double><<<grid, kThreads, 0, s>>>(a);
+            else if (cv) sell_kernel<false, true, double><<<grid, kThreads, 0, s>>>(a);
+            else sell_kernel<false, false, double><<<grid, kThreads, 0, s>>>(a);
+        }
+        QS_CUDA(cudaGetLastError());
+        note_launches(1);
+        return;
+    }
     SpmvArgs a{};
     a.rowptr = M.rowptr.as<int64_t>();
     a.words = M.words.as<uint32_t>();

@@ -18,7 +18,17 @@ struct Assembled {
     int ncodes = 0;
     int code_bits = 0;
     bool packed = true;
-    int lanes = 8;     // threads per row in the SpMV
+    int lanes = 8;     // threads per row in the CSR SpMV
+    // sliced-ELL copy for the single-operator product: slices of 32 rows (a
+    // permutation that sorts rows by length inside 4096-row windows), words
+    // column-major inside a slice, one thread per row
+    DevBuf sell_words;  // uint32 packed (or int32 column + uint16 code pairs as uint32/uint16 arrays)
+    DevBuf sell_cols, sell_codes;
+    DevBuf sell_ptr;    // int64 start of each slice
+    DevBuf sell_perm;   // int32 row of each slice position (-1 past the end)
+    DevBuf sell_len;    // uint16 length of each slice position's row
+    int64_t nslices = 0;
+    bool has_sell = false;
 };
 
 }  // namespace qs

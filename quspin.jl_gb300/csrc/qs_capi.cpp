@@ -112,6 +112,18 @@ int qs_basis_orbit_minima(const qs_basis* basis, uint64_t* out, int64_t n) {
     });
 }
 
+int qs_basis_stabilizers(const qs_basis* basis, uint16_t* out, int64_t n) {
+    return guard([&] {
+        const qs::Basis& b = basis->b;
+        if (n != b.n) throw qs::Error(QS_ERR_DIMENSION, "output length must equal Ns");
+        if (!b.symmetric) {
+            for (int64_t i = 0; i < n; ++i) out[i] = 1;
+            return;
+        }
+        QS_CUDA(cudaMemcpy(out, b.d_stab.p, n * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+    });
+}
+
 int qs_basis_states(const qs_basis* basis, uint64_t* out, int64_t n) {
     if (!basis) return QS_ERR_ARGUMENT;
     if (!basis->b.symmetric) return qs_basis_orbit_minima(basis, out, n);
@@ -247,6 +259,15 @@ int qs_op_matvec_noalloc(qs_op* op, int32_t flags, const double* alpha, const vo
 
 int qs_eigsh(qs_op* op, const qs_eigsh_opts* opts, double* values, void* vectors, qs_eigsh_info* info) {
     return guard([&] { qs::eigsh(*op->op, *opts, values, vectors, info); });
+}
+
+int qs_eigsh_batch(qs_op* const* ops, int32_t nops, const qs_eigsh_opts* opts, double* values, void** vectors,
+                   qs_eigsh_info* infos) {
+    return guard([&] {
+        std::vector<qs::Op*> v(nops);
+        for (int i = 0; i < nops; ++i) v[i] = ops[i]->op;
+        qs::eigsh_batch(v.data(), nops, *opts, values, vectors, infos);
+    });
 }
 
 int qs_expm_multiply(qs_op* op, const double* a, const double* v, double* out, double tol, int32_t krylov_dim,

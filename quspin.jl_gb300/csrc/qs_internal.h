@@ -118,6 +118,7 @@ struct Op {
     DevBuf d_progs;
     DevBuf d_diag;                  // complex diagonal (user + extracted), 2*n doubles
     DevBuf d_diag32;                // single-precision copy
+    DevBuf d_diag_re, d_diag32_re;  // real parts (read by real operators)
     DevBuf d_x, d_y;                // staging for host vectors
     DevBuf d_x32, d_y32;
     cudaStream_t stream = nullptr;      // stream in use

@@ -9,6 +9,7 @@ namespace qs {
 
 double eps23();
 void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eigsh_info* info);
+void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, void** vectors, qs_eigsh_info* infos);
 void expm_multiply(Op& op, std::complex<double> a, const double* v, double* out, double tol, int krylov_dim,
                    int precision);
 void evolve(Op& op, const double* v0, double t0, const double* times, int nt, int imag_time, double tol,

@@ -383,6 +383,13 @@ __global__ void diag_kernel(MvArgs a, const double* user, double* out) {
     }
 }
 
+__global__ void real_part_kernel(const double* in, double* out, float* out32, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        out[i] = in[2 * i];
+        out32[i] = (float)in[2 * i];
+    }
+}
+
 __global__ void to_single_kernel(const double* in, float* out, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = (float)in[i];
@@ -484,6 +491,11 @@ void op_prepare_device(Op& op) {
     op.d_diag32.alloc(2 * b.n * sizeof(float));
     to_single_kernel<<<mv_grid(2 * b.n), kMvThreads, 0, op.stream>>>(op.d_diag.as<double>(), op.d_diag32.as<float>(),
                                                                       2 * b.n);
+    QS_CUDA(cudaGetLastError());
+    op.d_diag_re.alloc(b.n * sizeof(double));
+    op.d_diag32_re.alloc(b.n * sizeof(float));
+    real_part_kernel<<<mv_grid(b.n), kMvThreads, 0, op.stream>>>(op.d_diag.as<double>(), op.d_diag_re.as<double>(),
+                                                                  op.d_diag32_re.as<float>(), b.n);
     QS_CUDA(cudaGetLastError());
     QS_CUDA(cudaStreamSynchronize(op.stream));
 }

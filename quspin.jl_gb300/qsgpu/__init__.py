@@ -9,11 +9,11 @@ from .basis import (SpinBasis1D, get_amp, int_to_state, normalization, represent
                     state_to_int, states)
 from .errors import ArgumentError, DimensionMismatch, ErrorException, UnsupportedError
 from .operators import (ExpmMultiplyParallel, Hamiltonian, OperatorTerm, QuantumLinearOperator, apply, eigsh,
-                        evolve, expm_multiply_parallel, isquantum_LinearOperator, set_a)
+                        eigsh_batch, evolve, expm_multiply_parallel, isquantum_LinearOperator, set_a)
 
 __all__ = [
     "SpinBasis1D", "states", "state_index", "state_at", "representative", "normalization", "get_amp",
-    "int_to_state", "state_to_int", "OperatorTerm", "QuantumLinearOperator", "Hamiltonian", "eigsh", "evolve",
+    "int_to_state", "state_to_int", "OperatorTerm", "QuantumLinearOperator", "Hamiltonian", "eigsh", "eigsh_batch", "evolve",
     "ExpmMultiplyParallel", "expm_multiply_parallel", "apply", "set_a", "isquantum_LinearOperator",
     "ArgumentError", "DimensionMismatch", "ErrorException", "UnsupportedError",
 ]

@@ -50,6 +50,7 @@ EXPORTS = (
     "qs_op_create", "qs_op_destroy", "qs_op_dtype", "qs_op_hermitian", "qs_op_set_diagonal", "qs_op_matvec",
     "qs_eigsh", "qs_expm_multiply", "qs_evolve", "qs_last_error", "qs_version", "qs_op_set_stream",
     "qs_launch_count", "qs_op_assemble", "qs_op_nnz", "qs_op_matvec_noalloc",
+    "qs_eigsh_batch", "qs_basis_stabilizers",
 )
 
 _lib = None
@@ -72,6 +73,7 @@ def load():
     L.qs_basis_group_order.restype = i32
     L.qs_basis_states.argtypes = [P, P, i64]
     L.qs_basis_orbit_minima.argtypes = [P, P, i64]
+    L.qs_basis_stabilizers.argtypes = [P, P, i64]
     L.qs_basis_state_index.argtypes = [P, P, i64, P]
     L.qs_basis_representative.argtypes = [P, P, i64, P, P, P, P]
     L.qs_op_create.argtypes = [P, ctypes.POINTER(Term), i32, P, i32, ctypes.POINTER(P)]
@@ -86,6 +88,8 @@ def load():
     L.qs_evolve.argtypes = [P, P, f64, P, i32, i32, f64, i32, i32, P]
     L.qs_op_set_stream.argtypes = [P, P]
     L.qs_op_matvec_noalloc.argtypes = [P, i32, P, P, i32, P, P, i32, i64]
+    L.qs_eigsh_batch.argtypes = [ctypes.POINTER(P), i32, ctypes.POINTER(EigshOpts), P, ctypes.POINTER(P),
+                                 ctypes.POINTER(EigshInfo)]
     L.qs_op_assemble.argtypes = [P]
     L.qs_op_nnz.argtypes = [P]
     L.qs_op_nnz.restype = i64

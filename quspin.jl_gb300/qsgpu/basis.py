@@ -85,6 +85,12 @@ class SpinBasis1D:
         _lib.check(_lib.load().qs_basis_orbit_minima(self._h, _lib.ptr(out), self.Ns))
         return out
 
+    def stabilizers(self):
+        """Stabiliser order of every column's orbit minimum (orbit size = group_order / stab)."""
+        out = np.zeros(self.Ns, dtype=np.uint16)
+        _lib.check(_lib.load().qs_basis_stabilizers(self._h, _lib.ptr(out), self.Ns))
+        return out
+
     def index_array(self, states):
         """0-based columns of many states at once (-1 where not represented)."""
         q = np.ascontiguousarray(states, dtype=np.uint64)

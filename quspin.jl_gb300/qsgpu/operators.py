@@ -262,6 +262,31 @@ def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, nc
     return (vals, vecs) if return_eigenvectors else vals
 
 
+def eigsh_batch(ops, k=1, which="SA", tol=0.0, ncv=None, maxiter=None, return_eigenvectors=False, infos=None):
+    """eigsh(op; k, which) on every operator of `ops` at once (one multi-sector
+    launch per Lanczos step).  Returns an (len(ops), k) array of eigenvalues and,
+    when asked, one Ns_i x k vector block per operator."""
+    w = str(which).upper()
+    if w not in ("SA", "LA"):
+        raise ArgumentError("which must be SA or LA on this engine")
+    n = len(ops)
+    arr = (ctypes.c_void_p * n)(*[o._h for o in ops])
+    opts = _lib.EigshOpts(int(k), 0 if w == "SA" else 1, float(tol), int(ncv or 0), int(maxiter or 0), 0, 0,
+                          None, _lib.QS_MEM_HOST)
+    vals = np.zeros((n, int(k)))
+    vecs = None
+    vptrs = None
+    if return_eigenvectors:
+        vecs = [np.zeros((o.Ns, int(k)), dtype=o.dtype, order="F") for o in ops]
+        vptrs = (ctypes.c_void_p * n)(*[v.ctypes.data for v in vecs])
+    inf = (_lib.EigshInfo * n)()
+    _lib.check(_lib.load().qs_eigsh_batch(arr, n, ctypes.byref(opts), _lib.ptr(vals), vptrs, inf))
+    if infos is not None:
+        infos.extend(dict(nconv=i.nconv, restarts=i.restarts, matvecs=i.matvecs, max_rel_residual=i.max_rel_residual,
+                          seconds=i.seconds) for i in inf)
+    return (vals, vecs) if return_eigenvectors else vals
+
+
 def evolve(H, v0, t0, times, eom="SE", iterate=False, imag_time=False, tol=1e-12, krylov_dim=30, precision="fp64"):
     """evolve(H, v0, t0, times; eom=:SE) for a static Hamiltonian (src/operators.jl:2073-2164)."""
     if str(eom) not in ("SE", "LvNE"):
