@@ -200,7 +200,9 @@ typedef struct {
     int32_t ncv;          /* Lanczos basis size, 0 = max(20, 2k+1) (Arpack.jl default) */
     int32_t maxiter;      /* restarts, 0 = 300 */
     int32_t precision;    /* 0 = FP64, 1 = FP32 matvec and vectors + FP64 polish,
-                             2 = FP64 vectors with double-float products (assembled operators) */
+                             2 = double-float (hi+lo float) Krylov vectors and products on the
+                             FP32 pipe + FP64 Rayleigh-quotient polish (assembled operators;
+                             matrix-free operators run this as 0) */
     int32_t want_vectors;
     const double *v0;     /* NULL or starting vector, dtype of op */
     int32_t mem;          /* QS_MEM_HOST or QS_MEM_DEVICE for v0 and vectors */
@@ -235,13 +237,16 @@ QS_API int qs_eigsh_batch(qs_op *const *ops, int32_t nops, const qs_eigsh_opts *
 
 /* apply(ExpmMultiplyParallel(A, a), v; tol) (tools.jl:1662-1708) and the
  * Krylov exponential action _krylov_expmv_vector (src/operators.jl:1758-1803):
- * out = exp(a * A) v with complex a.  v, out: Ns complex (host). */
+ * out = exp(a * A) v with complex a.  v, out: Ns complex (host).
+ * precision: 0 FP64, 1 FP32 Krylov vectors, 2 double-float Krylov vectors
+ * (assembled operators; otherwise FP64). */
 QS_API int qs_expm_multiply(qs_op *op, const double *a, const double *v, double *out, double tol,
                      int32_t krylov_dim, int32_t precision);
 
 /* evolve(H, v0, t0, times; eom=:SE, imag_time, tol, krylov_dim) for a static
  * Hamiltonian (src/operators.jl:2073-2164 via _krylov_expmv_times
- * 1805-1893): out is Ns x nt column-major complex (host). */
+ * 1805-1893): out is Ns x nt column-major complex (host); precision as for
+ * qs_expm_multiply. */
 QS_API int qs_evolve(qs_op *op, const double *v0, double t0, const double *times, int32_t nt, int32_t imag_time,
               double tol, int32_t krylov_dim, int32_t precision, double *out);
 

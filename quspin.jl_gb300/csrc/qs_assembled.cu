@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "qs_device.cuh"
+#include "qs_df.cuh"
 #include "qs_internal.h"
 
 namespace qs {
@@ -261,36 +262,6 @@ __global__ void __launch_bounds__(kThreads) spmv_kernel(SpmvArgs a) {
 // pairs, and products and sums are carried as unevaluated float pairs with
 // the error-free transformations TwoProd (via fma) and TwoSum (Knuth), i.e.
 // about 48 significand bits.  Only the per-row combination runs in FP64.
-
-struct DF {
-    float h, l;
-};
-
-__device__ __forceinline__ DF df_two_sum(float a, float b) {
-    float s = a + b;
-    float bb = s - a;
-    float e = (a - (s - bb)) + (b - bb);
-    return DF{s, e};
-}
-
-// acc += t * x  (t, x double-float)
-__device__ __forceinline__ void df_mac(DF& acc, float th, float tl, float xh, float xl) {
-    float p = th * xh;
-    float pe = fmaf(th, xh, -p);
-    pe = fmaf(th, xl, pe);
-    pe = fmaf(tl, xh, pe);
-    DF s = df_two_sum(acc.h, p);
-    acc.h = s.h;
-    acc.l = acc.l + (s.l + pe);
-}
-
-__device__ __forceinline__ DF df_add(DF a, DF b) {
-    DF s = df_two_sum(a.h, b.h);
-    s.l += a.l + b.l;
-    return df_two_sum(s.h, s.l);
-}
-
-__device__ __forceinline__ double df_to_double(DF a) { return (double)a.h + (double)a.l; }
 
 __device__ __forceinline__ float2 df_split(double v) {
     float h = __double2float_rn(v);
@@ -626,6 +597,75 @@ __global__ void __launch_bounds__(kThreads, 8) sell_df_kernel(SellArgs a, const 
     }
 }
 
+// Double-float storage in and out (the Krylov solvers' double-float vectors):
+// y = d .* x + rs(stab) * sum_j T[code_j] x[col_j], entirely on the FP32 pipe.
+template <bool kCM, bool kCV>
+__global__ void __launch_bounds__(kThreads, 8) sell_dfio_kernel(SellArgs a, const float4* __restrict__ tab_df,
+                                                                const float4* __restrict__ diag_df,
+                                                                const float2* __restrict__ rsq_df) {
+    __shared__ float4 tab[1024];
+    __shared__ float2 rsq[kMaxGroup + 1];
+    const bool smem_tab = a.ncodes <= 1024;
+    if (smem_tab)
+        for (int i = threadIdx.x; i < a.ncodes; i += blockDim.x) {
+            float4 v = tab_df[i];
+            if (a.conj) { v.z = -v.z; v.w = -v.w; }
+            tab[i] = v;
+        }
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) rsq[i] = rsq_df[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = warp0; s < a.nslices; s += nwarps) {
+        const int64_t r = s * kSlice + lane;
+        if (r >= a.n) continue;
+        const int len = a.len[r];
+        const int64_t base = a.sptr[s] + lane;
+        DF ar{0.f, 0.f}, ai{0.f, 0.f};
+#pragma unroll 4
+        for (int j = 0; j < len; ++j) {
+            uint32_t col, code;
+            sell_word<float>(a, base + (int64_t)j * kSlice, col, code);
+            float4 v;
+            if (smem_tab) v = tab[code];
+            else {
+                v = tab_df[code];
+                if (a.conj) { v.z = -v.z; v.w = -v.w; }
+            }
+            if (kCV) {
+                const float4 xv = __ldg((const float4*)a.x + col);
+                df_mac(ar, v.x, v.y, xv.x, xv.y);
+                df_mac(ai, v.x, v.y, xv.z, xv.w);
+                if (kCM) {
+                    df_mac(ar, -v.z, -v.w, xv.z, xv.w);
+                    df_mac(ai, v.z, v.w, xv.x, xv.y);
+                }
+            } else {
+                const float2 xv = __ldg((const float2*)a.x + col);
+                df_mac(ar, v.x, v.y, xv.x, xv.y);
+            }
+        }
+        const float2 sc = a.stab ? rsq[a.stab[r]] : make_float2(1.f, 0.f);
+        DF out_r = df_mul(ar, DF{sc.x, sc.y});
+        const float4 d = diag_df[r];   // re hi, re lo, im hi, im lo
+        const float dih = a.conj ? -d.z : d.z, dil = a.conj ? -d.w : d.w;
+        if (kCV) {
+            DF out_i = df_mul(ai, DF{sc.x, sc.y});
+            const float4 xv = ((const float4*)a.x)[r];
+            df_mac(out_r, d.x, d.y, xv.x, xv.y);
+            df_mac(out_r, -dih, -dil, xv.z, xv.w);
+            df_mac(out_i, d.x, d.y, xv.z, xv.w);
+            df_mac(out_i, dih, dil, xv.x, xv.y);
+            ((float4*)a.y)[r] = make_float4(out_r.h, out_r.l, out_i.h, out_i.l);
+        } else {
+            const float2 xv = ((const float2*)a.x)[r];
+            df_mac(out_r, d.x, d.y, xv.x, xv.y);
+            ((float2*)a.y)[r] = make_float2(out_r.h, out_r.l);
+        }
+    }
+}
+
 int grid_rows(int64_t threads_needed) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -774,6 +814,12 @@ void op_assemble(Op& op) {
     }
     M.table_df.alloc(ncodes * 4 * sizeof(float));
     QS_CUDA(cudaMemcpy(M.table_df.p, tdf.data(), ncodes * 4 * sizeof(float), cudaMemcpyHostToDevice));
+    {
+        std::vector<float> rq(2 * (kMaxGroup + 1), 0.f);
+        for (int i = 1; i <= kMaxGroup; ++i) df_split_host(1.0 / std::sqrt((double)i), rq[2 * i], rq[2 * i + 1]);
+        M.rsq_df.alloc(rq.size() * sizeof(float));
+        QS_CUDA(cudaMemcpy(M.rsq_df.p, rq.data(), rq.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
     M.xsplit.alloc((size_t)b.n * 4 * sizeof(float));
 
     cudaStream_t s = op.stream;
@@ -853,6 +899,7 @@ void op_assemble(Op& op) {
 void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
     const Basis& b = *op.basis;
     const Assembled& M = op.asm_;
+    if (c.df_io && !M.has_sell) throw Error(QS_ERR_UNSUPPORTED, "double-float vectors need the sliced layout");
     if (M.has_sell) {
         SellArgs a{};
         a.sptr = M.sell_ptr.as<int64_t>();
@@ -879,6 +926,17 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
         a.y = c.y;
         const bool cm = op.complex_mat, cv = c.y_complex;
         const int grid = grid_rows(M.nslices * kSlice);
+        if (c.df_io) {
+            const float4* td = M.table_df.as<float4>();
+            const float4* dd = op.d_diag_df.as<float4>();
+            const float2* rq = M.rsq_df.as<float2>();
+            if (cm) sell_dfio_kernel<true, true><<<grid, kThreads, 0, s>>>(a, td, dd, rq);
+            else if (cv) sell_dfio_kernel<false, true><<<grid, kThreads, 0, s>>>(a, td, dd, rq);
+            else sell_dfio_kernel<false, false><<<grid, kThreads, 0, s>>>(a, td, dd, rq);
+            QS_CUDA(cudaGetLastError());
+            note_launches(1);
+            return;
+        }
         if (c.df && !c.single) {
             a.table = M.table64.p;
             a.diag = op.d_diag.p;

@@ -14,6 +14,7 @@ struct Assembled {
     DevBuf table32;    // complex float value per code
     DevBuf table_df;   // per code: re hi, re lo, im hi, im lo (float)
     DevBuf xsplit;     // x split into float pairs for the double-float product
+    DevBuf rsq_df;     // 1/sqrt(stab) as float pairs, stab = 0 .. kMaxGroup
     int64_t nnz = 0;
     int ncodes = 0;
     int code_bits = 0;

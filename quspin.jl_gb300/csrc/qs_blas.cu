@@ -3,6 +3,7 @@
 // loop (dot / axpy! / norm in _krylov_factorization, src/operators.jl:
 // 1681-1726) and the reorthogonalisation ARPACK performs internally.
 #include "qs_blas.cuh"
+#include "qs_df.cuh"
 
 #include <algorithm>
 
@@ -214,6 +215,181 @@ __global__ void convert_kernel(const void* src, void* dst, int64_t n) {
     }
 }
 
+// ------------------------------------------------- double-float storage
+template <bool C>
+__device__ __forceinline__ void ld_df(const void* p, int64_t i, DF& re, DF& im) {
+    if (C) {
+        float4 v = ((const float4*)p)[i];
+        re = DF{v.x, v.y};
+        im = DF{v.z, v.w};
+    } else {
+        float2 v = ((const float2*)p)[i];
+        re = DF{v.x, v.y};
+        im = DF{0.f, 0.f};
+    }
+}
+template <bool C>
+__device__ __forceinline__ void st_df(void* p, int64_t i, DF re, DF im) {
+    if (C) ((float4*)p)[i] = make_float4(re.h, re.l, im.h, im.l);
+    else ((float2*)p)[i] = make_float2(re.h, re.l);
+}
+
+// partial[b][j] = sum over the block of conj(V_j) w, in double-float; only the
+// per-warp totals are converted to double.
+template <bool C>
+__global__ void __launch_bounds__(kThreads) dots_df_kernel(const void* V, int64_t ldv, int m, const void* w, int64_t n,
+                                                           double* partial) {
+    const int j0 = blockIdx.y * kJT;
+    DF re[kJT], im[kJT];
+#pragma unroll
+    for (int j = 0; j < kJT; ++j) re[j] = im[j] = DF{0.f, 0.f};
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+        DF wr, wi;
+        ld_df<C>(w, i, wr, wi);
+#pragma unroll
+        for (int j = 0; j < kJT; ++j) {
+            if (j0 + j < m) {
+                DF vr, vi;
+                ld_df<C>(V, (int64_t)(j0 + j) * ldv + i, vr, vi);
+                df_mac(re[j], vr.h, vr.l, wr.h, wr.l);
+                if (C) {
+                    df_mac(re[j], vi.h, vi.l, wi.h, wi.l);
+                    df_mac(im[j], vr.h, vr.l, wi.h, wi.l);
+                    df_mac(im[j], -vi.h, -vi.l, wr.h, wr.l);
+                }
+            }
+        }
+    }
+    __shared__ double sh[kThreads / 32][2 * kJT];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < kJT; ++j) {
+        for (int o = 16; o > 0; o >>= 1) {
+            re[j] = df_add(re[j], df_shfl_xor(re[j], o, 32));
+            if (C) im[j] = df_add(im[j], df_shfl_xor(im[j], o, 32));
+        }
+        if (lane == 0) {
+            sh[wid][2 * j] = df_to_double(re[j]);
+            sh[wid][2 * j + 1] = C ? df_to_double(im[j]) : 0.0;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * kJT) {
+        double t = 0;
+        for (int q = 0; q < kThreads / 32; ++q) t += sh[q][threadIdx.x];
+        const int j = threadIdx.x / 2;
+        if (j0 + j < m) partial[((int64_t)blockIdx.x * m + j0 + j) * 2 + (threadIdx.x & 1)] = t;
+    }
+}
+
+// w -= sum_j V_j h_j (mode 0) or out = sum_j V_j h_j (mode 1); hs holds each
+// complex h_j as four floats (re hi, re lo, im hi, im lo)
+template <bool C, int kMode>
+__global__ void __launch_bounds__(kThreads) update_df_kernel(void* w, const void* V, int64_t ldv, int m,
+                                                             const float4* h, int64_t n) {
+    __shared__ float4 hs[128];
+    for (int j = threadIdx.x; j < m; j += blockDim.x) hs[j] = h[j];
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+        DF ar{0.f, 0.f}, ai{0.f, 0.f};
+        for (int j = 0; j < m; ++j) {
+            DF vr, vi;
+            ld_df<C>(V, (int64_t)j * ldv + i, vr, vi);
+            const float4 hj = hs[j];
+            df_mac(ar, vr.h, vr.l, hj.x, hj.y);
+            if (C) {
+                df_mac(ar, -vi.h, -vi.l, hj.z, hj.w);
+                df_mac(ai, vr.h, vr.l, hj.z, hj.w);
+                df_mac(ai, vi.h, vi.l, hj.x, hj.y);
+            }
+        }
+        if (kMode == 0) {
+            DF wr, wi;
+            ld_df<C>(w, i, wr, wi);
+            st_df<C>(w, i, df_add(wr, df_neg(ar)), df_add(wi, df_neg(ai)));
+        } else {
+            st_df<C>(w, i, ar, ai);
+        }
+    }
+}
+
+// y = a x + b y, a complex and b real, both split into float pairs
+template <bool C>
+__global__ void axpby_df_kernel(void* y, const void* x, float4 a, float2 b, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+        DF xr, xi, yr{0.f, 0.f}, yi{0.f, 0.f};
+        ld_df<C>(x, i, xr, xi);
+        if (b.x != 0.f) ld_df<C>(y, i, yr, yi);
+        DF orr = df_mul(yr, DF{b.x, b.y}), oi = df_mul(yi, DF{b.x, b.y});
+        df_mac(orr, a.x, a.y, xr.h, xr.l);
+        if (C) {
+            df_mac(orr, -a.z, -a.w, xi.h, xi.l);
+            df_mac(oi, a.x, a.y, xi.h, xi.l);
+            df_mac(oi, a.z, a.w, xr.h, xr.l);
+        }
+        st_df<C>(y, i, orr, oi);
+    }
+}
+
+// tmp[:, c] = sum_j V[:, j] Y[j, c], Y (m x p, column-major) as float pairs
+template <bool C>
+__global__ void __launch_bounds__(kThreads) rotate_df_kernel(void* tmp, const void* V, int64_t ldv, int m, int p,
+                                                             const float2* Y, int64_t n) {
+    extern __shared__ float2 ysf[];
+    for (int k = threadIdx.x; k < m * p; k += blockDim.x) ysf[k] = Y[k];
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+        for (int c = 0; c < p; ++c) {
+            DF ar{0.f, 0.f}, ai{0.f, 0.f};
+            for (int j = 0; j < m; ++j) {
+                DF vr, vi;
+                ld_df<C>(V, (int64_t)j * ldv + i, vr, vi);
+                const float2 y = ysf[c * m + j];
+                df_mac(ar, vr.h, vr.l, y.x, y.y);
+                if (C) df_mac(ai, vi.h, vi.l, y.x, y.y);
+            }
+            st_df<C>(tmp, (int64_t)c * n + i, ar, ai);
+        }
+    }
+}
+
+template <bool C>
+__global__ void copy_cols_df_kernel(void* V, int64_t ldv, const void* tmp, int p, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads)
+        for (int c = 0; c < p; ++c) {
+            DF r, im;
+            ld_df<C>(tmp, (int64_t)c * n + i, r, im);
+            st_df<C>(V, (int64_t)c * ldv + i, r, im);
+        }
+}
+
+// double <-> double-float storage (same real/complex-ness)
+template <bool C>
+__global__ void to_df_kernel(const double* in, void* out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+        if (C) {
+            DF a = df_from_double(in[2 * i]), b = df_from_double(in[2 * i + 1]);
+            ((float4*)out)[i] = make_float4(a.h, a.l, b.h, b.l);
+        } else {
+            DF a = df_from_double(in[i]);
+            ((float2*)out)[i] = make_float2(a.h, a.l);
+        }
+    }
+}
+template <bool C>
+__global__ void from_df_kernel(const void* in, double* out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+        if (C) {
+            float4 v = ((const float4*)in)[i];
+            out[2 * i] = df_to_double(DF{v.x, v.y});
+            out[2 * i + 1] = df_to_double(DF{v.z, v.w});
+        } else {
+            float2 v = ((const float2*)in)[i];
+            out[i] = df_to_double(DF{v.x, v.y});
+        }
+    }
+}
+
 int nblocks(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, kMaxBlocks));
@@ -258,7 +434,13 @@ Blas::Blas(VKind k, int64_t n_, cudaStream_t st) : kind(k), n(n_), s(st) {
 void Blas::dots(const void* V, int64_t ldv, int m, const void* w, std::vector<cd>& h) {
     if (m > 128) throw Error(QS_ERR_UNSUPPORTED, "Krylov basis larger than 128 vectors");
     int nb = nblocks(n);
-    QS_DISPATCH(kind, launch_dots, V, ldv, m, w, n, partial.as<double>(), nb, s);
+    if (vk_df(kind)) {
+        dim3 grid(nb, (m + kJT - 1) / kJT);
+        if (kind == VKind::CDF64) dots_df_kernel<true><<<grid, kThreads, 0, s>>>(V, ldv, m, w, n, partial.as<double>());
+        else dots_df_kernel<false><<<grid, kThreads, 0, s>>>(V, ldv, m, w, n, partial.as<double>());
+    } else {
+        QS_DISPATCH(kind, launch_dots, V, ldv, m, w, n, partial.as<double>(), nb, s);
+    }
     QS_CUDA(cudaGetLastError());
     reduce_partials_kernel<<<m, 256, 0, s>>>(partial.as<double>(), nb, m, result.as<double>());
     QS_CUDA(cudaGetLastError());
@@ -270,8 +452,26 @@ void Blas::dots(const void* V, int64_t ldv, int m, const void* w, std::vector<cd
     for (int j = 0; j < m; ++j) h[j] = cd(hbuf[2 * j], hbuf[2 * j + 1]);
 }
 
+void Blas::upload_df(const std::vector<cd>& h, int m) {
+    fbuf.resize(4 * m);
+    for (int j = 0; j < m; ++j) {
+        df_split_host(h[j].real(), fbuf[4 * j], fbuf[4 * j + 1]);
+        df_split_host(h[j].imag(), fbuf[4 * j + 2], fbuf[4 * j + 3]);
+    }
+    QS_CUDA(cudaMemcpyAsync(coeffs.p, fbuf.data(), 4 * m * sizeof(float), cudaMemcpyHostToDevice, s));
+}
+
 void Blas::update(void* w, const void* V, int64_t ldv, int m, const std::vector<cd>& h) {
     if (m == 0) return;
+    if (vk_df(kind)) {
+        upload_df(h, m);
+        if (kind == VKind::CDF64) update_df_kernel<true, 0><<<nblocks(n), kThreads, 0, s>>>(w, V, ldv, m, coeffs.as<float4>(), n);
+        else update_df_kernel<false, 0><<<nblocks(n), kThreads, 0, s>>>(w, V, ldv, m, coeffs.as<float4>(), n);
+        QS_CUDA(cudaGetLastError());
+        note_launches(1);
+        QS_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
     hbuf.resize(2 * m);
     for (int j = 0; j < m; ++j) { hbuf[2 * j] = h[j].real(); hbuf[2 * j + 1] = h[j].imag(); }
     QS_CUDA(cudaMemcpyAsync(coeffs.p, hbuf.data(), 2 * m * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -282,6 +482,15 @@ void Blas::update(void* w, const void* V, int64_t ldv, int m, const std::vector<
 }
 
 void Blas::combine(void* out, const void* V, int64_t ldv, int m, const std::vector<cd>& c) {
+    if (vk_df(kind)) {
+        upload_df(c, m);
+        if (kind == VKind::CDF64) update_df_kernel<true, 1><<<nblocks(n), kThreads, 0, s>>>(out, V, ldv, m, coeffs.as<float4>(), n);
+        else update_df_kernel<false, 1><<<nblocks(n), kThreads, 0, s>>>(out, V, ldv, m, coeffs.as<float4>(), n);
+        QS_CUDA(cudaGetLastError());
+        note_launches(1);
+        QS_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
     hbuf.resize(2 * m);
     for (int j = 0; j < m; ++j) { hbuf[2 * j] = c[j].real(); hbuf[2 * j + 1] = c[j].imag(); }
     QS_CUDA(cudaMemcpyAsync(coeffs.p, hbuf.data(), 2 * m * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -303,13 +512,34 @@ cd Blas::dot(const void* a, const void* b) {
     return h[0];
 }
 
+static float4 split4(std::complex<double> a) {
+    float4 r;
+    df_split_host(a.real(), r.x, r.y);
+    df_split_host(a.imag(), r.z, r.w);
+    return r;
+}
+
 void Blas::scale(void* dst, const void* src, cd a) {
+    if (vk_df(kind)) {
+        if (kind == VKind::CDF64) axpby_df_kernel<true><<<nblocks(n), kThreads, 0, s>>>(dst, src, split4(a), make_float2(0.f, 0.f), n);
+        else axpby_df_kernel<false><<<nblocks(n), kThreads, 0, s>>>(dst, src, split4(a), make_float2(0.f, 0.f), n);
+        QS_CUDA(cudaGetLastError());
+        note_launches(1);
+        return;
+    }
     QS_DISPATCH(kind, launch_axpby, dst, src, a.real(), a.imag(), 0.0, n, s);
     QS_CUDA(cudaGetLastError());
     note_launches(1);
 }
 
 void Blas::axpy(void* y, const void* x, cd a) {
+    if (vk_df(kind)) {
+        if (kind == VKind::CDF64) axpby_df_kernel<true><<<nblocks(n), kThreads, 0, s>>>(y, x, split4(a), make_float2(1.f, 0.f), n);
+        else axpby_df_kernel<false><<<nblocks(n), kThreads, 0, s>>>(y, x, split4(a), make_float2(1.f, 0.f), n);
+        QS_CUDA(cudaGetLastError());
+        note_launches(1);
+        return;
+    }
     QS_DISPATCH(kind, launch_axpby, y, x, a.real(), a.imag(), 1.0, n, s);
     QS_CUDA(cudaGetLastError());
     note_launches(1);
@@ -320,6 +550,23 @@ void Blas::copy(void* dst, const void* src) {
 }
 
 void Blas::rotate(void* V, int64_t ldv, int m, int p, const std::vector<double>& Y, void* tmp) {
+    if (vk_df(kind)) {
+        fbuf.resize(2 * (size_t)m * p);
+        for (size_t k = 0; k < (size_t)m * p; ++k) df_split_host(Y[k], fbuf[2 * k], fbuf[2 * k + 1]);
+        QS_CUDA(cudaMemcpyAsync(coeffs.p, fbuf.data(), fbuf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+        const size_t sm = (size_t)m * p * sizeof(float2);
+        if (kind == VKind::CDF64) {
+            rotate_df_kernel<true><<<nblocks(n), kThreads, sm, s>>>(tmp, V, ldv, m, p, coeffs.as<float2>(), n);
+            copy_cols_df_kernel<true><<<nblocks(n), kThreads, 0, s>>>(V, ldv, tmp, p, n);
+        } else {
+            rotate_df_kernel<false><<<nblocks(n), kThreads, sm, s>>>(tmp, V, ldv, m, p, coeffs.as<float2>(), n);
+            copy_cols_df_kernel<false><<<nblocks(n), kThreads, 0, s>>>(V, ldv, tmp, p, n);
+        }
+        QS_CUDA(cudaGetLastError());
+        note_launches(2);
+        QS_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
     QS_CUDA(cudaMemcpyAsync(coeffs.p, Y.data(), (size_t)m * p * sizeof(double), cudaMemcpyHostToDevice, s));
     QS_DISPATCH(kind, launch_rotate, tmp, V, ldv, m, p, coeffs.as<double>(), n, s);
     QS_CUDA(cudaGetLastError());
@@ -330,6 +577,22 @@ void Blas::rotate(void* V, int64_t ldv, int m, int p, const std::vector<double>&
 void convert_vec(const void* src, VKind ks, void* dst, VKind kd, int64_t n, cudaStream_t s) {
     bool c = vk_complex(ks);
     if (c != vk_complex(kd)) throw Error(QS_ERR_ARGUMENT, "real/complex mismatch in a precision conversion");
+    if (vk_df(ks) || vk_df(kd)) {
+        if (ks == kd) {
+            QS_CUDA(cudaMemcpyAsync(dst, src, n * vk_bytes(ks), cudaMemcpyDeviceToDevice, s));
+        } else if (vk_df(kd) && (ks == VKind::F64 || ks == VKind::C128)) {
+            if (c) to_df_kernel<true><<<nblocks(n), kThreads, 0, s>>>((const double*)src, dst, n);
+            else to_df_kernel<false><<<nblocks(n), kThreads, 0, s>>>((const double*)src, dst, n);
+        } else if (vk_df(ks) && (kd == VKind::F64 || kd == VKind::C128)) {
+            if (c) from_df_kernel<true><<<nblocks(n), kThreads, 0, s>>>(src, (double*)dst, n);
+            else from_df_kernel<false><<<nblocks(n), kThreads, 0, s>>>(src, (double*)dst, n);
+        } else {
+            throw Error(QS_ERR_UNSUPPORTED, "double-float vectors convert to and from FP64 only");
+        }
+        QS_CUDA(cudaGetLastError());
+        note_launches(1);
+        return;
+    }
     bool s1 = vk_single(ks), s2 = vk_single(kd);
     if (s1 == s2) {
         QS_CUDA(cudaMemcpyAsync(dst, src, n * vk_bytes(ks), cudaMemcpyDeviceToDevice, s));

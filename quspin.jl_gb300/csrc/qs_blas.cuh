@@ -14,15 +14,19 @@
 namespace qs {
 
 // Storage of a Krylov vector: scalar type and real/complex.
-enum class VKind { F64 = 0, C128 = 1, F32 = 2, C64 = 3 };
-inline bool vk_complex(VKind k) { return k == VKind::C128 || k == VKind::C64; }
+// DF64 / CDF64: double-float storage, hi + lo float per real component.
+enum class VKind { F64 = 0, C128 = 1, F32 = 2, C64 = 3, DF64 = 4, CDF64 = 5 };
+inline bool vk_complex(VKind k) { return k == VKind::C128 || k == VKind::C64 || k == VKind::CDF64; }
 inline bool vk_single(VKind k) { return k == VKind::F32 || k == VKind::C64; }
+inline bool vk_df(VKind k) { return k == VKind::DF64 || k == VKind::CDF64; }
 inline size_t vk_bytes(VKind k) {
     switch (k) {
         case VKind::F64: return 8;
         case VKind::C128: return 16;
         case VKind::F32: return 4;
-        default: return 8;
+        case VKind::C64: return 8;
+        case VKind::DF64: return 8;
+        default: return 16;
     }
 }
 
@@ -37,7 +41,9 @@ struct Blas {
     DevBuf coeffs;    // small coefficient vectors on the device
     DevBuf result;    // reduced dot products
     std::vector<double> hbuf;
+    std::vector<float> fbuf;
     Blas(VKind k, int64_t n_, cudaStream_t st);
+    void upload_df(const std::vector<cd>& h, int m);
     // h_j = <V_j, w>, j < m
     void dots(const void* V, int64_t ld, int m, const void* w, std::vector<cd>& h);
     // w -= sum_j V_j h_j

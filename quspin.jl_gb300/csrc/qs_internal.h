@@ -119,6 +119,7 @@ struct Op {
     DevBuf d_diag;                  // complex diagonal (user + extracted), 2*n doubles
     DevBuf d_diag32;                // single-precision copy
     DevBuf d_diag_re, d_diag32_re;  // real parts (read by real operators)
+    DevBuf d_diag_df;               // diagonal as float pairs: re hi, re lo, im hi, im lo
     DevBuf d_x, d_y;                // staging for host vectors
     DevBuf d_x32, d_y32;
     cudaStream_t stream = nullptr;      // stream in use
@@ -147,6 +148,7 @@ struct MatvecCall {
     bool x_complex = false, y_complex = false;
     bool single = false;            // FP32 vectors and accumulation
     bool df = false;                // FP64 vectors, double-float products (assembled form)
+    bool df_io = false;             // double-float vectors in and out, alpha = 1, beta = 0
 };
 void op_prepare_device(Op& op);
 // qs_noalloc.cu

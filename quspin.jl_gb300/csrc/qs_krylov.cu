@@ -47,11 +47,21 @@ struct Ctx {
         c.y = y;
         c.x_complex = c.y_complex = vk_complex(vk);
         c.single = vk_single(vk);
-        c.df = df && !c.single;
+        c.df_io = vk_df(vk);
+        c.df = (df || c.df_io) && !c.single;
         op_matvec_device(op, c, s);
         ++matvecs;
     }
 };
+
+// Storage of the Krylov vectors for a precision code: 0 FP64, 1 FP32, 2
+// double-float (DF storage needs the sliced assembled layout, else FP64
+// vectors with double-float products where the operator is assembled).
+VKind krylov_kind(const Op& op, bool cpx, int precision) {
+    if (precision == 1) return cpx ? VKind::C64 : VKind::F32;
+    if (precision == 2 && op.assembled && op.asm_.has_sell) return cpx ? VKind::CDF64 : VKind::DF64;
+    return cpx ? VKind::C128 : VKind::F64;
+}
 
 // Deterministic pseudo-random start vector (normal entries).
 void random_vector(Ctx& c, void* dst, uint64_t seed) {
@@ -295,8 +305,9 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
     if (ncv <= k) ncv = std::min<int64_t>(n, k + 1);
     double tol = o.tol > 0 ? o.tol : kEps;
     int maxiter = o.maxiter > 0 ? o.maxiter : 300;
-    const bool single = o.precision == 1;
-    const VKind vk = single ? (cpx ? VKind::C64 : VKind::F32) : k64;
+    const VKind vk = krylov_kind(op, cpx, o.precision);
+    // reduced-precision vectors get an FP64 Rayleigh-quotient polish
+    const bool single = vk != k64;
     Ctx c(op, vk, o.precision == 2);
     DevBuf v0((size_t)n * vk_bytes(vk));
     const bool dev = o.mem == QS_MEM_DEVICE;
@@ -313,7 +324,7 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
         random_vector(c, v0.p, 20261203ull);
     }
     DevBuf X((size_t)n * k * vk_bytes(vk));
-    double tol_run = single ? std::max(tol, 2e-6) : tol;
+    double tol_run = vk_single(vk) ? std::max(tol, 2e-6) : tol;
     TRResult R = trlan(c, k, o.which, tol_run, ncv, maxiter, v0.p, X.p);
     int64_t mv = c.matvecs;
     std::vector<double> theta = R.theta;
@@ -493,8 +504,8 @@ void expm_multiply(Op& op, cd a, const double* v, double* out, double tol, int k
     const int64_t n = op.basis->n;
     if (tol <= 0) throw Error(QS_ERR_ARGUMENT, "tol must be positive");
     if (krylov_dim <= 0) throw Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
-    VKind vk = precision == 1 ? VKind::C64 : VKind::C128;
-    Ctx c(op, vk);
+    VKind vk = krylov_kind(op, true, precision);
+    Ctx c(op, vk, precision == 2);
     DevBuf d64(n * 16), dv((size_t)n * vk_bytes(vk)), dout((size_t)n * vk_bytes(vk));
     QS_CUDA(cudaMemcpyAsync(d64.p, v, n * 16, cudaMemcpyHostToDevice, op.stream));
     convert_vec(d64.p, VKind::C128, dv.p, vk, n, op.stream);
@@ -510,8 +521,8 @@ void evolve(Op& op, const double* v0, double t0, const double* times, int nt, in
     const int64_t n = op.basis->n;
     if (tol <= 0) throw Error(QS_ERR_ARGUMENT, "tol must be positive");
     if (krylov_dim <= 0) throw Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
-    VKind vk = precision == 1 ? VKind::C64 : VKind::C128;
-    Ctx c(op, vk);
+    VKind vk = krylov_kind(op, true, precision);
+    Ctx c(op, vk, precision == 2);
     DevBuf d64(n * 16), dv((size_t)n * vk_bytes(vk)), st((size_t)n * vk_bytes(vk));
     QS_CUDA(cudaMemcpyAsync(d64.p, v0, n * 16, cudaMemcpyHostToDevice, op.stream));
     convert_vec(d64.p, VKind::C128, dv.p, vk, n, op.stream);

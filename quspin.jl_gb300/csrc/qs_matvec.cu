@@ -25,6 +25,7 @@
 #include <atomic>
 
 #include "qs_device.cuh"
+#include "qs_df.cuh"
 #include "qs_internal.h"
 
 namespace qs {
@@ -383,6 +384,13 @@ __global__ void diag_kernel(MvArgs a, const double* user, double* out) {
     }
 }
 
+__global__ void diag_df_kernel(const double* in, float4* out, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        DF a = df_from_double(in[2 * i]), b = df_from_double(in[2 * i + 1]);
+        out[i] = make_float4(a.h, a.l, b.h, b.l);
+    }
+}
+
 __global__ void real_part_kernel(const double* in, double* out, float* out32, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         out[i] = in[2 * i];
@@ -492,6 +500,9 @@ void op_prepare_device(Op& op) {
     to_single_kernel<<<mv_grid(2 * b.n), kMvThreads, 0, op.stream>>>(op.d_diag.as<double>(), op.d_diag32.as<float>(),
                                                                       2 * b.n);
     QS_CUDA(cudaGetLastError());
+    op.d_diag_df.alloc(b.n * 4 * sizeof(float));
+    diag_df_kernel<<<mv_grid(b.n), kMvThreads, 0, op.stream>>>(op.d_diag.as<double>(), op.d_diag_df.as<float4>(), b.n);
+    QS_CUDA(cudaGetLastError());
     op.d_diag_re.alloc(b.n * sizeof(double));
     op.d_diag32_re.alloc(b.n * sizeof(float));
     real_part_kernel<<<mv_grid(b.n), kMvThreads, 0, op.stream>>>(op.d_diag.as<double>(), op.d_diag_re.as<double>(),
@@ -544,6 +555,7 @@ void op_matvec_device(Op& op, const MatvecCall& c, cudaStream_t s) {
         op_spmv_device(op, c, s);
         return;
     }
+    if (c.df_io) throw Error(QS_ERR_UNSUPPORTED, "double-float vectors need an assembled operator");
     if (c.single) {
         a.diag = op.d_diag32.p;
         launch_matvec<float>(b, a, cm, cv, s);

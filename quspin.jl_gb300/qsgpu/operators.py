@@ -229,6 +229,14 @@ class Hamiltonian(QuantumLinearOperator):
         return int(_lib.load().qs_op_nnz(self._h))
 
 
+def _precision_code(precision):
+    """0 = FP64, 1 = FP32 (+ FP64 polish), 2 = double-float on the FP32 pipe."""
+    codes = {"fp64": 0, "fp32": 1, "fp64df": 2}
+    if precision not in codes:
+        raise ArgumentError("precision must be fp64, fp32 or fp64df")
+    return codes[precision]
+
+
 def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, ncv=None, maxiter=None,
           precision="fp64", info=None):
     """eigsh(op; k, which=:SA, v0, tol, ncv, maxiter): k extremal eigenpairs."""
@@ -246,10 +254,8 @@ def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, nc
         vv = np.ascontiguousarray(v0, dtype=op.dtype)
         if vv.shape != (n,):
             raise DimensionMismatch("v0 must have length Ns")
-    if precision not in ("fp64", "fp32", "fp64df"):
-        raise ArgumentError("precision must be fp64, fp32 or fp64df")
     opts = _lib.EigshOpts(k, 0 if w == "SA" else 1, float(tol), int(ncv or 0), int(maxiter or 0),
-                          {"fp64": 0, "fp32": 1, "fp64df": 2}[precision], int(bool(return_eigenvectors)),
+                          _precision_code(precision), int(bool(return_eigenvectors)),
                           _lib.ptr(vv) if vv is not None else None, _lib.QS_MEM_HOST)
     vals = np.zeros(k)
     vecs = np.zeros((n, k), dtype=op.dtype, order="F") if return_eigenvectors else None
@@ -300,7 +306,7 @@ def evolve(H, v0, t0, times, eom="SE", iterate=False, imag_time=False, tol=1e-12
         raise DimensionMismatch("operator and vector dimensions do not match")
     out = np.zeros((H.Ns, ts.size), dtype=np.complex128, order="F")
     _lib.check(_lib.load().qs_evolve(H._h, _lib.ptr(v), float(t0), _lib.ptr(ts), ts.size, int(bool(imag_time)),
-                                     float(tol), int(krylov_dim), 1 if precision == "fp32" else 0, _lib.ptr(out)))
+                                     float(tol), int(krylov_dim), _precision_code(precision), _lib.ptr(out)))
     if iterate:
         return (out[:, i].copy() for i in range(ts.size))
     if scalar:
@@ -343,7 +349,7 @@ class ExpmMultiplyParallel:
             x = np.ascontiguousarray(cols[:, j], dtype=np.complex128)
             o = np.zeros_like(x)
             _lib.check(_lib.load().qs_expm_multiply(self.A._h, _lib.ptr(a), _lib.ptr(x), _lib.ptr(o), tol, 30,
-                                                    1 if precision == "fp32" else 0))
+                                                    _precision_code(precision)))
             res[:, j] = o
         res = res.reshape(v_in.shape)
         if work_array is not None:

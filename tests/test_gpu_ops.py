@@ -192,6 +192,43 @@ def test_evolve_symmetric_sector_vs_oracle(qs, ora):
     assert np.max(np.linalg.norm(got - want, axis=0)) < 1e-9
 
 
+@pytest.mark.parametrize("sym,model,L,nup,pauli", [
+    (dict(kblock=0, pblock=1, zblock=1), "j1j2", 16, 8, False),
+    (dict(kblock=3), "j1j2", 14, 7, False),
+    (dict(kblock=2), "tfim", 14, None, True),
+])
+def test_double_float_krylov_storage(qs, ora, sym, model, L, nup, pauli):
+    """Krylov vectors stored as hi+lo floats: eigenpairs and the exponential
+    action agree with the FP64 engine and the oracle to FP64-class accuracy."""
+    sp = spec(model, L)
+    b = qs.SpinBasis1D(L, nup=nup, pauli=pauli, **sym)
+    H = qs.Hamiltonian(b, models.to_terms(qs, sp))
+    rep = ora.RepBasis(L, nup=nup, pauli=pauli, **sym)
+    n = b.Ns
+    D = np.zeros((n, n), dtype=np.complex128)
+    e = np.zeros(n, dtype=np.complex128)
+    for j in range(n):
+        e[:] = 0
+        e[j] = 1
+        D[:, j] = rep.matvec(sp, e)
+    w = np.linalg.eigvalsh(D)
+    scale = np.abs(w).max()
+    vals, vecs = qs.eigsh(H, k=3, which="SA", tol=1e-12, precision="fp64df")
+    assert np.allclose(vals, w[:3], rtol=1e-11, atol=1e-11 * scale)
+    assert np.abs(D @ vecs - vecs * vals).max() < 1e-9 * scale
+    assert np.allclose(np.linalg.norm(vecs, axis=0), 1, atol=1e-12)
+    v = models.seeded(n, complex_=True)
+    v /= np.linalg.norm(v)
+    times = np.linspace(0.2, 1.0, 3)
+    got = qs.evolve(H, v, 0.0, times, tol=1e-11, precision="fp64df")
+    want = np.stack([sla.expm(-1j * t * D) @ v for t in times], axis=1)
+    assert np.max(np.abs(got - want)) < 1e-10
+    ref64 = qs.evolve(H, v, 0.0, times, tol=1e-11)
+    assert np.max(np.abs(got - ref64)) < 1e-10
+    E = qs.ExpmMultiplyParallel(H, -0.3 + 0.2j)
+    assert np.max(np.abs(E.apply(v, precision="fp64df") - sla.expm((-0.3 + 0.2j) * D) @ v)) < 1e-10
+
+
 def test_conjugated_complex_alpha_on_unreduced_basis(qs, ora):
     """The reference conjugates a complex alpha together with the term amplitudes
     when conjugated=true on an unreduced basis (src/operators.jl:2565, 2582) but
