@@ -225,13 +225,15 @@ QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *
 
 /* eigsh on nops Hermitian operators at once (e.g. every momentum / parity
  * sector of one model): the Lanczos iterations of all operators run in
- * lockstep, each step being one multi-sector launch per kernel over the
- * assembled operators (assembled here if needed); operators that converge
- * drop out.  Replaces the per-sector loop of block_diag_hamiltonian /
- * BlockOps (tools.jl:2213-2420) followed by eigsh on each block.  values:
- * nops * k, ascending per operator; vectors: NULL or nops pointers (each NULL
- * or Ns_i x k in the operator's dtype, host); infos: NULL or nops entries.
- * opts->v0 and opts->precision are ignored (seeded start vectors, FP64). */
+ * lockstep, each step being one launch per kernel over all operators'
+ * assembled forms (assembled here if needed), replayed from a captured CUDA
+ * graph; operators that converge drop out.  Replaces the per-sector loop of
+ * block_diag_hamiltonian / BlockOps (tools.jl:2213-2420) followed by eigsh on
+ * each block.  values: nops * k, ascending per operator; vectors: NULL or nops
+ * pointers (each NULL or Ns_i x k in the operator's dtype, host); infos: NULL
+ * or nops entries.  opts->precision: 0 FP64 Krylov vectors, 1 or 2
+ * double-float vectors on the FP32 pipe.  opts->v0 is ignored (seeded start
+ * vectors, the same seed as qs_eigsh). */
 QS_API int qs_eigsh_batch(qs_op *const *ops, int32_t nops, const qs_eigsh_opts *opts, double *values, void **vectors,
                           qs_eigsh_info *infos);
 

@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(kThreads) spmv_df_kernel(SpmvDFArgs da) {
 }
 
 // ----------------------------------------------------------- sliced ELL
-constexpr int kSlice = 32;
+constexpr int kSlice = kSellSlice;
 
 __global__ void sell_fill_kernel(const int64_t* rowptr, const uint32_t* words, const int32_t* cols,
                                  const uint16_t* codes, int packed, const int32_t* perm, const int64_t* sptr,

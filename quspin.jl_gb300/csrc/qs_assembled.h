@@ -5,6 +5,8 @@
 
 namespace qs {
 
+constexpr int kSellSlice = 32;   // rows per slice of the sliced-ELL layout
+
 struct Assembled {
     DevBuf rowptr;     // int64, n + 1
     DevBuf words;      // uint32 (column << code_bits) | code, when packed
@@ -20,9 +22,9 @@ struct Assembled {
     int code_bits = 0;
     bool packed = true;
     int lanes = 8;     // threads per row in the CSR SpMV
-    // sliced-ELL copy for the single-operator product: slices of 32 rows (a
-    // permutation that sorts rows by length inside 4096-row windows), words
-    // column-major inside a slice, one thread per row
+    // sliced-ELL copy: slices of kSellSlice consecutive rows in natural
+    // order, words column-major inside a slice (one thread per row), each
+    // row with its own length
     DevBuf sell_words;  // uint32 packed (or int32 column + uint16 code pairs as uint32/uint16 arrays)
     DevBuf sell_cols, sell_codes;
     DevBuf sell_ptr;    // int64 start of each slice

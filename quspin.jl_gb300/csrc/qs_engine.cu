@@ -1,0 +1,1046 @@
+// qs_engine.cu -- kernels and host side of the batched Krylov engine
+// (qs_engine.h), and the batched eigsh built on it.
+//
+// The reference solves symmetry sectors one at a time (block_diag_hamiltonian
+// / BlockOps, tools.jl:2213-2420, each an ARPACK run through eigsh,
+// src/operators.jl:1558-1640).  Here every sector is a slot and one launch of
+// each step kernel serves all of them.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <random>
+#include <tuple>
+
+#include "qs_blas.cuh"
+#include "qs_dense.h"
+#include "qs_df.cuh"
+#include "qs_engine.h"
+#include "qs_krylov.h"
+
+namespace qs {
+
+namespace {
+
+constexpr int kT = 256;       // threads per block
+constexpr int kJT = 8;        // vectors per dots block
+constexpr int kMaxM = 64;     // largest Krylov basis of a slot
+
+// ------------------------------------------------------------ arithmetic
+// The same kernel source runs on FP64 values (A = double) and on
+// double-float values (A = DF); a complex value is a pair of A.
+template <class A>
+struct CA {
+    A re, im;
+};
+
+__device__ __forceinline__ void mac(double& acc, double a, double b) { acc = fma(a, b, acc); }
+__device__ __forceinline__ void mac(DF& acc, DF a, DF b) { df_mac(acc, a.h, a.l, b.h, b.l); }
+__device__ __forceinline__ void msub(double& acc, double a, double b) { acc = fma(-a, b, acc); }
+__device__ __forceinline__ void msub(DF& acc, DF a, DF b) { df_mac(acc, -a.h, -a.l, b.h, b.l); }
+__device__ __forceinline__ double sub(double a, double b) { return a - b; }
+__device__ __forceinline__ DF sub(DF a, DF b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ double add(double a, double b) { return a + b; }
+__device__ __forceinline__ DF add(DF a, DF b) { return df_add(a, b); }
+__device__ __forceinline__ double mul(double a, double b) { return a * b; }
+__device__ __forceinline__ DF mul(DF a, DF b) { return df_mul(a, b); }
+__device__ __forceinline__ double to_d(double a) { return a; }
+__device__ __forceinline__ double to_d(DF a) { return df_to_double(a); }
+__device__ __forceinline__ double shfl(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ DF shfl(DF v, int o) { return df_shfl_xor(v, o, 32); }
+
+template <class A> __device__ __forceinline__ A zero();
+template <> __device__ __forceinline__ double zero<double>() { return 0.0; }
+template <> __device__ __forceinline__ DF zero<DF>() { return DF{0.f, 0.f}; }
+template <class A> __device__ __forceinline__ A one();
+template <> __device__ __forceinline__ double one<double>() { return 1.0; }
+template <> __device__ __forceinline__ DF one<DF>() { return DF{1.f, 0.f}; }
+template <class A> __device__ __forceinline__ A from_d(double v);
+template <> __device__ __forceinline__ double from_d<double>(double v) { return v; }
+template <> __device__ __forceinline__ DF from_d<DF>(double v) { return df_from_double(v); }
+
+// vector element i; 8 bytes per real component in both storages
+template <class A, bool CV> __device__ __forceinline__ CA<A> ldv(const void* p, int64_t i);
+template <> __device__ __forceinline__ CA<double> ldv<double, false>(const void* p, int64_t i) {
+    return CA<double>{((const double*)p)[i], 0.0};
+}
+template <> __device__ __forceinline__ CA<double> ldv<double, true>(const void* p, int64_t i) {
+    const double2 v = ((const double2*)p)[i];
+    return CA<double>{v.x, v.y};
+}
+template <> __device__ __forceinline__ CA<DF> ldv<DF, false>(const void* p, int64_t i) {
+    const float2 v = ((const float2*)p)[i];
+    return CA<DF>{DF{v.x, v.y}, DF{0.f, 0.f}};
+}
+template <> __device__ __forceinline__ CA<DF> ldv<DF, true>(const void* p, int64_t i) {
+    const float4 v = ((const float4*)p)[i];
+    return CA<DF>{DF{v.x, v.y}, DF{v.z, v.w}};
+}
+template <class A, bool CV> __device__ __forceinline__ void stv(void* p, int64_t i, CA<A> v);
+template <> __device__ __forceinline__ void stv<double, false>(void* p, int64_t i, CA<double> v) {
+    ((double*)p)[i] = v.re;
+}
+template <> __device__ __forceinline__ void stv<double, true>(void* p, int64_t i, CA<double> v) {
+    ((double2*)p)[i] = make_double2(v.re, v.im);
+}
+template <> __device__ __forceinline__ void stv<DF, false>(void* p, int64_t i, CA<DF> v) {
+    ((float2*)p)[i] = make_float2(v.re.h, v.re.l);
+}
+template <> __device__ __forceinline__ void stv<DF, true>(void* p, int64_t i, CA<DF> v) {
+    ((float4*)p)[i] = make_float4(v.re.h, v.re.l, v.im.h, v.im.l);
+}
+
+// matrix value of a code and diagonal of a row
+template <class A> __device__ __forceinline__ CA<A> ldtab(const SlotDev& S, int c);
+template <> __device__ __forceinline__ CA<double> ldtab<double>(const SlotDev& S, int c) {
+    const double2 v = __ldg(S.tab64 + c);
+    return CA<double>{v.x, v.y};
+}
+template <> __device__ __forceinline__ CA<DF> ldtab<DF>(const SlotDev& S, int c) {
+    const float4 v = __ldg(S.tabdf + c);
+    return CA<DF>{DF{v.x, v.y}, DF{v.z, v.w}};
+}
+template <class A> __device__ __forceinline__ CA<A> lddiag(const double2* d64, const float4* ddf, int64_t r);
+template <> __device__ __forceinline__ CA<double> lddiag<double>(const double2* d64, const float4*, int64_t r) {
+    const double2 v = d64[r];
+    return CA<double>{v.x, v.y};
+}
+template <> __device__ __forceinline__ CA<DF> lddiag<DF>(const double2*, const float4* ddf, int64_t r) {
+    const float4 v = ddf[r];
+    return CA<DF>{DF{v.x, v.y}, DF{v.z, v.w}};
+}
+template <class A> __device__ __forceinline__ A ldrsq(const void* t, int i);
+template <> __device__ __forceinline__ double ldrsq<double>(const void* t, int i) { return ((const double*)t)[i]; }
+template <> __device__ __forceinline__ DF ldrsq<DF>(const void* t, int i) {
+    const float2 v = ((const float2*)t)[i];
+    return DF{v.x, v.y};
+}
+
+__device__ __forceinline__ size_t esz(const SlotDev& S) { return S.cv ? 16 : 8; }
+__device__ __forceinline__ char* colp(const SlotDev& S, int c) { return (char*)S.V + (size_t)c * S.n * esz(S); }
+
+// ------------------------------------------------------------ SpMV
+// y = col(j + 1) = H col(j) on every stepping slot: sliced ELL, one thread per
+// row, the slot's value table staged in shared memory.
+template <class A, bool CV, bool CM>
+__device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA<A>* tab, bool smem_tab,
+                                          const A* rsq) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int64_t n = S.n;
+    const int64_t s0 = lb * S.spb, s1 = min(S.nslices, s0 + S.spb);
+    const void* x = colp(S, S.j);
+    void* y = colp(S, S.j + 1);
+    const int packed = S.packed, cb = S.code_bits;
+    const uint32_t cmask = S.code_mask;
+    const uint32_t* __restrict__ words = S.words;
+    const int32_t* __restrict__ cols = S.cols;
+    const uint16_t* __restrict__ codes = S.codes;
+    const uint16_t* __restrict__ len = S.len;
+    const uint16_t* __restrict__ stab = S.stab;
+    for (int64_t sl = s0 + warp; sl < s1; sl += nw) {
+        const int64_t r = sl * kSellSlice + lane;
+        if (r >= n) continue;
+        const int cnt = len[r];
+        const int64_t base = S.sptr[sl] + lane;
+        A ar = zero<A>(), ai = zero<A>();
+#pragma unroll 4
+        for (int t = 0; t < cnt; ++t) {
+            const int64_t o = base + (int64_t)t * kSellSlice;
+            uint32_t col, code;
+            if (packed) {
+                const uint32_t w = __ldg(words + o);
+                col = w >> cb;
+                code = w & cmask;
+            } else {
+                col = (uint32_t)__ldg(cols + o);
+                code = __ldg(codes + o);
+            }
+            const CA<A> v = smem_tab ? tab[code] : ldtab<A>(S, code);
+            const CA<A> xv = ldv<A, CV>(x, col);
+            mac(ar, v.re, xv.re);
+            if (CV) {
+                mac(ai, v.re, xv.im);
+                if (CM) {
+                    msub(ar, v.im, xv.im);
+                    mac(ai, v.im, xv.re);
+                }
+            }
+        }
+        const A sc = stab ? rsq[stab[r]] : one<A>();
+        CA<A> out;
+        out.re = mul(ar, sc);
+        out.im = CV ? mul(ai, sc) : zero<A>();
+        const CA<A> d = lddiag<A>(S.diag64, S.diagdf, r);
+        const CA<A> xr = ldv<A, CV>(x, r);
+        mac(out.re, d.re, xr.re);
+        if (CV) {
+            msub(out.re, d.im, xr.im);
+            mac(out.im, d.re, xr.im);
+            mac(out.im, d.im, xr.re);
+        }
+        stv<A, CV>(y, r, out);
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT) eng_spmv(const SlotDev* __restrict__ sl, const int* __restrict__ smap,
+                                               const void* __restrict__ rsqt) {
+    __shared__ CA<A> tab[1024];
+    __shared__ A rsq[kMaxGroup + 1];
+    const SlotDev& S = sl[smap[blockIdx.x]];
+    if (S.state != kSlotStep) return;
+    const bool smem_tab = S.ncodes <= 1024;
+    if (smem_tab)
+        for (int i = threadIdx.x; i < S.ncodes; i += blockDim.x) tab[i] = ldtab<A>(S, i);
+    if (S.stab)
+        for (int i = threadIdx.x; i <= S.max_stab; i += blockDim.x) rsq[i] = ldrsq<A>(rsqt, i);
+    __syncthreads();
+    const int64_t lb = blockIdx.x - S.sb_begin;
+    if (!S.cv) spmv_rows<A, false, false>(S, lb, tab, smem_tab, rsq);
+    else if (!S.cm) spmv_rows<A, true, false>(S, lb, tab, smem_tab, rsq);
+    else spmv_rows<A, true, true>(S, lb, tab, smem_tab, rsq);
+}
+
+// ------------------------------------------------------------ dots
+// mode 0 (step): partial[b][i] = <col i, col j+1>, i <= j;
+// mode 1 (normalise): partial[b][0] = <col ncol, col ncol>
+template <class A, bool CV>
+__device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t r1, int i0, int nv, const void* w,
+                                          A* re, A* im) {
+    const int64_t n = S.n;
+    const char* V = (const char*)S.V;
+    const size_t cs = (size_t)n * (CV ? 16 : 8);
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const CA<A> wv = ldv<A, CV>(w, r);
+#pragma unroll
+        for (int q = 0; q < kJT; ++q) {
+            if (i0 + q < nv) {
+                const CA<A> v = ldv<A, CV>(V + (size_t)(i0 + q) * cs, r);
+                mac(re[q], v.re, wv.re);
+                if (CV) {
+                    mac(re[q], v.im, wv.im);
+                    mac(im[q], v.re, wv.im);
+                    msub(im[q], v.im, wv.re);
+                }
+            }
+        }
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+                                               int mode, double* __restrict__ partial) {
+    const SlotDev& S = sl[rmap[blockIdx.x]];
+    if (S.state != (mode == 0 ? kSlotStep : kSlotNormalize)) return;
+    const int nv = mode == 0 ? S.j + 1 : 1;
+    const int i0 = blockIdx.y * kJT;
+    if (i0 >= nv) return;
+    const void* w = colp(S, mode == 0 ? S.j + 1 : S.ncol);
+    const int64_t lb = blockIdx.x - S.rb_begin;
+    const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
+    A re[kJT], im[kJT];
+#pragma unroll
+    for (int q = 0; q < kJT; ++q) re[q] = im[q] = zero<A>();
+    const int vbase = mode == 0 ? 0 : S.ncol;
+    if (S.cv) dots_rows<A, true>(S, r0, r1, vbase + i0, vbase + nv, w, re, im);
+    else dots_rows<A, false>(S, r0, r1, vbase + i0, vbase + nv, w, re, im);
+    __shared__ double sh[kT / 32][2 * kJT];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kJT; ++q) {
+        for (int o = 16; o > 0; o >>= 1) {
+            re[q] = add(re[q], shfl(re[q], o));
+            im[q] = add(im[q], shfl(im[q], o));
+        }
+        if (lane == 0) {
+            sh[wid][2 * q] = to_d(re[q]);
+            sh[wid][2 * q + 1] = to_d(im[q]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * kJT) {
+        double t = 0;
+        for (int q = 0; q < kT / 32; ++q) t += sh[q][threadIdx.x];
+        const int q = threadIdx.x / 2;
+        if (i0 + q < nv) partial[((size_t)blockIdx.x * mmax + i0 + q) * 2 + (threadIdx.x & 1)] = t;
+    }
+}
+
+// ------------------------------------------------------------ reduce
+// per slot and vector, the block partials summed in a fixed order.
+// mode 0: h1; 1: h2 and the record column; 2: the new norm; 3: normalise col 0
+__global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl, int mmax, int mode,
+                                                 const double* __restrict__ partial) {
+    const SlotDev& S = sl[blockIdx.x];
+    const int i = blockIdx.y;
+    if (mode == 3) {
+        if (S.state != kSlotNormalize || i) return;
+    } else {
+        if (S.state != kSlotStep) return;
+        if (mode == 2 ? i != 0 : i > S.j) return;
+    }
+    double re = 0, im = 0;
+    for (int b = threadIdx.x; b < S.rb_count; b += blockDim.x) {
+        re += partial[((size_t)(S.rb_begin + b) * mmax + i) * 2];
+        im += partial[((size_t)(S.rb_begin + b) * mmax + i) * 2 + 1];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    __shared__ double sr[kT / 32], si[kT / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        sr[wid] = re;
+        si[wid] = im;
+    }
+    __syncthreads();
+    if (threadIdx.x) return;
+    re = im = 0;
+    for (int q = 0; q < kT / 32; ++q) {
+        re += sr[q];
+        im += si[q];
+    }
+    const int ld = S.m + 1;
+    if (mode == 0) {
+        S.h1[i] = make_double2(re, im);
+    } else if (mode == 1) {
+        S.h2[i] = make_double2(re, im);
+        const double2 a = S.h1[i];
+        S.rec[(size_t)S.j * ld + i] = make_double2(a.x + re, a.y + im);
+    } else {
+        const double nb = sqrt(fmax(re, 0.0));
+        S.nrm[0] = re;
+        S.nrm[1] = nb > 0 ? 1.0 / nb : 0.0;
+        if (mode == 2) S.rec[(size_t)S.j * ld + S.j + 1] = make_double2(nb, 0.0);
+        else S.nrm[2] = nb;
+    }
+}
+
+// ------------------------------------------------------------ update
+// col(j+1) -= sum_i col(i) h_i (pass 0: h1, pass 1: h2); pass 1 also leaves
+// the block's part of ||col(j+1)||^2 in partial[b][0].
+template <class A, bool CV>
+__device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r1, int nv, const CA<A>* hs,
+                                         bool want_norm) {
+    const char* V = (const char*)S.V;
+    const size_t cs = (size_t)S.n * (CV ? 16 : 8);
+    void* w = (void*)(V + (size_t)(S.j + 1) * cs);
+    A nacc = zero<A>();
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        A ar = zero<A>(), ai = zero<A>();
+        for (int t = 0; t < nv; ++t) {
+            const CA<A> v = ldv<A, CV>(V + (size_t)t * cs, r);
+            const CA<A> h = hs[t];
+            mac(ar, v.re, h.re);
+            if (CV) {
+                msub(ar, v.im, h.im);
+                mac(ai, v.re, h.im);
+                mac(ai, v.im, h.re);
+            }
+        }
+        CA<A> o = ldv<A, CV>(w, r);
+        o.re = sub(o.re, ar);
+        if (CV) o.im = sub(o.im, ai);
+        stv<A, CV>(w, r, o);
+        if (want_norm) {
+            mac(nacc, o.re, o.re);
+            if (CV) mac(nacc, o.im, o.im);
+        }
+    }
+    return nacc;
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT) eng_update(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+                                                 int pass, double* __restrict__ partial) {
+    const SlotDev& S = sl[rmap[blockIdx.x]];
+    if (S.state != kSlotStep) return;
+    __shared__ CA<A> hs[kMaxM];
+    const int nv = S.j + 1;
+    const double2* h = pass ? S.h2 : S.h1;
+    for (int t = threadIdx.x; t < nv; t += blockDim.x) {
+        const double2 v = h[t];
+        hs[t] = CA<A>{from_d<A>(v.x), from_d<A>(v.y)};
+    }
+    __syncthreads();
+    const int64_t lb = blockIdx.x - S.rb_begin;
+    const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
+    A nacc = S.cv ? update_rows<A, true>(S, r0, r1, nv, hs, pass == 1) : update_rows<A, false>(S, r0, r1, nv, hs, pass == 1);
+    if (pass != 1) return;
+    for (int o = 16; o > 0; o >>= 1) nacc = add(nacc, shfl(nacc, o));
+    __shared__ double sh[kT / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = to_d(nacc);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int q = 0; q < kT / 32; ++q) t += sh[q];
+        partial[(size_t)blockIdx.x * mmax * 2] = t;
+        partial[(size_t)blockIdx.x * mmax * 2 + 1] = 0.0;
+    }
+}
+
+// ------------------------------------------------------------ scale / advance
+// mode 0: col(j+1) *= 1/beta on stepping slots; mode 1: col ncol on normalising slots
+template <class A>
+__global__ void __launch_bounds__(kT) eng_scale(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mode) {
+    const SlotDev& S = sl[rmap[blockIdx.x]];
+    if (S.state != (mode == 0 ? kSlotStep : kSlotNormalize)) return;
+    const A f = from_d<A>(S.nrm[1]);
+    void* w = colp(S, mode == 0 ? S.j + 1 : S.ncol);
+    const int64_t lb = blockIdx.x - S.rb_begin;
+    const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        if (S.cv) {
+            CA<A> v = ldv<A, true>(w, r);
+            v.re = mul(v.re, f);
+            v.im = mul(v.im, f);
+            stv<A, true>(w, r, v);
+        } else {
+            CA<A> v = ldv<A, false>(w, r);
+            v.re = mul(v.re, f);
+            stv<A, false>(w, r, v);
+        }
+    }
+}
+
+__global__ void eng_advance(SlotDev* sl, int nslots) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nslots) return;
+    SlotDev& S = sl[id];
+    if (S.state != kSlotStep) return;
+    S.j += 1;
+    if (S.j >= S.m) S.state = kSlotHold;
+}
+
+// ------------------------------------------------------------ rotate
+// V[:, out0 + c] = sum_{i < rot_in} V[:, i] Y[i, c] for c < p (through tmp),
+// then V[:, cdst] = V[:, carry]; rows are independent, each thread owns its rows.
+template <class A, bool CV>
+__device__ __forceinline__ void rotate_rows(const SlotDev& S, int64_t r0, int64_t r1) {
+    char* V = (char*)S.V;
+    char* T = (char*)S.tmp;
+    const size_t cs = (size_t)S.n * (CV ? 16 : 8);
+    const CA<A>* Y = (const CA<A>*)S.y;
+    const int nin = S.rot_in, p = S.p;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        for (int c = 0; c < p; ++c) {
+            A ar = zero<A>(), ai = zero<A>();
+            for (int i = 0; i < nin; ++i) {
+                const CA<A> v = ldv<A, CV>(V + (size_t)i * cs, r);
+                const CA<A> y = Y[(size_t)c * nin + i];
+                mac(ar, v.re, y.re);
+                msub(ar, v.im, y.im);
+                if (CV) {
+                    mac(ai, v.re, y.im);
+                    mac(ai, v.im, y.re);
+                }
+            }
+            stv<A, CV>(T + (size_t)c * cs, r, CA<A>{ar, ai});
+        }
+        for (int c = 0; c < p; ++c) stv<A, CV>(V + (size_t)(S.out0 + c) * cs, r, ldv<A, CV>(T + (size_t)c * cs, r));
+        if (S.carry >= 0) stv<A, CV>(V + (size_t)S.cdst * cs, r, ldv<A, CV>(V + (size_t)S.carry * cs, r));
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT) eng_rotate(const SlotDev* __restrict__ sl, const int* __restrict__ rmap) {
+    const SlotDev& S = sl[rmap[blockIdx.x]];
+    if (S.state != kSlotRotate) return;
+    const int64_t lb = blockIdx.x - S.rb_begin;
+    const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
+    if (S.cv) rotate_rows<A, true>(S, r0, r1);
+    else rotate_rows<A, false>(S, r0, r1);
+}
+
+// ------------------------------------------------------------ autotuner
+struct TuneKey {
+    bool df, cv, cm;
+    int size_class;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(df, cv, cm, size_class) < std::tie(o.df, o.cv, o.cm, o.size_class);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, Tiles> g_tuned;
+
+int size_class(int64_t n) { return (int)std::floor(2.0 * std::log2((double)std::max<int64_t>(n, 1))); }
+
+}  // namespace
+
+// ====================================================================== Engine
+Engine::Engine(bool df, cudaStream_t s) : df_(df), s_(s) {
+    std::vector<double> r64(kMaxGroup + 1, 0.0);
+    std::vector<float> rdf(2 * (kMaxGroup + 1), 0.f);
+    for (int i = 1; i <= kMaxGroup; ++i) {
+        r64[i] = 1.0 / std::sqrt((double)i);
+        df_split_host(r64[i], rdf[2 * i], rdf[2 * i + 1]);
+    }
+    rsq64_.alloc(r64.size() * sizeof(double));
+    rsqdf_.alloc(rdf.size() * sizeof(float));
+    QS_CUDA(cudaMemcpy(rsq64_.p, r64.data(), r64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    QS_CUDA(cudaMemcpy(rsqdf_.p, rdf.data(), rdf.size() * sizeof(float), cudaMemcpyHostToDevice));
+}
+
+Engine::~Engine() {
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+}
+
+Tiles Engine::tune(Op& op, int m, bool cv) {
+    const TuneKey key{df_, cv, op.complex_mat, size_class(op.basis->n)};
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) return it->second;
+    }
+    // time a few steps of this operator alone for every candidate tile pair
+    const int mt = std::min(m, 12);
+    Engine E(df_, s_);
+    int id = E.add(op, mt, cv, false);
+    E.seed(id, 1);
+    E.normalize({id});
+    cudaEvent_t e0, e1;
+    QS_CUDA(cudaEventCreate(&e0));
+    QS_CUDA(cudaEventCreate(&e1));
+    Tiles best;
+    float best_ms = 1e30f;
+    for (int rpb : {512, 1024, 2048})
+        for (int spb : {8, 16, 32}) {
+            E.slots_[id].d.rpb = rpb;
+            E.slots_[id].d.spb = spb;
+            E.maps_dirty_ = true;
+            E.start(id, 0);
+            E.run(2);  // captures the graph, warms up
+            E.start(id, 2);
+            QS_CUDA(cudaEventRecord(e0, s_));
+            E.run(std::min(6, mt - 2));
+            QS_CUDA(cudaEventRecord(e1, s_));
+            QS_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            QS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best.rpb = rpb;
+                best.spb = spb;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    launches_ += E.launches();
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tuned[key] = best;
+    return best;
+}
+
+size_t Engine::slot_bytes(int64_t n, int m, bool cv, int tmp_cols) {
+    const size_t es = cv ? 16 : 8;
+    const int tc = tmp_cols > 0 ? tmp_cols : m - 1;
+    return (size_t)(m + 1 + tc) * n * es + ((size_t)2 * m + (size_t)(m + 1) * m + (size_t)m * m) * 16 + 64;
+}
+
+int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols) {
+    if (m < 2 || m > kMaxM) throw Error(QS_ERR_ARGUMENT, "Krylov basis size must lie in 2:64");
+    if (op.complex_mat && !cv) throw Error(QS_ERR_ARGUMENT, "complex operators need complex vectors");
+    if (!op.assembled) op_assemble(op);
+    const Assembled& M = op.asm_;
+    if (!M.has_sell) throw Error(QS_ERR_UNSUPPORTED, "the batched engine needs the sliced assembled layout");
+    QS_CUDA(cudaStreamSynchronize(op.stream));
+    const int64_t n = op.basis->n;
+    Slot sl;
+    sl.op = &op;
+    SlotDev& d = sl.d;
+    d.sptr = M.sell_ptr.as<int64_t>();
+    d.len = M.sell_len.as<uint16_t>();
+    d.words = M.sell_words.as<uint32_t>();
+    d.cols = M.sell_cols.as<int32_t>();
+    d.codes = M.sell_codes.as<uint16_t>();
+    d.tab64 = M.table64.as<double2>();
+    d.tabdf = M.table_df.as<float4>();
+    d.stab = op.basis->symmetric ? op.basis->d_stab.as<uint16_t>() : nullptr;
+    d.diag64 = op.d_diag.as<double2>();
+    d.diagdf = op.d_diag_df.as<float4>();
+    d.code_mask = M.code_bits >= 32 ? 0xffffffffu : ((1u << M.code_bits) - 1u);
+    d.packed = M.packed;
+    d.code_bits = M.code_bits;
+    d.ncodes = M.ncodes;
+    d.max_stab = std::min(kMaxGroup, std::max(1, op.basis->group.ng));
+    d.cm = op.complex_mat;
+    d.cv = cv;
+    d.n = n;
+    d.nslices = M.nslices;
+    const size_t es = cv ? 16 : 8;
+    sl.V.alloc((size_t)(m + 1) * n * es);
+    const int tc = tmp_cols > 0 ? std::min(tmp_cols, m) : m - 1;
+    sl.tmp.alloc((size_t)tc * n * es);
+    QS_CUDA(cudaMemsetAsync(sl.V.p, 0, sl.V.bytes, s_));
+    // h1 (m), h2 (m), rec ((m+1) m) as double2, nrm (4 doubles)
+    const size_t nsmall = (size_t)2 * m + (size_t)(m + 1) * m;
+    sl.small.alloc(nsmall * sizeof(double2) + 4 * sizeof(double));
+    QS_CUDA(cudaMemsetAsync(sl.small.p, 0, sl.small.bytes, s_));
+    sl.y.alloc((size_t)m * m * 16);
+    d.V = sl.V.p;
+    d.tmp = sl.tmp.p;
+    d.h1 = sl.small.as<double2>();
+    d.h2 = d.h1 + m;
+    d.rec = d.h2 + m;
+    d.nrm = (double*)(d.rec + (size_t)(m + 1) * m);
+    d.y = sl.y.p;
+    d.m = m;
+    d.j = 0;
+    d.state = kSlotIdle;
+    d.carry = -1;
+    sl.tcols = tc;
+    Tiles t;
+    if (tune_tiles && n >= 4096 && m >= 4) t = tune(op, m, cv);
+    d.rpb = t.rpb;
+    d.spb = t.spb;
+    sl.live = true;
+    // reuse a dead slot index
+    int id = -1;
+    for (int i = 0; i < (int)slots_.size(); ++i)
+        if (!slots_[i].live) { id = i; break; }
+    if (id < 0) {
+        id = (int)slots_.size();
+        slots_.emplace_back();
+    }
+    slots_[id] = std::move(sl);
+    maps_dirty_ = dirty_ = true;
+    return id;
+}
+
+void Engine::remove(int id) {
+    if (!alive(id)) return;
+    QS_CUDA(cudaStreamSynchronize(s_));
+    slots_[id] = Slot();
+    maps_dirty_ = dirty_ = true;
+}
+
+void Engine::build_maps() {
+    nrb_ = nsb_ = 0;
+    mmax_ = 1;
+    for (auto& sl : slots_) {
+        SlotDev& d = sl.d;
+        if (!sl.live) {
+            d.state = kSlotIdle;
+            d.rb_begin = d.rb_count = d.sb_begin = d.sb_count = 0;
+            continue;
+        }
+        d.rb_begin = nrb_;
+        d.rb_count = (int)((d.n + d.rpb - 1) / d.rpb);
+        d.sb_begin = nsb_;
+        d.sb_count = (int)((d.nslices + d.spb - 1) / d.spb);
+        nrb_ += d.rb_count;
+        nsb_ += d.sb_count;
+        mmax_ = std::max(mmax_, d.m);
+    }
+    std::vector<int> rm(std::max(1, nrb_)), sm(std::max(1, nsb_));
+    for (int i = 0; i < (int)slots_.size(); ++i) {
+        const SlotDev& d = slots_[i].d;
+        for (int b = 0; b < d.rb_count; ++b) rm[d.rb_begin + b] = i;
+        for (int b = 0; b < d.sb_count; ++b) sm[d.sb_begin + b] = i;
+    }
+    if (rm.size() * sizeof(int) > cap_rmap_) {
+        cap_rmap_ = rm.size() * sizeof(int) * 2;
+        rmap_.alloc(cap_rmap_);
+    }
+    if (sm.size() * sizeof(int) > cap_smap_) {
+        cap_smap_ = sm.size() * sizeof(int) * 2;
+        smap_.alloc(cap_smap_);
+    }
+    const size_t pb = (size_t)std::max(1, nrb_) * mmax_ * 2 * sizeof(double);
+    if (pb > cap_partial_) {
+        cap_partial_ = pb * 2;
+        partial_.alloc(cap_partial_);
+    }
+    if ((int)slots_.size() > cap_slots_) {
+        cap_slots_ = std::max<int>(8, (int)slots_.size() * 2);
+        dslots_.alloc((size_t)cap_slots_ * sizeof(SlotDev));
+    }
+    QS_CUDA(cudaMemcpyAsync(rmap_.p, rm.data(), rm.size() * sizeof(int), cudaMemcpyHostToDevice, s_));
+    QS_CUDA(cudaMemcpyAsync(smap_.p, sm.data(), sm.size() * sizeof(int), cudaMemcpyHostToDevice, s_));
+    QS_CUDA(cudaStreamSynchronize(s_));
+    if (exec_) {
+        cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+    }
+    if (graph_) {
+        cudaGraphDestroy(graph_);
+        graph_ = nullptr;
+    }
+    maps_dirty_ = false;
+    dirty_ = true;
+}
+
+void Engine::sync_table() {
+    if (maps_dirty_) build_maps();
+    if (!dirty_) return;
+    std::vector<SlotDev> h(slots_.size());
+    for (size_t i = 0; i < slots_.size(); ++i) h[i] = slots_[i].d;
+    if (!h.empty())
+        QS_CUDA(cudaMemcpyAsync(dslots_.p, h.data(), h.size() * sizeof(SlotDev), cudaMemcpyHostToDevice, s_));
+    QS_CUDA(cudaStreamSynchronize(s_));
+    dirty_ = false;
+}
+
+void Engine::launch_step() {
+    const SlotDev* ds = dslots_.as<SlotDev>();
+    const int* rm = rmap_.as<int>();
+    const int* sm = smap_.as<int>();
+    double* pa = partial_.as<double>();
+    const int ns = (int)slots_.size();
+    const dim3 gd(nrb_, (mmax_ + kJT - 1) / kJT), gr(ns, mmax_);
+    if (df_) {
+        eng_spmv<DF><<<nsb_, kT, 0, s_>>>(ds, sm, rsqdf_.p);
+        eng_dots<DF><<<gd, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
+        eng_reduce<<<gr, kT, 0, s_>>>(ds, mmax_, 0, pa);
+        eng_update<DF><<<nrb_, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
+        eng_dots<DF><<<gd, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
+        eng_reduce<<<gr, kT, 0, s_>>>(ds, mmax_, 1, pa);
+        eng_update<DF><<<nrb_, kT, 0, s_>>>(ds, rm, mmax_, 1, pa);
+        eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 2, pa);
+        eng_scale<DF><<<nrb_, kT, 0, s_>>>(ds, rm, 0);
+    } else {
+        eng_spmv<double><<<nsb_, kT, 0, s_>>>(ds, sm, rsq64_.p);
+        eng_dots<double><<<gd, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
+        eng_reduce<<<gr, kT, 0, s_>>>(ds, mmax_, 0, pa);
+        eng_update<double><<<nrb_, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
+        eng_dots<double><<<gd, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
+        eng_reduce<<<gr, kT, 0, s_>>>(ds, mmax_, 1, pa);
+        eng_update<double><<<nrb_, kT, 0, s_>>>(ds, rm, mmax_, 1, pa);
+        eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 2, pa);
+        eng_scale<double><<<nrb_, kT, 0, s_>>>(ds, rm, 0);
+    }
+    eng_advance<<<(ns + 127) / 128, 128, 0, s_>>>(dslots_.as<SlotDev>(), ns);
+}
+
+void Engine::capture() {
+    QS_CUDA(cudaStreamBeginCapture(s_, cudaStreamCaptureModeRelaxed));
+    launch_step();
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s_, &g);
+    if (e != cudaSuccess) throw Error(QS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    graph_ = g;
+    QS_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
+}
+
+void Engine::start(int id, int j) {
+    SlotDev& d = slots_[id].d;
+    if (j < 0 || j >= d.m) throw Error(QS_ERR_ARGUMENT, "start column outside the Krylov basis");
+    d.j = j;
+    d.state = kSlotStep;
+    dirty_ = true;
+}
+
+int Engine::steps_to_event() const {
+    int best = 0;
+    for (const auto& sl : slots_)
+        if (sl.live && sl.d.state == kSlotStep) {
+            const int left = sl.d.m - sl.d.j;
+            best = best == 0 ? left : std::min(best, left);
+        }
+    return best;
+}
+
+void Engine::run(int nsteps) {
+    if (nsteps <= 0) return;
+    sync_table();
+    if (nrb_ == 0) return;
+    if (!exec_) capture();
+    for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
+    launches_ += 10 * (int64_t)nsteps;
+    // mirror the device step counters
+    for (auto& sl : slots_) {
+        if (!sl.live || sl.d.state != kSlotStep) continue;
+        const int adv = std::min(nsteps, sl.d.m - sl.d.j);
+        sl.d.j += adv;
+        sl.matvecs += adv;
+        if (sl.d.j >= sl.d.m) sl.d.state = kSlotHold;
+    }
+}
+
+void Engine::seed(int id, uint64_t sd) {
+    const SlotDev& d = slots_[id].d;
+    std::mt19937_64 rng(sd);
+    std::normal_distribution<double> nd(0.0, 1.0);
+    std::vector<double> h((d.cv ? 2 : 1) * d.n);
+    for (auto& v : h) v = nd(rng);
+    load(id, 0, h.data(), false);
+}
+
+void Engine::load(int id, int col, const double* v, bool device) {
+    const SlotDev& d = slots_[id].d;
+    const VKind k64 = d.cv ? VKind::C128 : VKind::F64;
+    const VKind ks = df_ ? (d.cv ? VKind::CDF64 : VKind::DF64) : k64;
+    const size_t bytes = (size_t)d.n * (d.cv ? 16 : 8);
+    char* dst = (char*)d.V + (size_t)col * bytes;
+    DevBuf st;
+    const void* src = v;
+    if (!device) {
+        st.alloc(bytes);
+        QS_CUDA(cudaMemcpyAsync(st.p, v, bytes, cudaMemcpyHostToDevice, s_));
+        src = st.p;
+    }
+    convert_vec(src, k64, dst, ks, d.n, s_);
+    ++launches_;
+    QS_CUDA(cudaStreamSynchronize(s_));
+}
+
+void Engine::store(int id, int col, double* out, bool device) {
+    const SlotDev& d = slots_[id].d;
+    const VKind k64 = d.cv ? VKind::C128 : VKind::F64;
+    const VKind ks = df_ ? (d.cv ? VKind::CDF64 : VKind::DF64) : k64;
+    const size_t bytes = (size_t)d.n * (d.cv ? 16 : 8);
+    const char* src = (const char*)d.V + (size_t)col * bytes;
+    if (device) {
+        convert_vec(src, ks, out, k64, d.n, s_);
+    } else {
+        DevBuf st(bytes);
+        convert_vec(src, ks, st.p, k64, d.n, s_);
+        QS_CUDA(cudaMemcpyAsync(out, st.p, bytes, cudaMemcpyDeviceToHost, s_));
+    }
+    ++launches_;
+    QS_CUDA(cudaStreamSynchronize(s_));
+}
+
+std::vector<double> Engine::normalize(const std::vector<int>& ids, int col) {
+    std::vector<int> saved(ids.size());
+    for (size_t q = 0; q < ids.size(); ++q) {
+        SlotDev& d = slots_[ids[q]].d;
+        if (col < 0 || col > d.m) throw Error(QS_ERR_ARGUMENT, "normalised column outside the Krylov basis");
+        saved[q] = d.state;
+        d.state = kSlotNormalize;
+        d.ncol = col;
+    }
+    dirty_ = true;
+    sync_table();
+    const SlotDev* ds = dslots_.as<SlotDev>();
+    const int* rm = rmap_.as<int>();
+    double* pa = partial_.as<double>();
+    const int ns = (int)slots_.size();
+    if (nrb_ > 0 && !ids.empty()) {
+        if (df_) {
+            eng_dots<DF><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 1, pa);
+            eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 3, pa);
+            eng_scale<DF><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
+        } else {
+            eng_dots<double><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 1, pa);
+            eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 3, pa);
+            eng_scale<double><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
+        }
+        QS_CUDA(cudaGetLastError());
+        launches_ += 3;
+    }
+    std::vector<double> out(ids.size());
+    for (size_t q = 0; q < ids.size(); ++q)
+        QS_CUDA(cudaMemcpyAsync(&out[q], slots_[ids[q]].d.nrm + 2, sizeof(double), cudaMemcpyDeviceToHost, s_));
+    QS_CUDA(cudaStreamSynchronize(s_));
+    for (size_t q = 0; q < ids.size(); ++q) slots_[ids[q]].d.state = saved[q];
+    dirty_ = true;
+    return out;
+}
+
+void Engine::rotate(const std::vector<RotReq>& reqs) {
+    if (reqs.empty()) return;
+    std::vector<int> saved(reqs.size());
+    for (size_t q = 0; q < reqs.size(); ++q) {
+        const RotReq& R = reqs[q];
+        Slot& sl = slots_[R.id];
+        SlotDev& d = sl.d;
+        const bool bad = R.nin < 0 || R.nin > d.m || R.p < 0 || R.p > sl.tcols || (R.p > 0 && R.nin < 1) ||
+                         R.out0 < 0 || R.out0 + R.p > d.m + 1 || R.Y.size() != (size_t)R.nin * R.p ||
+                         (R.carry >= 0 && (R.carry > d.m || R.cdst < 0 || R.cdst > d.m));
+        if (bad) throw Error(QS_ERR_ARGUMENT, "rotation shape outside the Krylov basis");
+        if (R.p > 0) {
+            // coefficients in the storage format: double2 or float4 (hi, lo pairs)
+            std::vector<double> c64;
+            std::vector<float> cdf;
+            const void* src;
+            size_t bytes;
+            if (df_) {
+                cdf.resize(4 * R.Y.size());
+                for (size_t i = 0; i < R.Y.size(); ++i) {
+                    df_split_host(R.Y[i].real(), cdf[4 * i], cdf[4 * i + 1]);
+                    df_split_host(R.Y[i].imag(), cdf[4 * i + 2], cdf[4 * i + 3]);
+                }
+                src = cdf.data();
+                bytes = cdf.size() * sizeof(float);
+            } else {
+                c64.resize(2 * R.Y.size());
+                for (size_t i = 0; i < R.Y.size(); ++i) {
+                    c64[2 * i] = R.Y[i].real();
+                    c64[2 * i + 1] = R.Y[i].imag();
+                }
+                src = c64.data();
+                bytes = c64.size() * sizeof(double);
+            }
+            QS_CUDA(cudaMemcpyAsync(d.y, src, bytes, cudaMemcpyHostToDevice, s_));
+            QS_CUDA(cudaStreamSynchronize(s_));
+        }
+        saved[q] = d.state;
+        d.state = kSlotRotate;
+        d.rot_in = R.nin;
+        d.p = R.p;
+        d.out0 = R.out0;
+        d.carry = R.carry;
+        d.cdst = R.cdst;
+    }
+    dirty_ = true;
+    sync_table();
+    if (nrb_ > 0) {
+        if (df_) eng_rotate<DF><<<nrb_, kT, 0, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>());
+        else eng_rotate<double><<<nrb_, kT, 0, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>());
+        QS_CUDA(cudaGetLastError());
+        ++launches_;
+    }
+    for (size_t q = 0; q < reqs.size(); ++q) {
+        SlotDev& d = slots_[reqs[q].id].d;
+        d.state = saved[q] == kSlotRotate ? kSlotIdle : saved[q];
+        d.carry = -1;
+        d.p = 0;
+    }
+    dirty_ = true;
+}
+
+void Engine::record(int id, std::vector<cd>& H) {
+    const SlotDev& d = slots_[id].d;
+    std::vector<double> h((size_t)2 * (d.m + 1) * d.m);
+    QS_CUDA(cudaMemcpyAsync(h.data(), d.rec, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s_));
+    QS_CUDA(cudaStreamSynchronize(s_));
+    H.resize((size_t)(d.m + 1) * d.m);
+    for (size_t i = 0; i < H.size(); ++i) H[i] = cd(h[2 * i], h[2 * i + 1]);
+}
+
+// ================================================================ batched eigsh
+// Thick-restart Lanczos (the iteration of eigsh in qs_krylov.cu) on every
+// operator at once; values: nops * k, ascending per operator.
+void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, void** vectors, qs_eigsh_info* infos) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (nops <= 0) throw Error(QS_ERR_ARGUMENT, "no operators");
+    const int k = o.k;
+    if (o.which != 0 && o.which != 1) throw Error(QS_ERR_UNSUPPORTED, "which must be SA or LA on this engine");
+    int m = o.ncv > 0 ? o.ncv : std::max(20, 2 * k + 1);
+    m = std::min(m, kMaxM);
+    for (int i = 0; i < nops; ++i) {
+        Op& op = *ops[i];
+        if (!op.hermitian) throw Error(QS_ERR_UNSUPPORTED, "eigsh on this engine needs Hermitian operators");
+        const int64_t n = op.basis->n;
+        if (k < 1 || k >= n - 1) throw Error(QS_ERR_ARGUMENT, "batched eigsh needs 1 <= k < Ns - 1 for every operator");
+        m = (int)std::min<int64_t>(m, n);
+    }
+    if (m <= k) throw Error(QS_ERR_ARGUMENT, "ncv must exceed k");
+    const double tol = o.tol > 0 ? o.tol : 2.220446049250313e-16;
+    const int maxiter = o.maxiter > 0 ? o.maxiter : 300;
+    const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
+    Engine E(o.precision != 0, ops[0]->stream);
+    std::vector<int> id(nops);
+    for (int i = 0; i < nops; ++i) {
+        id[i] = E.add(*ops[i], m, ops[i]->complex_mat);
+        E.seed(id[i], 20261203ull);
+    }
+    E.normalize(id);
+    struct St {
+        std::vector<double> T;
+        std::vector<double> theta;
+        double beta = 0, maxrel = 0;
+        int nconv = 0, restarts = 0, j0 = 0;
+        bool done = false;
+    };
+    std::vector<St> st(nops);
+    for (int i = 0; i < nops; ++i) {
+        st[i].T.assign((size_t)m * m, 0.0);
+        E.start(id[i], 0);
+    }
+    const int p = std::max(std::min(m - 2, k + (m - k) / 2), std::min(k, m - 1));
+    std::vector<cd> H;
+    int left = nops;
+    while (left > 0) {
+        const int steps = E.steps_to_event();
+        if (steps <= 0) throw Error(QS_ERR_CUDA, "batched eigsh lost its stepping slots");
+        E.run(steps);
+        std::vector<RotReq> rot;
+        std::vector<int> fin_slots;
+        for (int i = 0; i < nops; ++i) {
+            St& s = st[i];
+            if (s.done || E.slot(id[i]).state != kSlotHold) continue;
+            E.record(id[i], H);
+            for (int j = s.j0; j < m; ++j) {
+                s.T[(size_t)j * m + j] = H[(size_t)j * (m + 1) + j].real();
+                const double b = H[(size_t)j * (m + 1) + j + 1].real();
+                if (j + 1 < m) s.T[(size_t)j * m + j + 1] = s.T[(size_t)(j + 1) * m + j] = b;
+                else s.beta = b;
+            }
+            std::vector<double> w, Y;
+            sym_eig(m, s.T, w, Y);
+            std::vector<int> order(m);
+            for (int q = 0; q < m; ++q) order[q] = o.which == 0 ? q : m - 1 - q;
+            int nc = 0;
+            double mr = 0;
+            for (int q = 0; q < k; ++q) {
+                const int c = order[q];
+                const double bound = std::fabs(s.beta * Y[(size_t)(m - 1) * m + c]);
+                mr = std::max(mr, bound / std::max(eps23, std::fabs(w[c])));
+                if (bound <= tol * std::max(eps23, std::fabs(w[c]))) ++nc;
+            }
+            s.nconv = nc;
+            s.maxrel = mr;
+            s.theta.assign(k, 0.0);
+            for (int q = 0; q < k; ++q) s.theta[q] = w[order[q]];
+            const bool fin = nc >= k || s.restarts >= maxiter - 1;
+            const int keep = fin ? k : p;
+            std::vector<cd> Yc((size_t)m * keep);
+            for (int q = 0; q < keep; ++q)
+                for (int r = 0; r < m; ++r) Yc[(size_t)q * m + r] = cd(Y[(size_t)r * m + order[q]], 0.0);
+            RotReq R;
+            R.id = id[i];
+            R.Y = std::move(Yc);
+            R.nin = m;
+            R.p = keep;
+            R.carry = fin ? -1 : m;   // thick restart: the residual direction follows the Ritz vectors
+            R.cdst = keep;
+            rot.push_back(std::move(R));
+            if (fin) {
+                fin_slots.push_back(i);
+            } else {
+                std::fill(s.T.begin(), s.T.end(), 0.0);
+                for (int q = 0; q < p; ++q) {
+                    s.T[(size_t)q * m + q] = w[order[q]];
+                    const double c = s.beta * Y[(size_t)(m - 1) * m + order[q]];
+                    s.T[(size_t)q * m + p] = s.T[(size_t)p * m + q] = c;
+                }
+                s.j0 = p;
+                ++s.restarts;
+            }
+        }
+        E.rotate(rot);
+        for (const RotReq& R : rot)
+            if (R.carry >= 0) E.start(R.id, p);
+        for (int i : fin_slots) {
+            St& s = st[i];
+            s.done = true;
+            --left;
+            if (s.nconv < k) throw Error(QS_ERR_NOT_CONVERGED, "batched eigsh did not converge within maxiter restarts");
+            for (int q = 0; q < k; ++q) values[(size_t)i * k + q] = s.theta[q];
+            if (vectors && vectors[i]) {
+                const int64_t n = ops[i]->basis->n;
+                const int comps = ops[i]->complex_mat ? 2 : 1;
+                for (int q = 0; q < k; ++q) E.store(id[i], q, (double*)vectors[i] + (size_t)q * n * comps, false);
+            }
+            if (infos) {
+                infos[i].nconv = s.nconv;
+                infos[i].restarts = s.restarts;
+                infos[i].matvecs = E.matvecs(id[i]);
+                infos[i].max_rel_residual = s.maxrel;
+                infos[i].seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            }
+            E.remove(id[i]);
+        }
+    }
+    QS_CUDA(cudaStreamSynchronize(E.stream()));
+    note_launches(E.launches());
+}
+
+}  // namespace qs

@@ -1,0 +1,151 @@
+// qs_engine.h -- the batched Krylov engine: many Krylov processes ("slots"),
+// each on its own assembled operator and its own vectors, advanced together.
+//
+// One Lanczos/Arnoldi step of every stepping slot is a fixed sequence of ten
+// launches (SpMV, two CGS passes of dots + reduce + update, norm, scale,
+// advance), each covering all slots through a block -> slot map.  The step
+// counters live on the device, so the sequence is captured once in a CUDA
+// graph and replayed; the host only meets the device when a slot has filled
+// its basis (restart, convergence test, exponential).  The projected matrix of
+// every slot is recorded on the device in FP64 (column j of the Hessenberg
+// matrix: the summed CGS2 coefficients and the new norm).
+//
+// Vectors are stored either in FP64 or as double-float pairs (hi + lo float,
+// arithmetic on the FP32 pipe); both take 8 bytes per real component.  Each
+// slot has its own real/complex vector flag, so a slot's arithmetic does not
+// depend on which other slots share the launches.  Tile shapes (rows per
+// BLAS block, slices per SpMV block) are per slot, chosen by a timing
+// autotuner and cached per (storage, flags, size class).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <cstdint>
+#include <vector>
+
+#include "qs_internal.h"
+
+namespace qs {
+
+using cd = std::complex<double>;
+
+enum SlotState : int32_t { kSlotIdle = 0, kSlotStep = 1, kSlotRotate = 2, kSlotHold = 3, kSlotNormalize = 4 };
+
+// Device descriptor of one slot.
+struct SlotDev {
+    // operator: sliced ELL of the assembled form
+    const int64_t* sptr;
+    const uint16_t* len;
+    const uint32_t* words;
+    const int32_t* cols;
+    const uint16_t* codes;
+    const double2* tab64;   // complex value per code
+    const float4* tabdf;    // per code: re hi, re lo, im hi, im lo
+    const uint16_t* stab;   // stabiliser order per row (null without symmetry)
+    const double2* diag64;  // complex diagonal
+    const float4* diagdf;
+    uint32_t code_mask;
+    int32_t packed, code_bits, ncodes, max_stab;
+    int32_t cm, cv;         // complex matrix elements / complex vectors
+    int64_t n, nslices;
+    // Krylov storage
+    void* V;                // m + 1 columns of n
+    void* tmp;              // m columns of n (rotation)
+    double2* h1;            // m first-pass CGS coefficients
+    double2* h2;            // m second-pass CGS coefficients
+    double2* rec;           // (m + 1) x m projected matrix, column-major
+    void* y;                // rotation coefficients, rot_in x p column-major (storage format)
+    double* nrm;            // [0] squared norm, [1] 1 / norm, [2] norm of column 0 when normalised
+    int32_t m, j, state;
+    // rotation: V[:, out0 + c] = sum_{i < rot_in} V[:, i] Y[i, c] for c < p, then
+    // V[:, cdst] = V[:, carry] when carry >= 0
+    int32_t rot_in, p, out0, carry, cdst;
+    int32_t ncol;           // column normalised by normalize()
+    // tiles
+    int32_t rpb, spb;       // rows per BLAS block, slices per SpMV block
+    int32_t rb_begin, rb_count, sb_begin, sb_count;
+};
+
+struct Tiles {
+    int rpb = 1024, spb = 8;
+};
+
+// One slot's part of a rotate() call.
+struct RotReq {
+    int id = 0;
+    std::vector<cd> Y;   // nin x p, column-major
+    int nin = 0, p = 0, out0 = 0, carry = -1, cdst = 0;
+};
+
+class Engine {
+   public:
+    Engine(bool df, cudaStream_t s);
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    bool df() const { return df_; }
+    cudaStream_t stream() const { return s_; }
+    // Adds a slot of basis size m on an assembled operator (assembled here if
+    // needed).  cv: complex vectors (required for complex operators); tmp_cols:
+    // most rotation outputs (m - 1 when 0).
+    int add(Op& op, int m, bool cv, bool tune = true, int tmp_cols = 0);
+    // device bytes add() would allocate for a slot
+    static size_t slot_bytes(int64_t n, int m, bool cv, int tmp_cols = 0);
+    void remove(int id);
+    int count() const { return (int)slots_.size(); }
+    const SlotDev& slot(int id) const { return slots_[id].d; }
+    SlotDev& slot_mut(int id) { dirty_ = true; return slots_[id].d; }
+    bool alive(int id) const { return id >= 0 && id < (int)slots_.size() && slots_[id].live; }
+    Op& op(int id) { return *slots_[id].op; }
+
+    // column 0 <- seeded normal entries / an FP64 vector (host or device; real
+    // for real-vector slots, interleaved complex otherwise)
+    void seed(int id, uint64_t seed);
+    void load(int id, int col, const double* v, bool device);
+    // FP64 copy of a column (host or device destination)
+    void store(int id, int col, double* out, bool device);
+    // column col /= ||column col|| for the listed slots; returns the norms
+    std::vector<double> normalize(const std::vector<int>& ids, int col = 0);
+    // one launch for all listed rotations (RotReq)
+    void rotate(const std::vector<RotReq>& reqs);
+    // Starts stepping slot id from column j (columns 0..j orthonormal).
+    void start(int id, int j);
+    // Replays the step graph nsteps times (slots at m stop by themselves).
+    void run(int nsteps);
+    // Steps left before the first stepping slot fills its basis (0: none stepping).
+    int steps_to_event() const;
+    // Host copy of the projected matrix record ((m + 1) x m, column-major).
+    void record(int id, std::vector<cd>& H);
+    int64_t launches() const { return launches_; }
+    int64_t matvecs(int id) const { return slots_[id].matvecs; }
+
+   private:
+    struct Slot {
+        Op* op = nullptr;
+        SlotDev d{};
+        DevBuf V, tmp, small, y;
+        int tcols = 0;    // columns of tmp
+        bool live = false;
+        int64_t matvecs = 0;
+    };
+    void sync_table();
+    void build_maps();
+    void capture();
+    void launch_step();
+    Tiles tune(Op& op, int m, bool cv);
+    bool df_;
+    cudaStream_t s_;
+    std::vector<Slot> slots_;
+    DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_;
+    int nrb_ = 0, nsb_ = 0, mmax_ = 1, cap_slots_ = 0;
+    size_t cap_partial_ = 0, cap_rmap_ = 0, cap_smap_ = 0;
+    bool dirty_ = true, maps_dirty_ = true;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    int64_t launches_ = 0;
+    friend struct EngineTuner;
+};
+
+}  // namespace qs

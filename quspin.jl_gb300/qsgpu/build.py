@@ -23,7 +23,7 @@ SOURCES = [
     "qs_krylov.cu",
     "qs_assembled.cu",
     "qs_noalloc.cu",
-    "qs_batch.cu",
+    "qs_engine.cu",
     "qs_dense.cpp",
     "qs_op.cpp",
     "qs_capi.cpp",

@@ -268,17 +268,21 @@ def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, nc
     return (vals, vecs) if return_eigenvectors else vals
 
 
-def eigsh_batch(ops, k=1, which="SA", tol=0.0, ncv=None, maxiter=None, return_eigenvectors=False, infos=None):
-    """eigsh(op; k, which) on every operator of `ops` at once (one multi-sector
-    launch per Lanczos step).  Returns an (len(ops), k) array of eigenvalues and,
-    when asked, one Ns_i x k vector block per operator."""
+def eigsh_batch(ops, k=1, which="SA", tol=0.0, ncv=None, maxiter=None, return_eigenvectors=False, infos=None,
+                precision="fp64"):
+    """eigsh(op; k, which) on every operator of `ops` at once: each Lanczos
+    step is one launch per kernel for all operators, replayed from a CUDA
+    graph.  precision "fp64" stores the Krylov vectors in FP64, "fp64df" (or
+    "fp32") as double-float pairs on the FP32 pipe.  Returns an (len(ops), k)
+    array of eigenvalues and, when asked, one Ns_i x k vector block per
+    operator."""
     w = str(which).upper()
     if w not in ("SA", "LA"):
         raise ArgumentError("which must be SA or LA on this engine")
     n = len(ops)
     arr = (ctypes.c_void_p * n)(*[o._h for o in ops])
-    opts = _lib.EigshOpts(int(k), 0 if w == "SA" else 1, float(tol), int(ncv or 0), int(maxiter or 0), 0, 0,
-                          None, _lib.QS_MEM_HOST)
+    opts = _lib.EigshOpts(int(k), 0 if w == "SA" else 1, float(tol), int(ncv or 0), int(maxiter or 0),
+                          _precision_code(precision), 0, None, _lib.QS_MEM_HOST)
     vals = np.zeros((n, int(k)))
     vecs = None
     vptrs = None

@@ -20,7 +20,8 @@ def sectors(qs, L, nup, J2):
     return out
 
 
-def test_batched_ground_states_all_sectors(qs, ora):
+@pytest.mark.parametrize("precision", ["fp64", "fp64df"])
+def test_batched_ground_states_all_sectors(qs, ora, precision):
     L, nup = 14, 7
     sp = models.j1j2(L, 1.0, 0.3)
     terms = models.to_terms(qs, sp)
@@ -40,7 +41,8 @@ def test_batched_ground_states_all_sectors(qs, ora):
             H[:, j] = rep.matvec(sp, e)
         dense0.append(np.linalg.eigvalsh(H)[:2])
     infos = []
-    vals, vecs = qs.eigsh_batch(ops, k=2, tol=1e-12, return_eigenvectors=True, infos=infos)
+    vals, vecs = qs.eigsh_batch(ops, k=2, tol=1e-12, return_eigenvectors=True, infos=infos, precision=precision)
+    assert all(i["nconv"] >= 2 for i in infos)
     for i, op in enumerate(ops):
         assert np.allclose(vals[i], dense0[i], rtol=1e-10, atol=1e-10), (syms[i], vals[i], dense0[i])
         res = op.dot(vecs[i]) - vecs[i] * vals[i]
@@ -51,3 +53,45 @@ def test_batched_ground_states_all_sectors(qs, ora):
     full = qs.Hamiltonian(qs.SpinBasis1D(L, nup=nup, pauli=False), terms)
     e0 = qs.eigsh(full, k=1, tol=1e-12, return_eigenvectors=False)[0]
     assert abs(vals[:, 0].min() - e0) < 1e-10 * abs(e0)
+
+
+def test_batched_result_independent_of_batch(qs):
+    """A sector's eigenpairs are the same solved alone and inside a batch: each
+    slot's arithmetic and reductions depend only on its own operator."""
+    L, nup = 16, 8
+    terms = models.to_terms(qs, models.j1j2(L, 1.0, 0.5))
+    syms = [dict(kblock=0, pblock=1), dict(kblock=3), dict(kblock=8, pblock=-1), dict(kblock=5)]
+    ops = [qs.Hamiltonian(qs.SpinBasis1D(L, nup=nup, pauli=False, **s), terms) for s in syms]
+    for precision in ("fp64", "fp64df"):
+        together, vt = qs.eigsh_batch(ops, k=1, tol=1e-12, return_eigenvectors=True, precision=precision)
+        for i, op in enumerate(ops):
+            alone, va = qs.eigsh_batch([op], k=1, tol=1e-12, return_eigenvectors=True, precision=precision)
+            assert together[i, 0] == alone[0, 0], (precision, i)
+            assert np.array_equal(vt[i], va[0]), (precision, i)
+
+
+def test_batched_mixed_real_and_complex_sizes(qs, ora):
+    """Sectors of very different sizes, real and complex, with k=3."""
+    L = 12
+    sp = models.xxz(L, 1.0, 0.5)
+    terms = models.to_terms(qs, sp)
+    syms = [(6, dict()), (6, dict(kblock=1)), (4, dict(kblock=0)),
+            (5, dict(kblock=2))]
+    ops, dense = [], []
+    for nup, sym in syms:
+        b = qs.SpinBasis1D(L, nup=nup, pauli=False, **sym)
+        ops.append(qs.Hamiltonian(b, terms))
+        rep = ora.RepBasis(L, nup=nup, pauli=False, **sym)
+        n = rep.Ns
+        H = np.zeros((n, n), dtype=np.complex128)
+        e = np.zeros(n, dtype=np.complex128)
+        for j in range(n):
+            e[:] = 0
+            e[j] = 1
+            H[:, j] = rep.matvec(sp, e)
+        dense.append(np.linalg.eigvalsh(H)[:3])
+    for precision in ("fp64", "fp64df"):
+        vals, vecs = qs.eigsh_batch(ops, k=3, tol=1e-12, return_eigenvectors=True, precision=precision)
+        for i, op in enumerate(ops):
+            assert np.allclose(vals[i], dense[i], rtol=1e-10, atol=1e-10), (precision, i)
+            assert np.abs(op.dot(vecs[i]) - vecs[i] * vals[i]).max() < 1e-8
