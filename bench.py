@@ -341,6 +341,93 @@ def section_c4(qs, torch):
             "ground_energy": float(np.min(vs))}
 
 
+def serving_requests(n_req, rate, seed=20261203):
+    """The served mix: Poisson arrivals, L uniform in {18, 20, ..., 30}, nup
+    uniform in [L/2-2, L/2], kblock uniform in [0, L), 70 % eigsh k=1 (tol
+    1e-10) and 30 % evolve to t ~ U[0.5, 5] (krylov_dim 30, tol 1e-9) on the
+    J1-J2 chain (J2 = 0.5), seeded start vectors."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    reqs = []
+    for i in range(n_req):
+        L = int(rng.choice(np.arange(18, 31, 2)))
+        nup = int(rng.integers(L // 2 - 2, L // 2 + 1))
+        k = int(rng.integers(0, L))
+        kind = "eigsh" if rng.random() < 0.7 else "evolve"
+        t = float(rng.uniform(0.5, 5.0))
+        reqs.append({"arrival": float(arrivals[i]), "L": L, "nup": nup, "kblock": k, "kind": kind, "t": t,
+                     "seed": 1000 + i})
+    return reqs
+
+
+def section_c5(qs, torch, n_req=2000, rate=200.0, budget_gb=150.0, seq_sample=40):
+    """Config 5: the request loop under Poisson arrivals; p50/p99 latency
+    (completion - arrival) and solves/s, against the plain FP64 path (build
+    the sector, eigsh / evolve one request at a time) on the first
+    `seq_sample` requests."""
+    import threading
+    reqs = serving_requests(n_req, rate)
+    terms = {}
+
+    def terms_for(L):
+        if L not in terms:
+            terms[L] = [qs.OperatorTerm(o, c) for o, c in j1j2_spec(L, 1.0, 0.5)]
+        return terms[L]
+
+    def basis_of(r):
+        return dict(L=r["L"], nup=r["nup"], pauli=False, kblock=r["kblock"])
+
+    # the plain FP64 GPU path on a sample: one request at a time, no batching
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for r in reqs[:seq_sample]:
+        H = qs.Hamiltonian(qs.SpinBasis1D(**basis_of(r)), terms_for(r["L"]))
+        if r["kind"] == "eigsh":
+            qs.eigsh(H, k=1, which="SA", tol=1e-10, return_eigenvectors=False)
+        else:
+            rng = np.random.default_rng(r["seed"])
+            v = rng.standard_normal(H.Ns) + 1j * rng.standard_normal(H.Ns)
+            qs.evolve(H, v / np.linalg.norm(v), 0.0, [r["t"]], tol=1e-9, krylov_dim=30)
+        del H
+    t_seq = time.perf_counter() - t
+    out = {"workload": "%d requests, Poisson %.0f/s, L in 18..30 (even), J1-J2 J2=0.5, 70%% eigsh k=1 tol 1e-10, "
+                       "30%% evolve t~U[0.5,5] m=30 tol 1e-9, HBM budget %.0f GB" % (n_req, rate, budget_gb),
+           "sequential_fp64_sample": seq_sample, "sequential_fp64_solves_per_s": seq_sample / t_seq}
+    for prec in ("fp64df",):
+        srv = qs.Server(hbm_budget_gb=budget_gb, precision=prec)
+        tickets = [None] * n_req
+        t0 = time.perf_counter()
+
+        def client():
+            for i, r in enumerate(reqs):
+                dt = r["arrival"] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                if r["kind"] == "eigsh":
+                    tickets[i] = srv.submit_eigsh(basis_of(r), terms_for(r["L"]), k=1, tol=1e-10, seed=r["seed"])
+                else:
+                    tickets[i] = srv.submit_evolve(basis_of(r), terms_for(r["L"]), r["t"], tol=1e-9, krylov_dim=30,
+                                                   seed=r["seed"], want_vector=False)
+        th = threading.Thread(target=client)
+        th.start()
+        th.join()
+        res = [srv.wait(tk, timeout=3600) for tk in tickets]
+        wall = time.perf_counter() - t0
+        lat = np.array([x["done_s"] - x["submit_s"] for x in res])
+        first = min(x["submit_s"] for x in res)
+        last = max(x["done_s"] for x in res)
+        st = srv.stats()
+        srv.close()
+        out[prec] = {"solves_per_s": n_req / (last - first), "wall_s": wall,
+                     "p50_latency_ms": float(np.percentile(lat, 50) * 1e3),
+                     "p99_latency_ms": float(np.percentile(lat, 99) * 1e3),
+                     "mean_latency_ms": float(lat.mean() * 1e3),
+                     "operator_builds": st["builds"], "cache_hits": st["cache_hits"],
+                     "peak_device_gb": st["peak_bytes"] / 1e9, "failed": st["failed"],
+                     "speedup_vs_sequential_fp64": (n_req / (last - first)) / (seq_sample / t_seq)}
+    return out
+
+
 def run_ours(args, wl, world, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -479,7 +566,8 @@ def run_ours(args, wl, world, rank, local):
             return e0.elapsed_time(e1) / reps
         for name, fn in (("c1_xxz_L16", lambda: section_c1(qs, torch, timed_events)),
                          ("c4_batched_sectors_L26", lambda: section_c4(qs, torch)),
-                         ("c3_tfim_L30_evolve", lambda: section_c3(qs, torch))):
+                         ("c3_tfim_L30_evolve", lambda: section_c3(qs, torch)),
+                         ("c5_serving", lambda: section_c5(qs, torch, n_req=args.serve_requests))):
             try:
                 sections[name] = fn()
             except Exception as exc:  # a failing side workload must not hide the headline
@@ -533,7 +621,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="j1j2_L32_k0_p1_z1", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-sections", action="store_true", help="skip the side workloads (XXZ L=16, batched sectors, TFIM evolve)")
+    ap.add_argument("--no-sections", action="store_true",
+                    help="skip the side workloads (XXZ L=16, batched sectors, TFIM evolve, serving)")
+    ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -39,7 +39,8 @@ typedef enum {
     QS_ERR_NOMEM = 4,           /* OutOfMemoryError */
     QS_ERR_NOT_CONVERGED = 5,   /* ErrorException: Krylov / Lanczos did not converge */
     QS_ERR_UNSUPPORTED = 6,     /* ArgumentError: outside what this engine implements */
-    QS_ERR_TIMEOUT = 7          /* ErrorException: a bounded device wait ran out */
+    QS_ERR_TIMEOUT = 7,         /* ErrorException: a bounded device wait ran out */
+    QS_PENDING = 8              /* a served request is queued or running */
 } qs_status;
 
 typedef enum { QS_F64 = 0, QS_C128 = 1, QS_F32 = 2, QS_C64 = 3 } qs_dtype;
@@ -251,6 +252,80 @@ QS_API int qs_expm_multiply(qs_op *op, const double *a, const double *v, double 
  * qs_expm_multiply. */
 QS_API int qs_evolve(qs_op *op, const double *v0, double t0, const double *times, int32_t nt, int32_t imag_time,
               double tol, int32_t krylov_dim, int32_t precision, double *out);
+
+/* ---------------------------------------------------------------- serving */
+
+/* A request loop for ground-state and time-evolution solves of mixed sizes and
+ * sectors on one GPU, with no counterpart in the reference (which runs one
+ * solve per call, src/operators.jl:1558-1640, 2073-2164).  Requests are
+ * admitted in arrival order against a device-memory budget (basis, assembled
+ * operator and Krylov state are all counted), operators are cached by sector
+ * and terms, and every running solve advances in the same batched launches;
+ * requests arriving while others run join them as soon as they are built
+ * (continuous batching).  A result does not depend on what else was running. */
+typedef struct qs_server qs_server;
+
+typedef struct {
+    double hbm_budget_bytes;   /* device bytes the server may hold, 0 = 150e9 */
+    int32_t max_slots;         /* solves running at once, 0 = 64 */
+    int32_t precision;         /* 0 FP64 Krylov vectors, 2 double-float (FP32 pipe) */
+    int32_t disable_op_cache;  /* 1: free each operator with its last request */
+    int32_t chunk_steps;       /* Krylov steps between admissions, 0 = 8 */
+    int32_t builders;          /* threads building bases and operators, 0 = 4 */
+    int32_t device;            /* set by the library: the device current at creation */
+} qs_server_opts;
+
+typedef enum { QS_REQ_EIGSH = 0, QS_REQ_EVOLVE = 1 } qs_request_kind;
+
+typedef struct {
+    int32_t kind;              /* qs_request_kind */
+    qs_basis_spec basis;       /* the sector */
+    const qs_term *terms;      /* the static Hamiltonian; copied at submission */
+    int32_t nterms;
+    /* eigsh(H; k, which, tol, ncv, maxiter) */
+    int32_t k, which, ncv, maxiter;
+    double tol;                /* eigsh: 0 = machine epsilon; evolve: 0 = 1e-12 */
+    /* evolve(H, v0, 0, [t]; imag_time, krylov_dim) */
+    double t;
+    int32_t imag_time, krylov_dim;
+    const double *v0;          /* NULL: seeded start vector; evolve: Ns complex, eigsh: op dtype */
+    int64_t v0_len;            /* doubles in v0 */
+    uint64_t seed;             /* 0 = the seed qs_eigsh uses */
+    int32_t want_vector;       /* keep the eigenvectors / evolved state for qs_server_vector */
+} qs_request;
+
+typedef struct {
+    int32_t status;            /* QS_PENDING, QS_OK or the failure's status */
+    int32_t nvalues;
+    int64_t Ns;
+    double values[8];          /* eigsh: the first min(k, 8) eigenvalues */
+    double submit_s, admit_s, done_s;  /* seconds since the server started (-1: not yet) */
+    int64_t matvecs;
+    int32_t restarts;          /* eigsh: thick restarts; evolve: step halvings */
+    double error_estimate;     /* eigsh: max relative Ritz residual; evolve: last step's estimate */
+    int64_t vector_len;        /* doubles qs_server_vector returns */
+    char message[128];         /* failure text */
+} qs_result;
+
+typedef struct {
+    int64_t submitted, completed, failed, builds, cache_hits, evictions, steps, launches;
+    int64_t cached_ops, running, queued;
+    double bytes_in_use, peak_bytes;
+} qs_server_counters;
+
+QS_API int qs_server_create(const qs_server_opts *opts, qs_server **out);
+QS_API void qs_server_destroy(qs_server *server);
+/* Copies the request (terms and v0 included) and returns its ticket. */
+QS_API int qs_server_submit(qs_server *server, const qs_request *req, int64_t *ticket);
+/* Result so far; returns the request's status (QS_PENDING while running). */
+QS_API int qs_server_poll(qs_server *server, int64_t ticket, qs_result *out);
+/* Waits up to timeout_s seconds (<= 0: no limit) for the request to finish. */
+QS_API int qs_server_wait(qs_server *server, int64_t ticket, double timeout_s, qs_result *out);
+/* The kept eigenvectors (Ns x k, op dtype) or evolved state (Ns complex). */
+QS_API int qs_server_vector(qs_server *server, int64_t ticket, double *out, int64_t len);
+/* Forgets a finished request, or cancels one that is still queued or running. */
+QS_API int qs_server_release(qs_server *server, int64_t ticket);
+QS_API int qs_server_stats(qs_server *server, qs_server_counters *out);
 
 /* ----------------------------------------------------------------- errors */
 

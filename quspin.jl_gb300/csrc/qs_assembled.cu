@@ -424,21 +424,9 @@ struct SellArgs {
     void* y;
 };
 
-template <typename T>
-__device__ __forceinline__ void sell_word(const SellArgs& a, int64_t o, uint32_t& col, uint32_t& code) {
-    if (a.packed) {
-        const uint32_t w = __ldg(a.words + o);
-        col = w >> a.code_bits;
-        code = w & a.code_mask;
-    } else {
-        col = (uint32_t)__ldg(a.cols + o);
-        code = __ldg(a.codes + o);
-    }
-}
-
 // One thread per row: y[r] = beta y[r] + alpha (d[r] x[r] + rs(stab[r]) sum_j T[code_j] x[col_j])
-template <bool kCM, bool kCV, typename T>
-__global__ void __launch_bounds__(kThreads, 8) sell_kernel(SellArgs a) {
+template <bool kCM, bool kCV, typename T, bool kPacked>
+__global__ void __launch_bounds__(kThreads, 4) sell_kernel(SellArgs a) {
     using T2 = typename V2<T>::t;
     __shared__ T2 tab[1024];
     __shared__ T rsq[kMaxGroup + 1];
@@ -454,34 +442,39 @@ __global__ void __launch_bounds__(kThreads, 8) sell_kernel(SellArgs a) {
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const T2* __restrict__ gtab = (const T2*)a.table;
+    const bool conj = a.conj;
     for (int64_t s = warp0; s < a.nslices; s += nwarps) {
         const int64_t r = s * kSlice + lane;
         if (r >= a.n) continue;
         const int len = a.len[r];
         const int64_t base = a.sptr[s] + lane;
         T acc_r = 0, acc_i = 0;
-#pragma unroll 4
-        for (int j = 0; j < len; ++j) {
-            uint32_t col, code;
-            sell_word<T>(a, base + (int64_t)j * kSlice, col, code);
-            T2 v;
-            if (smem_tab) v = tab[code];
-            else {
-                v = ((const T2*)a.table)[code];
-                if (a.conj) v.y = -v.y;
-            }
-            if (kCV) {
-                const T2 xv = __ldg((const T2*)a.x + col);
-                if (kCM) {
-                    acc_r += v.x * xv.x - v.y * xv.y;
-                    acc_i += v.x * xv.y + v.y * xv.x;
-                } else {
-                    acc_r += v.x * xv.x;
-                    acc_i += v.x * xv.y;
-                }
-            } else {
-                acc_r += v.x * __ldg((const T*)a.x + col);
-            }
+        auto value = [&](uint32_t code) -> T2 {
+            if (smem_tab) return tab[code];
+            T2 v = gtab[code];
+            if (conj) v.y = -v.y;
+            return v;
+        };
+        if (kCV) {
+            const T2* __restrict__ x = (const T2*)a.x;
+            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return __ldg(x + c); },
+                                 [&](uint32_t code, T2 xv) {
+                                     const T2 v = value(code);
+                                     if (kCM) {
+                                         acc_r += v.x * xv.x - v.y * xv.y;
+                                         acc_i += v.x * xv.y + v.y * xv.x;
+                                     } else {
+                                         acc_r += v.x * xv.x;
+                                         acc_i += v.x * xv.y;
+                                     }
+                                 });
+        } else {
+            const T* __restrict__ x = (const T*)a.x;
+            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return __ldg(x + c); },
+                                 [&](uint32_t code, T xv) { acc_r += value(code).x * xv; });
         }
         const T sc = a.stab ? rsq[a.stab[r]] : (T)1;
         acc_r *= sc;
@@ -520,8 +513,8 @@ __global__ void __launch_bounds__(kThreads, 8) sell_kernel(SellArgs a) {
 
 // Double-float products, one thread per row; FP64 only in the per-row tail,
 // where all 32 lanes of a warp work on 32 rows.
-template <bool kCM, bool kCV>
-__global__ void __launch_bounds__(kThreads, 8) sell_df_kernel(SellArgs a, const float4* __restrict__ tab_df,
+template <bool kCM, bool kCV, bool kPacked>
+__global__ void __launch_bounds__(kThreads, 4) sell_df_kernel(SellArgs a, const float4* __restrict__ tab_df,
                                                            const void* __restrict__ xs) {
     __shared__ float4 tab[1024];
     __shared__ double rsq[kMaxGroup + 1];
@@ -537,34 +530,40 @@ __global__ void __launch_bounds__(kThreads, 8) sell_df_kernel(SellArgs a, const 
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool conj = a.conj;
     for (int64_t s = warp0; s < a.nslices; s += nwarps) {
         const int64_t r = s * kSlice + lane;
         if (r >= a.n) continue;
         const int len = a.len[r];
         const int64_t base = a.sptr[s] + lane;
         DF ar{0.f, 0.f}, ai{0.f, 0.f};
-#pragma unroll 4
-        for (int j = 0; j < len; ++j) {
-            uint32_t col, code;
-            sell_word<float>(a, base + (int64_t)j * kSlice, col, code);
-            float4 v;
-            if (smem_tab) v = tab[code];
-            else {
-                v = tab_df[code];
-                if (a.conj) { v.z = -v.z; v.w = -v.w; }
-            }
-            if (kCV) {
-                const float4 xv = __ldg((const float4*)xs + col);
-                df_mac(ar, v.x, v.y, xv.x, xv.y);
-                df_mac(ai, v.x, v.y, xv.z, xv.w);
-                if (kCM) {
-                    df_mac(ar, -v.z, -v.w, xv.z, xv.w);
-                    df_mac(ai, v.z, v.w, xv.x, xv.y);
-                }
-            } else {
-                const float2 xv = __ldg((const float2*)xs + col);
-                df_mac(ar, v.x, v.y, xv.x, xv.y);
-            }
+        auto value = [&](uint32_t code) -> float4 {
+            if (smem_tab) return tab[code];
+            float4 v = tab_df[code];
+            if (conj) { v.z = -v.z; v.w = -v.w; }
+            return v;
+        };
+        if (kCV) {
+            const float4* __restrict__ x = (const float4*)xs;
+            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return __ldg(x + c); },
+                                 [&](uint32_t code, float4 xv) {
+                                     const float4 v = value(code);
+                                     df_mac(ar, v.x, v.y, xv.x, xv.y);
+                                     df_mac(ai, v.x, v.y, xv.z, xv.w);
+                                     if (kCM) {
+                                         df_mac(ar, -v.z, -v.w, xv.z, xv.w);
+                                         df_mac(ai, v.z, v.w, xv.x, xv.y);
+                                     }
+                                 });
+        } else {
+            const float2* __restrict__ x = (const float2*)xs;
+            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return __ldg(x + c); },
+                                 [&](uint32_t code, float2 xv) {
+                                     const float4 v = value(code);
+                                     df_mac(ar, v.x, v.y, xv.x, xv.y);
+                                 });
         }
         const double sc = a.stab ? rsq[a.stab[r]] : 1.0;
         double acc_r = df_to_double(ar) * sc, acc_i = kCV ? df_to_double(ai) * sc : 0.0;
@@ -599,8 +598,8 @@ __global__ void __launch_bounds__(kThreads, 8) sell_df_kernel(SellArgs a, const 
 
 // Double-float storage in and out (the Krylov solvers' double-float vectors):
 // y = d .* x + rs(stab) * sum_j T[code_j] x[col_j], entirely on the FP32 pipe.
-template <bool kCM, bool kCV>
-__global__ void __launch_bounds__(kThreads, 8) sell_dfio_kernel(SellArgs a, const float4* __restrict__ tab_df,
+template <bool kCM, bool kCV, bool kPacked>
+__global__ void __launch_bounds__(kThreads, 4) sell_dfio_kernel(SellArgs a, const float4* __restrict__ tab_df,
                                                                 const float4* __restrict__ diag_df,
                                                                 const float2* __restrict__ rsq_df) {
     __shared__ float4 tab[1024];
@@ -617,34 +616,40 @@ __global__ void __launch_bounds__(kThreads, 8) sell_dfio_kernel(SellArgs a, cons
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool conj = a.conj;
     for (int64_t s = warp0; s < a.nslices; s += nwarps) {
         const int64_t r = s * kSlice + lane;
         if (r >= a.n) continue;
         const int len = a.len[r];
         const int64_t base = a.sptr[s] + lane;
         DF ar{0.f, 0.f}, ai{0.f, 0.f};
-#pragma unroll 4
-        for (int j = 0; j < len; ++j) {
-            uint32_t col, code;
-            sell_word<float>(a, base + (int64_t)j * kSlice, col, code);
-            float4 v;
-            if (smem_tab) v = tab[code];
-            else {
-                v = tab_df[code];
-                if (a.conj) { v.z = -v.z; v.w = -v.w; }
-            }
-            if (kCV) {
-                const float4 xv = __ldg((const float4*)a.x + col);
-                df_mac(ar, v.x, v.y, xv.x, xv.y);
-                df_mac(ai, v.x, v.y, xv.z, xv.w);
-                if (kCM) {
-                    df_mac(ar, -v.z, -v.w, xv.z, xv.w);
-                    df_mac(ai, v.z, v.w, xv.x, xv.y);
-                }
-            } else {
-                const float2 xv = __ldg((const float2*)a.x + col);
-                df_mac(ar, v.x, v.y, xv.x, xv.y);
-            }
+        auto value = [&](uint32_t code) -> float4 {
+            if (smem_tab) return tab[code];
+            float4 v = tab_df[code];
+            if (conj) { v.z = -v.z; v.w = -v.w; }
+            return v;
+        };
+        if (kCV) {
+            const float4* __restrict__ x = (const float4*)a.x;
+            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return __ldg(x + c); },
+                                 [&](uint32_t code, float4 xv) {
+                                     const float4 v = value(code);
+                                     df_mac(ar, v.x, v.y, xv.x, xv.y);
+                                     df_mac(ai, v.x, v.y, xv.z, xv.w);
+                                     if (kCM) {
+                                         df_mac(ar, -v.z, -v.w, xv.z, xv.w);
+                                         df_mac(ai, v.z, v.w, xv.x, xv.y);
+                                     }
+                                 });
+        } else {
+            const float2* __restrict__ x = (const float2*)a.x;
+            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return __ldg(x + c); },
+                                 [&](uint32_t code, float2 xv) {
+                                     const float4 v = value(code);
+                                     df_mac(ar, v.x, v.y, xv.x, xv.y);
+                                 });
         }
         const float2 sc = a.stab ? rsq[a.stab[r]] : make_float2(1.f, 0.f);
         DF out_r = df_mul(ar, DF{sc.x, sc.y});
@@ -930,9 +935,15 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
             const float4* td = M.table_df.as<float4>();
             const float4* dd = op.d_diag_df.as<float4>();
             const float2* rq = M.rsq_df.as<float2>();
-            if (cm) sell_dfio_kernel<true, true><<<grid, kThreads, 0, s>>>(a, td, dd, rq);
-            else if (cv) sell_dfio_kernel<false, true><<<grid, kThreads, 0, s>>>(a, td, dd, rq);
-            else sell_dfio_kernel<false, false><<<grid, kThreads, 0, s>>>(a, td, dd, rq);
+#define QS_DFIO(P)                                                                    \
+    do {                                                                              \
+        if (cm) sell_dfio_kernel<true, true, P><<<grid, kThreads, 0, s>>>(a, td, dd, rq);   \
+        else if (cv) sell_dfio_kernel<false, true, P><<<grid, kThreads, 0, s>>>(a, td, dd, rq); \
+        else sell_dfio_kernel<false, false, P><<<grid, kThreads, 0, s>>>(a, td, dd, rq);     \
+    } while (0)
+            if (a.packed) QS_DFIO(true);
+            else QS_DFIO(false);
+#undef QS_DFIO
             QS_CUDA(cudaGetLastError());
             note_launches(1);
             return;
@@ -946,9 +957,15 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
             else split_kernel<false><<<sg, kThreads, 0, s>>>(c.x, nullptr, M.xsplit.as<float2>(), b.n);
             QS_CUDA(cudaGetLastError());
             const float4* td = M.table_df.as<float4>();
-            if (cm) sell_df_kernel<true, true><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);
-            else if (cv) sell_df_kernel<false, true><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);
-            else sell_df_kernel<false, false><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);
+#define QS_DF(P)                                                                         \
+    do {                                                                                 \
+        if (cm) sell_df_kernel<true, true, P><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);    \
+        else if (cv) sell_df_kernel<false, true, P><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p); \
+        else sell_df_kernel<false, false, P><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);      \
+    } while (0)
+            if (a.packed) QS_DF(true);
+            else QS_DF(false);
+#undef QS_DF
             QS_CUDA(cudaGetLastError());
             note_launches(2);
             return;
@@ -957,16 +974,21 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
             a.table = M.table32.p;
             a.diag = op.d_diag32.p;
             a.diag_re = op.d_diag32_re.p;
-            if (cm) sell_kernel<true, true, float><<<grid, kThreads, 0, s>>>(a);
-            else if (cv) sell_kernel<false, true, float><<<grid, kThreads, 0, s>>>(a);
-            else sell_kernel<false, false, float><<<grid, kThreads, 0, s>>>(a);
+#define QS_SELL(T_, P)                                                                 \
+    do {                                                                               \
+        if (cm) sell_kernel<true, true, T_, P><<<grid, kThreads, 0, s>>>(a);                \
+        else if (cv) sell_kernel<false, true, T_, P><<<grid, kThreads, 0, s>>>(a);          \
+        else sell_kernel<false, false, T_, P><<<grid, kThreads, 0, s>>>(a);                 \
+    } while (0)
+            if (a.packed) QS_SELL(float, true);
+            else QS_SELL(float, false);
         } else {
             a.table = M.table64.p;
             a.diag = op.d_diag.p;
             a.diag_re = op.d_diag_re.p;
-            if (cm) sell_kernel<true, true, double><<<grid, kThreads, 0, s>>>(a);
-            else if (cv) sell_kernel<false, true, double><<<grid, kThreads, 0, s>>>(a);
-            else sell_kernel<false, false, double><<<grid, kThreads, 0, s>>>(a);
+            if (a.packed) QS_SELL(double, true);
+            else QS_SELL(double, false);
+#undef QS_SELL
         }
         QS_CUDA(cudaGetLastError());
         note_launches(1);

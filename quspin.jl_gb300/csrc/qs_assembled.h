@@ -7,6 +7,52 @@ namespace qs {
 
 constexpr int kSellSlice = 32;   // rows per slice of the sliced-ELL layout
 
+#ifdef __CUDACC__
+// The nonzeros of one sliced-ELL row (`len` of them from `base`, stride
+// kSellSlice), fed to acc(code, x[col]) with U words and then U gathers in
+// flight before any arithmetic: the product is bound by the latency of the
+// x gathers, and this keeps U of them outstanding per thread.
+template <int U, bool kPacked, class LoadX, class Acc>
+__device__ __forceinline__ void sell_row(const uint32_t* __restrict__ words, const int32_t* __restrict__ cols,
+                                         const uint16_t* __restrict__ codes, int64_t base, int len, int cb,
+                                         uint32_t cmask, LoadX ldx, Acc acc) {
+    int j = 0;
+    for (; j + U <= len; j += U) {
+        uint32_t col[U], code[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int64_t o = base + (int64_t)(j + u) * kSellSlice;
+            if (kPacked) {
+                const uint32_t w = __ldg(words + o);
+                col[u] = w >> cb;
+                code[u] = w & cmask;
+            } else {
+                col[u] = (uint32_t)__ldg(cols + o);
+                code[u] = __ldg(codes + o);
+            }
+        }
+        decltype(ldx(0u)) xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) xv[u] = ldx(col[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc(code[u], xv[u]);
+    }
+    for (; j < len; ++j) {
+        const int64_t o = base + (int64_t)j * kSellSlice;
+        uint32_t col, code;
+        if (kPacked) {
+            const uint32_t w = __ldg(words + o);
+            col = w >> cb;
+            code = w & cmask;
+        } else {
+            col = (uint32_t)__ldg(cols + o);
+            code = __ldg(codes + o);
+        }
+        acc(code, ldx(col));
+    }
+}
+#endif
+
 struct Assembled {
     DevBuf rowptr;     // int64, n + 1
     DevBuf words;      // uint32 (column << code_bits) | code, when packed

@@ -390,6 +390,33 @@ __global__ void from_df_kernel(const void* in, double* out, int64_t n) {
     }
 }
 
+// ------------------------------------------------------- seeded normals
+// splitmix64 (Steele, Lea & Flood 2014) of (seed, index) gives two uniforms;
+// Box-Muller turns them into a standard normal.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__global__ void fill_normal_kernel(void* dst, int kind, int64_t ncomp, uint64_t seed) {
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < ncomp; i += (int64_t)gridDim.x * kThreads) {
+        const uint64_t a = splitmix64(seed ^ splitmix64((uint64_t)i));
+        const uint64_t b = splitmix64(a);
+        const float u1 = (float)((a >> 40) + 1) * 5.9604644775390625e-8f;   // (0, 1]
+        const float u2 = (float)(b >> 40) * 5.9604644775390625e-8f;         // [0, 1)
+        const float g = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+        if (kind == 0) {
+            ((double*)dst)[i] = (double)g;
+        } else if (kind == 1) {
+            ((float*)dst)[i] = g;
+        } else {
+            ((float2*)dst)[i] = make_float2(g, 0.f);
+        }
+    }
+}
+
 int nblocks(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, kMaxBlocks));
@@ -572,6 +599,14 @@ void Blas::rotate(void* V, int64_t ldv, int m, int p, const std::vector<double>&
     QS_CUDA(cudaGetLastError());
     note_launches(2);
     QS_CUDA(cudaStreamSynchronize(s));
+}
+
+void fill_normal(void* dst, VKind k, int64_t n, uint64_t seed, cudaStream_t s) {
+    const int64_t ncomp = n * (vk_complex(k) ? 2 : 1);
+    const int kind = vk_df(k) ? 2 : (vk_single(k) ? 1 : 0);
+    fill_normal_kernel<<<nblocks(ncomp), kThreads, 0, s>>>(dst, kind, ncomp, seed);
+    QS_CUDA(cudaGetLastError());
+    note_launches(1);
 }
 
 void convert_vec(const void* src, VKind ks, void* dst, VKind kd, int64_t n, cudaStream_t s) {

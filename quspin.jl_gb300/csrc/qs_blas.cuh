@@ -64,4 +64,9 @@ struct Blas {
 // Conversions between storage precisions (same real/complex-ness).
 void convert_vec(const void* src, VKind ks, void* dst, VKind kd, int64_t n, cudaStream_t s);
 
+// dst = n elements of kind k with independent standard normal components, a
+// pure function of (seed, component index): the same vector on every run and
+// whatever else shares the device.
+void fill_normal(void* dst, VKind k, int64_t n, uint64_t seed, cudaStream_t s);
+
 }  // namespace qs

@@ -8,12 +8,16 @@
 #include "../../include/qsgpu.h"
 #include "qs_internal.h"
 #include "qs_krylov.h"
+#include "qs_server.h"
 
 struct qs_basis {
     qs::Basis b;
 };
 struct qs_op {
     qs::Op* op;
+};
+struct qs_server {
+    qs::Server* s;
 };
 
 namespace {
@@ -284,3 +288,64 @@ int qs_evolve(qs_op* op, const double* v0, double t0, const double* times, int32
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ serving
+int qs_server_create(const qs_server_opts* opts, qs_server** out) {
+    return guard([&] {
+        if (!out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        *out = nullptr;
+        *out = new qs_server{qs::server_create(opts)};
+    });
+}
+
+void qs_server_destroy(qs_server* server) {
+    if (!server) return;
+    qs::server_destroy(server->s);
+    delete server;
+}
+
+int qs_server_submit(qs_server* server, const qs_request* req, int64_t* ticket) {
+    return guard([&] {
+        if (!server || !ticket) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        *ticket = qs::server_submit(server->s, req);
+    });
+}
+
+int qs_server_poll(qs_server* server, int64_t ticket, qs_result* out) {
+    int st = QS_OK;
+    int rc = guard([&] {
+        if (!server) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        st = qs::server_poll(server->s, ticket, out);
+    });
+    return rc != QS_OK ? rc : st;
+}
+
+int qs_server_wait(qs_server* server, int64_t ticket, double timeout_s, qs_result* out) {
+    int st = QS_OK;
+    int rc = guard([&] {
+        if (!server) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        st = qs::server_wait(server->s, ticket, timeout_s, out);
+    });
+    return rc != QS_OK ? rc : st;
+}
+
+int qs_server_vector(qs_server* server, int64_t ticket, double* out, int64_t len) {
+    return guard([&] {
+        if (!server || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::server_vector(server->s, ticket, out, len);
+    });
+}
+
+int qs_server_release(qs_server* server, int64_t ticket) {
+    return guard([&] {
+        if (!server) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::server_release(server->s, ticket);
+    });
+}
+
+int qs_server_stats(qs_server* server, qs_server_counters* out) {
+    return guard([&] {
+        if (!server || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::server_stats(server->s, out);
+    });
+}

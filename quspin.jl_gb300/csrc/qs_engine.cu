@@ -124,7 +124,7 @@ __device__ __forceinline__ char* colp(const SlotDev& S, int c) { return (char*)S
 // ------------------------------------------------------------ SpMV
 // y = col(j + 1) = H col(j) on every stepping slot: sliced ELL, one thread per
 // row, the slot's value table staged in shared memory.
-template <class A, bool CV, bool CM>
+template <class A, bool CV, bool CM, bool PACKED>
 __device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA<A>* tab, bool smem_tab,
                                           const A* rsq) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -132,11 +132,8 @@ __device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA
     const int64_t s0 = lb * S.spb, s1 = min(S.nslices, s0 + S.spb);
     const void* x = colp(S, S.j);
     void* y = colp(S, S.j + 1);
-    const int packed = S.packed, cb = S.code_bits;
+    const int cb = S.code_bits;
     const uint32_t cmask = S.code_mask;
-    const uint32_t* __restrict__ words = S.words;
-    const int32_t* __restrict__ cols = S.cols;
-    const uint16_t* __restrict__ codes = S.codes;
     const uint16_t* __restrict__ len = S.len;
     const uint16_t* __restrict__ stab = S.stab;
     for (int64_t sl = s0 + warp; sl < s1; sl += nw) {
@@ -145,29 +142,19 @@ __device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA
         const int cnt = len[r];
         const int64_t base = S.sptr[sl] + lane;
         A ar = zero<A>(), ai = zero<A>();
-#pragma unroll 4
-        for (int t = 0; t < cnt; ++t) {
-            const int64_t o = base + (int64_t)t * kSellSlice;
-            uint32_t col, code;
-            if (packed) {
-                const uint32_t w = __ldg(words + o);
-                col = w >> cb;
-                code = w & cmask;
-            } else {
-                col = (uint32_t)__ldg(cols + o);
-                code = __ldg(codes + o);
-            }
-            const CA<A> v = smem_tab ? tab[code] : ldtab<A>(S, code);
-            const CA<A> xv = ldv<A, CV>(x, col);
-            mac(ar, v.re, xv.re);
-            if (CV) {
-                mac(ai, v.re, xv.im);
-                if (CM) {
-                    msub(ar, v.im, xv.im);
-                    mac(ai, v.im, xv.re);
-                }
-            }
-        }
+        sell_row<4, PACKED>(S.words, S.cols, S.codes, base, cnt, cb, cmask,
+                            [&](uint32_t c) { return ldv<A, CV>(x, c); },
+                            [&](uint32_t code, CA<A> xv) {
+                                const CA<A> v = smem_tab ? tab[code] : ldtab<A>(S, code);
+                                mac(ar, v.re, xv.re);
+                                if (CV) {
+                                    mac(ai, v.re, xv.im);
+                                    if (CM) {
+                                        msub(ar, v.im, xv.im);
+                                        mac(ai, v.im, xv.re);
+                                    }
+                                }
+                            });
         const A sc = stab ? rsq[stab[r]] : one<A>();
         CA<A> out;
         out.re = mul(ar, sc);
@@ -198,54 +185,98 @@ __global__ void __launch_bounds__(kT) eng_spmv(const SlotDev* __restrict__ sl, c
         for (int i = threadIdx.x; i <= S.max_stab; i += blockDim.x) rsq[i] = ldrsq<A>(rsqt, i);
     __syncthreads();
     const int64_t lb = blockIdx.x - S.sb_begin;
-    if (!S.cv) spmv_rows<A, false, false>(S, lb, tab, smem_tab, rsq);
-    else if (!S.cm) spmv_rows<A, true, false>(S, lb, tab, smem_tab, rsq);
-    else spmv_rows<A, true, true>(S, lb, tab, smem_tab, rsq);
+    if (S.packed) {
+        if (!S.cv) spmv_rows<A, false, false, true>(S, lb, tab, smem_tab, rsq);
+        else if (!S.cm) spmv_rows<A, true, false, true>(S, lb, tab, smem_tab, rsq);
+        else spmv_rows<A, true, true, true>(S, lb, tab, smem_tab, rsq);
+    } else {
+        if (!S.cv) spmv_rows<A, false, false, false>(S, lb, tab, smem_tab, rsq);
+        else if (!S.cm) spmv_rows<A, true, false, false>(S, lb, tab, smem_tab, rsq);
+        else spmv_rows<A, true, true, false>(S, lb, tab, smem_tab, rsq);
+    }
 }
 
 // ------------------------------------------------------------ dots
-// mode 0 (step): partial[b][i] = <col i, col j+1>, i <= j;
-// mode 1 (normalise): partial[b][0] = <col ncol, col ncol>
+// Partial sums per row block b live at partial[(b * P + i) * 2 + {re, im}],
+// P = mmax + 1; index mmax holds norms.
+// mode 0 (first pass): i in [first, j] with first = j for the three-term
+//   recurrence, else 0; DGKS slots also accumulate ||w||^2 at index mmax;
+// mode 1 (second pass, only where the step's flag asks): i in [0, j];
+// mode 2 (normalise): partial[b][0] = <col ncol, col ncol>.
 template <class A, bool CV>
 __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t r1, int i0, int nv, const void* w,
-                                          A* re, A* im) {
+                                          A* re, A* im, bool want_wn, A& wn) {
     const int64_t n = S.n;
     const char* V = (const char*)S.V;
     const size_t cs = (size_t)n * (CV ? 16 : 8);
+    // columns past nv repeat the last one (cached) so that every load of a row
+    // is issued before the arithmetic
+    const char* col[kJT];
+#pragma unroll
+    for (int q = 0; q < kJT; ++q) col[q] = V + (size_t)min(i0 + q, nv - 1) * cs;
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         const CA<A> wv = ldv<A, CV>(w, r);
+        CA<A> v[kJT];
+#pragma unroll
+        for (int q = 0; q < kJT; ++q) v[q] = ldv<A, CV>(col[q], r);
 #pragma unroll
         for (int q = 0; q < kJT; ++q) {
             if (i0 + q < nv) {
-                const CA<A> v = ldv<A, CV>(V + (size_t)(i0 + q) * cs, r);
-                mac(re[q], v.re, wv.re);
+                mac(re[q], v[q].re, wv.re);
                 if (CV) {
-                    mac(re[q], v.im, wv.im);
-                    mac(im[q], v.re, wv.im);
-                    msub(im[q], v.im, wv.re);
+                    mac(re[q], v[q].im, wv.im);
+                    mac(im[q], v[q].re, wv.im);
+                    msub(im[q], v[q].im, wv.re);
                 }
             }
+        }
+        if (want_wn) {
+            mac(wn, wv.re, wv.re);
+            if (CV) mac(wn, wv.im, wv.im);
         }
     }
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+__device__ __forceinline__ double block_sum(A v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v = add(v, shfl(v, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = to_d(v);
+    __syncthreads();
+    double t = 0;
+    for (int q = 0; q < kT / 32; ++q) t += sh[q];
+    return t;
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT, 2) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
                                                int mode, double* __restrict__ partial) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
-    if (S.state != (mode == 0 ? kSlotStep : kSlotNormalize)) return;
-    const int nv = mode == 0 ? S.j + 1 : 1;
-    const int i0 = blockIdx.y * kJT;
+    if (S.state != (mode == 2 ? kSlotNormalize : kSlotStep)) return;
+    if (mode == 1 && S.nrm[4] == 0.0) return;
+    const int P = mmax + 1;
+    int first, nv;
+    const void* w;
+    if (mode == 2) {
+        first = S.ncol;
+        nv = S.ncol + 1;
+        w = colp(S, S.ncol);
+    } else {
+        first = (mode == 0 && S.orth == 2) ? S.j : 0;
+        nv = S.j + 1;
+        w = colp(S, S.j + 1);
+    }
+    const int i0 = first + blockIdx.y * kJT;
     if (i0 >= nv) return;
-    const void* w = colp(S, mode == 0 ? S.j + 1 : S.ncol);
+    const bool want_wn = mode == 0 && S.orth == 1 && blockIdx.y == 0;
     const int64_t lb = blockIdx.x - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
-    A re[kJT], im[kJT];
+    A re[kJT], im[kJT], wn = zero<A>();
 #pragma unroll
     for (int q = 0; q < kJT; ++q) re[q] = im[q] = zero<A>();
-    const int vbase = mode == 0 ? 0 : S.ncol;
-    if (S.cv) dots_rows<A, true>(S, r0, r1, vbase + i0, vbase + nv, w, re, im);
-    else dots_rows<A, false>(S, r0, r1, vbase + i0, vbase + nv, w, re, im);
+    if (S.cv) dots_rows<A, true>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
+    else dots_rows<A, false>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
     __shared__ double sh[kT / 32][2 * kJT];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -264,27 +295,56 @@ __global__ void __launch_bounds__(kT) eng_dots(const SlotDev* __restrict__ sl, c
         double t = 0;
         for (int q = 0; q < kT / 32; ++q) t += sh[q][threadIdx.x];
         const int q = threadIdx.x / 2;
-        if (i0 + q < nv) partial[((size_t)blockIdx.x * mmax + i0 + q) * 2 + (threadIdx.x & 1)] = t;
+        const int i = mode == 2 ? 0 : i0 + q;
+        if (i0 + q < nv) partial[((size_t)blockIdx.x * P + i) * 2 + (threadIdx.x & 1)] = t;
+    }
+    if (want_wn) {
+        __shared__ double sw[kT / 32];
+        const double t = block_sum(wn, sw);
+        if (threadIdx.x == 0) {
+            partial[((size_t)blockIdx.x * P + mmax) * 2] = t;
+            partial[((size_t)blockIdx.x * P + mmax) * 2 + 1] = 0.0;
+        }
     }
 }
 
 // ------------------------------------------------------------ reduce
-// per slot and vector, the block partials summed in a fixed order.
-// mode 0: h1; 1: h2 and the record column; 2: the new norm; 3: normalise col 0
+// Per slot and vector, the block partials summed in a fixed order, then:
+// mode 0: h1 (and ||w||^2; the three-term recurrence takes beta_{j-1} from the record)
+// mode 1: ||w'||^2 after the first pass; decides the second pass; without it the
+//         step's record column and norm are final
+// mode 2: h2 and the record column h1 + h2 (second pass only)
+// mode 3: ||w''||^2 (second pass only)
+// mode 4: norm of the normalised column
 __global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl, int mmax, int mode,
                                                  const double* __restrict__ partial) {
     const SlotDev& S = sl[blockIdx.x];
-    const int i = blockIdx.y;
-    if (mode == 3) {
+    int i = blockIdx.y;
+    if (mode == 4) {
         if (S.state != kSlotNormalize || i) return;
     } else {
         if (S.state != kSlotStep) return;
-        if (mode == 2 ? i != 0 : i > S.j) return;
+        if ((mode == 2 || mode == 3) && S.nrm[4] == 0.0) return;
+        if (mode == 0) {
+            const int first = S.orth == 2 ? S.j : 0;
+            // blocks y = 0..j cover the vectors; y = mmax the DGKS norm
+            if (i == mmax) {
+                if (S.orth != 1) return;
+            } else if (i < first || i > S.j) {
+                return;
+            }
+        } else if (mode == 1 || mode == 3) {
+            if (i) return;
+            i = mmax;
+        } else if (i > S.j) {
+            return;
+        }
     }
+    const int P = mmax + 1;
     double re = 0, im = 0;
     for (int b = threadIdx.x; b < S.rb_count; b += blockDim.x) {
-        re += partial[((size_t)(S.rb_begin + b) * mmax + i) * 2];
-        im += partial[((size_t)(S.rb_begin + b) * mmax + i) * 2 + 1];
+        re += partial[((size_t)(S.rb_begin + b) * P + i) * 2];
+        im += partial[((size_t)(S.rb_begin + b) * P + i) * 2 + 1];
     }
     for (int o = 16; o > 0; o >>= 1) {
         re += __shfl_xor_sync(0xffffffffu, re, o);
@@ -304,34 +364,53 @@ __global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl,
         im += si[q];
     }
     const int ld = S.m + 1;
+    const int j = S.j;
+    double2* col = S.rec + (size_t)j * ld;
     if (mode == 0) {
-        S.h1[i] = make_double2(re, im);
+        if (i == mmax) {
+            S.nrm[3] = re;
+        } else {
+            S.h1[i] = make_double2(re, im);
+            if (S.orth == 2) S.h1[j - 1 >= 0 ? j - 1 : 0] = j > 0 ? S.rec[(size_t)(j - 1) * ld + j] : S.h1[0];
+        }
     } else if (mode == 1) {
+        const double nb = sqrt(fmax(re, 0.0));
+        const bool second = S.orth == 0 || (S.orth == 1 && nb < 0.717 * sqrt(fmax(S.nrm[3], 0.0)));
+        S.nrm[4] = second ? 1.0 : 0.0;
+        if (!second) {
+            // the first pass is final: record column j and the new norm
+            const int first = S.orth == 2 ? (j > 0 ? j - 1 : 0) : 0;
+            for (int q = first; q <= j; ++q) col[q] = S.h1[q];
+            col[j + 1] = make_double2(nb, 0.0);
+            S.nrm[0] = re;
+            S.nrm[1] = nb > 0 ? 1.0 / nb : 0.0;
+        }
+    } else if (mode == 2) {
         S.h2[i] = make_double2(re, im);
         const double2 a = S.h1[i];
-        S.rec[(size_t)S.j * ld + i] = make_double2(a.x + re, a.y + im);
+        col[i] = make_double2(a.x + re, a.y + im);
     } else {
         const double nb = sqrt(fmax(re, 0.0));
         S.nrm[0] = re;
         S.nrm[1] = nb > 0 ? 1.0 / nb : 0.0;
-        if (mode == 2) S.rec[(size_t)S.j * ld + S.j + 1] = make_double2(nb, 0.0);
+        if (mode == 3) col[j + 1] = make_double2(nb, 0.0);
         else S.nrm[2] = nb;
     }
 }
 
 // ------------------------------------------------------------ update
-// col(j+1) -= sum_i col(i) h_i (pass 0: h1, pass 1: h2); pass 1 also leaves
-// the block's part of ||col(j+1)||^2 in partial[b][0].
+// col(j+1) -= sum_i col(i) h_i over the pass's vectors (pass 0: h1 from
+// `first`, pass 1: h2 over 0..j, only where the step's flag asks), leaving the
+// block's part of ||col(j+1)||^2 at partial[b][mmax].
 template <class A, bool CV>
-__device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r1, int nv, const CA<A>* hs,
-                                         bool want_norm) {
+__device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r1, int first, int nv, const CA<A>* hs) {
     const char* V = (const char*)S.V;
     const size_t cs = (size_t)S.n * (CV ? 16 : 8);
     void* w = (void*)(V + (size_t)(S.j + 1) * cs);
     A nacc = zero<A>();
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         A ar = zero<A>(), ai = zero<A>();
-        for (int t = 0; t < nv; ++t) {
+        for (int t = first; t < nv; ++t) {
             const CA<A> v = ldv<A, CV>(V + (size_t)t * cs, r);
             const CA<A> h = hs[t];
             mac(ar, v.re, h.re);
@@ -345,10 +424,8 @@ __device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r
         o.re = sub(o.re, ar);
         if (CV) o.im = sub(o.im, ai);
         stv<A, CV>(w, r, o);
-        if (want_norm) {
-            mac(nacc, o.re, o.re);
-            if (CV) mac(nacc, o.im, o.im);
-        }
+        mac(nacc, o.re, o.re);
+        if (CV) mac(nacc, o.im, o.im);
     }
     return nacc;
 }
@@ -358,28 +435,25 @@ __global__ void __launch_bounds__(kT) eng_update(const SlotDev* __restrict__ sl,
                                                  int pass, double* __restrict__ partial) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
     if (S.state != kSlotStep) return;
+    if (pass == 1 && S.nrm[4] == 0.0) return;
     __shared__ CA<A> hs[kMaxM];
     const int nv = S.j + 1;
+    const int first = (pass == 0 && S.orth == 2) ? (S.j > 0 ? S.j - 1 : 0) : 0;
     const double2* h = pass ? S.h2 : S.h1;
-    for (int t = threadIdx.x; t < nv; t += blockDim.x) {
+    for (int t = first + threadIdx.x; t < nv; t += blockDim.x) {
         const double2 v = h[t];
         hs[t] = CA<A>{from_d<A>(v.x), from_d<A>(v.y)};
     }
     __syncthreads();
     const int64_t lb = blockIdx.x - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
-    A nacc = S.cv ? update_rows<A, true>(S, r0, r1, nv, hs, pass == 1) : update_rows<A, false>(S, r0, r1, nv, hs, pass == 1);
-    if (pass != 1) return;
-    for (int o = 16; o > 0; o >>= 1) nacc = add(nacc, shfl(nacc, o));
+    A nacc = S.cv ? update_rows<A, true>(S, r0, r1, first, nv, hs) : update_rows<A, false>(S, r0, r1, first, nv, hs);
     __shared__ double sh[kT / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) sh[wid] = to_d(nacc);
-    __syncthreads();
+    const double t = block_sum(nacc, sh);
     if (threadIdx.x == 0) {
-        double t = 0;
-        for (int q = 0; q < kT / 32; ++q) t += sh[q];
-        partial[(size_t)blockIdx.x * mmax * 2] = t;
-        partial[(size_t)blockIdx.x * mmax * 2 + 1] = 0.0;
+        const int P = mmax + 1;
+        partial[((size_t)blockIdx.x * P + mmax) * 2] = t;
+        partial[((size_t)blockIdx.x * P + mmax) * 2 + 1] = 0.0;
     }
 }
 
@@ -426,6 +500,7 @@ __device__ __forceinline__ void rotate_rows(const SlotDev& S, int64_t r0, int64_
     const size_t cs = (size_t)S.n * (CV ? 16 : 8);
     const CA<A>* Y = (const CA<A>*)S.y;
     const int nin = S.rot_in, p = S.p;
+    const bool yreal = S.yreal;
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         for (int c = 0; c < p; ++c) {
             A ar = zero<A>(), ai = zero<A>();
@@ -433,10 +508,10 @@ __device__ __forceinline__ void rotate_rows(const SlotDev& S, int64_t r0, int64_
                 const CA<A> v = ldv<A, CV>(V + (size_t)i * cs, r);
                 const CA<A> y = Y[(size_t)c * nin + i];
                 mac(ar, v.re, y.re);
-                msub(ar, v.im, y.im);
-                if (CV) {
-                    mac(ai, v.re, y.im);
-                    mac(ai, v.im, y.re);
+                if (CV) mac(ai, v.im, y.re);
+                if (!yreal) {
+                    msub(ar, v.im, y.im);
+                    if (CV) mac(ai, v.re, y.im);
                 }
             }
             stv<A, CV>(T + (size_t)c * cs, r, CA<A>{ar, ai});
@@ -486,6 +561,7 @@ Engine::Engine(bool df, cudaStream_t s) : df_(df), s_(s) {
 }
 
 Engine::~Engine() {
+    cudaStreamSynchronize(s_);
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
 }
@@ -539,10 +615,12 @@ Tiles Engine::tune(Op& op, int m, bool cv) {
 size_t Engine::slot_bytes(int64_t n, int m, bool cv, int tmp_cols) {
     const size_t es = cv ? 16 : 8;
     const int tc = tmp_cols > 0 ? tmp_cols : m - 1;
-    return (size_t)(m + 1 + tc) * n * es + ((size_t)2 * m + (size_t)(m + 1) * m + (size_t)m * m) * 16 + 64;
+    return (size_t)(m + 1 + tc) * n * es + ((size_t)2 * m + (size_t)(m + 1) * m + (size_t)m * m) * 16 + 128;
 }
 
-int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols) {
+int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols, int orth) {
+    if (orth < 0 || orth > 2 || (orth == 2 && !op.hermitian))
+        throw Error(QS_ERR_ARGUMENT, "the three-term recurrence needs a Hermitian operator");
     if (m < 2 || m > kMaxM) throw Error(QS_ERR_ARGUMENT, "Krylov basis size must lie in 2:64");
     if (op.complex_mat && !cv) throw Error(QS_ERR_ARGUMENT, "complex operators need complex vectors");
     if (!op.assembled) op_assemble(op);
@@ -573,26 +651,26 @@ int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols) {
     d.n = n;
     d.nslices = M.nslices;
     const size_t es = cv ? 16 : 8;
-    sl.V.alloc((size_t)(m + 1) * n * es);
+    sl.V.alloc((size_t)(m + 1) * n * es, s_);
     const int tc = tmp_cols > 0 ? std::min(tmp_cols, m) : m - 1;
-    sl.tmp.alloc((size_t)tc * n * es);
+    sl.tmp.alloc((size_t)tc * n * es, s_);
     QS_CUDA(cudaMemsetAsync(sl.V.p, 0, sl.V.bytes, s_));
     // h1 (m), h2 (m), rec ((m+1) m) as double2, nrm (4 doubles)
     const size_t nsmall = (size_t)2 * m + (size_t)(m + 1) * m;
-    sl.small.alloc(nsmall * sizeof(double2) + 4 * sizeof(double));
+    sl.small.alloc(nsmall * sizeof(double2) + 8 * sizeof(double), s_);
     QS_CUDA(cudaMemsetAsync(sl.small.p, 0, sl.small.bytes, s_));
-    sl.y.alloc((size_t)m * m * 16);
     d.V = sl.V.p;
     d.tmp = sl.tmp.p;
     d.h1 = sl.small.as<double2>();
     d.h2 = d.h1 + m;
     d.rec = d.h2 + m;
     d.nrm = (double*)(d.rec + (size_t)(m + 1) * m);
-    d.y = sl.y.p;
+    d.y = nullptr;
     d.m = m;
     d.j = 0;
     d.state = kSlotIdle;
     d.carry = -1;
+    d.orth = orth;
     sl.tcols = tc;
     Tiles t;
     if (tune_tiles && n >= 4096 && m >= 4) t = tune(op, m, cv);
@@ -614,8 +692,7 @@ int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols) {
 
 void Engine::remove(int id) {
     if (!alive(id)) return;
-    QS_CUDA(cudaStreamSynchronize(s_));
-    slots_[id] = Slot();
+    slots_[id] = Slot();   // pooled buffers wait for this stream's work before reuse
     maps_dirty_ = dirty_ = true;
 }
 
@@ -651,7 +728,7 @@ void Engine::build_maps() {
         cap_smap_ = sm.size() * sizeof(int) * 2;
         smap_.alloc(cap_smap_);
     }
-    const size_t pb = (size_t)std::max(1, nrb_) * mmax_ * 2 * sizeof(double);
+    const size_t pb = (size_t)std::max(1, nrb_) * (mmax_ + 1) * 2 * sizeof(double);
     if (pb > cap_partial_) {
         cap_partial_ = pb * 2;
         partial_.alloc(cap_partial_);
@@ -686,35 +763,31 @@ void Engine::sync_table() {
     dirty_ = false;
 }
 
+template <class A>
+static void launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const int* sm, double* pa, const void* rsq,
+                          int nrb, int nsb, int mmax, int ns, cudaStream_t s) {
+    const dim3 gd(nrb, (mmax + kJT - 1) / kJT);
+    eng_spmv<A><<<nsb, kT, 0, s>>>(ds, sm, rsq);
+    eng_dots<A><<<gd, kT, 0, s>>>(ds, rm, mmax, 0, pa);
+    eng_reduce<<<dim3(ns, mmax + 1), kT, 0, s>>>(ds, mmax, 0, pa);
+    eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 0, pa);
+    eng_reduce<<<dim3(ns, 1), kT, 0, s>>>(ds, mmax, 1, pa);
+    eng_dots<A><<<gd, kT, 0, s>>>(ds, rm, mmax, 1, pa);
+    eng_reduce<<<dim3(ns, mmax), kT, 0, s>>>(ds, mmax, 2, pa);
+    eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 1, pa);
+    eng_reduce<<<dim3(ns, 1), kT, 0, s>>>(ds, mmax, 3, pa);
+    eng_scale<A><<<nrb, kT, 0, s>>>(ds, rm, 0);
+    eng_advance<<<(ns + 127) / 128, 128, 0, s>>>(dsw, ns);
+}
+
 void Engine::launch_step() {
-    const SlotDev* ds = dslots_.as<SlotDev>();
-    const int* rm = rmap_.as<int>();
-    const int* sm = smap_.as<int>();
-    double* pa = partial_.as<double>();
     const int ns = (int)slots_.size();
-    const dim3 gd(nrb_, (mmax_ + kJT - 1) / kJT), gr(ns, mmax_);
-    if (df_) {
-        eng_spmv<DF><<<nsb_, kT, 0, s_>>>(ds, sm, rsqdf_.p);
-        eng_dots<DF><<<gd, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
-        eng_reduce<<<gr, kT, 0, s_>>>(ds, mmax_, 0, pa);
-        eng_update<DF><<<nrb_, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
-        eng_dots<DF><<<gd, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
-        eng_reduce<<<gr, kT, 0, s_>>>(ds, mmax_, 1, pa);
-        eng_update<DF><<<nrb_, kT, 0, s_>>>(ds, rm, mmax_, 1, pa);
-        eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 2, pa);
-        eng_scale<DF><<<nrb_, kT, 0, s_>>>(ds, rm, 0);
-    } else {
-        eng_spmv<double><<<nsb_, kT, 0, s_>>>(ds, sm, rsq64_.p);
-        eng_dots<double><<<gd, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
-        eng_reduce<<<gr, kT, 0, s_>>>(ds, mmax_, 0, pa);
-        eng_update<double><<<nrb_, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
-        eng_dots<double><<<gd, kT, 0, s_>>>(ds, rm, mmax_, 0, pa);
-        eng_reduce<<<gr, kT, 0, s_>>>(ds, mmax_, 1, pa);
-        eng_update<double><<<nrb_, kT, 0, s_>>>(ds, rm, mmax_, 1, pa);
-        eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 2, pa);
-        eng_scale<double><<<nrb_, kT, 0, s_>>>(ds, rm, 0);
-    }
-    eng_advance<<<(ns + 127) / 128, 128, 0, s_>>>(dslots_.as<SlotDev>(), ns);
+    if (df_)
+        launch_step_t<DF>(dslots_.as<SlotDev>(), dslots_.as<SlotDev>(), rmap_.as<int>(), smap_.as<int>(),
+                          partial_.as<double>(), rsqdf_.p, nrb_, nsb_, mmax_, ns, s_);
+    else
+        launch_step_t<double>(dslots_.as<SlotDev>(), dslots_.as<SlotDev>(), rmap_.as<int>(), smap_.as<int>(),
+                              partial_.as<double>(), rsq64_.p, nrb_, nsb_, mmax_, ns, s_);
 }
 
 void Engine::capture() {
@@ -751,7 +824,7 @@ void Engine::run(int nsteps) {
     if (nrb_ == 0) return;
     if (!exec_) capture();
     for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
-    launches_ += 10 * (int64_t)nsteps;
+    launches_ += 11 * (int64_t)nsteps;
     // mirror the device step counters
     for (auto& sl : slots_) {
         if (!sl.live || sl.d.state != kSlotStep) continue;
@@ -764,11 +837,9 @@ void Engine::run(int nsteps) {
 
 void Engine::seed(int id, uint64_t sd) {
     const SlotDev& d = slots_[id].d;
-    std::mt19937_64 rng(sd);
-    std::normal_distribution<double> nd(0.0, 1.0);
-    std::vector<double> h((d.cv ? 2 : 1) * d.n);
-    for (auto& v : h) v = nd(rng);
-    load(id, 0, h.data(), false);
+    const VKind ks = df_ ? (d.cv ? VKind::CDF64 : VKind::DF64) : (d.cv ? VKind::C128 : VKind::F64);
+    fill_normal(d.V, ks, d.n, sd, s_);
+    ++launches_;
 }
 
 void Engine::load(int id, int col, const double* v, bool device) {
@@ -777,10 +848,10 @@ void Engine::load(int id, int col, const double* v, bool device) {
     const VKind ks = df_ ? (d.cv ? VKind::CDF64 : VKind::DF64) : k64;
     const size_t bytes = (size_t)d.n * (d.cv ? 16 : 8);
     char* dst = (char*)d.V + (size_t)col * bytes;
-    DevBuf st;
+    PoolBuf st;
     const void* src = v;
     if (!device) {
-        st.alloc(bytes);
+        st.alloc(bytes, s_);
         QS_CUDA(cudaMemcpyAsync(st.p, v, bytes, cudaMemcpyHostToDevice, s_));
         src = st.p;
     }
@@ -798,7 +869,7 @@ void Engine::store(int id, int col, double* out, bool device) {
     if (device) {
         convert_vec(src, ks, out, k64, d.n, s_);
     } else {
-        DevBuf st(bytes);
+        PoolBuf st(bytes, s_);
         convert_vec(src, ks, st.p, k64, d.n, s_);
         QS_CUDA(cudaMemcpyAsync(out, st.p, bytes, cudaMemcpyDeviceToHost, s_));
     }
@@ -823,12 +894,12 @@ std::vector<double> Engine::normalize(const std::vector<int>& ids, int col) {
     const int ns = (int)slots_.size();
     if (nrb_ > 0 && !ids.empty()) {
         if (df_) {
-            eng_dots<DF><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 1, pa);
-            eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 3, pa);
+            eng_dots<DF><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 2, pa);
+            eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 4, pa);
             eng_scale<DF><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
         } else {
-            eng_dots<double><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 1, pa);
-            eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 3, pa);
+            eng_dots<double><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 2, pa);
+            eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 4, pa);
             eng_scale<double><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
         }
         QS_CUDA(cudaGetLastError());
@@ -845,7 +916,21 @@ std::vector<double> Engine::normalize(const std::vector<int>& ids, int col) {
 
 void Engine::rotate(const std::vector<RotReq>& reqs) {
     if (reqs.empty()) return;
+    // every slot's coefficients in the storage format (double2, or float4 hi/lo
+    // pairs) packed into one upload
+    size_t total = 0;
+    for (const RotReq& R : reqs) total += R.Y.size();
+    if (total * 16 > cap_y_) {
+        cap_y_ = std::max<size_t>(total * 16 * 2, 1 << 16);
+        QS_CUDA(cudaStreamSynchronize(s_));
+        ybuf_.alloc(cap_y_);
+    }
+    std::vector<double> c64;
+    std::vector<float> cdf;
+    if (df_) cdf.resize(4 * total);
+    else c64.resize(2 * total);
     std::vector<int> saved(reqs.size());
+    size_t off = 0;
     for (size_t q = 0; q < reqs.size(); ++q) {
         const RotReq& R = reqs[q];
         Slot& sl = slots_[R.id];
@@ -854,40 +939,32 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
                          R.out0 < 0 || R.out0 + R.p > d.m + 1 || R.Y.size() != (size_t)R.nin * R.p ||
                          (R.carry >= 0 && (R.carry > d.m || R.cdst < 0 || R.cdst > d.m));
         if (bad) throw Error(QS_ERR_ARGUMENT, "rotation shape outside the Krylov basis");
-        if (R.p > 0) {
-            // coefficients in the storage format: double2 or float4 (hi, lo pairs)
-            std::vector<double> c64;
-            std::vector<float> cdf;
-            const void* src;
-            size_t bytes;
+        bool yreal = true;
+        for (size_t i = 0; i < R.Y.size(); ++i) {
+            const double re = R.Y[i].real(), im = R.Y[i].imag();
+            if (im != 0.0) yreal = false;
             if (df_) {
-                cdf.resize(4 * R.Y.size());
-                for (size_t i = 0; i < R.Y.size(); ++i) {
-                    df_split_host(R.Y[i].real(), cdf[4 * i], cdf[4 * i + 1]);
-                    df_split_host(R.Y[i].imag(), cdf[4 * i + 2], cdf[4 * i + 3]);
-                }
-                src = cdf.data();
-                bytes = cdf.size() * sizeof(float);
+                df_split_host(re, cdf[4 * (off + i)], cdf[4 * (off + i) + 1]);
+                df_split_host(im, cdf[4 * (off + i) + 2], cdf[4 * (off + i) + 3]);
             } else {
-                c64.resize(2 * R.Y.size());
-                for (size_t i = 0; i < R.Y.size(); ++i) {
-                    c64[2 * i] = R.Y[i].real();
-                    c64[2 * i + 1] = R.Y[i].imag();
-                }
-                src = c64.data();
-                bytes = c64.size() * sizeof(double);
+                c64[2 * (off + i)] = re;
+                c64[2 * (off + i) + 1] = im;
             }
-            QS_CUDA(cudaMemcpyAsync(d.y, src, bytes, cudaMemcpyHostToDevice, s_));
-            QS_CUDA(cudaStreamSynchronize(s_));
         }
         saved[q] = d.state;
         d.state = kSlotRotate;
+        d.y = (char*)ybuf_.p + off * 16;
+        d.yreal = yreal;
         d.rot_in = R.nin;
         d.p = R.p;
         d.out0 = R.out0;
         d.carry = R.carry;
         d.cdst = R.cdst;
+        off += R.Y.size();
     }
+    if (total)
+        QS_CUDA(cudaMemcpyAsync(ybuf_.p, df_ ? (const void*)cdf.data() : (const void*)c64.data(), total * 16,
+                                cudaMemcpyHostToDevice, s_));
     dirty_ = true;
     sync_table();
     if (nrb_ > 0) {
@@ -906,12 +983,80 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
 }
 
 void Engine::record(int id, std::vector<cd>& H) {
-    const SlotDev& d = slots_[id].d;
-    std::vector<double> h((size_t)2 * (d.m + 1) * d.m);
-    QS_CUDA(cudaMemcpyAsync(h.data(), d.rec, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s_));
+    std::vector<std::vector<cd>> all;
+    records({id}, all);
+    H = std::move(all[0]);
+}
+
+void Engine::records(const std::vector<int>& ids, std::vector<std::vector<cd>>& H) {
+    H.assign(ids.size(), {});
+    for (size_t q = 0; q < ids.size(); ++q) {
+        const SlotDev& d = slots_[ids[q]].d;
+        H[q].resize((size_t)(d.m + 1) * d.m);   // std::complex<double> is two doubles
+        QS_CUDA(cudaMemcpyAsync(H[q].data(), d.rec, H[q].size() * sizeof(cd), cudaMemcpyDeviceToHost, s_));
+    }
     QS_CUDA(cudaStreamSynchronize(s_));
-    H.resize((size_t)(d.m + 1) * d.m);
-    for (size_t i = 0; i < H.size(); ++i) H[i] = cd(h[2 * i], h[2 * i + 1]);
+}
+
+// ================================================================ eigsh task
+void EigTask::init(int k_, int which_, double tol_, int m_, int maxiter_) {
+    k = k_;
+    which = which_;
+    m = m_;
+    tol = tol_ > 0 ? tol_ : 2.220446049250313e-16;
+    maxiter = maxiter_ > 0 ? maxiter_ : 300;
+    p = std::max(std::min(m - 2, k + (m - k) / 2), std::min(k, m - 1));
+    T.assign((size_t)m * m, 0.0);
+    theta.assign(k, 0.0);
+    beta = maxrel = 0;
+    nconv = restarts = j0 = 0;
+}
+
+bool EigTask::on_hold(const std::vector<cd>& H, int id, RotReq& rot) {
+    static const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
+    for (int j = j0; j < m; ++j) {
+        T[(size_t)j * m + j] = H[(size_t)j * (m + 1) + j].real();
+        const double b = H[(size_t)j * (m + 1) + j + 1].real();
+        if (j + 1 < m) T[(size_t)j * m + j + 1] = T[(size_t)(j + 1) * m + j] = b;
+        else beta = b;
+    }
+    std::vector<double> w, Y;
+    sym_eig(m, T, w, Y);
+    std::vector<int> order(m);
+    for (int q = 0; q < m; ++q) order[q] = which == 0 ? q : m - 1 - q;
+    int nc = 0;
+    double mr = 0;
+    for (int q = 0; q < k; ++q) {
+        const int c = order[q];
+        const double bound = std::fabs(beta * Y[(size_t)(m - 1) * m + c]);
+        mr = std::max(mr, bound / std::max(eps23, std::fabs(w[c])));
+        if (bound <= tol * std::max(eps23, std::fabs(w[c]))) ++nc;
+    }
+    nconv = nc;
+    maxrel = mr;
+    for (int q = 0; q < k; ++q) theta[q] = w[order[q]];
+    const bool fin = nc >= k || restarts >= maxiter - 1;
+    const int keep = fin ? k : p;
+    rot.id = id;
+    rot.Y.assign((size_t)m * keep, cd(0, 0));
+    for (int q = 0; q < keep; ++q)
+        for (int r = 0; r < m; ++r) rot.Y[(size_t)q * m + r] = cd(Y[(size_t)r * m + order[q]], 0.0);
+    rot.nin = m;
+    rot.p = keep;
+    rot.out0 = 0;
+    rot.carry = fin ? -1 : m;   // thick restart: the residual direction follows the Ritz vectors
+    rot.cdst = keep;
+    if (!fin) {
+        std::fill(T.begin(), T.end(), 0.0);
+        for (int q = 0; q < p; ++q) {
+            T[(size_t)q * m + q] = w[order[q]];
+            const double c = beta * Y[(size_t)(m - 1) * m + order[q]];
+            T[(size_t)q * m + p] = T[(size_t)p * m + q] = c;
+        }
+        j0 = p;
+        ++restarts;
+    }
+    return fin;
 }
 
 // ================================================================ batched eigsh
@@ -932,108 +1077,56 @@ void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, voi
         m = (int)std::min<int64_t>(m, n);
     }
     if (m <= k) throw Error(QS_ERR_ARGUMENT, "ncv must exceed k");
-    const double tol = o.tol > 0 ? o.tol : 2.220446049250313e-16;
-    const int maxiter = o.maxiter > 0 ? o.maxiter : 300;
-    const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
     Engine E(o.precision != 0, ops[0]->stream);
     std::vector<int> id(nops);
+    std::vector<EigTask> task(nops);
     for (int i = 0; i < nops; ++i) {
         id[i] = E.add(*ops[i], m, ops[i]->complex_mat);
         E.seed(id[i], 20261203ull);
+        task[i].init(k, o.which, o.tol, m, o.maxiter);
     }
     E.normalize(id);
-    struct St {
-        std::vector<double> T;
-        std::vector<double> theta;
-        double beta = 0, maxrel = 0;
-        int nconv = 0, restarts = 0, j0 = 0;
-        bool done = false;
-    };
-    std::vector<St> st(nops);
-    for (int i = 0; i < nops; ++i) {
-        st[i].T.assign((size_t)m * m, 0.0);
-        E.start(id[i], 0);
-    }
-    const int p = std::max(std::min(m - 2, k + (m - k) / 2), std::min(k, m - 1));
-    std::vector<cd> H;
+    for (int i = 0; i < nops; ++i) E.start(id[i], 0);
+    std::vector<char> done(nops, 0);
     int left = nops;
     while (left > 0) {
         const int steps = E.steps_to_event();
         if (steps <= 0) throw Error(QS_ERR_CUDA, "batched eigsh lost its stepping slots");
         E.run(steps);
         std::vector<RotReq> rot;
-        std::vector<int> fin_slots;
-        for (int i = 0; i < nops; ++i) {
-            St& s = st[i];
-            if (s.done || E.slot(id[i]).state != kSlotHold) continue;
-            E.record(id[i], H);
-            for (int j = s.j0; j < m; ++j) {
-                s.T[(size_t)j * m + j] = H[(size_t)j * (m + 1) + j].real();
-                const double b = H[(size_t)j * (m + 1) + j + 1].real();
-                if (j + 1 < m) s.T[(size_t)j * m + j + 1] = s.T[(size_t)(j + 1) * m + j] = b;
-                else s.beta = b;
+        std::vector<int> fin, hold, hold_ids;
+        for (int i = 0; i < nops; ++i)
+            if (!done[i] && E.slot(id[i]).state == kSlotHold) {
+                hold.push_back(i);
+                hold_ids.push_back(id[i]);
             }
-            std::vector<double> w, Y;
-            sym_eig(m, s.T, w, Y);
-            std::vector<int> order(m);
-            for (int q = 0; q < m; ++q) order[q] = o.which == 0 ? q : m - 1 - q;
-            int nc = 0;
-            double mr = 0;
-            for (int q = 0; q < k; ++q) {
-                const int c = order[q];
-                const double bound = std::fabs(s.beta * Y[(size_t)(m - 1) * m + c]);
-                mr = std::max(mr, bound / std::max(eps23, std::fabs(w[c])));
-                if (bound <= tol * std::max(eps23, std::fabs(w[c]))) ++nc;
-            }
-            s.nconv = nc;
-            s.maxrel = mr;
-            s.theta.assign(k, 0.0);
-            for (int q = 0; q < k; ++q) s.theta[q] = w[order[q]];
-            const bool fin = nc >= k || s.restarts >= maxiter - 1;
-            const int keep = fin ? k : p;
-            std::vector<cd> Yc((size_t)m * keep);
-            for (int q = 0; q < keep; ++q)
-                for (int r = 0; r < m; ++r) Yc[(size_t)q * m + r] = cd(Y[(size_t)r * m + order[q]], 0.0);
+        std::vector<std::vector<cd>> H;
+        E.records(hold_ids, H);
+        for (size_t q = 0; q < hold.size(); ++q) {
+            const int i = hold[q];
             RotReq R;
-            R.id = id[i];
-            R.Y = std::move(Yc);
-            R.nin = m;
-            R.p = keep;
-            R.carry = fin ? -1 : m;   // thick restart: the residual direction follows the Ritz vectors
-            R.cdst = keep;
+            if (task[i].on_hold(H[q], id[i], R)) fin.push_back(i);
             rot.push_back(std::move(R));
-            if (fin) {
-                fin_slots.push_back(i);
-            } else {
-                std::fill(s.T.begin(), s.T.end(), 0.0);
-                for (int q = 0; q < p; ++q) {
-                    s.T[(size_t)q * m + q] = w[order[q]];
-                    const double c = s.beta * Y[(size_t)(m - 1) * m + order[q]];
-                    s.T[(size_t)q * m + p] = s.T[(size_t)p * m + q] = c;
-                }
-                s.j0 = p;
-                ++s.restarts;
-            }
         }
         E.rotate(rot);
         for (const RotReq& R : rot)
-            if (R.carry >= 0) E.start(R.id, p);
-        for (int i : fin_slots) {
-            St& s = st[i];
-            s.done = true;
+            if (R.carry >= 0) E.start(R.id, task[0].p);
+        for (int i : fin) {
+            const EigTask& t = task[i];
+            done[i] = 1;
             --left;
-            if (s.nconv < k) throw Error(QS_ERR_NOT_CONVERGED, "batched eigsh did not converge within maxiter restarts");
-            for (int q = 0; q < k; ++q) values[(size_t)i * k + q] = s.theta[q];
+            if (t.nconv < k) throw Error(QS_ERR_NOT_CONVERGED, "batched eigsh did not converge within maxiter restarts");
+            for (int q = 0; q < k; ++q) values[(size_t)i * k + q] = t.theta[q];
             if (vectors && vectors[i]) {
                 const int64_t n = ops[i]->basis->n;
                 const int comps = ops[i]->complex_mat ? 2 : 1;
                 for (int q = 0; q < k; ++q) E.store(id[i], q, (double*)vectors[i] + (size_t)q * n * comps, false);
             }
             if (infos) {
-                infos[i].nconv = s.nconv;
-                infos[i].restarts = s.restarts;
+                infos[i].nconv = t.nconv;
+                infos[i].restarts = t.restarts;
                 infos[i].matvecs = E.matvecs(id[i]);
-                infos[i].max_rel_residual = s.maxrel;
+                infos[i].max_rel_residual = t.maxrel;
                 infos[i].seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             }
             E.remove(id[i]);

@@ -1,9 +1,10 @@
 // qs_engine.h -- the batched Krylov engine: many Krylov processes ("slots"),
 // each on its own assembled operator and its own vectors, advanced together.
 //
-// One Lanczos/Arnoldi step of every stepping slot is a fixed sequence of ten
-// launches (SpMV, two CGS passes of dots + reduce + update, norm, scale,
-// advance), each covering all slots through a block -> slot map.  The step
+// One Lanczos/Arnoldi step of every stepping slot is a fixed sequence of
+// eleven launches (SpMV; dots + reduce + update with the norm fused; the
+// conditional second Gram-Schmidt pass; scale; advance), each covering all
+// slots through a block -> slot map.  The step
 // counters live on the device, so the sequence is captured once in a CUDA
 // graph and replayed; the host only meets the device when a slot has filled
 // its basis (restart, convergence test, exponential).  The projected matrix of
@@ -56,11 +57,20 @@ struct SlotDev {
     double2* h2;            // m second-pass CGS coefficients
     double2* rec;           // (m + 1) x m projected matrix, column-major
     void* y;                // rotation coefficients, rot_in x p column-major (storage format)
-    double* nrm;            // [0] squared norm, [1] 1 / norm, [2] norm of column 0 when normalised
+    // [0] squared norm of the new direction, [1] its inverse norm, [2] norm of
+    // a normalised column, [3] ||w||^2 before orthogonalisation, [4] 1 when the
+    // second Gram-Schmidt pass runs in this step
+    double* nrm;
     int32_t m, j, state;
+    // orthogonalisation of a step: 0 classical Gram-Schmidt twice (CGS2);
+    // 1 CGS with the DGKS correction only when ||w'|| < 0.717 ||w|| (ARPACK's
+    // dsaitr test); 2 Lanczos three-term recurrence (Hermitian operators,
+    // the reference's Krylov exponential)
+    int32_t orth;
     // rotation: V[:, out0 + c] = sum_{i < rot_in} V[:, i] Y[i, c] for c < p, then
     // V[:, cdst] = V[:, carry] when carry >= 0
     int32_t rot_in, p, out0, carry, cdst;
+    int32_t yreal;          // rotation coefficients are real
     int32_t ncol;           // column normalised by normalize()
     // tiles
     int32_t rpb, spb;       // rows per BLAS block, slices per SpMV block
@@ -90,7 +100,7 @@ class Engine {
     // Adds a slot of basis size m on an assembled operator (assembled here if
     // needed).  cv: complex vectors (required for complex operators); tmp_cols:
     // most rotation outputs (m - 1 when 0).
-    int add(Op& op, int m, bool cv, bool tune = true, int tmp_cols = 0);
+    int add(Op& op, int m, bool cv, bool tune = true, int tmp_cols = 0, int orth = 1);
     // device bytes add() would allocate for a slot
     static size_t slot_bytes(int64_t n, int m, bool cv, int tmp_cols = 0);
     void remove(int id);
@@ -118,6 +128,8 @@ class Engine {
     int steps_to_event() const;
     // Host copy of the projected matrix record ((m + 1) x m, column-major).
     void record(int id, std::vector<cd>& H);
+    // The same for several slots with one synchronisation.
+    void records(const std::vector<int>& ids, std::vector<std::vector<cd>>& H);
     int64_t launches() const { return launches_; }
     int64_t matvecs(int id) const { return slots_[id].matvecs; }
 
@@ -125,7 +137,7 @@ class Engine {
     struct Slot {
         Op* op = nullptr;
         SlotDev d{};
-        DevBuf V, tmp, small, y;
+        PoolBuf V, tmp, small;
         int tcols = 0;    // columns of tmp
         bool live = false;
         int64_t matvecs = 0;
@@ -138,7 +150,8 @@ class Engine {
     bool df_;
     cudaStream_t s_;
     std::vector<Slot> slots_;
-    DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_;
+    DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_, ybuf_;
+    size_t cap_y_ = 0;
     int nrb_ = 0, nsb_ = 0, mmax_ = 1, cap_slots_ = 0;
     size_t cap_partial_ = 0, cap_rmap_ = 0, cap_smap_ = 0;
     bool dirty_ = true, maps_dirty_ = true;
@@ -146,6 +159,22 @@ class Engine {
     cudaGraphExec_t exec_ = nullptr;
     int64_t launches_ = 0;
     friend struct EngineTuner;
+};
+
+// Thick-restart Lanczos (Wu-Simon) on one slot, ARPACK's convergence test:
+// the state kept on the host between the slot's Hold events.
+struct EigTask {
+    int k = 1, which = 0, m = 20, p = 10, maxiter = 300;
+    double tol = 0;
+    std::vector<double> T, theta;
+    double beta = 0, maxrel = 0;
+    int nconv = 0, restarts = 0, j0 = 0;
+    void init(int k_, int which_, double tol_, int m_, int maxiter_);
+    // Called when the slot has filled its basis, with its record H: Ritz
+    // values, then either a thick restart (rot keeps p Ritz vectors and the
+    // residual direction; returns false, restart the slot at column p) or the
+    // final rotation (k Ritz vectors into columns 0..k-1; returns true).
+    bool on_hold(const std::vector<cd>& H, int id, RotReq& rot);
 };
 
 }  // namespace qs

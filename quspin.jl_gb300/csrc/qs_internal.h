@@ -58,6 +58,45 @@ struct DevBuf {
     template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 
+// Cached device allocations for buffers that live for one solve (Krylov
+// bases, slot storage): freed blocks are kept for reuse up to a cap (a tenth
+// of device memory, at most 32 GB), so a solve does not pay cudaMalloc /
+// cudaFree for its large buffers.  A block returned with pool_put carries an
+// event recorded on the stream that last used it; pool_get waits for that
+// event before handing the block out again.  pool_trim() frees every cached
+// block.
+void* pool_get(size_t bytes);
+void pool_put(void* p, size_t bytes, cudaStream_t last_use);
+void pool_trim();
+
+struct PoolBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaStream_t s = nullptr;   // the stream the buffer is used on
+    PoolBuf() = default;
+    PoolBuf(size_t n, cudaStream_t st) { alloc(n, st); }
+    PoolBuf(const PoolBuf&) = delete;
+    PoolBuf& operator=(const PoolBuf&) = delete;
+    PoolBuf(PoolBuf&& o) noexcept : p(o.p), bytes(o.bytes), s(o.s) { o.p = nullptr; o.bytes = 0; }
+    PoolBuf& operator=(PoolBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; bytes = o.bytes; s = o.s; o.p = nullptr; o.bytes = 0; }
+        return *this;
+    }
+    ~PoolBuf() { release(); }
+    void alloc(size_t n, cudaStream_t st) {
+        release();
+        s = st;
+        if (n) p = pool_get(n);
+        bytes = n;
+    }
+    void release() {
+        if (p) pool_put(p, bytes, s);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
 // Symmetry generator in the reference's order (src/basis.jl:691-735).
 enum GenKind { GEN_T = 0, GEN_P, GEN_Z, GEN_PZ, GEN_ZA, GEN_ZB };
 struct Generator {

@@ -63,17 +63,9 @@ VKind krylov_kind(const Op& op, bool cpx, int precision) {
     return cpx ? VKind::C128 : VKind::F64;
 }
 
-// Deterministic pseudo-random start vector (normal entries).
+// Deterministic pseudo-random start vector (normal entries, generated on the device).
 void random_vector(Ctx& c, void* dst, uint64_t seed) {
-    std::mt19937_64 rng(seed);
-    std::normal_distribution<double> nd(0.0, 1.0);
-    bool cpx = vk_complex(c.vk);
-    std::vector<double> h((cpx ? 2 : 1) * c.n);
-    for (auto& v : h) v = nd(rng);
-    VKind k64 = cpx ? VKind::C128 : VKind::F64;
-    DevBuf tmp(h.size() * sizeof(double));
-    QS_CUDA(cudaMemcpyAsync(tmp.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c.s));
-    convert_vec(tmp.p, k64, dst, c.vk, c.n, c.s);
+    fill_normal(dst, c.vk, c.n, seed, c.s);
     QS_CUDA(cudaStreamSynchronize(c.s));
 }
 

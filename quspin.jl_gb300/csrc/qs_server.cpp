@@ -1,0 +1,788 @@
+// qs_server.cpp -- the request loop: ground-state (eigsh) and time-evolution
+// (evolve) solves of mixed sizes and sectors, continuously batched on one GPU.
+//
+// Requests arrive through qs_server_submit from any thread.  A builder thread
+// admits them in arrival order against a device-memory budget (operator,
+// basis and Krylov state are all counted), builds the basis and the assembled
+// operator on its own streams (or takes it from a cache of operators keyed by
+// sector and terms), and hands it to the engine thread.  The engine thread
+// owns one batched Krylov engine (qs_engine.h): new requests become slots as
+// soon as they are built, whatever the phase of the running ones, and every
+// Krylov step of every running solve is one replay of the captured step
+// graph.  A slot's arithmetic depends only on its own operator and vectors,
+// so a result is the same alone and in the mix.
+//
+// eigsh follows the thick-restart Lanczos of qs_eigsh (src/operators.jl:
+// 1558-1640 / 3367-3408 through ARPACK); evolve follows _krylov_expmv_vector
+// (src/operators.jl:1758-1803): a Krylov projection of krylov_dim steps, the
+// error estimate |s| h_{m+1,m} beta |e_m^T exp(sH) e_1|, and on failure the
+// same two half steps with half the tolerance, up to depth 14.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/qsgpu.h"
+#include "qs_dense.h"
+#include "qs_engine.h"
+#include "qs_internal.h"
+#include "qs_server.h"
+
+namespace qs {
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+size_t basis_bytes(const Basis& b) {
+    return b.d_group.bytes + b.d_reps.bytes + b.d_stab.bytes + b.d_split.bytes + b.d_binom.bytes + b.d_index.bytes +
+           b.d_fast_chi.bytes + b.d_level_groups.bytes + b.d_level0.bytes;
+}
+
+size_t op_bytes(const Op& o) {
+    const Assembled& M = o.asm_;
+    return o.d_progs.bytes + o.d_diag.bytes + o.d_diag32.bytes + o.d_diag_re.bytes + o.d_diag32_re.bytes +
+           o.d_diag_df.bytes + o.d_x.bytes + o.d_y.bytes + o.d_x32.bytes + o.d_y32.bytes + M.rowptr.bytes +
+           M.words.bytes + M.cols.bytes + M.codes.bytes + M.table64.bytes + M.table32.bytes + M.table_df.bytes +
+           M.xsplit.bytes + M.rsq_df.bytes + M.sell_words.bytes + M.sell_cols.bytes + M.sell_codes.bytes +
+           M.sell_ptr.bytes + M.sell_perm.bytes + M.sell_len.bytes;
+}
+
+double binom(int n, int k) {
+    if (k < 0 || k > n) return 0;
+    double r = 1;
+    for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+    return r;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ server state
+struct TermCopy {
+    std::string op;
+    std::vector<double> coeffs;
+    std::vector<int32_t> sites;
+    int32_t n = 0, cc = 0;
+};
+
+struct CachedOp {
+    std::string key;
+    std::unique_ptr<Basis> basis;
+    Op* op = nullptr;
+    size_t bytes = 0;
+    int users = 0;
+    uint64_t last_use = 0;
+    ~CachedOp() {
+        delete op;
+    }
+};
+
+struct Request {
+    int64_t ticket = 0;
+    qs_request r{};
+    std::vector<TermCopy> terms;
+    std::vector<double> v0;
+    std::string key;
+    double t_submit = 0, t_admit = -1, t_done = -1;
+    std::atomic<int> status{QS_PENDING};
+    bool cancel = false;
+    std::string error;
+    std::vector<double> values;
+    std::vector<double> vec;
+    int64_t n = 0, matvecs = 0;
+    int restarts = 0;
+    double err = 0;
+    // runtime
+    std::shared_ptr<CachedOp> op;
+    size_t slot_reserved = 0;
+    int slot = -1;
+    bool cv = false;
+    int m = 0;
+    // eigsh
+    EigTask eig;
+    // evolve: segments (scale, tol, depth) still to apply, norm of the start
+    struct Seg {
+        cd scale;
+        double tol;
+        int depth;
+    };
+    std::deque<Seg> segs;
+    double beta = 0;
+};
+
+struct Server {
+    qs_server_opts opts{};
+    cudaStream_t stream = nullptr;
+    Clock::time_point t0 = Clock::now();
+    std::mutex mu;
+    std::condition_variable cv_build, cv_engine, cv_done;
+    std::deque<std::shared_ptr<Request>> pending;   // submitted, not yet admitted
+    std::deque<std::shared_ptr<Request>> ready;     // built, waiting for a slot
+    std::map<int64_t, std::shared_ptr<Request>> all;
+    std::map<std::string, std::shared_ptr<CachedOp>> cache;
+    std::map<std::string, int> building;             // keys a builder is working on
+    int64_t next_ticket = 1;
+    size_t used = 0, peak = 0;
+    int running = 0;
+    bool stop = false;
+    uint64_t use_clock = 0;
+    qs_server_counters stats{};
+    std::vector<std::shared_ptr<CachedOp>> graveyard;   // evicted, freed outside the lock
+    std::vector<std::thread> builders;
+    std::thread engine;
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+};
+
+namespace {
+
+std::string make_key(const qs_request& r, const std::vector<TermCopy>& terms) {
+    std::string k;
+    auto put = [&](const void* p, size_t n) { k.append((const char*)p, n); };
+    put(&r.basis, sizeof(r.basis));
+    for (const TermCopy& t : terms) {
+        k += t.op;
+        k += '|';
+        put(&t.n, sizeof(t.n));
+        put(&t.cc, sizeof(t.cc));
+        put(t.coeffs.data(), t.coeffs.size() * sizeof(double));
+        put(t.sites.data(), t.sites.size() * sizeof(int32_t));
+    }
+    return k;
+}
+
+// Upper estimate of the device bytes of a request before anything is built.
+size_t estimate_bytes(const Request& q, bool cached, int64_t n_known) {
+    const qs_basis_spec& sp = q.r.basis;
+    const int L = sp.L;
+    const double parent = sp.nup >= 0 ? binom(L, sp.nup) : std::ldexp(1.0, L);
+    double order = 1;
+    if (sp.has_kblock) order *= std::max(1, L / std::max(1, sp.a));
+    for (int b : {sp.pblock, sp.zblock, sp.pzblock, sp.zAblock, sp.zBblock})
+        if (b) order *= 2;
+    double n = n_known > 0 ? (double)n_known : std::ceil(parent / order * 1.2) + 64;
+    double offd = 1;
+    for (const TermCopy& t : q.terms)
+        if (t.op.find_first_of("+-xy") != std::string::npos) offd += t.n;
+    double total = 0;
+    if (!cached) {
+        total += parent * 4 + n * 32;                    // rank index, representatives, stabilisers
+        total += n * offd * 4 * 2.4 + n * (16 * 6 + 8);  // CSR + sliced words, diagonals, staging
+    }
+    const int m = q.r.kind == QS_REQ_EIGSH ? std::max(20, 2 * q.r.k + 1) : (q.r.krylov_dim > 0 ? q.r.krylov_dim : 30);
+    total += (double)Engine::slot_bytes((int64_t)n, std::min(m, 64), true, 0);
+    return (size_t)total;
+}
+
+void finish(Server& S, const std::shared_ptr<Request>& q, int status, const std::string& err) {
+    std::lock_guard<std::mutex> g(S.mu);
+    q->t_done = S.now();
+    q->error = err;
+    if (q->op) {
+        q->op->users--;
+        q->op->last_use = ++S.use_clock;
+        if (S.opts.disable_op_cache && q->op->users == 0 && S.cache.count(q->op->key)) {
+            // without the cache an operator's bytes go with its last request
+            S.cache.erase(q->op->key);
+            S.used -= std::min(S.used, q->op->bytes);
+            S.graveyard.push_back(q->op);
+        }
+        q->op.reset();
+    }
+    S.used -= std::min(S.used, q->slot_reserved);
+    q->slot_reserved = 0;
+    if (status == QS_OK) S.stats.completed++;
+    else S.stats.failed++;
+    S.running--;
+    q->status.store(status);
+    S.cv_build.notify_all();
+    S.cv_done.notify_all();
+}
+
+// Frees cached operators nobody uses, oldest first, until `need` more bytes fit.
+bool make_room(Server& S, size_t need) {
+    while (S.used + need > (size_t)S.opts.hbm_budget_bytes) {
+        std::shared_ptr<CachedOp> victim;
+        for (auto& kv : S.cache)
+            if (kv.second->users == 0 && (!victim || kv.second->last_use < victim->last_use)) victim = kv.second;
+        if (!victim) return false;
+        S.used -= std::min(S.used, victim->bytes);
+        S.cache.erase(victim->key);
+        S.graveyard.push_back(victim);
+        S.stats.evictions++;
+    }
+    return true;
+}
+
+// ------------------------------------------------------------ builder thread
+void builder_loop(Server& S) {
+    int dev = S.opts.device;
+    cudaSetDevice(dev);
+    while (true) {
+        std::shared_ptr<Request> q;
+        std::shared_ptr<CachedOp> hit;
+        size_t est = 0;
+        {
+            // free evicted operators without holding the lock (cudaFree waits for the device)
+            std::vector<std::shared_ptr<CachedOp>> dead;
+            {
+                std::lock_guard<std::mutex> g(S.mu);
+                dead.swap(S.graveyard);
+            }
+            dead.clear();
+        }
+        {
+            std::unique_lock<std::mutex> g(S.mu);
+            // admit the oldest pending request whose sector no other builder is
+            // building, once its estimate fits the budget
+            while (true) {
+                if (S.stop) return;
+                auto pos = S.pending.begin();
+                while (pos != S.pending.end() && !(*pos)->cancel && S.building.count((*pos)->key)) ++pos;
+                if (pos != S.pending.end()) {
+                    q = *pos;
+                    if (q->cancel) {
+                        S.pending.erase(pos);
+                        q->t_done = S.now();
+                        q->error = "cancelled";
+                        q->status.store(QS_ERR_ARGUMENT);
+                        S.stats.failed++;
+                        S.cv_done.notify_all();
+                        q.reset();
+                        continue;
+                    }
+                    auto it = S.cache.find(q->key);
+                    hit = it != S.cache.end() ? it->second : nullptr;
+                    est = estimate_bytes(*q, (bool)hit, hit ? hit->basis->n : 0);
+                    if (hit) hit->users++;   // pin while waiting for room
+                    const bool fits = make_room(S, est);
+                    if (hit) hit->users--;
+                    if (fits && S.running < S.opts.max_slots) {
+                        S.pending.erase(pos);
+                        if (!hit) S.building[q->key]++;
+                        S.used += est;
+                        S.peak = std::max(S.peak, S.used);
+                        S.running++;
+                        if (hit) hit->users++;
+                        break;
+                    }
+                    if (!fits && S.running == 0) {
+                        // nothing will free memory (unused operators were evicted):
+                        // the request alone exceeds the budget
+                        S.pending.erase(pos);
+                        q->t_done = S.now();
+                        q->error = "request exceeds the device memory budget";
+                        q->status.store(QS_ERR_NOMEM);
+                        S.stats.failed++;
+                        S.cv_done.notify_all();
+                        q.reset();
+                        continue;
+                    }
+                }
+                S.cv_build.wait_for(g, std::chrono::milliseconds(50));
+            }
+            q->t_admit = S.now();
+        }
+        // build outside the lock
+        std::string err;
+        int status = QS_OK;
+        bool built = false;   // a new operator joined the cache (its bytes stay counted)
+        try {
+            if (hit) {
+                q->op = hit;
+                std::lock_guard<std::mutex> g(S.mu);
+                S.stats.cache_hits++;
+            } else {
+                auto c = std::make_shared<CachedOp>();
+                c->key = q->key;
+                c->basis = std::make_unique<Basis>();
+                c->basis->spec = q->r.basis;
+                basis_build(*c->basis);
+                std::vector<qs_term> tv(q->terms.size());
+                for (size_t i = 0; i < q->terms.size(); ++i) {
+                    const TermCopy& t = q->terms[i];
+                    tv[i] = qs_term{t.op.c_str(), t.n, t.coeffs.data(), t.sites.data(), t.cc};
+                }
+                c->op = op_create(c->basis.get(), tv.data(), (int)tv.size(), nullptr,
+                                  QS_CHECK_SYMM | QS_CHECK_HERM | QS_CHECK_PCON);
+                op_assemble(*c->op);
+                // the engine reads only the sliced layout: drop the row-compressed copy
+                Assembled& M = c->op->asm_;
+                M.rowptr.release();
+                M.words.release();
+                M.cols.release();
+                M.codes.release();
+                M.xsplit.release();
+                QS_CUDA(cudaStreamSynchronize(c->op->stream));
+                c->bytes = basis_bytes(*c->basis) + op_bytes(*c->op);
+                c->users = 1;
+                q->op = c;
+                std::lock_guard<std::mutex> g(S.mu);
+                S.cache[c->key] = c;
+                built = true;
+                S.stats.builds++;
+            }
+            if (!q->op->op->hermitian && q->r.kind == QS_REQ_EIGSH)
+                throw Error(QS_ERR_UNSUPPORTED, "eigsh on this engine needs a Hermitian operator");
+            q->n = q->op->basis->n;
+            const bool cv = q->r.kind == QS_REQ_EVOLVE || q->op->op->complex_mat;
+            int m;
+            if (q->r.kind == QS_REQ_EIGSH) {
+                m = q->r.ncv > 0 ? q->r.ncv : std::max(20, 2 * q->r.k + 1);
+                m = (int)std::min<int64_t>(std::min(m, 64), q->n);
+                if (q->r.k < 1 || q->r.k >= q->n - 1 || m <= q->r.k)
+                    throw Error(QS_ERR_ARGUMENT, "served eigsh needs 1 <= k < Ns - 1");
+            } else {
+                m = q->r.krylov_dim > 0 ? q->r.krylov_dim : 30;
+                m = (int)std::min<int64_t>(std::min(m, 64), q->n);
+                if (m < 2) throw Error(QS_ERR_ARGUMENT, "served evolve needs Ns >= 2");
+            }
+            q->cv = cv;
+            q->m = m;
+            // replace the estimate by what is really held: the slot, and a new
+            // operator (which stays counted while it is cached)
+            std::lock_guard<std::mutex> g(S.mu);
+            const size_t slot = Engine::slot_bytes(q->n, m, cv, q->r.kind == QS_REQ_EIGSH ? 0 : 1);
+            S.used = S.used - std::min(S.used, est) + slot + (built ? q->op->bytes : 0);
+            S.peak = std::max(S.peak, S.used);
+            est = 0;
+            built = false;
+            q->slot_reserved = slot;
+        } catch (const Error& e) {
+            status = e.status;
+            err = e.what();
+        } catch (const std::exception& e) {
+            status = QS_ERR_CUDA;
+            err = e.what();
+        }
+        if (!hit) {
+            std::lock_guard<std::mutex> g(S.mu);
+            if (--S.building[q->key] <= 0) S.building.erase(q->key);
+            S.cv_build.notify_all();
+        }
+        if (status != QS_OK) {
+            {
+                std::lock_guard<std::mutex> g(S.mu);
+                S.used = S.used - std::min(S.used, est) + (built && q->op ? q->op->bytes : 0);
+                q->slot_reserved = 0;
+            }
+            if (q->op) {
+                finish(S, q, status, err);
+            } else {
+                std::lock_guard<std::mutex> g(S.mu);
+                q->t_done = S.now();
+                q->error = err;
+                S.running--;
+                S.stats.failed++;
+                q->status.store(status);
+                S.cv_done.notify_all();
+                S.cv_build.notify_all();
+            }
+            continue;
+        }
+        std::lock_guard<std::mutex> g(S.mu);
+        S.ready.push_back(q);
+        S.cv_engine.notify_all();
+    }
+}
+
+// ------------------------------------------------------------ engine thread
+void engine_loop(Server& S) {
+    cudaSetDevice(S.opts.device);
+    Engine E(S.opts.precision != 0, S.stream);
+    std::vector<std::shared_ptr<Request>> live;
+    auto fail = [&](const std::shared_ptr<Request>& q, int st, const std::string& e) {
+        if (q->slot >= 0) E.remove(q->slot);
+        q->slot = -1;
+        finish(S, q, st, e);
+    };
+    while (true) {
+        std::vector<std::shared_ptr<Request>> fresh;
+        {
+            std::unique_lock<std::mutex> g(S.mu);
+            if (S.stop) break;
+            if (S.ready.empty() && E.steps_to_event() == 0)
+                S.cv_engine.wait_for(g, std::chrono::milliseconds(20));
+            if (S.stop) break;
+            while (!S.ready.empty()) {
+                fresh.push_back(S.ready.front());
+                S.ready.pop_front();
+            }
+        }
+        // new slots join between steps, whatever the phase of the others
+        std::vector<int> norm_ids;
+        std::vector<std::shared_ptr<Request>> norm_q;
+        for (auto& q : fresh) {
+            try {
+                if (q->cancel) throw Error(QS_ERR_ARGUMENT, "cancelled");
+                // eigsh: CGS with ARPACK's DGKS test; evolve: the reference's Krylov
+                // recurrence (three-term for Hermitian operators, else CGS2)
+                const int orth = q->r.kind == QS_REQ_EIGSH ? 1 : (q->op->op->hermitian ? 2 : 0);
+                q->slot = E.add(*q->op->op, q->m, q->cv, true, q->r.kind == QS_REQ_EIGSH ? 0 : 1, orth);
+                const int comps = q->cv ? 2 : 1;
+                if (!q->v0.empty()) {
+                    if ((int64_t)q->v0.size() != q->n * comps) throw Error(QS_ERR_DIMENSION, "v0 must have length Ns");
+                    E.load(q->slot, 0, q->v0.data(), false);
+                } else {
+                    E.seed(q->slot, q->r.seed ? q->r.seed : 20261203ull);
+                }
+                if (q->r.kind == QS_REQ_EIGSH) q->eig.init(q->r.k, q->r.which, q->r.tol, q->m, q->r.maxiter);
+                norm_ids.push_back(q->slot);
+                norm_q.push_back(q);
+                live.push_back(q);
+            } catch (const Error& e) {
+                fail(q, e.status, e.what());
+            } catch (const std::exception& e) {
+                fail(q, QS_ERR_CUDA, e.what());
+            }
+        }
+        if (!norm_ids.empty()) {
+            std::vector<double> nrm = E.normalize(norm_ids);
+            for (size_t i = 0; i < norm_q.size(); ++i) {
+                Request& q = *norm_q[i];
+                if (q.r.kind == QS_REQ_EVOLVE) {
+                    q.beta = nrm[i];
+                    const cd s = q.r.imag_time ? cd(-q.r.t, 0) : cd(0, -q.r.t);
+                    if (q.beta == 0 || q.r.t == 0) {
+                        q.segs.clear();
+                    } else {
+                        q.segs.push_back(Request::Seg{s, q.r.tol > 0 ? q.r.tol : 1e-12, 0});
+                    }
+                }
+                if (q.r.kind == QS_REQ_EIGSH || !q.segs.empty()) E.start(q.slot, 0);
+            }
+            // evolve requests with nothing to do (t = 0 or v0 = 0) finish at once:
+            // exp(0) v = v is the start vector
+            for (auto& qp : norm_q) {
+                Request& q = *qp;
+                if (q.r.kind == QS_REQ_EVOLVE && q.segs.empty()) {
+                    if (q.r.want_vector) {
+                        q.vec.resize(q.n * 2);
+                        E.store(q.slot, 0, q.vec.data(), false);
+                        for (double& v : q.vec) v *= q.beta;
+                    }
+                    E.remove(q.slot);
+                    q.slot = -1;
+                    finish(S, qp, QS_OK, "");
+                }
+            }
+        }
+        live.erase(std::remove_if(live.begin(), live.end(), [](const std::shared_ptr<Request>& q) { return q->slot < 0; }),
+                   live.end());
+        const int steps = E.steps_to_event();
+        if (steps == 0) continue;
+        // a bounded chunk keeps admission latency low for new arrivals
+        E.run(std::min(steps, S.opts.chunk_steps > 0 ? S.opts.chunk_steps : steps));
+        {
+            std::lock_guard<std::mutex> g(S.mu);
+            S.stats.steps++;
+        }
+        // ---- events: slots that filled their basis
+        std::vector<RotReq> rot;
+        std::vector<std::shared_ptr<Request>> eig_fin, evo_ev, holding;
+        std::vector<int> hold_ids;
+        for (auto& qp : live)
+            if (qp->slot >= 0 && E.slot(qp->slot).state == kSlotHold) {
+                holding.push_back(qp);
+                hold_ids.push_back(qp->slot);
+            }
+        std::vector<std::vector<cd>> Hs;
+        if (!hold_ids.empty()) E.records(hold_ids, Hs);
+        for (size_t hq = 0; hq < holding.size(); ++hq) {
+            auto& qp = holding[hq];
+            Request& q = *qp;
+            try {
+                if (q.r.kind == QS_REQ_EIGSH) {
+                    RotReq R;
+                    if (q.eig.on_hold(Hs[hq], q.slot, R)) eig_fin.push_back(qp);
+                    rot.push_back(std::move(R));
+                } else {
+                    // Krylov projection exp(s H_m) e_1 of the current segment
+                    const std::vector<cd>& H = Hs[hq];
+                    const int m = q.m;
+                    int c = m;
+                    double hn2 = 0;
+                    for (int j = 0; j < m; ++j) {
+                        for (int i = 0; i <= j + 1; ++i) hn2 += std::norm(H[(size_t)j * (m + 1) + i]);
+                        if (std::abs(H[(size_t)j * (m + 1) + j + 1]) <= 100 * 2.220446049250313e-16 *
+                                                                              std::max(1.0, std::sqrt(hn2))) {
+                            c = j + 1;
+                            break;
+                        }
+                    }
+                    const Request::Seg sg = q.segs.front();
+                    std::vector<cd> A((size_t)c * c), Ex;
+                    for (int i = 0; i < c; ++i)
+                        for (int j = 0; j < c; ++j) A[(size_t)i * c + j] = sg.scale * H[(size_t)j * (m + 1) + i];
+                    expm_complex(c, A, Ex);
+                    RotReq R;
+                    R.id = q.slot;
+                    R.nin = c;
+                    R.p = 1;
+                    R.out0 = m;   // the candidate goes to column m; column 0 keeps the segment's start
+                    R.Y.resize(c);
+                    for (int i = 0; i < c; ++i) R.Y[i] = Ex[(size_t)i * c] * q.beta;
+                    const bool est_on = c == m && m < q.n;
+                    q.err = est_on ? std::abs(sg.scale) * std::abs(H[(size_t)(m - 1) * (m + 1) + m]) * q.beta *
+                                         std::abs(Ex[(size_t)(c - 1) * c])
+                                   : 0.0;
+                    rot.push_back(std::move(R));
+                    evo_ev.push_back(qp);
+                }
+            } catch (const Error& e) {
+                fail(qp, e.status, e.what());
+            } catch (const std::exception& e) {
+                fail(qp, QS_ERR_CUDA, e.what());
+            }
+        }
+        rot.erase(std::remove_if(rot.begin(), rot.end(), [&](const RotReq& R) { return !E.alive(R.id); }), rot.end());
+        E.rotate(rot);
+        for (auto& qp : eig_fin) {
+            Request& q = *qp;
+            q.values = q.eig.theta;
+            q.restarts = q.eig.restarts;
+            q.err = q.eig.maxrel;
+            q.matvecs = E.matvecs(q.slot);
+            int st = QS_OK;
+            std::string e;
+            if (q.eig.nconv < q.eig.k) {
+                st = QS_ERR_NOT_CONVERGED;
+                e = "eigsh did not converge within maxiter restarts";
+            } else if (q.r.want_vector) {
+                const int comps = q.cv ? 2 : 1;
+                q.vec.resize((size_t)q.n * comps * q.eig.k);
+                for (int i = 0; i < q.eig.k; ++i) E.store(q.slot, i, q.vec.data() + (size_t)i * q.n * comps, false);
+            }
+            E.remove(q.slot);
+            q.slot = -1;
+            finish(S, qp, st, e);
+        }
+        for (auto& qp : live) {
+            Request& q = *qp;
+            if (q.slot >= 0 && q.r.kind == QS_REQ_EIGSH && E.slot(q.slot).state == kSlotHold) E.start(q.slot, q.eig.p);
+        }
+        // normalise the candidates (column m of each slot, grouped by m), then
+        // accept or split
+        std::map<int, std::vector<std::shared_ptr<Request>>> by_m;
+        for (auto& qp : evo_ev) by_m[qp->m].push_back(qp);
+        std::vector<RotReq> copies;
+        std::vector<std::shared_ptr<Request>> evo_done;
+        for (auto& kv : by_m) {
+            std::vector<int> ids;
+            for (auto& qp : kv.second) ids.push_back(qp->slot);
+            std::vector<double> nr = E.normalize(ids, kv.first);
+            for (size_t i = 0; i < kv.second.size(); ++i) {
+                Request& q = *kv.second[i];
+                const Request::Seg sg = q.segs.front();
+                q.matvecs = E.matvecs(q.slot);
+                if (q.err <= sg.tol * std::max(1.0, nr[i])) {
+                    // accept: the candidate becomes the next segment's start
+                    q.segs.pop_front();
+                    q.beta = nr[i];
+                    RotReq R;
+                    R.id = q.slot;
+                    R.carry = q.m;
+                    R.cdst = 0;
+                    copies.push_back(std::move(R));
+                    if (q.segs.empty()) evo_done.push_back(kv.second[i]);
+                } else if (sg.depth >= 14) {
+                    q.segs.clear();
+                    q.restarts = -1;
+                } else {
+                    q.segs.pop_front();
+                    q.segs.push_front(Request::Seg{sg.scale / 2.0, sg.tol / 2, sg.depth + 1});
+                    q.segs.push_front(Request::Seg{sg.scale / 2.0, sg.tol / 2, sg.depth + 1});
+                    q.restarts++;
+                }
+            }
+        }
+        E.rotate(copies);
+        for (auto& qp : evo_ev) {
+            Request& q = *qp;
+            if (q.slot < 0) continue;
+            if (q.restarts == -1) {
+                fail(qp, QS_ERR_NOT_CONVERGED, "Krylov exponential action did not converge; increase krylov_dim");
+                continue;
+            }
+            if (std::find(evo_done.begin(), evo_done.end(), qp) != evo_done.end()) {
+                if (q.r.want_vector) {
+                    q.vec.resize((size_t)q.n * 2);
+                    E.store(q.slot, 0, q.vec.data(), false);
+                    for (double& v : q.vec) v *= q.beta;
+                }
+                E.remove(q.slot);
+                q.slot = -1;
+                finish(S, qp, QS_OK, "");
+            } else {
+                E.start(q.slot, 0);
+            }
+        }
+        live.erase(std::remove_if(live.begin(), live.end(), [](const std::shared_ptr<Request>& q) { return q->slot < 0; }),
+                   live.end());
+        {
+            std::lock_guard<std::mutex> g(S.mu);
+            S.stats.launches = E.launches();
+        }
+    }
+    note_launches(E.launches());
+}
+
+}  // namespace
+
+Server* server_create(const qs_server_opts* o) {
+    auto* S = new Server();
+    if (o) S->opts = *o;
+    if (S->opts.hbm_budget_bytes <= 0) S->opts.hbm_budget_bytes = 150e9;
+    if (S->opts.max_slots <= 0) S->opts.max_slots = 64;
+    if (S->opts.chunk_steps < 0) S->opts.chunk_steps = 0;
+    if (S->opts.chunk_steps == 0) S->opts.chunk_steps = 8;
+    QS_CUDA(cudaGetDevice(&S->opts.device));
+    QS_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    if (S->opts.builders <= 0) S->opts.builders = 4;
+    for (int i = 0; i < S->opts.builders; ++i) S->builders.emplace_back(builder_loop, std::ref(*S));
+    S->engine = std::thread(engine_loop, std::ref(*S));
+    return S;
+}
+
+void server_destroy(Server* S) {
+    {
+        std::lock_guard<std::mutex> g(S->mu);
+        S->stop = true;
+        S->cv_build.notify_all();
+        S->cv_engine.notify_all();
+    }
+    for (auto& t : S->builders)
+        if (t.joinable()) t.join();
+    if (S->engine.joinable()) S->engine.join();
+    cudaStreamSynchronize(S->stream);
+    {
+        std::lock_guard<std::mutex> g(S->mu);
+        for (auto& kv : S->all) kv.second->op.reset();
+        S->cache.clear();
+    }
+    cudaStreamDestroy(S->stream);
+    delete S;
+}
+
+int64_t server_submit(Server* S, const qs_request* r) {
+    if (!r) throw Error(QS_ERR_ARGUMENT, "null request");
+    if (r->kind != QS_REQ_EIGSH && r->kind != QS_REQ_EVOLVE) throw Error(QS_ERR_ARGUMENT, "unknown request kind");
+    if (r->nterms < 0 || (r->nterms > 0 && !r->terms)) throw Error(QS_ERR_ARGUMENT, "terms missing");
+    if (r->kind == QS_REQ_EIGSH && r->which != 0 && r->which != 1)
+        throw Error(QS_ERR_UNSUPPORTED, "which must be SA or LA on this engine");
+    auto q = std::make_shared<Request>();
+    q->r = *r;
+    q->r.terms = nullptr;
+    q->r.v0 = nullptr;
+    for (int i = 0; i < r->nterms; ++i) {
+        const qs_term& t = r->terms[i];
+        if (!t.op) throw Error(QS_ERR_ARGUMENT, "term without an operator string");
+        TermCopy c;
+        c.op = t.op;
+        c.n = t.n_couplings;
+        c.cc = t.complex_coeffs;
+        int arity = 0;
+        for (char ch : c.op)
+            if (ch != '|') ++arity;
+        c.coeffs.assign(t.coeffs, t.coeffs + 2 * (size_t)std::max(0, t.n_couplings));
+        c.sites.assign(t.sites, t.sites + (size_t)arity * std::max(0, t.n_couplings));
+        q->terms.push_back(std::move(c));
+    }
+    if (r->v0) {
+        if (r->v0_len <= 0) throw Error(QS_ERR_ARGUMENT, "v0_len must give the length of v0 in doubles");
+        q->v0.assign(r->v0, r->v0 + r->v0_len);
+    }
+    q->key = make_key(q->r, q->terms);
+    std::lock_guard<std::mutex> g(S->mu);
+    q->ticket = S->next_ticket++;
+    q->t_submit = S->now();
+    S->all[q->ticket] = q;
+    S->pending.push_back(q);
+    S->stats.submitted++;
+    S->cv_build.notify_all();
+    return q->ticket;
+}
+
+static void fill_result(Server* S, const Request& q, qs_result* out) {
+    if (!out) return;
+    std::memset(out, 0, sizeof(*out));
+    out->status = q.status.load();
+    out->Ns = q.n;
+    const int nv = (int)std::min<size_t>(q.values.size(), 8);
+    for (int i = 0; i < nv; ++i) out->values[i] = q.values[i];
+    out->nvalues = nv;
+    out->submit_s = q.t_submit;
+    out->admit_s = q.t_admit;
+    out->done_s = q.t_done;
+    out->matvecs = q.matvecs;
+    out->restarts = q.restarts;
+    out->error_estimate = q.err;
+    out->vector_len = (int64_t)q.vec.size();
+    std::snprintf(out->message, sizeof(out->message), "%s", q.error.c_str());
+    (void)S;
+}
+
+int server_poll(Server* S, int64_t ticket, qs_result* out) {
+    std::lock_guard<std::mutex> g(S->mu);
+    auto it = S->all.find(ticket);
+    if (it == S->all.end()) throw Error(QS_ERR_ARGUMENT, "unknown ticket");
+    fill_result(S, *it->second, out);
+    return it->second->status.load();
+}
+
+int server_wait(Server* S, int64_t ticket, double timeout_s, qs_result* out) {
+    std::unique_lock<std::mutex> g(S->mu);
+    auto it = S->all.find(ticket);
+    if (it == S->all.end()) throw Error(QS_ERR_ARGUMENT, "unknown ticket");
+    std::shared_ptr<Request> q = it->second;
+    auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(
+                                       std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 1e9));
+    while (q->status.load() == QS_PENDING) {
+        if (S->cv_done.wait_until(g, deadline) == std::cv_status::timeout) break;
+    }
+    fill_result(S, *q, out);
+    return q->status.load();
+}
+
+void server_vector(Server* S, int64_t ticket, double* out, int64_t len) {
+    std::lock_guard<std::mutex> g(S->mu);
+    auto it = S->all.find(ticket);
+    if (it == S->all.end()) throw Error(QS_ERR_ARGUMENT, "unknown ticket");
+    const Request& q = *it->second;
+    if (q.status.load() != QS_OK) throw Error(QS_ERR_ARGUMENT, "request has no result");
+    if (len != (int64_t)q.vec.size()) throw Error(QS_ERR_DIMENSION, "vector length does not match the result");
+    std::memcpy(out, q.vec.data(), q.vec.size() * sizeof(double));
+}
+
+void server_release(Server* S, int64_t ticket) {
+    std::lock_guard<std::mutex> g(S->mu);
+    auto it = S->all.find(ticket);
+    if (it == S->all.end()) throw Error(QS_ERR_ARGUMENT, "unknown ticket");
+    if (it->second->status.load() == QS_PENDING) {
+        it->second->cancel = true;
+        return;
+    }
+    S->all.erase(it);
+}
+
+void server_stats(Server* S, qs_server_counters* out) {
+    std::lock_guard<std::mutex> g(S->mu);
+    *out = S->stats;
+    out->bytes_in_use = (double)S->used;
+    out->peak_bytes = (double)S->peak;
+    out->cached_ops = (int64_t)S->cache.size();
+    out->running = S->running;
+    out->queued = (int64_t)S->pending.size();
+}
+
+}  // namespace qs

@@ -10,10 +10,11 @@ from .basis import (SpinBasis1D, get_amp, int_to_state, normalization, represent
 from .errors import ArgumentError, DimensionMismatch, ErrorException, UnsupportedError
 from .operators import (ExpmMultiplyParallel, Hamiltonian, OperatorTerm, QuantumLinearOperator, apply, eigsh,
                         eigsh_batch, evolve, expm_multiply_parallel, isquantum_LinearOperator, set_a)
+from .server import Server
 
 __all__ = [
     "SpinBasis1D", "states", "state_index", "state_at", "representative", "normalization", "get_amp",
     "int_to_state", "state_to_int", "OperatorTerm", "QuantumLinearOperator", "Hamiltonian", "eigsh", "eigsh_batch", "evolve",
     "ExpmMultiplyParallel", "expm_multiply_parallel", "apply", "set_a", "isquantum_LinearOperator",
-    "ArgumentError", "DimensionMismatch", "ErrorException", "UnsupportedError",
+    "ArgumentError", "DimensionMismatch", "ErrorException", "UnsupportedError", "Server",
 ]

@@ -38,6 +38,32 @@ class EigshInfo(ctypes.Structure):
     _fields_ = [("nconv", i32), ("restarts", i32), ("matvecs", i64), ("max_rel_residual", f64), ("seconds", f64)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", f64), ("max_slots", i32), ("precision", i32), ("disable_op_cache", i32),
+                ("chunk_steps", i32), ("builders", i32), ("device", i32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", i32), ("basis", BasisSpec), ("terms", ctypes.POINTER(Term)), ("nterms", i32),
+                ("k", i32), ("which", i32), ("ncv", i32), ("maxiter", i32), ("tol", f64), ("t", f64),
+                ("imag_time", i32), ("krylov_dim", i32), ("v0", P), ("v0_len", i64), ("seed", ctypes.c_uint64),
+                ("want_vector", i32)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", i32), ("nvalues", i32), ("Ns", i64), ("values", f64 * 8), ("submit_s", f64),
+                ("admit_s", f64), ("done_s", f64), ("matvecs", i64), ("restarts", i32), ("error_estimate", f64),
+                ("vector_len", i64), ("message", ctypes.c_char * 128)]
+
+
+class ServerCounters(ctypes.Structure):
+    _fields_ = [(n, i64) for n in ("submitted", "completed", "failed", "builds", "cache_hits", "evictions", "steps",
+                                   "launches", "cached_ops", "running", "queued")] + [
+        ("bytes_in_use", f64), ("peak_bytes", f64)]
+
+
+QS_PENDING = 8
+QS_REQ_EIGSH, QS_REQ_EVOLVE = 0, 1
 QS_F64, QS_C128, QS_F32, QS_C64 = 0, 1, 2, 3
 QS_MEM_HOST, QS_MEM_DEVICE = 0, 1
 QS_CHECK_SYMM, QS_CHECK_HERM, QS_CHECK_PCON, QS_DIAG_COMPLEX = 1, 2, 4, 8
@@ -51,6 +77,8 @@ EXPORTS = (
     "qs_eigsh", "qs_expm_multiply", "qs_evolve", "qs_last_error", "qs_version", "qs_op_set_stream",
     "qs_launch_count", "qs_op_assemble", "qs_op_nnz", "qs_op_matvec_noalloc",
     "qs_eigsh_batch", "qs_basis_stabilizers",
+    "qs_server_create", "qs_server_destroy", "qs_server_submit", "qs_server_poll", "qs_server_wait",
+    "qs_server_vector", "qs_server_release", "qs_server_stats",
 )
 
 _lib = None
@@ -90,6 +118,15 @@ def load():
     L.qs_op_matvec_noalloc.argtypes = [P, i32, P, P, i32, P, P, i32, i64]
     L.qs_eigsh_batch.argtypes = [ctypes.POINTER(P), i32, ctypes.POINTER(EigshOpts), P, ctypes.POINTER(P),
                                  ctypes.POINTER(EigshInfo)]
+    L.qs_server_create.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(P)]
+    L.qs_server_destroy.argtypes = [P]
+    L.qs_server_destroy.restype = None
+    L.qs_server_submit.argtypes = [P, ctypes.POINTER(Request), ctypes.POINTER(i64)]
+    L.qs_server_poll.argtypes = [P, i64, ctypes.POINTER(Result)]
+    L.qs_server_wait.argtypes = [P, i64, f64, ctypes.POINTER(Result)]
+    L.qs_server_vector.argtypes = [P, i64, P, i64]
+    L.qs_server_release.argtypes = [P, i64]
+    L.qs_server_stats.argtypes = [P, ctypes.POINTER(ServerCounters)]
     L.qs_op_assemble.argtypes = [P]
     L.qs_op_nnz.argtypes = [P]
     L.qs_op_nnz.restype = i64

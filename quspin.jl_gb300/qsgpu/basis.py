@@ -13,28 +13,36 @@ from . import _lib
 from .errors import ArgumentError
 
 
+def basis_spec(L, nup=None, Nup=None, m=None, S="1/2", pauli=True, a=1, kblock=None, pblock=None, zblock=None,
+               pzblock=None, zAblock=None, zBblock=None):
+    """The C struct of SpinBasis1D(L; ...) keyword arguments, validated."""
+    if str(S) not in ("1/2", "0.5"):
+        raise ArgumentError("only spin-1/2 bases run on this engine")
+    if not (1 <= int(L) <= 63):
+        raise ArgumentError("L must be between 1 and 63")
+    if nup is not None and Nup is not None:
+        raise ArgumentError("specify only one of nup and Nup")
+    sel = Nup if nup is None else nup
+    if m is not None:
+        if sel is not None:
+            raise ArgumentError("m cannot be combined with nup or Nup")
+        sel = int(round((float(m) + 0.5) * L))
+    if sel is not None and not (0 <= int(sel) <= L):
+        raise ArgumentError("nup must lie between 0 and L")
+    return _lib.BasisSpec(int(L), -1 if sel is None else int(sel), int(bool(pauli)), int(a),
+                          int(kblock is not None), int(kblock or 0), int(pblock or 0), int(zblock or 0),
+                          int(pzblock or 0), int(zAblock or 0), int(zBblock or 0))
+
+
 class SpinBasis1D:
     """SpinBasis1D(L; nup, pauli, a, kblock, pblock, zblock, pzblock, zAblock, zBblock)."""
 
     def __init__(self, L, nup=None, Nup=None, m=None, S="1/2", pauli=True, a=1, kblock=None, pblock=None,
                  zblock=None, pzblock=None, zAblock=None, zBblock=None):
-        if str(S) not in ("1/2", "0.5"):
-            raise ArgumentError("only spin-1/2 bases run on this engine")
-        if not (1 <= int(L) <= 63):
-            raise ArgumentError("L must be between 1 and 63")
-        if nup is not None and Nup is not None:
-            raise ArgumentError("specify only one of nup and Nup")
-        sel = Nup if nup is None else nup
-        if m is not None:
-            if sel is not None:
-                raise ArgumentError("m cannot be combined with nup or Nup")
-            sel = int(round((float(m) + 0.5) * L))
-        if sel is not None and not (0 <= int(sel) <= L):
-            raise ArgumentError("nup must lie between 0 and L")
+        spec = basis_spec(L, nup=nup, Nup=Nup, m=m, S=S, pauli=pauli, a=a, kblock=kblock, pblock=pblock,
+                          zblock=zblock, pzblock=pzblock, zAblock=zAblock, zBblock=zBblock)
+        sel = None if spec.nup < 0 else spec.nup
         lib = _lib.load()
-        spec = _lib.BasisSpec(int(L), -1 if sel is None else int(sel), int(bool(pauli)), int(a),
-                              int(kblock is not None), int(kblock or 0), int(pblock or 0), int(zblock or 0),
-                              int(pzblock or 0), int(zAblock or 0), int(zBblock or 0))
         h = ctypes.c_void_p()
         _lib.check(lib.qs_basis_create(ctypes.byref(spec), ctypes.byref(h)))
         self._h = h

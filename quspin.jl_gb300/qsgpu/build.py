@@ -27,6 +27,8 @@ SOURCES = [
     "qs_dense.cpp",
     "qs_op.cpp",
     "qs_capi.cpp",
+    "qs_server.cpp",
+    "qs_pool.cpp",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -76,7 +78,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         list(ex.map(run, cmds))
     if cmds or not os.path.exists(LIB) or _stale(LIB, objs):
-        link = [cc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs]
+        link = [cc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs, "-lpthread"]
         run(link)
     return LIB
 
