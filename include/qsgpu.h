@@ -219,9 +219,11 @@ typedef struct {
 
 /* eigsh(op; k, which=:SA, v0, tol, ncv, maxiter) (src/operators.jl:3367-3408):
  * values ascending (k doubles); vectors Ns x k column-major in the op dtype
- * (host).  A thick-restart Lanczos with full reorthogonalisation replaces the
- * ARPACK implicitly restarted Lanczos; convergence is ARPACK's test
- * ||r_i|| <= tol * max(eps^(2/3), |theta_i|). */
+ * (host, or device with opts->mem).  A thick-restart Lanczos with full
+ * reorthogonalisation replaces the ARPACK implicitly restarted Lanczos;
+ * convergence is ARPACK's test ||r_i|| <= tol * max(eps^(2/3), |theta_i|).
+ * Assembled operators (qs_op_assemble) run on the batched engine with one
+ * operator (as qs_eigsh_batch) unless opts->precision is 1. */
 QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *vectors, qs_eigsh_info *info);
 
 /* eigsh on nops Hermitian operators at once (e.g. every momentum / parity
@@ -233,8 +235,9 @@ QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *
  * each block.  values: nops * k, ascending per operator; vectors: NULL or nops
  * pointers (each NULL or Ns_i x k in the operator's dtype, host); infos: NULL
  * or nops entries.  opts->precision: 0 FP64 Krylov vectors, 1 or 2
- * double-float vectors on the FP32 pipe.  opts->v0 is ignored (seeded start
- * vectors, the same seed as qs_eigsh). */
+ * double-float vectors on the FP32 pipe.  opts->v0 is used when nops is 1,
+ * else every operator starts from seeded normal entries (the same seed as
+ * qs_eigsh); opts->mem applies to v0 and the vectors. */
 QS_API int qs_eigsh_batch(qs_op *const *ops, int32_t nops, const qs_eigsh_opts *opts, double *values, void **vectors,
                           qs_eigsh_info *infos);
 

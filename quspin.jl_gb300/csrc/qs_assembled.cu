@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -425,8 +426,8 @@ struct SellArgs {
 };
 
 // One thread per row: y[r] = beta y[r] + alpha (d[r] x[r] + rs(stab[r]) sum_j T[code_j] x[col_j])
-template <bool kCM, bool kCV, typename T, bool kPacked>
-__global__ void __launch_bounds__(kThreads, 4) sell_kernel(SellArgs a) {
+template <bool kCM, bool kCV, typename T, bool kPacked, int U, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) sell_kernel(SellArgs a) {
     using T2 = typename V2<T>::t;
     __shared__ T2 tab[1024];
     __shared__ T rsq[kMaxGroup + 1];
@@ -458,7 +459,7 @@ __global__ void __launch_bounds__(kThreads, 4) sell_kernel(SellArgs a) {
         };
         if (kCV) {
             const T2* __restrict__ x = (const T2*)a.x;
-            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
                                  [&](uint32_t c) { return __ldg(x + c); },
                                  [&](uint32_t code, T2 xv) {
                                      const T2 v = value(code);
@@ -472,7 +473,7 @@ __global__ void __launch_bounds__(kThreads, 4) sell_kernel(SellArgs a) {
                                  });
         } else {
             const T* __restrict__ x = (const T*)a.x;
-            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
                                  [&](uint32_t c) { return __ldg(x + c); },
                                  [&](uint32_t code, T xv) { acc_r += value(code).x * xv; });
         }
@@ -513,8 +514,8 @@ __global__ void __launch_bounds__(kThreads, 4) sell_kernel(SellArgs a) {
 
 // Double-float products, one thread per row; FP64 only in the per-row tail,
 // where all 32 lanes of a warp work on 32 rows.
-template <bool kCM, bool kCV, bool kPacked>
-__global__ void __launch_bounds__(kThreads, 4) sell_df_kernel(SellArgs a, const float4* __restrict__ tab_df,
+template <bool kCM, bool kCV, bool kPacked, int U, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) sell_df_kernel(SellArgs a, const float4* __restrict__ tab_df,
                                                            const void* __restrict__ xs) {
     __shared__ float4 tab[1024];
     __shared__ double rsq[kMaxGroup + 1];
@@ -545,7 +546,7 @@ __global__ void __launch_bounds__(kThreads, 4) sell_df_kernel(SellArgs a, const 
         };
         if (kCV) {
             const float4* __restrict__ x = (const float4*)xs;
-            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
                                  [&](uint32_t c) { return __ldg(x + c); },
                                  [&](uint32_t code, float4 xv) {
                                      const float4 v = value(code);
@@ -558,7 +559,7 @@ __global__ void __launch_bounds__(kThreads, 4) sell_df_kernel(SellArgs a, const 
                                  });
         } else {
             const float2* __restrict__ x = (const float2*)xs;
-            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
                                  [&](uint32_t c) { return __ldg(x + c); },
                                  [&](uint32_t code, float2 xv) {
                                      const float4 v = value(code);
@@ -598,8 +599,8 @@ __global__ void __launch_bounds__(kThreads, 4) sell_df_kernel(SellArgs a, const 
 
 // Double-float storage in and out (the Krylov solvers' double-float vectors):
 // y = d .* x + rs(stab) * sum_j T[code_j] x[col_j], entirely on the FP32 pipe.
-template <bool kCM, bool kCV, bool kPacked>
-__global__ void __launch_bounds__(kThreads, 4) sell_dfio_kernel(SellArgs a, const float4* __restrict__ tab_df,
+template <bool kCM, bool kCV, bool kPacked, int U, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) sell_dfio_kernel(SellArgs a, const float4* __restrict__ tab_df,
                                                                 const float4* __restrict__ diag_df,
                                                                 const float2* __restrict__ rsq_df) {
     __shared__ float4 tab[1024];
@@ -631,7 +632,7 @@ __global__ void __launch_bounds__(kThreads, 4) sell_dfio_kernel(SellArgs a, cons
         };
         if (kCV) {
             const float4* __restrict__ x = (const float4*)a.x;
-            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
                                  [&](uint32_t c) { return __ldg(x + c); },
                                  [&](uint32_t code, float4 xv) {
                                      const float4 v = value(code);
@@ -644,7 +645,7 @@ __global__ void __launch_bounds__(kThreads, 4) sell_dfio_kernel(SellArgs a, cons
                                  });
         } else {
             const float2* __restrict__ x = (const float2*)a.x;
-            sell_row<4, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
                                  [&](uint32_t c) { return __ldg(x + c); },
                                  [&](uint32_t code, float2 xv) {
                                      const float4 v = value(code);
@@ -931,24 +932,39 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
         a.y = c.y;
         const bool cm = op.complex_mat, cv = c.y_complex;
         const int grid = grid_rows(M.nslices * kSlice);
+        // variants: (gathers in flight per thread, resident blocks per SM)
+#define QS_VARIANTS(LAUNCH, v)                  \
+    do {                                        \
+        if ((v) == 0) LAUNCH(1, 8);             \
+        else if ((v) == 1) LAUNCH(2, 6);        \
+        else LAUNCH(4, 4);                      \
+    } while (0)
+#define QS_SHAPES(K, U_, B_, ...)                                                        \
+    do {                                                                                 \
+        if (a.packed) {                                                                  \
+            if (cm) K<true, true, true, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);        \
+            else if (cv) K<false, true, true, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);  \
+            else K<false, false, true, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);         \
+        } else {                                                                         \
+            if (cm) K<true, true, false, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);       \
+            else if (cv) K<false, true, false, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__); \
+            else K<false, false, false, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);        \
+        }                                                                                \
+    } while (0)
+        int kind;
+        std::function<void(int)> launch;
+        const float4* td = M.table_df.as<float4>();
         if (c.df_io) {
-            const float4* td = M.table_df.as<float4>();
+            kind = 3;
             const float4* dd = op.d_diag_df.as<float4>();
             const float2* rq = M.rsq_df.as<float2>();
-#define QS_DFIO(P)                                                                    \
-    do {                                                                              \
-        if (cm) sell_dfio_kernel<true, true, P><<<grid, kThreads, 0, s>>>(a, td, dd, rq);   \
-        else if (cv) sell_dfio_kernel<false, true, P><<<grid, kThreads, 0, s>>>(a, td, dd, rq); \
-        else sell_dfio_kernel<false, false, P><<<grid, kThreads, 0, s>>>(a, td, dd, rq);     \
-    } while (0)
-            if (a.packed) QS_DFIO(true);
-            else QS_DFIO(false);
-#undef QS_DFIO
-            QS_CUDA(cudaGetLastError());
-            note_launches(1);
-            return;
-        }
-        if (c.df && !c.single) {
+            launch = [&, td, dd, rq](int v) {
+#define L_DFIO(U_, B_) QS_SHAPES(sell_dfio_kernel, U_, B_, a, td, dd, rq)
+                QS_VARIANTS(L_DFIO, v);
+#undef L_DFIO
+            };
+        } else if (c.df && !c.single) {
+            kind = 2;
             a.table = M.table64.p;
             a.diag = op.d_diag.p;
             a.diag_re = op.d_diag_re.p;
@@ -956,40 +972,93 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
             if (cv) split_kernel<true><<<sg, kThreads, 0, s>>>(c.x, M.xsplit.as<float4>(), nullptr, b.n);
             else split_kernel<false><<<sg, kThreads, 0, s>>>(c.x, nullptr, M.xsplit.as<float2>(), b.n);
             QS_CUDA(cudaGetLastError());
-            const float4* td = M.table_df.as<float4>();
-#define QS_DF(P)                                                                         \
-    do {                                                                                 \
-        if (cm) sell_df_kernel<true, true, P><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);    \
-        else if (cv) sell_df_kernel<false, true, P><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p); \
-        else sell_df_kernel<false, false, P><<<grid, kThreads, 0, s>>>(a, td, M.xsplit.p);      \
-    } while (0)
-            if (a.packed) QS_DF(true);
-            else QS_DF(false);
-#undef QS_DF
-            QS_CUDA(cudaGetLastError());
-            note_launches(2);
-            return;
-        }
-        if (c.single) {
+            note_launches(1);
+            const void* xs = M.xsplit.p;
+            launch = [&, td, xs](int v) {
+#define L_DF(U_, B_) QS_SHAPES(sell_df_kernel, U_, B_, a, td, xs)
+                QS_VARIANTS(L_DF, v);
+#undef L_DF
+            };
+        } else if (c.single) {
+            kind = 1;
             a.table = M.table32.p;
             a.diag = op.d_diag32.p;
             a.diag_re = op.d_diag32_re.p;
-#define QS_SELL(T_, P)                                                                 \
-    do {                                                                               \
-        if (cm) sell_kernel<true, true, T_, P><<<grid, kThreads, 0, s>>>(a);                \
-        else if (cv) sell_kernel<false, true, T_, P><<<grid, kThreads, 0, s>>>(a);          \
-        else sell_kernel<false, false, T_, P><<<grid, kThreads, 0, s>>>(a);                 \
+            launch = [&](int v) {
+#define K32(CM_, CV_, P_, U_, B_) sell_kernel<CM_, CV_, float, P_, U_, B_>
+#define L_32(U_, B_)                                                                           \
+    do {                                                                                       \
+        if (a.packed) {                                                                        \
+            if (cm) sell_kernel<true, true, float, true, U_, B_><<<grid, kThreads, 0, s>>>(a);       \
+            else if (cv) sell_kernel<false, true, float, true, U_, B_><<<grid, kThreads, 0, s>>>(a); \
+            else sell_kernel<false, false, float, true, U_, B_><<<grid, kThreads, 0, s>>>(a);        \
+        } else {                                                                               \
+            if (cm) sell_kernel<true, true, float, false, U_, B_><<<grid, kThreads, 0, s>>>(a);      \
+            else if (cv) sell_kernel<false, true, float, false, U_, B_><<<grid, kThreads, 0, s>>>(a);\
+            else sell_kernel<false, false, float, false, U_, B_><<<grid, kThreads, 0, s>>>(a);       \
+        }                                                                                      \
     } while (0)
-            if (a.packed) QS_SELL(float, true);
-            else QS_SELL(float, false);
+                QS_VARIANTS(L_32, v);
+#undef L_32
+#undef K32
+            };
         } else {
+            kind = 0;
             a.table = M.table64.p;
             a.diag = op.d_diag.p;
             a.diag_re = op.d_diag_re.p;
-            if (a.packed) QS_SELL(double, true);
-            else QS_SELL(double, false);
-#undef QS_SELL
+            launch = [&](int v) {
+#define L_64(U_, B_)                                                                            \
+    do {                                                                                        \
+        if (a.packed) {                                                                         \
+            if (cm) sell_kernel<true, true, double, true, U_, B_><<<grid, kThreads, 0, s>>>(a);       \
+            else if (cv) sell_kernel<false, true, double, true, U_, B_><<<grid, kThreads, 0, s>>>(a); \
+            else sell_kernel<false, false, double, true, U_, B_><<<grid, kThreads, 0, s>>>(a);        \
+        } else {                                                                                \
+            if (cm) sell_kernel<true, true, double, false, U_, B_><<<grid, kThreads, 0, s>>>(a);      \
+            else if (cv) sell_kernel<false, true, double, false, U_, B_><<<grid, kThreads, 0, s>>>(a);\
+            else sell_kernel<false, false, double, false, U_, B_><<<grid, kThreads, 0, s>>>(a);       \
+        }                                                                                       \
+    } while (0)
+                QS_VARIANTS(L_64, v);
+#undef L_64
+            };
         }
+#undef QS_SHAPES
+#undef QS_VARIANTS
+        int& var = op.asm_.sell_variant[kind];
+        if (var < 0 && !c.no_tune) {
+            // choose the variant by timing, when repeating the product is harmless
+            // (beta = 0) and the stream is not being captured into a graph
+            cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+            QS_CUDA(cudaStreamIsCapturing(s, &cap));
+            if (a.beta_zero && cap == cudaStreamCaptureStatusNone) {
+                cudaEvent_t e0, e1;
+                QS_CUDA(cudaEventCreate(&e0));
+                QS_CUDA(cudaEventCreate(&e1));
+                float best = 1e30f;
+                int bv = 2;
+                for (int v = 0; v < 3; ++v) {
+                    launch(v);
+                    QS_CUDA(cudaGetLastError());
+                    QS_CUDA(cudaEventRecord(e0, s));
+                    for (int r = 0; r < 3; ++r) launch(v);
+                    QS_CUDA(cudaEventRecord(e1, s));
+                    QS_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0;
+                    QS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    if (ms < best) {
+                        best = ms;
+                        bv = v;
+                    }
+                }
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                note_launches(12);
+                var = bv;
+            }
+        }
+        launch(var < 0 ? 2 : var);
         QS_CUDA(cudaGetLastError());
         note_launches(1);
         return;

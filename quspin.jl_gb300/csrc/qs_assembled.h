@@ -78,6 +78,10 @@ struct Assembled {
     DevBuf sell_len;    // uint16 length of each slice position's row
     int64_t nslices = 0;
     bool has_sell = false;
+    // sliced-ELL kernel variant (gathers in flight x resident blocks) per
+    // product kind (FP64, FP32, double-float with FP64 vectors, double-float
+    // vectors), chosen by timing on the first product that allows it (-1: not yet)
+    int sell_variant[4] = {-1, -1, -1, -1};
 };
 
 }  // namespace qs

@@ -585,7 +585,7 @@ Tiles Engine::tune(Op& op, int m, bool cv) {
     Tiles best;
     float best_ms = 1e30f;
     for (int rpb : {512, 1024, 2048})
-        for (int spb : {8, 16, 32}) {
+        for (int spb : {16, 64, 256}) {
             E.slots_[id].d.rpb = rpb;
             E.slots_[id].d.spb = spb;
             E.maps_dirty_ = true;
@@ -877,7 +877,7 @@ void Engine::store(int id, int col, double* out, bool device) {
     QS_CUDA(cudaStreamSynchronize(s_));
 }
 
-std::vector<double> Engine::normalize(const std::vector<int>& ids, int col) {
+std::vector<double> Engine::normalize(const std::vector<int>& ids, int col, bool scale) {
     std::vector<int> saved(ids.size());
     for (size_t q = 0; q < ids.size(); ++q) {
         SlotDev& d = slots_[ids[q]].d;
@@ -896,14 +896,14 @@ std::vector<double> Engine::normalize(const std::vector<int>& ids, int col) {
         if (df_) {
             eng_dots<DF><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 2, pa);
             eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 4, pa);
-            eng_scale<DF><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
+            if (scale) eng_scale<DF><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
         } else {
             eng_dots<double><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 2, pa);
             eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 4, pa);
-            eng_scale<double><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
+            if (scale) eng_scale<double><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
         }
         QS_CUDA(cudaGetLastError());
-        launches_ += 3;
+        launches_ += scale ? 3 : 2;
     }
     std::vector<double> out(ids.size());
     for (size_t q = 0; q < ids.size(); ++q)
@@ -1080,9 +1080,11 @@ void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, voi
     Engine E(o.precision != 0, ops[0]->stream);
     std::vector<int> id(nops);
     std::vector<EigTask> task(nops);
+    const bool dev = o.mem == QS_MEM_DEVICE;
     for (int i = 0; i < nops; ++i) {
         id[i] = E.add(*ops[i], m, ops[i]->complex_mat);
-        E.seed(id[i], 20261203ull);
+        if (o.v0 && nops == 1) E.load(id[i], 0, o.v0, dev);   // a start vector only for a single operator
+        else E.seed(id[i], 20261203ull);
         task[i].init(k, o.which, o.tol, m, o.maxiter);
     }
     E.normalize(id);
@@ -1120,7 +1122,7 @@ void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, voi
             if (vectors && vectors[i]) {
                 const int64_t n = ops[i]->basis->n;
                 const int comps = ops[i]->complex_mat ? 2 : 1;
-                for (int q = 0; q < k; ++q) E.store(id[i], q, (double*)vectors[i] + (size_t)q * n * comps, false);
+                for (int q = 0; q < k; ++q) E.store(id[i], q, (double*)vectors[i] + (size_t)q * n * comps, dev);
             }
             if (infos) {
                 infos[i].nconv = t.nconv;
@@ -1132,6 +1134,259 @@ void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, voi
             E.remove(id[i]);
         }
     }
+    QS_CUDA(cudaStreamSynchronize(E.stream()));
+    note_launches(E.launches());
+}
+
+// ================================================================ Krylov exponential
+void krylov_project(const std::vector<cd>& H, int m, bool hermitian, cd scale, int& c, std::vector<cd>& coef,
+                    double& terminal) {
+    const int ld = m + 1;
+    auto h = [&](int i, int j) { return H[(size_t)j * ld + i]; };
+    // completed steps: the reference stops when the new norm is below
+    // 100 eps max(1, ||H||_F) of the Hessenberg matrix built so far
+    c = m;
+    double hn2 = 0;
+    for (int j = 0; j < m; ++j) {
+        const double tn = std::abs(h(j + 1, j));
+        if (hermitian) {
+            hn2 += std::norm(h(j, j)) + tn * tn + (j < m - 1 ? tn * tn : 0.0);
+        } else {
+            for (int i = 0; i <= j; ++i) hn2 += std::norm(h(i, j));
+            hn2 += tn * tn;
+        }
+        if (tn <= 100 * 2.220446049250313e-16 * std::max(1.0, std::sqrt(hn2))) {
+            c = j + 1;
+            break;
+        }
+    }
+    terminal = std::abs(h(c, c - 1));
+    coef.assign(c, cd(0, 0));
+    if (hermitian) {
+        std::vector<double> T((size_t)c * c, 0.0), w, U;
+        for (int i = 0; i < c; ++i) {
+            T[(size_t)i * c + i] = h(i, i).real();
+            if (i + 1 < c) T[(size_t)i * c + i + 1] = T[(size_t)(i + 1) * c + i] = h(i + 1, i).real();
+        }
+        sym_eig(c, T, w, U);
+        for (int r = 0; r < c; ++r) {
+            cd acc(0, 0);
+            for (int q = 0; q < c; ++q) acc += U[(size_t)r * c + q] * (std::exp(scale * w[q]) * U[q]);
+            coef[r] = acc;
+        }
+    } else {
+        std::vector<cd> A((size_t)c * c), E;
+        for (int i = 0; i < c; ++i)
+            for (int j = 0; j < c; ++j) A[(size_t)i * c + j] = scale * h(i, j);
+        expm_complex(c, A, E);
+        for (int r = 0; r < c; ++r) coef[r] = E[(size_t)r * c];
+    }
+}
+
+void EvoTask::init(int m_, int64_t n_, bool herm, cd scale, double tol, double beta0, bool split) {
+    m = m_;
+    n = n_;
+    hermitian = herm;
+    beta = beta0;
+    err = 0;
+    halvings = 0;
+    segs.clear();
+    if (beta0 == 0 || scale == cd(0, 0)) return;
+    if (split) {
+        segs.push_back(Seg{scale / 2.0, tol / 2, 1});
+        segs.push_back(Seg{scale / 2.0, tol / 2, 1});
+        halvings = 1;
+    } else {
+        segs.push_back(Seg{scale, tol, 0});
+    }
+}
+
+void EvoTask::on_hold(const std::vector<cd>& H, int id, RotReq& rot) {
+    const Seg sg = segs.front();
+    int c;
+    std::vector<cd> coef;
+    double terminal;
+    krylov_project(H, m, hermitian, sg.scale, c, coef, terminal);
+    rot = RotReq();
+    rot.id = id;
+    rot.nin = c;
+    rot.p = 1;
+    rot.out0 = m;   // the candidate goes to column m; column 0 keeps the segment's start
+    rot.Y.resize(c);
+    for (int i = 0; i < c; ++i) rot.Y[i] = coef[i] * beta;
+    const bool est_on = c == m && m < n;
+    err = est_on ? std::abs(sg.scale) * terminal * beta * std::abs(coef[c - 1]) : 0.0;
+}
+
+bool EvoTask::after_norm(double nr, int id, RotReq& copy, bool& accepted) {
+    const Seg sg = segs.front();
+    accepted = err <= sg.tol * std::max(1.0, nr);
+    if (accepted) {
+        segs.pop_front();
+        beta = nr;
+        copy = RotReq();
+        copy.id = id;
+        copy.carry = m;
+        copy.cdst = 0;
+        return true;
+    }
+    if (sg.depth >= 14) return false;
+    segs.pop_front();
+    segs.push_front(Seg{sg.scale / 2.0, sg.tol / 2, sg.depth + 1});
+    segs.push_front(Seg{sg.scale / 2.0, sg.tol / 2, sg.depth + 1});
+    ++halvings;
+    return true;
+}
+
+// Runs EvoTasks on their slots until all are done; out_cols[i] receives
+// beta * column 0 (host, Ns complex) of task i.
+static void run_evo_slots(Engine& E, std::vector<int>& ids, std::vector<EvoTask>& tasks,
+                          const std::vector<double*>& outs) {
+    const size_t nt = tasks.size();
+    std::vector<char> fin(nt, 0);
+    size_t left = 0;
+    for (size_t i = 0; i < nt; ++i) {
+        if (tasks[i].done()) fin[i] = 1;
+        else {
+            E.start(ids[i], 0);
+            ++left;
+        }
+    }
+    auto emit = [&](size_t i) {
+        const int64_t n = tasks[i].n;
+        E.store(ids[i], 0, outs[i], false);
+        const double b = tasks[i].beta;
+        for (int64_t q = 0; q < 2 * n; ++q) outs[i][q] *= b;
+    };
+    for (size_t i = 0; i < nt; ++i)
+        if (fin[i]) emit(i);
+    while (left > 0) {
+        const int steps = E.steps_to_event();
+        if (steps <= 0) throw Error(QS_ERR_CUDA, "Krylov exponential lost its stepping slots");
+        E.run(steps);
+        std::vector<size_t> hold;
+        std::vector<int> hold_ids;
+        for (size_t i = 0; i < nt; ++i)
+            if (!fin[i] && E.slot(ids[i]).state == kSlotHold) {
+                hold.push_back(i);
+                hold_ids.push_back(ids[i]);
+            }
+        std::vector<std::vector<cd>> H;
+        E.records(hold_ids, H);
+        std::vector<RotReq> rot(hold.size());
+        for (size_t q = 0; q < hold.size(); ++q) tasks[hold[q]].on_hold(H[q], ids[hold[q]], rot[q]);
+        E.rotate(rot);
+        const int m = tasks[hold[0]].m;   // one krylov_dim per call
+        std::vector<double> nr = E.normalize(hold_ids, m);
+        std::vector<RotReq> copies;
+        std::vector<size_t> done_now;
+        for (size_t q = 0; q < hold.size(); ++q) {
+            const size_t i = hold[q];
+            RotReq cp;
+            bool acc = false;
+            if (!tasks[i].after_norm(nr[q], ids[i], cp, acc))
+                throw Error(QS_ERR_NOT_CONVERGED, "Krylov exponential action did not converge; increase krylov_dim");
+            if (acc) copies.push_back(std::move(cp));
+            if (tasks[i].done()) done_now.push_back(i);
+        }
+        E.rotate(copies);
+        for (size_t i : done_now) {
+            emit(i);
+            fin[i] = 1;
+            --left;
+            E.remove(ids[i]);
+        }
+        for (size_t q = 0; q < hold.size(); ++q)
+            if (!fin[hold[q]]) E.start(ids[hold[q]], 0);
+    }
+}
+
+void evolve_engine(Op& op, const double* v0, const std::vector<cd>& scales, double tol, int krylov_dim, int precision,
+                   bool normalise, double* out) {
+    const int64_t n = op.basis->n;
+    const int nt = (int)scales.size();
+    if (nt == 0) return;
+    const int m = (int)std::min<int64_t>(std::min(krylov_dim, kMaxM), n);
+    if (m < 2) throw Error(QS_ERR_UNSUPPORTED, "the engine needs a Krylov dimension of at least 2");
+    const bool herm = op.hermitian;
+    const int orth = herm ? 2 : 0;
+    auto copy_v0 = [&](int i) { std::copy(v0, v0 + 2 * n, out + (size_t)i * 2 * n); };
+    Engine E(precision != 0, op.stream);
+    // one factorisation from v0 serves every time whose estimate passes
+    const int f = E.add(op, m, true, true, 1, orth);
+    E.load(f, 0, v0, false);
+    const double beta = E.normalize({f})[0];
+    bool all_zero = true;
+    for (const cd& sc : scales) all_zero = all_zero && sc == cd(0, 0);
+    if (beta == 0 || all_zero) {
+        for (int i = 0; i < nt; ++i) copy_v0(i);
+        return;
+    }
+    E.start(f, 0);
+    E.run(m);
+    std::vector<cd> H;
+    E.record(f, H);
+    std::vector<int> failing;
+    for (int i = 0; i < nt; ++i) {
+        if (scales[i] == cd(0, 0)) {
+            copy_v0(i);
+            continue;
+        }
+        int c;
+        std::vector<cd> coef;
+        double terminal;
+        krylov_project(H, m, herm, scales[i], c, coef, terminal);
+        RotReq R;
+        R.id = f;
+        R.nin = c;
+        R.p = 1;
+        R.out0 = m;
+        R.Y.resize(c);
+        for (int r = 0; r < c; ++r) R.Y[r] = coef[r] * beta;
+        E.rotate({R});
+        const double nr = E.normalize({f}, m, false)[0];
+        const bool est_on = c == m && m < n;
+        const double est = est_on ? std::abs(scales[i]) * terminal * beta * std::abs(coef[c - 1]) : 0.0;
+        if (est > tol * std::max(1.0, nr)) failing.push_back(i);
+        else E.store(f, m, out + (size_t)i * 2 * n, false);
+    }
+    E.remove(f);
+    // the failing times: the recursion from v0, concurrently, in waves that fit in memory
+    if (!failing.empty()) {
+        size_t fr = 0, tot = 0;
+        QS_CUDA(cudaMemGetInfo(&fr, &tot));
+        const size_t per = Engine::slot_bytes(n, m, true, 1);
+        const int wave = (int)std::max<size_t>(1, std::min<size_t>(failing.size(), (fr / 2) / std::max<size_t>(per, 1)));
+        for (size_t w0 = 0; w0 < failing.size(); w0 += wave) {
+            const size_t w1 = std::min(failing.size(), w0 + wave);
+            std::vector<int> ids;
+            std::vector<EvoTask> tasks;
+            std::vector<double*> outs;
+            for (size_t q = w0; q < w1; ++q) {
+                const int i = failing[q];
+                const int id = E.add(op, m, true, true, 1, orth);
+                E.load(id, 0, v0, false);
+                ids.push_back(id);
+                outs.push_back(out + (size_t)i * 2 * n);
+            }
+            std::vector<double> b0 = E.normalize(ids);
+            for (size_t q = w0; q < w1; ++q) {
+                EvoTask t;
+                // the recursion's first attempt is the shared factorisation, which failed
+                t.init(m, n, herm, scales[failing[q]], tol, b0[q - w0], true);
+                tasks.push_back(t);
+            }
+            run_evo_slots(E, ids, tasks, outs);
+        }
+    }
+    if (normalise)
+        for (int i = 0; i < nt; ++i) {
+            double* o = out + (size_t)i * 2 * n;
+            double s2 = 0;
+            for (int64_t q = 0; q < 2 * n; ++q) s2 += o[q] * o[q];
+            const double inv = s2 > 0 ? 1.0 / std::sqrt(s2) : 0.0;
+            for (int64_t q = 0; q < 2 * n; ++q) o[q] *= inv;
+        }
     QS_CUDA(cudaStreamSynchronize(E.stream()));
     note_launches(E.launches());
 }

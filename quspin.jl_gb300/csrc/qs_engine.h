@@ -23,6 +23,7 @@
 
 #include <complex>
 #include <cstdint>
+#include <deque>
 #include <vector>
 
 #include "qs_internal.h"
@@ -78,7 +79,7 @@ struct SlotDev {
 };
 
 struct Tiles {
-    int rpb = 1024, spb = 8;
+    int rpb = 1024, spb = 64;
 };
 
 // One slot's part of a rotate() call.
@@ -116,8 +117,9 @@ class Engine {
     void load(int id, int col, const double* v, bool device);
     // FP64 copy of a column (host or device destination)
     void store(int id, int col, double* out, bool device);
-    // column col /= ||column col|| for the listed slots; returns the norms
-    std::vector<double> normalize(const std::vector<int>& ids, int col = 0);
+    // column col /= ||column col|| for the listed slots (scale = false: only
+    // measure); returns the norms
+    std::vector<double> normalize(const std::vector<int>& ids, int col = 0, bool scale = true);
     // one launch for all listed rotations (RotReq)
     void rotate(const std::vector<RotReq>& reqs);
     // Starts stepping slot id from column j (columns 0..j orthonormal).
@@ -176,5 +178,50 @@ struct EigTask {
     // final rotation (k Ritz vectors into columns 0..k-1; returns true).
     bool on_hold(const std::vector<cd>& H, int id, RotReq& rot);
 };
+
+// Krylov projection of a filled record H ((m + 1) x m, column-major):
+// the completed size c (the reference's breakdown test, tn <= 100 eps
+// max(1, ||H||_F) on the matrix built so far), coef = exp(s H_c) e_1 (for a
+// Hermitian recurrence through the eigen-decomposition of the real
+// tridiagonal, as the reference does, else Pade), and the terminal norm
+// H(c, c - 1).  src/operators.jl:1655-1756.
+void krylov_project(const std::vector<cd>& H, int m, bool hermitian, cd scale, int& c, std::vector<cd>& coef,
+                    double& terminal);
+
+// The reference's _krylov_expmv_vector (src/operators.jl:1758-1803) on one
+// slot: the recursion is a queue of segments (scale, tol, depth) applied in
+// order; column 0 holds the current segment's start / beta.
+struct EvoTask {
+    struct Seg {
+        cd scale;
+        double tol;
+        int depth;
+    };
+    int m = 30;
+    int64_t n = 0;
+    bool hermitian = true;
+    std::deque<Seg> segs;
+    double beta = 0, err = 0;
+    int halvings = 0;
+    // split: the full-scale attempt is known to fail (it was the shared
+    // factorisation), so start from the two half steps it would produce
+    void init(int m_, int64_t n_, bool herm, cd scale, double tol, double beta0, bool split = false);
+    bool done() const { return segs.empty(); }
+    // The slot filled its basis: the candidate beta V_c exp(s H_c) e_1 goes to
+    // column m (rot); the error estimate is kept.
+    void on_hold(const std::vector<cd>& H, int id, RotReq& rot);
+    // With the candidate's norm: accepted (copy column m to column 0 through
+    // `copy`, beta = nr) or split into two half steps.  Returns false when the
+    // depth limit is reached.
+    bool after_norm(double nr, int id, RotReq& copy, bool& accepted);
+};
+
+// evolve / expm_multiply on an assembled operator through the engine:
+// _krylov_expmv_times (src/operators.jl:1805-1893): one factorisation from v0
+// for all times, and for every time whose error estimate fails the
+// recursion from v0, those running concurrently as slots.  out: Ns x nt
+// complex (host).
+void evolve_engine(Op& op, const double* v0, const std::vector<cd>& scales, double tol, int krylov_dim, int precision,
+                   bool normalise, double* out);
 
 }  // namespace qs

@@ -188,6 +188,7 @@ struct MatvecCall {
     bool single = false;            // FP32 vectors and accumulation
     bool df = false;                // FP64 vectors, double-float products (assembled form)
     bool df_io = false;             // double-float vectors in and out, alpha = 1, beta = 0
+    bool no_tune = false;           // never time kernel variants inside this call
 };
 void op_prepare_device(Op& op);
 // qs_noalloc.cu

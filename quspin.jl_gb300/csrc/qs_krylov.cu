@@ -22,6 +22,7 @@
 #include "qs_blas.cuh"
 #include "qs_dense.h"
 #include "qs_internal.h"
+#include "qs_engine.h"
 #include "qs_krylov.h"
 
 namespace qs {
@@ -292,6 +293,15 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
         }
         return;
     }
+    if (op.assembled && op.asm_.has_sell && o.precision != 1 && k < n - 1) {
+        // assembled operators: the batched engine with one slot (graph-replayed
+        // steps, device-resident Lanczos coefficients, ARPACK's DGKS test)
+        Op* one = &op;
+        void* vec = vectors;
+        eigsh_batch(&one, 1, o, values, o.want_vectors ? &vec : nullptr, info);
+        if (info) info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return;
+    }
     int ncv = o.ncv > 0 ? o.ncv : std::max(20, 2 * k + 1);
     ncv = std::min(ncv, 64);
     if (ncv <= k) ncv = std::min<int64_t>(n, k + 1);
@@ -496,6 +506,10 @@ void expm_multiply(Op& op, cd a, const double* v, double* out, double tol, int k
     const int64_t n = op.basis->n;
     if (tol <= 0) throw Error(QS_ERR_ARGUMENT, "tol must be positive");
     if (krylov_dim <= 0) throw Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
+    if (op.assembled && op.asm_.has_sell && precision != 1 && krylov_dim <= 64 && n >= 2) {
+        evolve_engine(op, v, {a}, tol, krylov_dim, precision, false, out);
+        return;
+    }
     VKind vk = krylov_kind(op, true, precision);
     Ctx c(op, vk, precision == 2);
     DevBuf d64(n * 16), dv((size_t)n * vk_bytes(vk)), dout((size_t)n * vk_bytes(vk));
@@ -513,6 +527,15 @@ void evolve(Op& op, const double* v0, double t0, const double* times, int nt, in
     const int64_t n = op.basis->n;
     if (tol <= 0) throw Error(QS_ERR_ARGUMENT, "tol must be positive");
     if (krylov_dim <= 0) throw Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
+    if (op.assembled && op.asm_.has_sell && precision != 1 && krylov_dim <= 64 && n >= 2) {
+        std::vector<cd> sc(nt);
+        for (int i = 0; i < nt; ++i) {
+            const double off = times[i] - t0;
+            sc[i] = imag_time ? cd(-off, 0) : cd(0, -off);
+        }
+        evolve_engine(op, v0, sc, tol, krylov_dim, precision, imag_time != 0, out);
+        return;
+    }
     VKind vk = krylov_kind(op, true, precision);
     Ctx c(op, vk, precision == 2);
     DevBuf d64(n * 16), dv((size_t)n * vk_bytes(vk)), st((size_t)n * vk_bytes(vk));

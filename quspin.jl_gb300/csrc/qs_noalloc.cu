@@ -77,6 +77,7 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
                                          std::to_string(vb) + " bytes (use qs_op_matvec)");
     unsigned char* stage = stage_address();
     MatvecCall c;
+    c.no_tune = true;   // variant timing would create events
     c.flags = flags;
     c.alpha = alpha;
     c.beta = beta;

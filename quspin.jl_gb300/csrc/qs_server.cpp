@@ -108,16 +108,8 @@ struct Request {
     int slot = -1;
     bool cv = false;
     int m = 0;
-    // eigsh
-    EigTask eig;
-    // evolve: segments (scale, tol, depth) still to apply, norm of the start
-    struct Seg {
-        cd scale;
-        double tol;
-        int depth;
-    };
-    std::deque<Seg> segs;
-    double beta = 0;
+    EigTask eig;   // eigsh
+    EvoTask evo;   // evolve
 };
 
 struct Server {
@@ -451,25 +443,20 @@ void engine_loop(Server& S) {
             for (size_t i = 0; i < norm_q.size(); ++i) {
                 Request& q = *norm_q[i];
                 if (q.r.kind == QS_REQ_EVOLVE) {
-                    q.beta = nrm[i];
                     const cd s = q.r.imag_time ? cd(-q.r.t, 0) : cd(0, -q.r.t);
-                    if (q.beta == 0 || q.r.t == 0) {
-                        q.segs.clear();
-                    } else {
-                        q.segs.push_back(Request::Seg{s, q.r.tol > 0 ? q.r.tol : 1e-12, 0});
-                    }
+                    q.evo.init(q.m, q.n, q.op->op->hermitian, s, q.r.tol > 0 ? q.r.tol : 1e-12, nrm[i]);
                 }
-                if (q.r.kind == QS_REQ_EIGSH || !q.segs.empty()) E.start(q.slot, 0);
+                if (q.r.kind == QS_REQ_EIGSH || !q.evo.done()) E.start(q.slot, 0);
             }
             // evolve requests with nothing to do (t = 0 or v0 = 0) finish at once:
             // exp(0) v = v is the start vector
             for (auto& qp : norm_q) {
                 Request& q = *qp;
-                if (q.r.kind == QS_REQ_EVOLVE && q.segs.empty()) {
+                if (q.r.kind == QS_REQ_EVOLVE && q.evo.done()) {
                     if (q.r.want_vector) {
                         q.vec.resize(q.n * 2);
                         E.store(q.slot, 0, q.vec.data(), false);
-                        for (double& v : q.vec) v *= q.beta;
+                        for (double& v : q.vec) v *= q.evo.beta;
                     }
                     E.remove(q.slot);
                     q.slot = -1;
@@ -508,34 +495,8 @@ void engine_loop(Server& S) {
                     rot.push_back(std::move(R));
                 } else {
                     // Krylov projection exp(s H_m) e_1 of the current segment
-                    const std::vector<cd>& H = Hs[hq];
-                    const int m = q.m;
-                    int c = m;
-                    double hn2 = 0;
-                    for (int j = 0; j < m; ++j) {
-                        for (int i = 0; i <= j + 1; ++i) hn2 += std::norm(H[(size_t)j * (m + 1) + i]);
-                        if (std::abs(H[(size_t)j * (m + 1) + j + 1]) <= 100 * 2.220446049250313e-16 *
-                                                                              std::max(1.0, std::sqrt(hn2))) {
-                            c = j + 1;
-                            break;
-                        }
-                    }
-                    const Request::Seg sg = q.segs.front();
-                    std::vector<cd> A((size_t)c * c), Ex;
-                    for (int i = 0; i < c; ++i)
-                        for (int j = 0; j < c; ++j) A[(size_t)i * c + j] = sg.scale * H[(size_t)j * (m + 1) + i];
-                    expm_complex(c, A, Ex);
                     RotReq R;
-                    R.id = q.slot;
-                    R.nin = c;
-                    R.p = 1;
-                    R.out0 = m;   // the candidate goes to column m; column 0 keeps the segment's start
-                    R.Y.resize(c);
-                    for (int i = 0; i < c; ++i) R.Y[i] = Ex[(size_t)i * c] * q.beta;
-                    const bool est_on = c == m && m < q.n;
-                    q.err = est_on ? std::abs(sg.scale) * std::abs(H[(size_t)(m - 1) * (m + 1) + m]) * q.beta *
-                                         std::abs(Ex[(size_t)(c - 1) * c])
-                                   : 0.0;
+                    q.evo.on_hold(Hs[hq], q.slot, R);
                     rot.push_back(std::move(R));
                     evo_ev.push_back(qp);
                 }
@@ -583,27 +544,18 @@ void engine_loop(Server& S) {
             std::vector<double> nr = E.normalize(ids, kv.first);
             for (size_t i = 0; i < kv.second.size(); ++i) {
                 Request& q = *kv.second[i];
-                const Request::Seg sg = q.segs.front();
                 q.matvecs = E.matvecs(q.slot);
-                if (q.err <= sg.tol * std::max(1.0, nr[i])) {
-                    // accept: the candidate becomes the next segment's start
-                    q.segs.pop_front();
-                    q.beta = nr[i];
-                    RotReq R;
-                    R.id = q.slot;
-                    R.carry = q.m;
-                    R.cdst = 0;
-                    copies.push_back(std::move(R));
-                    if (q.segs.empty()) evo_done.push_back(kv.second[i]);
-                } else if (sg.depth >= 14) {
-                    q.segs.clear();
-                    q.restarts = -1;
-                } else {
-                    q.segs.pop_front();
-                    q.segs.push_front(Request::Seg{sg.scale / 2.0, sg.tol / 2, sg.depth + 1});
-                    q.segs.push_front(Request::Seg{sg.scale / 2.0, sg.tol / 2, sg.depth + 1});
-                    q.restarts++;
+                RotReq cp;
+                bool accepted = false;
+                if (!q.evo.after_norm(nr[i], q.slot, cp, accepted)) {
+                    q.restarts = -1;   // depth limit
+                    continue;
                 }
+                q.restarts = q.evo.halvings;
+                q.err = q.evo.err;
+                // accepted: the candidate becomes the next segment's start
+                if (accepted) copies.push_back(std::move(cp));
+                if (q.evo.done()) evo_done.push_back(kv.second[i]);
             }
         }
         E.rotate(copies);
@@ -618,7 +570,7 @@ void engine_loop(Server& S) {
                 if (q.r.want_vector) {
                     q.vec.resize((size_t)q.n * 2);
                     E.store(q.slot, 0, q.vec.data(), false);
-                    for (double& v : q.vec) v *= q.beta;
+                    for (double& v : q.vec) v *= q.evo.beta;
                 }
                 E.remove(q.slot);
                 q.slot = -1;
