@@ -25,7 +25,7 @@ namespace qs {
 namespace {
 
 constexpr int kT = 256;       // threads per block
-constexpr int kJT = 8;        // vectors per dots block
+constexpr int kJT = 4;        // vectors per dots block
 constexpr int kMaxM = 64;     // largest Krylov basis of a slot
 
 // ------------------------------------------------------------ arithmetic
@@ -214,11 +214,7 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
     const char* col[kJT];
 #pragma unroll
     for (int q = 0; q < kJT; ++q) col[q] = V + (size_t)min(i0 + q, nv - 1) * cs;
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        const CA<A> wv = ldv<A, CV>(w, r);
-        CA<A> v[kJT];
-#pragma unroll
-        for (int q = 0; q < kJT; ++q) v[q] = ldv<A, CV>(col[q], r);
+    auto row = [&](const CA<A>& wv, const CA<A>* v) {
 #pragma unroll
         for (int q = 0; q < kJT; ++q) {
             if (i0 + q < nv) {
@@ -234,6 +230,27 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
             mac(wn, wv.re, wv.re);
             if (CV) mac(wn, wv.im, wv.im);
         }
+    };
+    // two rows per iteration: 2 (kJT + 1) loads issued before the arithmetic
+    const int64_t step = blockDim.x;
+    int64_t r = r0 + threadIdx.x;
+    for (; r + step < r1; r += 2 * step) {
+        const CA<A> w0 = ldv<A, CV>(w, r), w1 = ldv<A, CV>(w, r + step);
+        CA<A> v0[kJT], v1[kJT];
+#pragma unroll
+        for (int q = 0; q < kJT; ++q) {
+            v0[q] = ldv<A, CV>(col[q], r);
+            v1[q] = ldv<A, CV>(col[q], r + step);
+        }
+        row(w0, v0);
+        row(w1, v1);
+    }
+    if (r < r1) {
+        const CA<A> w0 = ldv<A, CV>(w, r);
+        CA<A> v0[kJT];
+#pragma unroll
+        for (int q = 0; q < kJT; ++q) v0[q] = ldv<A, CV>(col[q], r);
+        row(w0, v0);
     }
 }
 
@@ -250,7 +267,7 @@ __device__ __forceinline__ double block_sum(A v, double* sh) {
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT, 2) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+__global__ void __launch_bounds__(kT, 4) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
                                                int mode, double* __restrict__ partial) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
     if (S.state != (mode == 2 ? kSlotNormalize : kSlotStep)) return;
@@ -279,15 +296,16 @@ __global__ void __launch_bounds__(kT, 2) eng_dots(const SlotDev* __restrict__ sl
     else dots_rows<A, false>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
     __shared__ double sh[kT / 32][2 * kJT];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const bool cv = S.cv;
 #pragma unroll
     for (int q = 0; q < kJT; ++q) {
         for (int o = 16; o > 0; o >>= 1) {
             re[q] = add(re[q], shfl(re[q], o));
-            im[q] = add(im[q], shfl(im[q], o));
+            if (cv) im[q] = add(im[q], shfl(im[q], o));
         }
         if (lane == 0) {
             sh[wid][2 * q] = to_d(re[q]);
-            sh[wid][2 * q + 1] = to_d(im[q]);
+            sh[wid][2 * q + 1] = cv ? to_d(im[q]) : 0.0;
         }
     }
     __syncthreads();
