@@ -426,18 +426,26 @@ __device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r
     const size_t cs = (size_t)S.n * (CV ? 16 : 8);
     void* w = (void*)(V + (size_t)(S.j + 1) * cs);
     A nacc = zero<A>();
+    auto term = [&](A& ar, A& ai, const CA<A>& v, const CA<A>& h) {
+        mac(ar, v.re, h.re);
+        if (CV) {
+            msub(ar, v.im, h.im);
+            mac(ai, v.re, h.im);
+            mac(ai, v.im, h.re);
+        }
+    };
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         A ar = zero<A>(), ai = zero<A>();
-        for (int t = first; t < nv; ++t) {
-            const CA<A> v = ldv<A, CV>(V + (size_t)t * cs, r);
-            const CA<A> h = hs[t];
-            mac(ar, v.re, h.re);
-            if (CV) {
-                msub(ar, v.im, h.im);
-                mac(ai, v.re, h.im);
-                mac(ai, v.im, h.re);
-            }
+        int t = first;
+        // four vector loads in flight before their arithmetic
+        for (; t + 4 <= nv; t += 4) {
+            CA<A> v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = ldv<A, CV>(V + (size_t)(t + u) * cs, r);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) term(ar, ai, v[u], hs[t + u]);
         }
+        for (; t < nv; ++t) term(ar, ai, ldv<A, CV>(V + (size_t)t * cs, r), hs[t]);
         CA<A> o = ldv<A, CV>(w, r);
         o.re = sub(o.re, ar);
         if (CV) o.im = sub(o.im, ai);
@@ -449,7 +457,7 @@ __device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT) eng_update(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+__global__ void __launch_bounds__(kT, 4) eng_update(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
                                                  int pass, double* __restrict__ partial) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
     if (S.state != kSlotStep) return;
@@ -520,18 +528,26 @@ __device__ __forceinline__ void rotate_rows(const SlotDev& S, int64_t r0, int64_
     const int nin = S.rot_in, p = S.p;
     const bool yreal = S.yreal;
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        auto term = [&](A& ar, A& ai, const CA<A>& v, const CA<A>& y) {
+            mac(ar, v.re, y.re);
+            if (CV) mac(ai, v.im, y.re);
+            if (!yreal) {
+                msub(ar, v.im, y.im);
+                if (CV) mac(ai, v.re, y.im);
+            }
+        };
         for (int c = 0; c < p; ++c) {
             A ar = zero<A>(), ai = zero<A>();
-            for (int i = 0; i < nin; ++i) {
-                const CA<A> v = ldv<A, CV>(V + (size_t)i * cs, r);
-                const CA<A> y = Y[(size_t)c * nin + i];
-                mac(ar, v.re, y.re);
-                if (CV) mac(ai, v.im, y.re);
-                if (!yreal) {
-                    msub(ar, v.im, y.im);
-                    if (CV) mac(ai, v.re, y.im);
-                }
+            const CA<A>* Yc = Y + (size_t)c * nin;
+            int i = 0;
+            for (; i + 4 <= nin; i += 4) {
+                CA<A> v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = ldv<A, CV>(V + (size_t)(i + u) * cs, r);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) term(ar, ai, v[u], Yc[i + u]);
             }
+            for (; i < nin; ++i) term(ar, ai, ldv<A, CV>(V + (size_t)i * cs, r), Yc[i]);
             stv<A, CV>(T + (size_t)c * cs, r, CA<A>{ar, ai});
         }
         for (int c = 0; c < p; ++c) stv<A, CV>(V + (size_t)(S.out0 + c) * cs, r, ldv<A, CV>(T + (size_t)c * cs, r));
@@ -540,7 +556,7 @@ __device__ __forceinline__ void rotate_rows(const SlotDev& S, int64_t r0, int64_
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT) eng_rotate(const SlotDev* __restrict__ sl, const int* __restrict__ rmap) {
+__global__ void __launch_bounds__(kT, 4) eng_rotate(const SlotDev* __restrict__ sl, const int* __restrict__ rmap) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
     if (S.state != kSlotRotate) return;
     const int64_t lb = blockIdx.x - S.rb_begin;
