@@ -1,7 +1,8 @@
 // qs_dense.cpp -- small dense FP64 linear algebra for the Krylov drivers
 // (projected matrices of order <= ~100).  Written from published algorithms:
-//   * cyclic Jacobi eigenvalue method for real symmetric matrices
-//     (Golub & Van Loan, Matrix Computations, 4th ed., section 8.5);
+//   * Householder tridiagonalisation and the implicit symmetric QR step with
+//     a Wilkinson shift (Golub & Van Loan, Matrix Computations, 4th ed.,
+//     section 8.3);
 //   * scaling and squaring with the [13/13] Pade approximant for exp(A)
 //     (Higham, SIAM J. Matrix Anal. Appl. 26 (2005) 1179-1193).
 #include "qs_dense.h"
@@ -12,57 +13,112 @@
 
 namespace qs {
 
-void sym_eig(int n, const std::vector<double>& A_in, std::vector<double>& w, std::vector<double>& Z) {
-    std::vector<double> A(A_in);
-    Z.assign((size_t)n * n, 0.0);
-    for (int i = 0; i < n; ++i) Z[(size_t)i * n + i] = 1.0;
-    auto a = [&](int i, int j) -> double& { return A[(size_t)i * n + j]; };
-    auto z = [&](int i, int j) -> double& { return Z[(size_t)i * n + j]; };
-    for (int sweep = 0; sweep < 100; ++sweep) {
-        double off = 0.0, tot = 0.0;
-        for (int i = 0; i < n; ++i)
-            for (int j = 0; j < n; ++j) {
-                double v = a(i, j) * a(i, j);
-                tot += v;
-                if (i != j) off += v;
-            }
-        if (off <= 1e-34 * tot || off == 0.0) break;
-        for (int p = 0; p < n - 1; ++p)
-            for (int q = p + 1; q < n; ++q) {
-                double apq = a(p, q);
-                if (apq == 0.0) continue;
-                double app = a(p, p), aqq = a(q, q);
-                double theta = (aqq - app) / (2.0 * apq);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-                double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < n; ++k) {
-                    double akp = a(k, p), akq = a(k, q);
-                    a(k, p) = c * akp - s * akq;
-                    a(k, q) = s * akp + c * akq;
-                }
-                for (int k = 0; k < n; ++k) {
-                    double apk = a(p, k), aqk = a(q, k);
-                    a(p, k) = c * apk - s * aqk;
-                    a(q, k) = s * apk + c * aqk;
-                }
-                for (int k = 0; k < n; ++k) {
-                    double zkp = z(k, p), zkq = z(k, q);
-                    z(k, p) = c * zkp - s * zkq;
-                    z(k, q) = s * zkp + c * zkq;
-                }
-            }
+namespace {
+
+// One implicit symmetric QR step with a Wilkinson shift on the unreduced block
+// lo..hi of the tridiagonal (d, e), chasing the bulge with Givens rotations
+// G = [c -s; s c] (T <- G^T T G) that are accumulated into Q <- Q G.
+void qr_step(std::vector<double>& d, std::vector<double>& e, int lo, int hi, std::vector<double>& Q, int n) {
+    const double a = d[hi - 1], b = e[hi - 1], cc = d[hi];
+    const double delta = 0.5 * (a - cc);
+    const double mu = cc - b * b / (delta + std::copysign(std::hypot(delta, b), delta));
+    double x = d[lo] - mu, z = e[lo];
+    for (int k = lo; k < hi; ++k) {
+        double r = std::hypot(x, z), c = 1.0, s = 0.0;
+        if (r != 0.0) {
+            c = x / r;
+            s = z / r;
+        }
+        if (k > lo) e[k - 1] = r;   // the previous bulge is annihilated
+        const double dk = d[k], dk1 = d[k + 1], ek = e[k];
+        d[k] = c * c * dk + 2.0 * c * s * ek + s * s * dk1;
+        d[k + 1] = s * s * dk - 2.0 * c * s * ek + c * c * dk1;
+        e[k] = c * s * (dk1 - dk) + (c * c - s * s) * ek;
+        if (k + 1 < hi) {
+            const double bulge = s * e[k + 1];
+            e[k + 1] *= c;
+            x = e[k];
+            z = bulge;
+        }
+        for (int i = 0; i < n; ++i) {
+            double* q = &Q[(size_t)i * n];
+            const double qk = q[k], qk1 = q[k + 1];
+            q[k] = c * qk + s * qk1;
+            q[k + 1] = -s * qk + c * qk1;
+        }
     }
-    // sort ascending
+}
+
+}  // namespace
+
+// Householder reduction to tridiagonal form, then implicit QR steps with
+// Wilkinson shifts (Golub & Van Loan, Matrix Computations, 4th ed.,
+// algorithms 8.3.1 and 8.3.2), eigenvectors accumulated throughout.
+void sym_eig(int n, const std::vector<double>& A_in, std::vector<double>& w, std::vector<double>& Z) {
+    std::vector<double> A(A_in), Q((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) Q[(size_t)i * n + i] = 1.0;
+    auto a = [&](int i, int j) -> double& { return A[(size_t)i * n + j]; };
+    std::vector<double> v(n), p(n), q(n);
+    for (int k = 0; k + 2 < n; ++k) {
+        double alpha2 = 0;
+        for (int i = k + 1; i < n; ++i) alpha2 += a(i, k) * a(i, k);
+        if (alpha2 == 0.0) continue;
+        const double alpha = -std::copysign(std::sqrt(alpha2), a(k + 1, k));
+        double vv = 0;
+        for (int i = k + 1; i < n; ++i) {
+            v[i] = a(i, k) - (i == k + 1 ? alpha : 0.0);
+            vv += v[i] * v[i];
+        }
+        if (vv == 0.0) continue;
+        const double beta = 2.0 / vv;
+        // H S H on the trailing block S = A[k+1:, k+1:] with H = I - beta v v^T
+        double vp = 0;
+        for (int i = k + 1; i < n; ++i) {
+            double t = 0;
+            for (int j = k + 1; j < n; ++j) t += a(i, j) * v[j];
+            p[i] = beta * t;
+            vp += v[i] * p[i];
+        }
+        const double K = 0.5 * beta * vp;
+        for (int i = k + 1; i < n; ++i) q[i] = p[i] - K * v[i];
+        for (int i = k + 1; i < n; ++i)
+            for (int j = k + 1; j < n; ++j) a(i, j) -= v[i] * q[j] + q[i] * v[j];
+        a(k + 1, k) = a(k, k + 1) = alpha;
+        for (int i = k + 2; i < n; ++i) a(i, k) = a(k, i) = 0.0;
+        for (int r = 0; r < n; ++r) {
+            double* qr = &Q[(size_t)r * n];
+            double t = 0;
+            for (int j = k + 1; j < n; ++j) t += qr[j] * v[j];
+            t *= beta;
+            for (int j = k + 1; j < n; ++j) qr[j] -= t * v[j];
+        }
+    }
+    std::vector<double> d(n), e(std::max(n - 1, 1), 0.0);
+    for (int i = 0; i < n; ++i) d[i] = a(i, i);
+    for (int i = 0; i + 1 < n; ++i) e[i] = a(i + 1, i);
+    const double eps = 2.220446049250313e-16;
+    int hi = n - 1, iters = 0;
+    while (hi > 0) {
+        if (std::fabs(e[hi - 1]) <= eps * (std::fabs(d[hi - 1]) + std::fabs(d[hi]))) {
+            e[hi - 1] = 0.0;
+            --hi;
+            continue;
+        }
+        int lo = hi - 1;
+        while (lo > 0 && std::fabs(e[lo - 1]) > eps * (std::fabs(d[lo - 1]) + std::fabs(d[lo]))) --lo;
+        if (lo > 0) e[lo - 1] = 0.0;
+        qr_step(d, e, lo, hi, Q, n);
+        if (++iters > 50 * n) throw std::runtime_error("symmetric eigensolver did not converge");
+    }
     std::vector<int> idx(n);
     for (int i = 0; i < n; ++i) idx[i] = i;
-    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return a(x, x) < a(y, y); });
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return d[x] < d[y]; });
     w.resize(n);
-    std::vector<double> Zs((size_t)n * n);
+    Z.assign((size_t)n * n, 0.0);
     for (int c = 0; c < n; ++c) {
-        w[c] = a(idx[c], idx[c]);
-        for (int r = 0; r < n; ++r) Zs[(size_t)r * n + c] = Z[(size_t)r * n + idx[c]];
+        w[c] = d[idx[c]];
+        for (int r = 0; r < n; ++r) Z[(size_t)r * n + c] = Q[(size_t)r * n + idx[c]];
     }
-    Z.swap(Zs);
 }
 
 namespace {

@@ -13,6 +13,7 @@
 #include <mutex>
 #include <random>
 #include <tuple>
+#include <type_traits>
 
 #include "qs_blas.cuh"
 #include "qs_dense.h"
@@ -231,10 +232,11 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
             if (CV) mac(wn, wv.im, wv.im);
         }
     };
-    // two rows per iteration: 2 (kJT + 1) loads issued before the arithmetic
+    // real vectors: two rows per iteration, 2 (kJT + 1) loads issued before the
+    // arithmetic; complex vectors hold twice the data per row, one row at a time
     const int64_t step = blockDim.x;
     int64_t r = r0 + threadIdx.x;
-    for (; r + step < r1; r += 2 * step) {
+    for (; !CV && r + step < r1; r += 2 * step) {
         const CA<A> w0 = ldv<A, CV>(w, r), w1 = ldv<A, CV>(w, r + step);
         CA<A> v0[kJT], v1[kJT];
 #pragma unroll
@@ -245,7 +247,7 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
         row(w0, v0);
         row(w1, v1);
     }
-    if (r < r1) {
+    for (; r < r1; r += step) {
         const CA<A> w0 = ldv<A, CV>(w, r);
         CA<A> v0[kJT];
 #pragma unroll
@@ -267,7 +269,7 @@ __device__ __forceinline__ double block_sum(A v, double* sh) {
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT, 4) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+__global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
                                                int mode, double* __restrict__ partial) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
     if (S.state != (mode == 2 ? kSlotNormalize : kSlotStep)) return;
@@ -1165,9 +1167,12 @@ void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, voi
                 infos[i].max_rel_residual = t.maxrel;
                 infos[i].seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             }
-            E.remove(id[i]);
+            // parked, not removed: removing would rebuild the block maps and
+            // recapture the step graph; the slot's blocks exit at once
+            E.slot_mut(id[i]).state = kSlotIdle;
         }
     }
+    for (int i = 0; i < nops; ++i) E.remove(id[i]);
     QS_CUDA(cudaStreamSynchronize(E.stream()));
     note_launches(E.launches());
 }
