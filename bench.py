@@ -55,9 +55,12 @@ def j1j2_spec(L, J1=1.0, J2=0.5):
 
 
 WORKLOADS = {
+    # traffic: dram bytes read + written by one launch of the FP64 sliced-ELL
+    # product on this workload, from an ncu capture of
+    # `bench.py --profile-range product64` on a GB300
     "j1j2_L32_k0_p1_z1": dict(L=32, nup=16, sym=dict(kblock=0, pblock=1, zblock=1), J2=0.5,
                               desc="Heisenberg J1-J2 chain L=32, nup=16, kblock=0, pblock=+1, zblock=+1, "
-                                   "J1=1.0, J2=0.5"),
+                                   "J1=1.0, J2=0.5", traffic=801.39e6 + 36.99e6),
     "j1j2_L24_k0_p1_z1": dict(L=24, nup=12, sym=dict(kblock=0, pblock=1, zblock=1), J2=0.5,
                               desc="Heisenberg J1-J2 chain L=24, nup=12, kblock=0, pblock=+1, zblock=+1 (small case)"),
 }
@@ -442,6 +445,51 @@ def section_c5(qs, torch, n_req=2000, rate=200.0, budget_gb=150.0, seq_sample=40
     return out
 
 
+def profile_range(kind):
+    """One unit of work inside cudaProfilerStart/Stop, after warm-up, for
+    `ncu --profile-from-start off`: a product of the default sector in FP64,
+    FP32 or double-float ("product64", "product32", "productdf"), its
+    matrix-free product ("matrixfree"), or one batched
+    double-float ground-state solve of all J1-J2 sectors at L = 24 or 26
+    ("batch24", "batch26")."""
+    import torch
+    import qsgpu as qs
+    if kind.startswith("product") or kind == "matrixfree":
+        L = 32
+        b = qs.SpinBasis1D(L, nup=16, pauli=False, kblock=0, pblock=1, zblock=1)
+        terms = [qs.OperatorTerm(o, c) for o, c in j1j2_spec(L, 1.0, 0.5)]
+        if kind == "matrixfree":
+            H = qs.QuantumLinearOperator(b, terms)
+        else:
+            H = qs.Hamiltonian(b, terms)
+        prec = {"product64": "fp64", "product32": "fp32", "productdf": "fp64df", "matrixfree": "fp64"}[kind]
+        x = np.random.default_rng(20261203).standard_normal(b.Ns)
+        for _ in range(3):
+            H.dot(x, precision=prec)   # the first product times the kernel variants
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        y = H.dot(x, precision=prec)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_range": kind, "N": b.Ns, "ynorm": float(np.linalg.norm(y))}))
+        return
+    L = int(kind[len("batch"):])
+    terms = [qs.OperatorTerm(o, c) for o, c in j1j2_spec(L, 1.0, 0.3)]
+    syms = []
+    for k in range(L):
+        syms += [dict(kblock=k, pblock=1), dict(kblock=k, pblock=-1)] if k in (0, L // 2) else [dict(kblock=k)]
+    ops = [qs.Hamiltonian(qs.SpinBasis1D(L, nup=L // 2, pauli=False, **sy), terms) for sy in syms]
+    qs.eigsh_batch(ops, k=1, tol=1e-10, precision="fp64df")
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    t = time.perf_counter()
+    qs.eigsh_batch(ops, k=1, tol=1e-10, precision="fp64df")
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_range": kind, "sectors": len(ops), "states": sum(o.Ns for o in ops), "seconds": dt}))
+
+
 def run_ours(args, wl, world, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -603,7 +651,8 @@ def run_ours(args, wl, world, rank, local):
                    "basis_build_s": round(t_basis, 3), "assemble_s": round(t_asm, 3),
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind, "kernel": "sell_kernel (assembled H.v, sliced ELL)"},
+                     "traffic": wl.get("traffic"), "peak_kind": peak_kind,
+                     "kernel": "sell_kernel (assembled H.v, sliced ELL)"},
         "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": int(launches),
         "clocks": clk,
@@ -643,7 +692,13 @@ def main():
     ap.add_argument("--no-sections", action="store_true",
                     help="skip the side workloads (XXZ L=16, batched sectors, TFIM evolve, serving)")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving workload")
+    ap.add_argument("--profile-range", default=None,
+                    choices=["product64", "product32", "productdf", "matrixfree", "batch24", "batch26"],
+                    help="run one unit inside cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     args = ap.parse_args()
+    if args.profile_range:
+        profile_range(args.profile_range)
+        return
     if args.warmup < 3:
         args.warmup = 3
     wl = WORKLOADS[args.workload]

@@ -1240,7 +1240,12 @@ void EvoTask::init(int m_, int64_t n_, bool herm, cd scale, double tol, double b
     }
 }
 
-void EvoTask::on_hold(const std::vector<cd>& H, int id, RotReq& rot) {
+void EvoTask::on_hold(const std::vector<cd>& Hrec, int id, RotReq& rot) {
+    H = Hrec;
+    project(id, rot);
+}
+
+void EvoTask::project(int id, RotReq& rot) {
     const Seg sg = segs.front();
     int c;
     std::vector<cd> coef;
@@ -1257,24 +1262,23 @@ void EvoTask::on_hold(const std::vector<cd>& H, int id, RotReq& rot) {
     err = est_on ? std::abs(sg.scale) * terminal * beta * std::abs(coef[c - 1]) : 0.0;
 }
 
-bool EvoTask::after_norm(double nr, int id, RotReq& copy, bool& accepted) {
+int EvoTask::after_norm(double nr, int id, RotReq& copy) {
     const Seg sg = segs.front();
-    accepted = err <= sg.tol * std::max(1.0, nr);
-    if (accepted) {
+    if (err <= sg.tol * std::max(1.0, nr)) {
         segs.pop_front();
         beta = nr;
         copy = RotReq();
         copy.id = id;
         copy.carry = m;
         copy.cdst = 0;
-        return true;
+        return 1;
     }
-    if (sg.depth >= 14) return false;
+    if (sg.depth >= 14) return -1;
     segs.pop_front();
     segs.push_front(Seg{sg.scale / 2.0, sg.tol / 2, sg.depth + 1});
     segs.push_front(Seg{sg.scale / 2.0, sg.tol / 2, sg.depth + 1});
     ++halvings;
-    return true;
+    return 0;
 }
 
 // Runs EvoTasks on their slots until all are done; out_cols[i] receives
@@ -1314,29 +1318,44 @@ static void run_evo_slots(Engine& E, std::vector<int>& ids, std::vector<EvoTask>
         E.records(hold_ids, H);
         std::vector<RotReq> rot(hold.size());
         for (size_t q = 0; q < hold.size(); ++q) tasks[hold[q]].on_hold(H[q], ids[hold[q]], rot[q]);
-        E.rotate(rot);
         const int m = tasks[hold[0]].m;   // one krylov_dim per call
-        std::vector<double> nr = E.normalize(hold_ids, m);
-        std::vector<RotReq> copies;
-        std::vector<size_t> done_now;
-        for (size_t q = 0; q < hold.size(); ++q) {
-            const size_t i = hold[q];
-            RotReq cp;
-            bool acc = false;
-            if (!tasks[i].after_norm(nr[q], ids[i], cp, acc))
-                throw Error(QS_ERR_NOT_CONVERGED, "Krylov exponential action did not converge; increase krylov_dim");
-            if (acc) copies.push_back(std::move(cp));
-            if (tasks[i].done()) done_now.push_back(i);
+        std::vector<size_t> proj = hold, done_now, restart;
+        // project, measure, decide; rejected slots project their half step from
+        // the same basis until every slot is accepted
+        while (!proj.empty()) {
+            E.rotate(rot);
+            std::vector<int> pid;
+            for (size_t i : proj) pid.push_back(ids[i]);
+            std::vector<double> nr = E.normalize(pid, m);
+            std::vector<RotReq> copies, next_rot;
+            std::vector<size_t> next;
+            for (size_t q = 0; q < proj.size(); ++q) {
+                const size_t i = proj[q];
+                RotReq cp;
+                const int r = tasks[i].after_norm(nr[q], ids[i], cp);
+                if (r < 0)
+                    throw Error(QS_ERR_NOT_CONVERGED, "Krylov exponential action did not converge; increase krylov_dim");
+                if (r == 1) {
+                    copies.push_back(std::move(cp));
+                    (tasks[i].done() ? done_now : restart).push_back(i);
+                } else {
+                    RotReq R;
+                    tasks[i].project(ids[i], R);
+                    next_rot.push_back(std::move(R));
+                    next.push_back(i);
+                }
+            }
+            E.rotate(copies);
+            rot.swap(next_rot);
+            proj.swap(next);
         }
-        E.rotate(copies);
         for (size_t i : done_now) {
             emit(i);
             fin[i] = 1;
             --left;
             E.remove(ids[i]);
         }
-        for (size_t q = 0; q < hold.size(); ++q)
-            if (!fin[hold[q]]) E.start(ids[hold[q]], 0);
+        for (size_t i : restart) E.start(ids[i], 0);
     }
 }
 

@@ -190,7 +190,11 @@ void krylov_project(const std::vector<cd>& H, int m, bool hermitian, cd scale, i
 
 // The reference's _krylov_expmv_vector (src/operators.jl:1758-1803) on one
 // slot: the recursion is a queue of segments (scale, tol, depth) applied in
-// order; column 0 holds the current segment's start / beta.
+// order; column 0 holds the current segment's start / beta.  A rejected step
+// is replaced by two half steps whose first starts from the same vector: its
+// Krylov factorisation would be the same (the engine is deterministic), so
+// the kept record and basis are projected again instead of recomputed, and a
+// new factorisation is built only from an accepted state.
 struct EvoTask {
     struct Seg {
         cd scale;
@@ -203,17 +207,21 @@ struct EvoTask {
     std::deque<Seg> segs;
     double beta = 0, err = 0;
     int halvings = 0;
+    std::vector<cd> H;   // record of the factorisation of column 0's state
     // split: the full-scale attempt is known to fail (it was the shared
     // factorisation), so start from the two half steps it would produce
     void init(int m_, int64_t n_, bool herm, cd scale, double tol, double beta0, bool split = false);
     bool done() const { return segs.empty(); }
-    // The slot filled its basis: the candidate beta V_c exp(s H_c) e_1 goes to
+    // The slot filled its basis: keeps the record and projects the front
+    // segment (project).
+    void on_hold(const std::vector<cd>& Hrec, int id, RotReq& rot);
+    // The candidate beta V_c exp(s H_c) e_1 of the front segment goes to
     // column m (rot); the error estimate is kept.
-    void on_hold(const std::vector<cd>& H, int id, RotReq& rot);
-    // With the candidate's norm: accepted (copy column m to column 0 through
-    // `copy`, beta = nr) or split into two half steps.  Returns false when the
-    // depth limit is reached.
-    bool after_norm(double nr, int id, RotReq& copy, bool& accepted);
+    void project(int id, RotReq& rot);
+    // With the candidate's norm: 1 accepted (copy column m to column 0 through
+    // `copy`, beta = nr; a new factorisation is due unless done()), 0 rejected
+    // and split (call project again: same basis), -1 depth limit reached.
+    int after_norm(double nr, int id, RotReq& copy);
 };
 
 // evolve / expm_multiply on an assembled operator through the engine:

@@ -533,51 +533,65 @@ void engine_loop(Server& S) {
             if (q.slot >= 0 && q.r.kind == QS_REQ_EIGSH && E.slot(q.slot).state == kSlotHold) E.start(q.slot, q.eig.p);
         }
         // normalise the candidates (column m of each slot, grouped by m), then
-        // accept or split
-        std::map<int, std::vector<std::shared_ptr<Request>>> by_m;
-        for (auto& qp : evo_ev) by_m[qp->m].push_back(qp);
-        std::vector<RotReq> copies;
-        std::vector<std::shared_ptr<Request>> evo_done;
-        for (auto& kv : by_m) {
-            std::vector<int> ids;
-            for (auto& qp : kv.second) ids.push_back(qp->slot);
-            std::vector<double> nr = E.normalize(ids, kv.first);
-            for (size_t i = 0; i < kv.second.size(); ++i) {
-                Request& q = *kv.second[i];
-                q.matvecs = E.matvecs(q.slot);
-                RotReq cp;
-                bool accepted = false;
-                if (!q.evo.after_norm(nr[i], q.slot, cp, accepted)) {
-                    q.restarts = -1;   // depth limit
-                    continue;
+        // accept, or split and project the first half step from the same basis
+        std::vector<std::shared_ptr<Request>> proj = evo_ev, evo_done, evo_restart, evo_fail;
+        bool first_round = true;
+        while (!proj.empty()) {
+            if (!first_round) {
+                std::vector<RotReq> again;
+                for (auto& qp : proj) {
+                    RotReq R;
+                    qp->evo.project(qp->slot, R);
+                    again.push_back(std::move(R));
                 }
-                q.restarts = q.evo.halvings;
-                q.err = q.evo.err;
-                // accepted: the candidate becomes the next segment's start
-                if (accepted) copies.push_back(std::move(cp));
-                if (q.evo.done()) evo_done.push_back(kv.second[i]);
+                E.rotate(again);
             }
+            first_round = false;
+            std::map<int, std::vector<std::shared_ptr<Request>>> by_m;
+            for (auto& qp : proj) by_m[qp->m].push_back(qp);
+            std::vector<RotReq> copies;
+            std::vector<std::shared_ptr<Request>> next;
+            for (auto& kv : by_m) {
+                std::vector<int> ids;
+                for (auto& qp : kv.second) ids.push_back(qp->slot);
+                std::vector<double> nr = E.normalize(ids, kv.first);
+                for (size_t i = 0; i < kv.second.size(); ++i) {
+                    Request& q = *kv.second[i];
+                    RotReq cp;
+                    const int r = q.evo.after_norm(nr[i], q.slot, cp);
+                    q.restarts = q.evo.halvings;
+                    q.err = q.evo.err;
+                    if (r < 0) {
+                        evo_fail.push_back(kv.second[i]);
+                    } else if (r == 1) {
+                        // accepted: the candidate becomes the next segment's start
+                        copies.push_back(std::move(cp));
+                        (q.evo.done() ? evo_done : evo_restart).push_back(kv.second[i]);
+                    } else {
+                        next.push_back(kv.second[i]);
+                    }
+                }
+            }
+            E.rotate(copies);
+            proj.swap(next);
         }
-        E.rotate(copies);
-        for (auto& qp : evo_ev) {
+        for (auto& qp : evo_fail)
+            fail(qp, QS_ERR_NOT_CONVERGED, "Krylov exponential action did not converge; increase krylov_dim");
+        for (auto& qp : evo_done) {
             Request& q = *qp;
-            if (q.slot < 0) continue;
-            if (q.restarts == -1) {
-                fail(qp, QS_ERR_NOT_CONVERGED, "Krylov exponential action did not converge; increase krylov_dim");
-                continue;
+            q.matvecs = E.matvecs(q.slot);
+            if (q.r.want_vector) {
+                q.vec.resize((size_t)q.n * 2);
+                E.store(q.slot, 0, q.vec.data(), false);
+                for (double& v : q.vec) v *= q.evo.beta;
             }
-            if (std::find(evo_done.begin(), evo_done.end(), qp) != evo_done.end()) {
-                if (q.r.want_vector) {
-                    q.vec.resize((size_t)q.n * 2);
-                    E.store(q.slot, 0, q.vec.data(), false);
-                    for (double& v : q.vec) v *= q.evo.beta;
-                }
-                E.remove(q.slot);
-                q.slot = -1;
-                finish(S, qp, QS_OK, "");
-            } else {
-                E.start(q.slot, 0);
-            }
+            E.remove(q.slot);
+            q.slot = -1;
+            finish(S, qp, QS_OK, "");
+        }
+        for (auto& qp : evo_restart) {
+            qp->matvecs = E.matvecs(qp->slot);
+            E.start(qp->slot, 0);
         }
         live.erase(std::remove_if(live.begin(), live.end(), [](const std::shared_ptr<Request>& q) { return q->slot < 0; }),
                    live.end());
