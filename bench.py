@@ -449,11 +449,27 @@ def profile_range(kind):
     """One unit of work inside cudaProfilerStart/Stop, after warm-up, for
     `ncu --profile-from-start off`: a product of the default sector in FP64,
     FP32 or double-float ("product64", "product32", "productdf"), its
-    matrix-free product ("matrixfree"), or one batched
+    matrix-free product ("matrixfree"), one Lanczos ground state of it
+    ("lanczos64", "lanczosdf"), or one batched
     double-float ground-state solve of all J1-J2 sectors at L = 24 or 26
     ("batch24", "batch26")."""
     import torch
     import qsgpu as qs
+    if kind in ("lanczos64", "lanczosdf"):
+        L = 32
+        b = qs.SpinBasis1D(L, nup=16, pauli=False, kblock=0, pblock=1, zblock=1)
+        H = qs.Hamiltonian(b, [qs.OperatorTerm(o, c) for o, c in j1j2_spec(L, 1.0, 0.5)])
+        prec = "fp64" if kind == "lanczos64" else "fp64df"
+        qs.eigsh(H, k=1, which="SA", tol=1e-10, return_eigenvectors=False, precision=prec)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        t = time.perf_counter()
+        v = qs.eigsh(H, k=1, which="SA", tol=1e-10, return_eigenvectors=False, precision=prec)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_range": kind, "e0": float(v[0]), "seconds": dt}))
+        return
     if kind.startswith("product") or kind == "matrixfree":
         L = 32
         b = qs.SpinBasis1D(L, nup=16, pauli=False, kblock=0, pblock=1, zblock=1)
@@ -693,7 +709,8 @@ def main():
                     help="skip the side workloads (XXZ L=16, batched sectors, TFIM evolve, serving)")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving workload")
     ap.add_argument("--profile-range", default=None,
-                    choices=["product64", "product32", "productdf", "matrixfree", "batch24", "batch26"],
+                    choices=["product64", "product32", "productdf", "matrixfree", "lanczos64", "lanczosdf",
+                             "batch24", "batch26"],
                     help="run one unit inside cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     args = ap.parse_args()
     if args.profile_range:

@@ -278,3 +278,37 @@ def test_assembled_matches_matrix_free(qs, ora, L, nup, pauli, sym, model):
     if H.dtype == np.float64:
         xr = models.seeded(b.Ns)
         assert np.max(np.abs(H.dot(xr) - op.dot(xr))) <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("sym", [dict(), dict(kblock=2)])
+def test_expm_of_a_non_hermitian_assembled_operator(qs, ora, sym):
+    """A non-Hermitian assembled operator takes the Arnoldi (CGS2) path of the
+    Krylov exponential (src/operators.jl:1655-1731, non-Hermitian branch):
+    compared with dense expm, for one vector and for several times."""
+    L, nup = 10, 5
+    bonds = [(i, i % L + 1) for i in range(1, L + 1)]
+    sp = [("+-", [(1.0, a, b) for a, b in bonds]), ("-+", [(0.35, a, b) for a, b in bonds]),
+          ("zz", [(0.4, a, b) for a, b in bonds])]
+    b = qs.SpinBasis1D(L, nup=nup, pauli=False, **sym)
+    H = qs.Hamiltonian(b, models.to_terms(qs, sp), check_herm=False)
+    assert H.assembled
+    rep = ora.RepBasis(L, nup=nup, pauli=False, **sym)
+    n = b.Ns
+    D = np.zeros((n, n), dtype=np.complex128)
+    e = np.zeros(n, dtype=np.complex128)
+    for j in range(n):
+        e[:] = 0
+        e[j] = 1
+        D[:, j] = rep.matvec(sp, e)
+    assert np.abs(D - D.conj().T).max() > 0.1          # really non-Hermitian
+    v = models.seeded(n, complex_=True)
+    v /= np.linalg.norm(v)
+    for a in (-0.7 + 0.4j, 1.3j):
+        want = sla.expm(a * D) @ v
+        for prec in ("fp64", "fp64df"):
+            got = qs.ExpmMultiplyParallel(H, a).apply(v, tol=1e-12, precision=prec)
+            assert np.linalg.norm(got - want) < 1e-9 * max(1.0, np.linalg.norm(want)), (a, prec)
+    times = np.array([0.3, 1.1, 2.0])
+    got = qs.evolve(H, v, 0.0, times, tol=1e-11)
+    want = np.stack([sla.expm(-1j * t * D) @ v for t in times], axis=1)
+    assert np.max(np.linalg.norm(got - want, axis=0) / np.linalg.norm(want, axis=0)) < 1e-9
