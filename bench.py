@@ -336,11 +336,36 @@ def section_c4(qs, torch):
     t_warm = time.perf_counter() - t
     timed = {}
     vals = {}
+    infos = []
     for prec in ("fp64", "fp64df"):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        vals[prec] = qs.eigsh_batch(ops, k=1, tol=1e-10, precision=prec)[:, 0]
+        vals[prec] = qs.eigsh_batch(ops, k=1, tol=1e-10, precision=prec, infos=infos if prec == "fp64" else None)[:, 0]
         timed[prec] = time.perf_counter() - t
+    # the CPU restatement of the reference matvec on all host cores, timed on a
+    # row sample of one k = 1 sector and scaled by the products these solves used
+    cpu = None
+    try:
+        import oracle
+        oracle.lib()
+        nthreads = os.cpu_count() or 1
+        rb = oracle.RepBasis(L, nup=13, pauli=False, nthreads=nthreads, kblock=1)
+        x = np.random.default_rng(1).standard_normal(rb.Ns).astype(np.complex128)
+        d = rb.diagonal(spec)
+        pk = oracle.pack_terms(spec)
+        rows, tt, blk = 0, 0.0, 4096
+        while tt < 3.0 and rows < rb.Ns:
+            r1 = min(rb.Ns, rows + blk)
+            t = time.perf_counter()
+            rb.matvec(spec, x, diag=d, rows=(rows, r1), packed=pk)
+            tt += time.perf_counter() - t
+            rows, blk = r1, blk * 2
+        row_matvecs = sum(o.Ns * i["matvecs"] for o, i in zip(ops, infos))
+        cpu = {"cores": nthreads, "kind": "port", "seconds_per_row": tt / rows,
+               "estimated_solves_per_s": len(ops) / (row_matvecs * tt / rows),
+               "sample": f"{rows} rows of the k=1 sector; products only (the FP64 batched solves' counts)"}
+    except Exception as exc:  # the estimate is reported, never required
+        cpu = {"error": f"{type(exc).__name__}: {exc}"}
     # the plain FP64 GPU path: one eigsh per sector
     t = time.perf_counter()
     vs = np.array([qs.eigsh(o, k=1, which="SA", tol=1e-10, return_eigenvectors=False)[0] for o in ops])
@@ -355,7 +380,7 @@ def section_c4(qs, torch):
             "batched_fp64df_speedup": t_seq / timed["fp64df"],
             "max_rel_diff_fp64_batched_vs_sequential": float(np.max(np.abs(vals["fp64"] - vs))) / scale,
             "max_rel_diff_fp64df_batched_vs_sequential": float(np.max(np.abs(vals["fp64df"] - vs))) / scale,
-            "ground_energy": float(np.min(vs))}
+            "ground_energy": float(np.min(vs)), "cpu_port_estimate": cpu}
 
 
 def serving_requests(n_req, rate, seed=20261203):
@@ -410,8 +435,8 @@ def section_c5(qs, torch, n_req=2000, rate=200.0, budget_gb=150.0, seq_sample=40
     out = {"workload": "%d requests, Poisson %.0f/s, L in 18..30 (even), J1-J2 J2=0.5, 70%% eigsh k=1 tol 1e-10, "
                        "30%% evolve t~U[0.5,5] m=30 tol 1e-9, HBM budget %.0f GB" % (n_req, rate, budget_gb),
            "sequential_fp64_sample": seq_sample, "sequential_fp64_solves_per_s": seq_sample / t_seq}
-    for prec in ("fp64df",):
-        srv = qs.Server(hbm_budget_gb=budget_gb, precision=prec)
+    for name, prec, policy in (("fp64df", "fp64df", "fifo"), ("fp64df_smallest_first", "fp64df", "sjf")):
+        srv = qs.Server(hbm_budget_gb=budget_gb, precision=prec, policy=policy)
         tickets = [None] * n_req
         t0 = time.perf_counter()
 
@@ -435,7 +460,7 @@ def section_c5(qs, torch, n_req=2000, rate=200.0, budget_gb=150.0, seq_sample=40
         last = max(x["done_s"] for x in res)
         st = srv.stats()
         srv.close()
-        out[prec] = {"solves_per_s": n_req / (last - first), "wall_s": wall,
+        out[name] = {"policy": policy, "solves_per_s": n_req / (last - first), "wall_s": wall,
                      "p50_latency_ms": float(np.percentile(lat, 50) * 1e3),
                      "p99_latency_ms": float(np.percentile(lat, 99) * 1e3),
                      "mean_latency_ms": float(lat.mean() * 1e3),

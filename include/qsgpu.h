@@ -275,6 +275,10 @@ typedef struct {
     int32_t disable_op_cache;  /* 1: free each operator with its last request */
     int32_t chunk_steps;       /* Krylov steps between admissions, 0 = 8 */
     int32_t builders;          /* threads building bases and operators, 0 = 4 */
+    int32_t policy;            /* admission order: 0 arrival (FIFO); 1 smallest estimated
+                                  work first, a request waiting longer than max_wait_s
+                                  going first regardless */
+    double max_wait_s;         /* policy 1 aging limit, 0 = 10 s */
     int32_t device;            /* set by the library: the device current at creation */
 } qs_server_opts;
 

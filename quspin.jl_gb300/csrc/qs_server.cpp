@@ -95,7 +95,7 @@ struct Request {
     std::string key;
     double t_submit = 0, t_admit = -1, t_done = -1;
     std::atomic<int> status{QS_PENDING};
-    bool cancel = false;
+    std::atomic<bool> cancel{false};
     std::string error;
     std::vector<double> values;
     std::vector<double> vec;
@@ -104,6 +104,7 @@ struct Request {
     double err = 0;
     // runtime
     std::shared_ptr<CachedOp> op;
+    double work = 0;   // estimated work (row-products), for the smallest-first policy
     size_t slot_reserved = 0;
     int slot = -1;
     bool cv = false;
@@ -235,12 +236,23 @@ void builder_loop(Server& S) {
         }
         {
             std::unique_lock<std::mutex> g(S.mu);
-            // admit the oldest pending request whose sector no other builder is
-            // building, once its estimate fits the budget
+            // admit the oldest pending request (or, with the smallest-first policy,
+            // the least work unless the oldest has waited max_wait_s) whose sector
+            // no other builder is building, once its estimate fits the budget
             while (true) {
                 if (S.stop) return;
                 auto pos = S.pending.begin();
                 while (pos != S.pending.end() && !(*pos)->cancel && S.building.count((*pos)->key)) ++pos;
+                if (S.opts.policy == 1 && pos != S.pending.end() && !(*pos)->cancel &&
+                    S.now() - (*pos)->t_submit < S.opts.max_wait_s) {
+                    for (auto it = pos; it != S.pending.end(); ++it) {
+                        if ((*it)->cancel) {
+                            pos = it;
+                            break;
+                        }
+                        if (!S.building.count((*it)->key) && (*it)->work < (*pos)->work) pos = it;
+                    }
+                }
                 if (pos != S.pending.end()) {
                     q = *pos;
                     if (q->cancel) {
@@ -466,6 +478,20 @@ void engine_loop(Server& S) {
         }
         live.erase(std::remove_if(live.begin(), live.end(), [](const std::shared_ptr<Request>& q) { return q->slot < 0; }),
                    live.end());
+        // requests released while running stop here, between steps
+        {
+            std::vector<std::shared_ptr<Request>> cancelled;
+            {
+                std::lock_guard<std::mutex> g(S.mu);
+                for (auto& q : live)
+                    if (q->cancel && q->slot >= 0) cancelled.push_back(q);
+            }
+            for (auto& q : cancelled) fail(q, QS_ERR_ARGUMENT, "cancelled");
+            if (!cancelled.empty())
+                live.erase(std::remove_if(live.begin(), live.end(),
+                                          [](const std::shared_ptr<Request>& q) { return q->slot < 0; }),
+                           live.end());
+        }
         const int steps = E.steps_to_event();
         if (steps == 0) continue;
         // a bounded chunk keeps admission latency low for new arrivals
@@ -606,12 +632,14 @@ void engine_loop(Server& S) {
 }  // namespace
 
 Server* server_create(const qs_server_opts* o) {
+    if (o && o->policy != 0 && o->policy != 1) throw Error(QS_ERR_ARGUMENT, "unknown admission policy");
     auto* S = new Server();
     if (o) S->opts = *o;
     if (S->opts.hbm_budget_bytes <= 0) S->opts.hbm_budget_bytes = 150e9;
     if (S->opts.max_slots <= 0) S->opts.max_slots = 64;
     if (S->opts.chunk_steps < 0) S->opts.chunk_steps = 0;
     if (S->opts.chunk_steps == 0) S->opts.chunk_steps = 8;
+    if (S->opts.max_wait_s <= 0) S->opts.max_wait_s = 10.0;
     QS_CUDA(cudaGetDevice(&S->opts.device));
     QS_CUDA(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
     if (S->opts.builders <= 0) S->opts.builders = 4;
@@ -669,6 +697,17 @@ int64_t server_submit(Server* S, const qs_request* r) {
         q->v0.assign(r->v0, r->v0 + r->v0_len);
     }
     q->key = make_key(q->r, q->terms);
+    {
+        // rough work estimate: sector size x expected products (a ground state
+        // ~150; an exponential ~30 per unit of |t| times the chain length)
+        const qs_basis_spec& sp = q->r.basis;
+        const double parent = sp.nup >= 0 ? binom(sp.L, sp.nup) : std::ldexp(1.0, sp.L);
+        double order = sp.has_kblock ? std::max(1, sp.L / std::max(1, sp.a)) : 1;
+        for (int b : {sp.pblock, sp.zblock, sp.pzblock, sp.zAblock, sp.zBblock})
+            if (b) order *= 2;
+        const double prods = q->r.kind == QS_REQ_EIGSH ? 150.0 : 30.0 * std::max(1.0, std::fabs(q->r.t) * sp.L / 8.0);
+        q->work = parent / order * prods;
+    }
     std::lock_guard<std::mutex> g(S->mu);
     q->ticket = S->next_ticket++;
     q->t_submit = S->now();

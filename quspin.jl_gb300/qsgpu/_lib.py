@@ -40,7 +40,7 @@ class EigshInfo(ctypes.Structure):
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", f64), ("max_slots", i32), ("precision", i32), ("disable_op_cache", i32),
-                ("chunk_steps", i32), ("builders", i32), ("device", i32)]
+                ("chunk_steps", i32), ("builders", i32), ("policy", i32), ("max_wait_s", f64), ("device", i32)]
 
 
 class Request(ctypes.Structure):

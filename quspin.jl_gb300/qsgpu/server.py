@@ -28,9 +28,14 @@ def _result_dict(r):
 
 class Server:
     def __init__(self, hbm_budget_gb=150.0, max_slots=64, precision="fp64df", op_cache=True, chunk_steps=8,
-                 builders=4):
+                 builders=4, policy="fifo", max_wait_s=10.0):
+        """policy "fifo" admits in arrival order; "sjf" admits the smallest
+        estimated work first, except a request waiting longer than max_wait_s."""
+        if policy not in ("fifo", "sjf"):
+            raise ArgumentError("policy must be fifo or sjf")
         opts = _lib.ServerOpts(float(hbm_budget_gb) * 1e9, int(max_slots), _precision_code(precision),
-                               0 if op_cache else 1, int(chunk_steps), int(builders), 0)
+                               0 if op_cache else 1, int(chunk_steps), int(builders),
+                               0 if policy == "fifo" else 1, float(max_wait_s), 0)
         h = ctypes.c_void_p()
         _lib.check(_lib.load().qs_server_create(ctypes.byref(opts), ctypes.byref(h)))
         self._h = h

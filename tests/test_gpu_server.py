@@ -126,5 +126,30 @@ def test_release_cancels_a_queued_request(qs):
         srv.wait(first, timeout=300)
         r = srv.poll(queued)
         assert r["status"] != 0 or r["values"]   # cancelled, or finished before the release landed
+        # a running request stops between steps
+        big = srv.submit_evolve(dict(L=26, nup=13, pauli=False, kblock=1), j1j2_terms(qs, 26), 400.0, tol=1e-12)
+        import time
+        time.sleep(0.3)
+        srv.release(big)
+        with pytest.raises(qs.ArgumentError):
+            srv.wait(big, timeout=300)
         with pytest.raises(qs.ArgumentError):
             srv.poll(123456)
+
+
+def test_smallest_first_policy_completes_every_request(qs):
+    """The smallest-work-first admission order serves the same requests with the
+    same results; an unknown policy is an argument error."""
+    L = 16
+    terms = j1j2_terms(qs, L)
+    reqs = [dict(L=L, nup=8, pauli=False, kblock=k) for k in range(6)] + \
+           [dict(L=12, nup=6, pauli=False, kblock=k) for k in range(4)]
+    results = {}
+    for policy in ("fifo", "sjf"):
+        with qs.Server(precision="fp64df", policy=policy, max_slots=2) as srv:
+            ts = [srv.submit_eigsh(b, terms if b["L"] == L else j1j2_terms(qs, b["L"]), k=1, tol=1e-10, seed=7)
+                  for b in reqs]
+            results[policy] = [srv.wait(t, timeout=300)["values"][0] for t in ts]
+    assert results["fifo"] == results["sjf"]
+    with pytest.raises(qs.ArgumentError):
+        qs.Server(policy="lifo")
