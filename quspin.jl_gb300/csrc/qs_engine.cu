@@ -202,7 +202,8 @@ __global__ void __launch_bounds__(kT) eng_spmv(const SlotDev* __restrict__ sl, c
 // P = mmax + 1; index mmax holds norms.
 // mode 0 (first pass): i in [first, j] with first = j for the three-term
 //   recurrence, else 0; DGKS slots also accumulate ||w||^2 at index mmax;
-// mode 1 (second pass, only where the step's flag asks): i in [0, j];
+// mode 1 (second pass, only where the step's flag asks): i in [0, j] (the step
+//   itself takes these dots from the first update, see eng_update);
 // mode 2 (normalise): partial[b][0] = <col ncol, col ncol>.
 template <class A, bool CV>
 __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t r1, int i0, int nv, const void* w,
@@ -268,6 +269,33 @@ __device__ __forceinline__ double block_sum(A v, double* sh) {
     return t;
 }
 
+// Block sums of the kJT accumulators into row[(base + q) * 2 + {re, im}] for
+// the vectors i0 + q < nv (row: the block's slice of the partial buffer).
+template <class A>
+__device__ __forceinline__ void dots_epilogue(A* re, A* im, bool cv, int i0, int nv, int base, double* row) {
+    __shared__ double sh[kT / 32][2 * kJT];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kJT; ++q) {
+        for (int o = 16; o > 0; o >>= 1) {
+            re[q] = add(re[q], shfl(re[q], o));
+            if (cv) im[q] = add(im[q], shfl(im[q], o));
+        }
+        if (lane == 0) {
+            sh[wid][2 * q] = to_d(re[q]);
+            sh[wid][2 * q + 1] = cv ? to_d(im[q]) : 0.0;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * kJT) {
+        double t = 0;
+        for (int q = 0; q < kT / 32; ++q) t += sh[q][threadIdx.x];
+        const int q = threadIdx.x / 2;
+        if (i0 + q < nv) row[(base + q) * 2 + (threadIdx.x & 1)] = t;
+    }
+    __syncthreads();   // sh is reused by the next call
+}
+
 template <class A>
 __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
                                                int mode, double* __restrict__ partial) {
@@ -296,28 +324,7 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_do
     for (int q = 0; q < kJT; ++q) re[q] = im[q] = zero<A>();
     if (S.cv) dots_rows<A, true>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
     else dots_rows<A, false>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
-    __shared__ double sh[kT / 32][2 * kJT];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const bool cv = S.cv;
-#pragma unroll
-    for (int q = 0; q < kJT; ++q) {
-        for (int o = 16; o > 0; o >>= 1) {
-            re[q] = add(re[q], shfl(re[q], o));
-            if (cv) im[q] = add(im[q], shfl(im[q], o));
-        }
-        if (lane == 0) {
-            sh[wid][2 * q] = to_d(re[q]);
-            sh[wid][2 * q + 1] = cv ? to_d(im[q]) : 0.0;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < 2 * kJT) {
-        double t = 0;
-        for (int q = 0; q < kT / 32; ++q) t += sh[q][threadIdx.x];
-        const int q = threadIdx.x / 2;
-        const int i = mode == 2 ? 0 : i0 + q;
-        if (i0 + q < nv) partial[((size_t)blockIdx.x * P + i) * 2 + (threadIdx.x & 1)] = t;
-    }
+    dots_epilogue<A>(re, im, S.cv, i0, nv, mode == 2 ? 0 : i0, partial + (size_t)blockIdx.x * P * 2);
     if (want_wn) {
         __shared__ double sw[kT / 32];
         const double t = block_sum(wn, sw);
@@ -421,7 +428,8 @@ __global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl,
 // ------------------------------------------------------------ update
 // col(j+1) -= sum_i col(i) h_i over the pass's vectors (pass 0: h1 from
 // `first`, pass 1: h2 over 0..j, only where the step's flag asks), leaving the
-// block's part of ||col(j+1)||^2 at partial[b][mmax].
+// block's part of ||col(j+1)||^2 at partial[b][mmax]; pass 0 of a Gram-Schmidt
+// slot also leaves the second-pass dots at partial[b][0..j].
 template <class A, bool CV>
 __device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r1, int first, int nv, const CA<A>* hs) {
     const char* V = (const char*)S.V;
@@ -459,7 +467,7 @@ __device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT, 4) eng_update(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+__global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_update(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
                                                  int pass, double* __restrict__ partial) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
     if (S.state != kSlotStep) return;
@@ -478,10 +486,25 @@ __global__ void __launch_bounds__(kT, 4) eng_update(const SlotDev* __restrict__ 
     A nacc = S.cv ? update_rows<A, true>(S, r0, r1, first, nv, hs) : update_rows<A, false>(S, r0, r1, first, nv, hs);
     __shared__ double sh[kT / 32];
     const double t = block_sum(nacc, sh);
+    const int P = mmax + 1;
     if (threadIdx.x == 0) {
-        const int P = mmax + 1;
         partial[((size_t)blockIdx.x * P + mmax) * 2] = t;
         partial[((size_t)blockIdx.x * P + mmax) * 2 + 1] = 0.0;
+    }
+    if (pass == 0 && S.orth != 2) {
+        // the Gram-Schmidt slots' second-pass dots V^* w' over this block's rows,
+        // while V and w' are still in cache; used when the DGKS test asks for
+        // the second pass
+        const void* w = colp(S, S.j + 1);
+        double* row = partial + (size_t)blockIdx.x * P * 2;
+        for (int c0 = 0; c0 < nv; c0 += kJT) {
+            A re[kJT], im[kJT], dummy = zero<A>();
+#pragma unroll
+            for (int q = 0; q < kJT; ++q) re[q] = im[q] = zero<A>();
+            if (S.cv) dots_rows<A, true>(S, r0, r1, c0, nv, w, re, im, false, dummy);
+            else dots_rows<A, false>(S, r0, r1, c0, nv, w, re, im, false, dummy);
+            dots_epilogue<A>(re, im, S.cv, c0, nv, c0, row);
+        }
     }
 }
 
@@ -808,7 +831,6 @@ static void launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const 
     eng_reduce<<<dim3(ns, mmax + 1), kT, 0, s>>>(ds, mmax, 0, pa);
     eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 0, pa);
     eng_reduce<<<dim3(ns, 1), kT, 0, s>>>(ds, mmax, 1, pa);
-    eng_dots<A><<<gd, kT, 0, s>>>(ds, rm, mmax, 1, pa);
     eng_reduce<<<dim3(ns, mmax), kT, 0, s>>>(ds, mmax, 2, pa);
     eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 1, pa);
     eng_reduce<<<dim3(ns, 1), kT, 0, s>>>(ds, mmax, 3, pa);
@@ -860,7 +882,7 @@ void Engine::run(int nsteps) {
     if (nrb_ == 0) return;
     if (!exec_) capture();
     for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
-    launches_ += 11 * (int64_t)nsteps;
+    launches_ += 10 * (int64_t)nsteps;
     // mirror the device step counters
     for (auto& sl : slots_) {
         if (!sl.live || sl.d.state != kSlotStep) continue;

@@ -1,10 +1,10 @@
 // qs_engine.h -- the batched Krylov engine: many Krylov processes ("slots"),
 // each on its own assembled operator and its own vectors, advanced together.
 //
-// One Lanczos/Arnoldi step of every stepping slot is a fixed sequence of
-// eleven launches (SpMV; dots + reduce + update with the norm fused; the
-// conditional second Gram-Schmidt pass; scale; advance), each covering all
-// slots through a block -> slot map.  The step
+// One Lanczos/Arnoldi step of every stepping slot is a fixed sequence of ten
+// launches (SpMV; dots + reduce; the update with the norm and the second
+// pass's dots fused; the conditional second Gram-Schmidt update; scale;
+// advance), each covering all slots through a block -> slot map.  The step
 // counters live on the device, so the sequence is captured once in a CUDA
 // graph and replayed; the host only meets the device when a slot has filled
 // its basis (restart, convergence test, exponential).  The projected matrix of
