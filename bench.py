@@ -331,13 +331,13 @@ def section_c4(qs, torch):
     sizes = [o.Ns for o in ops]
     # warm-up: tile autotuning (cached per size class) and graph capture
     t = time.perf_counter()
-    for prec in ("fp64", "fp64df"):
+    for prec in ("fp64", "fp64df", "fp32"):
         qs.eigsh_batch(ops, k=1, tol=1e-10, precision=prec)
     t_warm = time.perf_counter() - t
     timed = {}
     vals = {}
     infos = []
-    for prec in ("fp64", "fp64df"):
+    for prec in ("fp64", "fp64df", "fp32"):
         torch.cuda.synchronize()
         t = time.perf_counter()
         vals[prec] = qs.eigsh_batch(ops, k=1, tol=1e-10, precision=prec, infos=infos if prec == "fp64" else None)[:, 0]
@@ -376,6 +376,9 @@ def section_c4(qs, torch):
             "sequential_fp64_solves_per_s": len(ops) / t_seq,
             "batched_fp64_solves_per_s": len(ops) / timed["fp64"],
             "batched_fp64df_solves_per_s": len(ops) / timed["fp64df"],
+            "batched_fp32_polished_solves_per_s": len(ops) / timed["fp32"],
+            "batched_fp32_polished_speedup": t_seq / timed["fp32"],
+            "max_rel_diff_fp32_batched_vs_sequential": float(np.max(np.abs(vals["fp32"] - vs))) / scale,
             "batched_fp64_speedup": t_seq / timed["fp64"],
             "batched_fp64df_speedup": t_seq / timed["fp64df"],
             "max_rel_diff_fp64_batched_vs_sequential": float(np.max(np.abs(vals["fp64"] - vs))) / scale,

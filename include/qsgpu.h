@@ -223,7 +223,7 @@ typedef struct {
  * reorthogonalisation replaces the ARPACK implicitly restarted Lanczos;
  * convergence is ARPACK's test ||r_i|| <= tol * max(eps^(2/3), |theta_i|).
  * Assembled operators (qs_op_assemble) run on the batched engine with one
- * operator (as qs_eigsh_batch) unless opts->precision is 1. */
+ * operator (as qs_eigsh_batch). */
 QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *vectors, qs_eigsh_info *info);
 
 /* eigsh on nops Hermitian operators at once (e.g. every momentum / parity
@@ -234,8 +234,10 @@ QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *
  * block_diag_hamiltonian / BlockOps (tools.jl:2213-2420) followed by eigsh on
  * each block.  values: nops * k, ascending per operator; vectors: NULL or nops
  * pointers (each NULL or Ns_i x k in the operator's dtype, host); infos: NULL
- * or nops entries.  opts->precision: 0 FP64 Krylov vectors, 1 or 2
- * double-float vectors on the FP32 pipe.  opts->v0 is used when nops is 1,
+ * or nops entries.  opts->precision: 0 FP64 Krylov vectors, 1 FP32 vectors
+ * and products then an FP64 Rayleigh-quotient polish (a double-float
+ * refinement where the polish misses the tolerance), 2 double-float vectors
+ * on the FP32 pipe.  opts->v0 is used when nops is 1,
  * else every operator starts from seeded normal entries (the same seed as
  * qs_eigsh); opts->mem applies to v0 and the vectors. */
 QS_API int qs_eigsh_batch(qs_op *const *ops, int32_t nops, const qs_eigsh_opts *opts, double *values, void **vectors,

@@ -51,16 +51,27 @@ __device__ __forceinline__ double to_d(double a) { return a; }
 __device__ __forceinline__ double to_d(DF a) { return df_to_double(a); }
 __device__ __forceinline__ double shfl(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 __device__ __forceinline__ DF shfl(DF v, int o) { return df_shfl_xor(v, o, 32); }
+// FP32 storage and arithmetic (the FP32 form)
+__device__ __forceinline__ void mac(float& acc, float a, float b) { acc = fmaf(a, b, acc); }
+__device__ __forceinline__ void msub(float& acc, float a, float b) { acc = fmaf(-a, b, acc); }
+__device__ __forceinline__ float sub(float a, float b) { return a - b; }
+__device__ __forceinline__ float add(float a, float b) { return a + b; }
+__device__ __forceinline__ float mul(float a, float b) { return a * b; }
+__device__ __forceinline__ double to_d(float a) { return (double)a; }
+__device__ __forceinline__ float shfl(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 
 template <class A> __device__ __forceinline__ A zero();
 template <> __device__ __forceinline__ double zero<double>() { return 0.0; }
 template <> __device__ __forceinline__ DF zero<DF>() { return DF{0.f, 0.f}; }
+template <> __device__ __forceinline__ float zero<float>() { return 0.f; }
 template <class A> __device__ __forceinline__ A one();
 template <> __device__ __forceinline__ double one<double>() { return 1.0; }
 template <> __device__ __forceinline__ DF one<DF>() { return DF{1.f, 0.f}; }
+template <> __device__ __forceinline__ float one<float>() { return 1.f; }
 template <class A> __device__ __forceinline__ A from_d(double v);
 template <> __device__ __forceinline__ double from_d<double>(double v) { return v; }
 template <> __device__ __forceinline__ DF from_d<DF>(double v) { return df_from_double(v); }
+template <> __device__ __forceinline__ float from_d<float>(double v) { return (float)v; }
 
 // vector element i; 8 bytes per real component in both storages
 template <class A, bool CV> __device__ __forceinline__ CA<A> ldv(const void* p, int64_t i);
@@ -79,7 +90,20 @@ template <> __device__ __forceinline__ CA<DF> ldv<DF, true>(const void* p, int64
     const float4 v = ((const float4*)p)[i];
     return CA<DF>{DF{v.x, v.y}, DF{v.z, v.w}};
 }
+template <> __device__ __forceinline__ CA<float> ldv<float, false>(const void* p, int64_t i) {
+    return CA<float>{((const float*)p)[i], 0.f};
+}
+template <> __device__ __forceinline__ CA<float> ldv<float, true>(const void* p, int64_t i) {
+    const float2 v = ((const float2*)p)[i];
+    return CA<float>{v.x, v.y};
+}
 template <class A, bool CV> __device__ __forceinline__ void stv(void* p, int64_t i, CA<A> v);
+template <> __device__ __forceinline__ void stv<float, false>(void* p, int64_t i, CA<float> v) {
+    ((float*)p)[i] = v.re;
+}
+template <> __device__ __forceinline__ void stv<float, true>(void* p, int64_t i, CA<float> v) {
+    ((float2*)p)[i] = make_float2(v.re, v.im);
+}
 template <> __device__ __forceinline__ void stv<double, false>(void* p, int64_t i, CA<double> v) {
     ((double*)p)[i] = v.re;
 }
@@ -103,14 +127,22 @@ template <> __device__ __forceinline__ CA<DF> ldtab<DF>(const SlotDev& S, int c)
     const float4 v = __ldg(S.tabdf + c);
     return CA<DF>{DF{v.x, v.y}, DF{v.z, v.w}};
 }
-template <class A> __device__ __forceinline__ CA<A> lddiag(const double2* d64, const float4* ddf, int64_t r);
-template <> __device__ __forceinline__ CA<double> lddiag<double>(const double2* d64, const float4*, int64_t r) {
-    const double2 v = d64[r];
+template <> __device__ __forceinline__ CA<float> ldtab<float>(const SlotDev& S, int c) {
+    const float2 v = __ldg(S.tab32 + c);
+    return CA<float>{v.x, v.y};
+}
+template <class A> __device__ __forceinline__ CA<A> lddiag(const SlotDev& S, int64_t r);
+template <> __device__ __forceinline__ CA<double> lddiag<double>(const SlotDev& S, int64_t r) {
+    const double2 v = S.diag64[r];
     return CA<double>{v.x, v.y};
 }
-template <> __device__ __forceinline__ CA<DF> lddiag<DF>(const double2*, const float4* ddf, int64_t r) {
-    const float4 v = ddf[r];
+template <> __device__ __forceinline__ CA<DF> lddiag<DF>(const SlotDev& S, int64_t r) {
+    const float4 v = S.diagdf[r];
     return CA<DF>{DF{v.x, v.y}, DF{v.z, v.w}};
+}
+template <> __device__ __forceinline__ CA<float> lddiag<float>(const SlotDev& S, int64_t r) {
+    const float2 v = S.diag32[r];
+    return CA<float>{v.x, v.y};
 }
 template <class A> __device__ __forceinline__ A ldrsq(const void* t, int i);
 template <> __device__ __forceinline__ double ldrsq<double>(const void* t, int i) { return ((const double*)t)[i]; }
@@ -118,9 +150,14 @@ template <> __device__ __forceinline__ DF ldrsq<DF>(const void* t, int i) {
     const float2 v = ((const float2*)t)[i];
     return DF{v.x, v.y};
 }
+template <> __device__ __forceinline__ float ldrsq<float>(const void* t, int i) { return ((const float*)t)[i]; }
 
-__device__ __forceinline__ size_t esz(const SlotDev& S) { return S.cv ? 16 : 8; }
-__device__ __forceinline__ char* colp(const SlotDev& S, int c) { return (char*)S.V + (size_t)c * S.n * esz(S); }
+// bytes of one vector element: 8 per real component in FP64 and double-float,
+// 4 in FP32
+template <class A, bool CV> __host__ __device__ constexpr size_t vbytes() { return sizeof(A) * (CV ? 2 : 1); }
+template <class A> __device__ __forceinline__ char* colp(const SlotDev& S, int c) {
+    return (char*)S.V + (size_t)c * S.n * (S.cv ? vbytes<A, true>() : vbytes<A, false>());
+}
 
 // ------------------------------------------------------------ SpMV
 // y = col(j + 1) = H col(j) on every stepping slot: sliced ELL, one thread per
@@ -131,8 +168,8 @@ __device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int64_t n = S.n;
     const int64_t s0 = lb * S.spb, s1 = min(S.nslices, s0 + S.spb);
-    const void* x = colp(S, S.j);
-    void* y = colp(S, S.j + 1);
+    const void* x = colp<A>(S, S.j);
+    void* y = colp<A>(S, S.j + 1);
     const int cb = S.code_bits;
     const uint32_t cmask = S.code_mask;
     const uint16_t* __restrict__ len = S.len;
@@ -160,7 +197,7 @@ __device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA
         CA<A> out;
         out.re = mul(ar, sc);
         out.im = CV ? mul(ai, sc) : zero<A>();
-        const CA<A> d = lddiag<A>(S.diag64, S.diagdf, r);
+        const CA<A> d = lddiag<A>(S, r);
         const CA<A> xr = ldv<A, CV>(x, r);
         mac(out.re, d.re, xr.re);
         if (CV) {
@@ -210,7 +247,7 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
                                           A* re, A* im, bool want_wn, A& wn) {
     const int64_t n = S.n;
     const char* V = (const char*)S.V;
-    const size_t cs = (size_t)n * (CV ? 16 : 8);
+    const size_t cs = (size_t)n * vbytes<A, CV>();
     // columns past nv repeat the last one (cached) so that every load of a row
     // is issued before the arithmetic
     const char* col[kJT];
@@ -308,11 +345,11 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_do
     if (mode == 2) {
         first = S.ncol;
         nv = S.ncol + 1;
-        w = colp(S, S.ncol);
+        w = colp<A>(S, S.ncol);
     } else {
         first = (mode == 0 && S.orth == 2) ? S.j : 0;
         nv = S.j + 1;
-        w = colp(S, S.j + 1);
+        w = colp<A>(S, S.j + 1);
     }
     const int i0 = first + blockIdx.y * kJT;
     if (i0 >= nv) return;
@@ -433,7 +470,7 @@ __global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl,
 template <class A, bool CV>
 __device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r1, int first, int nv, const CA<A>* hs) {
     const char* V = (const char*)S.V;
-    const size_t cs = (size_t)S.n * (CV ? 16 : 8);
+    const size_t cs = (size_t)S.n * vbytes<A, CV>();
     void* w = (void*)(V + (size_t)(S.j + 1) * cs);
     A nacc = zero<A>();
     auto term = [&](A& ar, A& ai, const CA<A>& v, const CA<A>& h) {
@@ -495,7 +532,7 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_up
         // the Gram-Schmidt slots' second-pass dots V^* w' over this block's rows,
         // while V and w' are still in cache; used when the DGKS test asks for
         // the second pass
-        const void* w = colp(S, S.j + 1);
+        const void* w = colp<A>(S, S.j + 1);
         double* row = partial + (size_t)blockIdx.x * P * 2;
         for (int c0 = 0; c0 < nv; c0 += kJT) {
             A re[kJT], im[kJT], dummy = zero<A>();
@@ -515,7 +552,7 @@ __global__ void __launch_bounds__(kT) eng_scale(const SlotDev* __restrict__ sl, 
     const SlotDev& S = sl[rmap[blockIdx.x]];
     if (S.state != (mode == 0 ? kSlotStep : kSlotNormalize)) return;
     const A f = from_d<A>(S.nrm[1]);
-    void* w = colp(S, mode == 0 ? S.j + 1 : S.ncol);
+    void* w = colp<A>(S, mode == 0 ? S.j + 1 : S.ncol);
     const int64_t lb = blockIdx.x - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
@@ -548,7 +585,7 @@ template <class A, bool CV>
 __device__ __forceinline__ void rotate_rows(const SlotDev& S, int64_t r0, int64_t r1) {
     char* V = (char*)S.V;
     char* T = (char*)S.tmp;
-    const size_t cs = (size_t)S.n * (CV ? 16 : 8);
+    const size_t cs = (size_t)S.n * vbytes<A, CV>();
     const CA<A>* Y = (const CA<A>*)S.y;
     const int nin = S.rot_in, p = S.p;
     const bool yreal = S.yreal;
@@ -590,12 +627,27 @@ __global__ void __launch_bounds__(kT, 4) eng_rotate(const SlotDev* __restrict__ 
     else rotate_rows<A, false>(S, r0, r1);
 }
 
+// Runs f with a value of the step arithmetic's type for storage st.
+template <class F>
+void with_store(Store st, F&& f) {
+    if (st == Store::DF) f(DF{0.f, 0.f});
+    else if (st == Store::F32) f(0.0f);
+    else f(0.0);
+}
+
+VKind store_kind(Store st, bool cv) {
+    if (st == Store::DF) return cv ? VKind::CDF64 : VKind::DF64;
+    if (st == Store::F32) return cv ? VKind::C64 : VKind::F32;
+    return cv ? VKind::C128 : VKind::F64;
+}
+
 // ------------------------------------------------------------ autotuner
 struct TuneKey {
-    bool df, cv, cm;
+    int st;
+    bool cv, cm;
     int size_class;
     bool operator<(const TuneKey& o) const {
-        return std::tie(df, cv, cm, size_class) < std::tie(o.df, o.cv, o.cm, o.size_class);
+        return std::tie(st, cv, cm, size_class) < std::tie(o.st, o.cv, o.cm, o.size_class);
     }
 };
 std::mutex g_tune_mu;
@@ -606,17 +658,20 @@ int size_class(int64_t n) { return (int)std::floor(2.0 * std::log2((double)std::
 }  // namespace
 
 // ====================================================================== Engine
-Engine::Engine(bool df, cudaStream_t s) : df_(df), s_(s) {
+Engine::Engine(Store st, cudaStream_t s) : st_(st), s_(s) {
     std::vector<double> r64(kMaxGroup + 1, 0.0);
-    std::vector<float> rdf(2 * (kMaxGroup + 1), 0.f);
+    std::vector<float> rdf(2 * (kMaxGroup + 1), 0.f), r32(kMaxGroup + 1, 0.f);
     for (int i = 1; i <= kMaxGroup; ++i) {
         r64[i] = 1.0 / std::sqrt((double)i);
         df_split_host(r64[i], rdf[2 * i], rdf[2 * i + 1]);
+        r32[i] = (float)r64[i];
     }
     rsq64_.alloc(r64.size() * sizeof(double));
     rsqdf_.alloc(rdf.size() * sizeof(float));
+    rsq32_.alloc(r32.size() * sizeof(float));
     QS_CUDA(cudaMemcpy(rsq64_.p, r64.data(), r64.size() * sizeof(double), cudaMemcpyHostToDevice));
     QS_CUDA(cudaMemcpy(rsqdf_.p, rdf.data(), rdf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    QS_CUDA(cudaMemcpy(rsq32_.p, r32.data(), r32.size() * sizeof(float), cudaMemcpyHostToDevice));
 }
 
 Engine::~Engine() {
@@ -626,7 +681,7 @@ Engine::~Engine() {
 }
 
 Tiles Engine::tune(Op& op, int m, bool cv) {
-    const TuneKey key{df_, cv, op.complex_mat, size_class(op.basis->n)};
+    const TuneKey key{(int)st_, cv, op.complex_mat, size_class(op.basis->n)};
     {
         std::lock_guard<std::mutex> g(g_tune_mu);
         auto it = g_tuned.find(key);
@@ -634,7 +689,7 @@ Tiles Engine::tune(Op& op, int m, bool cv) {
     }
     // time a few steps of this operator alone for every candidate tile pair
     const int mt = std::min(m, 12);
-    Engine E(df_, s_);
+    Engine E(st_, s_);
     int id = E.add(op, mt, cv, false);
     E.seed(id, 1);
     E.normalize({id});
@@ -671,8 +726,8 @@ Tiles Engine::tune(Op& op, int m, bool cv) {
     return best;
 }
 
-size_t Engine::slot_bytes(int64_t n, int m, bool cv, int tmp_cols) {
-    const size_t es = cv ? 16 : 8;
+size_t Engine::slot_bytes(int64_t n, int m, bool cv, int tmp_cols, Store st) {
+    const size_t es = store_bytes(st, cv);
     const int tc = tmp_cols > 0 ? tmp_cols : m - 1;
     return (size_t)(m + 1 + tc) * n * es + ((size_t)2 * m + (size_t)(m + 1) * m + (size_t)m * m) * 16 + 128;
 }
@@ -700,6 +755,8 @@ int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols, int orth)
     d.stab = op.basis->symmetric ? op.basis->d_stab.as<uint16_t>() : nullptr;
     d.diag64 = op.d_diag.as<double2>();
     d.diagdf = op.d_diag_df.as<float4>();
+    d.tab32 = M.table32.as<float2>();
+    d.diag32 = op.d_diag32.as<float2>();
     d.code_mask = M.code_bits >= 32 ? 0xffffffffu : ((1u << M.code_bits) - 1u);
     d.packed = M.packed;
     d.code_bits = M.code_bits;
@@ -709,7 +766,7 @@ int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols, int orth)
     d.cv = cv;
     d.n = n;
     d.nslices = M.nslices;
-    const size_t es = cv ? 16 : 8;
+    const size_t es = store_bytes(st_, cv);
     sl.V.alloc((size_t)(m + 1) * n * es, s_);
     const int tc = tmp_cols > 0 ? std::min(tmp_cols, m) : m - 1;
     sl.tmp.alloc((size_t)tc * n * es, s_);
@@ -840,12 +897,12 @@ static void launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const 
 
 void Engine::launch_step() {
     const int ns = (int)slots_.size();
-    if (df_)
-        launch_step_t<DF>(dslots_.as<SlotDev>(), dslots_.as<SlotDev>(), rmap_.as<int>(), smap_.as<int>(),
-                          partial_.as<double>(), rsqdf_.p, nrb_, nsb_, mmax_, ns, s_);
-    else
-        launch_step_t<double>(dslots_.as<SlotDev>(), dslots_.as<SlotDev>(), rmap_.as<int>(), smap_.as<int>(),
-                              partial_.as<double>(), rsq64_.p, nrb_, nsb_, mmax_, ns, s_);
+    const void* rsq = st_ == Store::DF ? rsqdf_.p : (st_ == Store::F32 ? rsq32_.p : rsq64_.p);
+    with_store(st_, [&](auto tag) {
+        using A = decltype(tag);
+        launch_step_t<A>(dslots_.as<SlotDev>(), dslots_.as<SlotDev>(), rmap_.as<int>(), smap_.as<int>(),
+                         partial_.as<double>(), rsq, nrb_, nsb_, mmax_, ns, s_);
+    });
 }
 
 void Engine::capture() {
@@ -895,17 +952,16 @@ void Engine::run(int nsteps) {
 
 void Engine::seed(int id, uint64_t sd) {
     const SlotDev& d = slots_[id].d;
-    const VKind ks = df_ ? (d.cv ? VKind::CDF64 : VKind::DF64) : (d.cv ? VKind::C128 : VKind::F64);
-    fill_normal(d.V, ks, d.n, sd, s_);
+    fill_normal(d.V, store_kind(st_, d.cv), d.n, sd, s_);
     ++launches_;
 }
 
 void Engine::load(int id, int col, const double* v, bool device) {
     const SlotDev& d = slots_[id].d;
     const VKind k64 = d.cv ? VKind::C128 : VKind::F64;
-    const VKind ks = df_ ? (d.cv ? VKind::CDF64 : VKind::DF64) : k64;
-    const size_t bytes = (size_t)d.n * (d.cv ? 16 : 8);
-    char* dst = (char*)d.V + (size_t)col * bytes;
+    const VKind ks = store_kind(st_, d.cv);
+    const size_t bytes = (size_t)d.n * (d.cv ? 16 : 8);   // FP64 input
+    char* dst = (char*)d.V + (size_t)col * d.n * store_bytes(st_, d.cv);
     PoolBuf st;
     const void* src = v;
     if (!device) {
@@ -921,9 +977,9 @@ void Engine::load(int id, int col, const double* v, bool device) {
 void Engine::store(int id, int col, double* out, bool device) {
     const SlotDev& d = slots_[id].d;
     const VKind k64 = d.cv ? VKind::C128 : VKind::F64;
-    const VKind ks = df_ ? (d.cv ? VKind::CDF64 : VKind::DF64) : k64;
-    const size_t bytes = (size_t)d.n * (d.cv ? 16 : 8);
-    const char* src = (const char*)d.V + (size_t)col * bytes;
+    const VKind ks = store_kind(st_, d.cv);
+    const size_t bytes = (size_t)d.n * (d.cv ? 16 : 8);   // FP64 output
+    const char* src = (const char*)d.V + (size_t)col * d.n * store_bytes(st_, d.cv);
     if (device) {
         convert_vec(src, ks, out, k64, d.n, s_);
     } else {
@@ -951,15 +1007,12 @@ std::vector<double> Engine::normalize(const std::vector<int>& ids, int col, bool
     double* pa = partial_.as<double>();
     const int ns = (int)slots_.size();
     if (nrb_ > 0 && !ids.empty()) {
-        if (df_) {
-            eng_dots<DF><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 2, pa);
+        with_store(st_, [&](auto tag) {
+            using A = decltype(tag);
+            eng_dots<A><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 2, pa);
             eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 4, pa);
-            if (scale) eng_scale<DF><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
-        } else {
-            eng_dots<double><<<dim3(nrb_, 1), kT, 0, s_>>>(ds, rm, mmax_, 2, pa);
-            eng_reduce<<<dim3(ns, 1), kT, 0, s_>>>(ds, mmax_, 4, pa);
-            if (scale) eng_scale<double><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
-        }
+            if (scale) eng_scale<A><<<nrb_, kT, 0, s_>>>(ds, rm, 1);
+        });
         QS_CUDA(cudaGetLastError());
         launches_ += scale ? 3 : 2;
     }
@@ -974,19 +1027,20 @@ std::vector<double> Engine::normalize(const std::vector<int>& ids, int col, bool
 
 void Engine::rotate(const std::vector<RotReq>& reqs) {
     if (reqs.empty()) return;
-    // every slot's coefficients in the storage format (double2, or float4 hi/lo
-    // pairs) packed into one upload
+    // every slot's coefficients in the storage's complex format (double2,
+    // float4 hi/lo pairs, or float2), packed into one upload
+    const size_t eb = st_ == Store::F32 ? 8 : 16;
     size_t total = 0;
     for (const RotReq& R : reqs) total += R.Y.size();
-    if (total * 16 > cap_y_) {
-        cap_y_ = std::max<size_t>(total * 16 * 2, 1 << 16);
+    if (total * eb > cap_y_) {
+        cap_y_ = std::max<size_t>(total * eb * 2, 1 << 16);
         QS_CUDA(cudaStreamSynchronize(s_));
         ybuf_.alloc(cap_y_);
     }
     std::vector<double> c64;
-    std::vector<float> cdf;
-    if (df_) cdf.resize(4 * total);
-    else c64.resize(2 * total);
+    std::vector<float> c32;
+    if (st_ == Store::F64) c64.resize(2 * total);
+    else c32.resize((st_ == Store::DF ? 4 : 2) * total);
     std::vector<int> saved(reqs.size());
     size_t off = 0;
     for (size_t q = 0; q < reqs.size(); ++q) {
@@ -1000,18 +1054,22 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
         bool yreal = true;
         for (size_t i = 0; i < R.Y.size(); ++i) {
             const double re = R.Y[i].real(), im = R.Y[i].imag();
+            const size_t e = off + i;
             if (im != 0.0) yreal = false;
-            if (df_) {
-                df_split_host(re, cdf[4 * (off + i)], cdf[4 * (off + i) + 1]);
-                df_split_host(im, cdf[4 * (off + i) + 2], cdf[4 * (off + i) + 3]);
+            if (st_ == Store::DF) {
+                df_split_host(re, c32[4 * e], c32[4 * e + 1]);
+                df_split_host(im, c32[4 * e + 2], c32[4 * e + 3]);
+            } else if (st_ == Store::F32) {
+                c32[2 * e] = (float)re;
+                c32[2 * e + 1] = (float)im;
             } else {
-                c64[2 * (off + i)] = re;
-                c64[2 * (off + i) + 1] = im;
+                c64[2 * e] = re;
+                c64[2 * e + 1] = im;
             }
         }
         saved[q] = d.state;
         d.state = kSlotRotate;
-        d.y = (char*)ybuf_.p + off * 16;
+        d.y = (char*)ybuf_.p + off * eb;
         d.yreal = yreal;
         d.rot_in = R.nin;
         d.p = R.p;
@@ -1021,13 +1079,15 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
         off += R.Y.size();
     }
     if (total)
-        QS_CUDA(cudaMemcpyAsync(ybuf_.p, df_ ? (const void*)cdf.data() : (const void*)c64.data(), total * 16,
-                                cudaMemcpyHostToDevice, s_));
+        QS_CUDA(cudaMemcpyAsync(ybuf_.p, st_ == Store::F64 ? (const void*)c64.data() : (const void*)c32.data(),
+                                total * eb, cudaMemcpyHostToDevice, s_));
     dirty_ = true;
     sync_table();
     if (nrb_ > 0) {
-        if (df_) eng_rotate<DF><<<nrb_, kT, 0, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>());
-        else eng_rotate<double><<<nrb_, kT, 0, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>());
+        with_store(st_, [&](auto tag) {
+            using A = decltype(tag);
+            eng_rotate<A><<<nrb_, kT, 0, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>());
+        });
         QS_CUDA(cudaGetLastError());
         ++launches_;
     }
@@ -1135,16 +1195,20 @@ void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, voi
         m = (int)std::min<int64_t>(m, n);
     }
     if (m <= k) throw Error(QS_ERR_ARGUMENT, "ncv must exceed k");
-    Engine E(o.precision != 0, ops[0]->stream);
+    const bool fp32 = o.precision == 1;
+    Engine E(o.precision == 0 ? Store::F64 : (fp32 ? Store::F32 : Store::DF), ops[0]->stream);
     std::vector<int> id(nops);
     std::vector<EigTask> task(nops);
     const bool dev = o.mem == QS_MEM_DEVICE;
+    // the FP32 form converges to what FP32 vectors resolve, then an FP64 polish
+    const double tol_run = fp32 ? std::max(o.tol > 0 ? o.tol : 2.220446049250313e-16, 2e-6) : o.tol;
     for (int i = 0; i < nops; ++i) {
         id[i] = E.add(*ops[i], m, ops[i]->complex_mat);
         if (o.v0 && nops == 1) E.load(id[i], 0, o.v0, dev);   // a start vector only for a single operator
         else E.seed(id[i], 20261203ull);
-        task[i].init(k, o.which, o.tol, m, o.maxiter);
+        task[i].init(k, o.which, tol_run, m, o.maxiter);
     }
+    std::vector<PoolBuf> promoted(fp32 ? nops : 0);   // FP64 Ritz vectors of the FP32 form
     E.normalize(id);
     for (int i = 0; i < nops; ++i) E.start(id[i], 0);
     std::vector<char> done(nops, 0);
@@ -1177,9 +1241,12 @@ void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, voi
             --left;
             if (t.nconv < k) throw Error(QS_ERR_NOT_CONVERGED, "batched eigsh did not converge within maxiter restarts");
             for (int q = 0; q < k; ++q) values[(size_t)i * k + q] = t.theta[q];
-            if (vectors && vectors[i]) {
-                const int64_t n = ops[i]->basis->n;
-                const int comps = ops[i]->complex_mat ? 2 : 1;
+            const int64_t n = ops[i]->basis->n;
+            const int comps = ops[i]->complex_mat ? 2 : 1;
+            if (fp32) {
+                promoted[i].alloc((size_t)k * n * comps * sizeof(double), E.stream());
+                for (int q = 0; q < k; ++q) E.store(id[i], q, promoted[i].as<double>() + (size_t)q * n * comps, true);
+            } else if (vectors && vectors[i]) {
                 for (int q = 0; q < k; ++q) E.store(id[i], q, (double*)vectors[i] + (size_t)q * n * comps, dev);
             }
             if (infos) {
@@ -1197,6 +1264,80 @@ void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, voi
     for (int i = 0; i < nops; ++i) E.remove(id[i]);
     QS_CUDA(cudaStreamSynchronize(E.stream()));
     note_launches(E.launches());
+    if (!fp32) return;
+    // FP64 polish of the FP32 form: the Rayleigh quotient of every promoted Ritz
+    // vector with the FP64 product; where the quadratic bound ||r||^2 / gap
+    // misses the tolerance, a double-float thick-restart solve from the
+    // promoted ground vector finishes the job
+    const double tol = o.tol > 0 ? o.tol : 2.220446049250313e-16;
+    const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
+    for (int i = 0; i < nops; ++i) {
+        Op& op = *ops[i];
+        const int64_t n = op.basis->n;
+        const bool cpx = op.complex_mat;
+        const int comps = cpx ? 2 : 1;
+        const VKind k64 = cpx ? VKind::C128 : VKind::F64;
+        Blas B(k64, n, op.stream);
+        PoolBuf Ax((size_t)n * comps * sizeof(double), op.stream);
+        std::vector<double> th(k);
+        bool refine = false;
+        double maxrel = 0;
+        for (int q = 0; q < k; ++q) {
+            double* xq = promoted[i].as<double>() + (size_t)q * n * comps;
+            const double nx = B.norm(xq);
+            B.scale(xq, xq, cd(1.0 / nx, 0));
+            MatvecCall c;
+            c.x = xq;
+            c.y = Ax.p;
+            c.x_complex = c.y_complex = cpx;
+            op_matvec_device(op, c, op.stream);
+            th[q] = B.dot(xq, Ax.p).real();
+            B.axpy(Ax.p, xq, cd(-th[q], 0));
+            const double rn = B.norm(Ax.p);
+            double gap = 1e300;
+            for (int q2 = 0; q2 < k; ++q2)
+                if (q2 != q) gap = std::min(gap, std::fabs(values[(size_t)i * k + q2] - th[q]));
+            if (gap == 1e300) gap = std::max(1e-300, std::fabs(th[q]));
+            maxrel = std::max(maxrel, rn / std::max(eps23, std::fabs(th[q])));
+            if (rn * rn / gap > tol * std::max(1.0, std::fabs(th[q]))) refine = true;
+        }
+        if (refine) {
+            qs_eigsh_opts r = o;
+            r.precision = 2;
+            r.v0 = promoted[i].as<double>();
+            r.mem = QS_MEM_DEVICE;
+            r.want_vectors = vectors && vectors[i];
+            std::vector<double> vals(k);
+            void* vec = (vectors && vectors[i]) ? vectors[i] : nullptr;
+            PoolBuf vdev;
+            if (vec && !dev) {
+                vdev.alloc((size_t)k * n * comps * sizeof(double), op.stream);
+                vec = vdev.p;
+            }
+            qs_eigsh_info inf{};
+            Op* one = &op;
+            eigsh_batch(&one, 1, r, vals.data(), vec ? &vec : nullptr, &inf);
+            for (int q = 0; q < k; ++q) values[(size_t)i * k + q] = vals[q];
+            if (vectors && vectors[i] && !dev)
+                QS_CUDA(cudaMemcpy(vectors[i], vdev.p, vdev.bytes, cudaMemcpyDeviceToHost));
+            if (infos) {
+                infos[i].matvecs += inf.matvecs;
+                infos[i].restarts += inf.restarts;
+                infos[i].max_rel_residual = inf.max_rel_residual;
+            }
+        } else {
+            for (int q = 0; q < k; ++q) values[(size_t)i * k + q] = th[q];
+            if (vectors && vectors[i])
+                QS_CUDA(cudaMemcpyAsync(vectors[i], promoted[i].p, promoted[i].bytes,
+                                        dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, op.stream));
+            if (infos) {
+                infos[i].matvecs += k;
+                infos[i].max_rel_residual = maxrel;
+            }
+        }
+        QS_CUDA(cudaStreamSynchronize(op.stream));
+        if (infos) infos[i].seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
 }
 
 // ================================================================ Krylov exponential
@@ -1391,7 +1532,7 @@ void evolve_engine(Op& op, const double* v0, const std::vector<cd>& scales, doub
     const bool herm = op.hermitian;
     const int orth = herm ? 2 : 0;
     auto copy_v0 = [&](int i) { std::copy(v0, v0 + 2 * n, out + (size_t)i * 2 * n); };
-    Engine E(precision != 0, op.stream);
+    Engine E(precision == 0 ? Store::F64 : Store::DF, op.stream);
     // one factorisation from v0 serves every time whose estimate passes
     const int f = E.add(op, m, true, true, 1, orth);
     E.load(f, 0, v0, false);
@@ -1435,7 +1576,7 @@ void evolve_engine(Op& op, const double* v0, const std::vector<cd>& scales, doub
     if (!failing.empty()) {
         size_t fr = 0, tot = 0;
         QS_CUDA(cudaMemGetInfo(&fr, &tot));
-        const size_t per = Engine::slot_bytes(n, m, true, 1);
+        const size_t per = Engine::slot_bytes(n, m, true, 1, E.store());
         const int wave = (int)std::max<size_t>(1, std::min<size_t>(failing.size(), (fr / 2) / std::max<size_t>(per, 1)));
         for (size_t w0 = 0; w0 < failing.size(); w0 += wave) {
             const size_t w1 = std::min(failing.size(), w0 + wave);

@@ -47,6 +47,8 @@ struct SlotDev {
     const uint16_t* stab;   // stabiliser order per row (null without symmetry)
     const double2* diag64;  // complex diagonal
     const float4* diagdf;
+    const float2* tab32;    // FP32 storage: complex value per code and diagonal
+    const float2* diag32;
     uint32_t code_mask;
     int32_t packed, code_bits, ncodes, max_stab;
     int32_t cm, cv;         // complex matrix elements / complex vectors
@@ -78,6 +80,9 @@ struct SlotDev {
     int32_t rb_begin, rb_count, sb_begin, sb_count;
 };
 
+// Storage of a slot's Krylov vectors (and the arithmetic of the step kernels).
+enum class Store : int32_t { F64 = 0, DF = 1, F32 = 2 };
+
 struct Tiles {
     int rpb = 1024, spb = 64;
 };
@@ -91,19 +96,19 @@ struct RotReq {
 
 class Engine {
    public:
-    Engine(bool df, cudaStream_t s);
+    Engine(Store st, cudaStream_t s);
     ~Engine();
     Engine(const Engine&) = delete;
     Engine& operator=(const Engine&) = delete;
 
-    bool df() const { return df_; }
+    Store store() const { return st_; }
     cudaStream_t stream() const { return s_; }
     // Adds a slot of basis size m on an assembled operator (assembled here if
     // needed).  cv: complex vectors (required for complex operators); tmp_cols:
     // most rotation outputs (m - 1 when 0).
     int add(Op& op, int m, bool cv, bool tune = true, int tmp_cols = 0, int orth = 1);
     // device bytes add() would allocate for a slot
-    static size_t slot_bytes(int64_t n, int m, bool cv, int tmp_cols = 0);
+    static size_t slot_bytes(int64_t n, int m, bool cv, int tmp_cols = 0, Store st = Store::F64);
     void remove(int id);
     int count() const { return (int)slots_.size(); }
     const SlotDev& slot(int id) const { return slots_[id].d; }
@@ -149,10 +154,10 @@ class Engine {
     void capture();
     void launch_step();
     Tiles tune(Op& op, int m, bool cv);
-    bool df_;
+    Store st_;
     cudaStream_t s_;
     std::vector<Slot> slots_;
-    DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_, ybuf_;
+    DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_, rsq32_, ybuf_;
     size_t cap_y_ = 0;
     int nrb_ = 0, nsb_ = 0, mmax_ = 1, cap_slots_ = 0;
     size_t cap_partial_ = 0, cap_rmap_ = 0, cap_smap_ = 0;
@@ -178,6 +183,9 @@ struct EigTask {
     // final rotation (k Ritz vectors into columns 0..k-1; returns true).
     bool on_hold(const std::vector<cd>& H, int id, RotReq& rot);
 };
+
+// Element bytes of a vector in storage st (cv: complex).
+inline size_t store_bytes(Store st, bool cv) { return (st == Store::F32 ? 4 : 8) * (cv ? 2 : 1); }
 
 // Krylov projection of a filled record H ((m + 1) x m, column-major):
 // the completed size c (the reference's breakdown test, tn <= 100 eps

@@ -293,7 +293,7 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
         }
         return;
     }
-    if (op.assembled && op.asm_.has_sell && o.precision != 1 && k < n - 1) {
+    if (op.assembled && op.asm_.has_sell && k < n - 1) {
         // assembled operators: the batched engine with one slot (graph-replayed
         // steps, device-resident Lanczos coefficients, ARPACK's DGKS test)
         Op* one = &op;

@@ -356,7 +356,8 @@ void builder_loop(Server& S) {
             // replace the estimate by what is really held: the slot, and a new
             // operator (which stays counted while it is cached)
             std::lock_guard<std::mutex> g(S.mu);
-            const size_t slot = Engine::slot_bytes(q->n, m, cv, q->r.kind == QS_REQ_EIGSH ? 0 : 1);
+            const size_t slot = Engine::slot_bytes(q->n, m, cv, q->r.kind == QS_REQ_EIGSH ? 0 : 1,
+                                                   S.opts.precision == 0 ? Store::F64 : Store::DF);
             S.used = S.used - std::min(S.used, est) + slot + (built ? q->op->bytes : 0);
             S.peak = std::max(S.peak, S.used);
             est = 0;
@@ -403,7 +404,9 @@ void builder_loop(Server& S) {
 // ------------------------------------------------------------ engine thread
 void engine_loop(Server& S) {
     cudaSetDevice(S.opts.device);
-    Engine E(S.opts.precision != 0, S.stream);
+    // served solves use FP64 or double-float Krylov vectors (precision 1 runs
+    // as double-float: the FP32 form needs the per-solve FP64 polish)
+    Engine E(S.opts.precision == 0 ? Store::F64 : Store::DF, S.stream);
     std::vector<std::shared_ptr<Request>> live;
     auto fail = [&](const std::shared_ptr<Request>& q, int st, const std::string& e) {
         if (q->slot >= 0) E.remove(q->slot);

@@ -272,10 +272,11 @@ def eigsh_batch(ops, k=1, which="SA", tol=0.0, ncv=None, maxiter=None, return_ei
                 precision="fp64"):
     """eigsh(op; k, which) on every operator of `ops` at once: each Lanczos
     step is one launch per kernel for all operators, replayed from a CUDA
-    graph.  precision "fp64" stores the Krylov vectors in FP64, "fp64df" (or
-    "fp32") as double-float pairs on the FP32 pipe.  Returns an (len(ops), k)
-    array of eigenvalues and, when asked, one Ns_i x k vector block per
-    operator."""
+    graph.  precision "fp64" stores the Krylov vectors in FP64, "fp64df" as
+    double-float pairs on the FP32 pipe, "fp32" in FP32 followed by an FP64
+    Rayleigh-quotient polish (and a double-float refinement where the polish
+    misses the tolerance).  Returns an (len(ops), k) array of eigenvalues and,
+    when asked, one Ns_i x k vector block per operator."""
     w = str(which).upper()
     if w not in ("SA", "LA"):
         raise ArgumentError("which must be SA or LA on this engine")

@@ -20,7 +20,7 @@ def sectors(qs, L, nup, J2):
     return out
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp64df"])
+@pytest.mark.parametrize("precision", ["fp64", "fp64df", "fp32"])
 def test_batched_ground_states_all_sectors(qs, ora, precision):
     L, nup = 14, 7
     sp = models.j1j2(L, 1.0, 0.3)
@@ -43,10 +43,13 @@ def test_batched_ground_states_all_sectors(qs, ora, precision):
     infos = []
     vals, vecs = qs.eigsh_batch(ops, k=2, tol=1e-12, return_eigenvectors=True, infos=infos, precision=precision)
     assert all(i["nconv"] >= 2 for i in infos)
+    # the FP32 form polishes the eigenvalues to FP64 accuracy (Rayleigh quotient
+    # with the FP64 product); its vectors keep FP32-level residuals
+    res_tol = 1e-6 if precision == "fp32" else 1e-8
     for i, op in enumerate(ops):
         assert np.allclose(vals[i], dense0[i], rtol=1e-10, atol=1e-10), (syms[i], vals[i], dense0[i])
         res = op.dot(vecs[i]) - vecs[i] * vals[i]
-        assert np.abs(res).max() < 1e-8
+        assert np.abs(res).max() < res_tol
         single = qs.eigsh(op, k=2, tol=1e-12, return_eigenvectors=False)
         assert np.allclose(single, vals[i], rtol=1e-10, atol=1e-10)
     # the union of sector ground energies contains the global ground energy
@@ -90,8 +93,9 @@ def test_batched_mixed_real_and_complex_sizes(qs, ora):
             e[j] = 1
             H[:, j] = rep.matvec(sp, e)
         dense.append(np.linalg.eigvalsh(H)[:3])
-    for precision in ("fp64", "fp64df"):
+    for precision in ("fp64", "fp64df", "fp32"):
         vals, vecs = qs.eigsh_batch(ops, k=3, tol=1e-12, return_eigenvectors=True, precision=precision)
         for i, op in enumerate(ops):
             assert np.allclose(vals[i], dense[i], rtol=1e-10, atol=1e-10), (precision, i)
-            assert np.abs(op.dot(vecs[i]) - vecs[i] * vals[i]).max() < 1e-8
+            res_tol = 1e-6 if precision == "fp32" else 1e-8
+            assert np.abs(op.dot(vecs[i]) - vecs[i] * vals[i]).max() < res_tol
