@@ -1,7 +1,7 @@
 """CPU oracle for the QuSpin.jl spin-1/2 hot path.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` as the checker.  The shipped library never
+CPU-baseline leg of ``bench.py``, to compare against.  The shipped library never
 imports it.
 
 Two restatements of the reference, see ``qs_oracle.c``:

@@ -1,7 +1,7 @@
 """Builds libqsgpu.so in-tree for sm_103a with nvcc (no GPU needed).
 
 Each translation unit is compiled in parallel, then linked with the static CUDA
-runtime, so the library loads with nothing but the driver.
+runtime, so the library loads with nothing but the NVIDIA kernel driver.
 """
 from __future__ import annotations
 
