@@ -438,7 +438,8 @@ def section_c5(qs, torch, n_req=2000, rate=200.0, budget_gb=150.0, seq_sample=40
     out = {"workload": "%d requests, Poisson %.0f/s, L in 18..30 (even), J1-J2 J2=0.5, 70%% eigsh k=1 tol 1e-10, "
                        "30%% evolve t~U[0.5,5] m=30 tol 1e-9, HBM budget %.0f GB" % (n_req, rate, budget_gb),
            "sequential_fp64_sample": seq_sample, "sequential_fp64_solves_per_s": seq_sample / t_seq}
-    for name, prec, policy in (("fp64df", "fp64df", "fifo"), ("fp64df_smallest_first", "fp64df", "sjf")):
+    for name, prec, policy in (("fp64df", "fp64df", "fifo"), ("fp64df_smallest_first", "fp64df", "sjf"),
+                               ("fp32_smallest_first", "fp32", "sjf")):
         srv = qs.Server(hbm_budget_gb=budget_gb, precision=prec, policy=policy)
         tickets = [None] * n_req
         t0 = time.perf_counter()

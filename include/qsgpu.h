@@ -273,7 +273,10 @@ typedef struct qs_server qs_server;
 typedef struct {
     double hbm_budget_bytes;   /* device bytes the server may hold, 0 = 150e9 */
     int32_t max_slots;         /* solves running at once, 0 = 64 */
-    int32_t precision;         /* 0 FP64 Krylov vectors, 2 double-float (FP32 pipe) */
+    int32_t precision;         /* 0 FP64 Krylov vectors, 2 double-float (FP32 pipe);
+                                  1 eigsh in FP32 with an FP64 polish of each result
+                                  (double-float refinement where the polish misses
+                                  tol), evolve in double-float */
     int32_t disable_op_cache;  /* 1: free each operator with its last request */
     int32_t chunk_steps;       /* Krylov steps between admissions, 0 = 8 */
     int32_t builders;          /* threads building bases and operators, 0 = 4 */

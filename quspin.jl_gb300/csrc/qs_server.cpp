@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "../../include/qsgpu.h"
+#include "qs_blas.cuh"
 #include "qs_dense.h"
 #include "qs_engine.h"
 #include "qs_internal.h"
@@ -107,6 +108,8 @@ struct Request {
     double work = 0;   // estimated work (row-products), for the smallest-first policy
     size_t slot_reserved = 0;
     int slot = -1;
+    int lane = 0;            // engine holding the slot (1: the FP32 lane)
+    bool polished = false;   // an FP32 solve already went through its FP64 polish
     bool cv = false;
     int m = 0;
     EigTask eig;   // eigsh
@@ -356,8 +359,8 @@ void builder_loop(Server& S) {
             // replace the estimate by what is really held: the slot, and a new
             // operator (which stays counted while it is cached)
             std::lock_guard<std::mutex> g(S.mu);
-            const size_t slot = Engine::slot_bytes(q->n, m, cv, q->r.kind == QS_REQ_EIGSH ? 0 : 1,
-                                                   S.opts.precision == 0 ? Store::F64 : Store::DF);
+            const Store st = S.opts.precision == 0 ? Store::F64 : Store::DF;   // FP32 slots are smaller
+            const size_t slot = Engine::slot_bytes(q->n, m, cv, q->r.kind == QS_REQ_EIGSH ? 0 : 1, st);
             S.used = S.used - std::min(S.used, est) + slot + (built ? q->op->bytes : 0);
             S.peak = std::max(S.peak, S.used);
             est = 0;
@@ -402,101 +405,167 @@ void builder_loop(Server& S) {
 }
 
 // ------------------------------------------------------------ engine thread
+// One engine and the requests whose slots it holds.
+struct Lane {
+    int id;
+    Engine E;
+    std::vector<std::shared_ptr<Request>> live;
+    Lane(int i, Store st, cudaStream_t s) : id(i), E(st, s) {}
+};
+
 void engine_loop(Server& S) {
     cudaSetDevice(S.opts.device);
-    // served solves use FP64 or double-float Krylov vectors (precision 1 runs
-    // as double-float: the FP32 form needs the per-solve FP64 polish)
-    Engine E(S.opts.precision == 0 ? Store::F64 : Store::DF, S.stream);
-    std::vector<std::shared_ptr<Request>> live;
+    // lane 0: FP64 or double-float vectors (evolve; eigsh unless the FP32 form
+    // is asked for; the FP32 form's refinements).  Lane 1, with precision 1:
+    // eigsh in FP32, each result polished in FP64 before it is returned.
+    const bool fp32 = S.opts.precision == 1;
+    Lane lane0(0, S.opts.precision == 0 ? Store::F64 : Store::DF, S.stream);
+    std::unique_ptr<Lane> lane1;
+    cudaStream_t s1 = nullptr;
+    if (fp32) {
+        QS_CUDA(cudaStreamCreateWithFlags(&s1, cudaStreamNonBlocking));
+        lane1.reset(new Lane(1, Store::F32, s1));
+    }
+    auto lane_of = [&](const Request& q) -> Lane& { return q.lane == 1 ? *lane1 : lane0; };
     auto fail = [&](const std::shared_ptr<Request>& q, int st, const std::string& e) {
-        if (q->slot >= 0) E.remove(q->slot);
+        if (q->slot >= 0) lane_of(*q).E.remove(q->slot);
         q->slot = -1;
         finish(S, q, st, e);
     };
-    while (true) {
-        std::vector<std::shared_ptr<Request>> fresh;
-        {
-            std::unique_lock<std::mutex> g(S.mu);
-            if (S.stop) break;
-            if (S.ready.empty() && E.steps_to_event() == 0)
-                S.cv_engine.wait_for(g, std::chrono::milliseconds(20));
-            if (S.stop) break;
-            while (!S.ready.empty()) {
-                fresh.push_back(S.ready.front());
-                S.ready.pop_front();
-            }
-        }
-        // new slots join between steps, whatever the phase of the others
+    // drops finished requests and those handed to the other lane
+    auto prune = [](Lane& ln) {
+        ln.live.erase(std::remove_if(ln.live.begin(), ln.live.end(),
+                                     [&](const std::shared_ptr<Request>& q) { return q->slot < 0 || q->lane != ln.id; }),
+                      ln.live.end());
+    };
+    // Adds the requests to a lane: slots, start vectors (host v0, device v0, or
+    // seeded), one normalisation, then stepping.
+    auto admit = [&](Lane& ln, std::vector<std::shared_ptr<Request>>& reqs,
+                     const std::vector<const double*>& dev_v0) {
+        Engine& E = ln.E;
         std::vector<int> norm_ids;
         std::vector<std::shared_ptr<Request>> norm_q;
-        for (auto& q : fresh) {
+        for (size_t r = 0; r < reqs.size(); ++r) {
+            auto& q = reqs[r];
             try {
                 if (q->cancel) throw Error(QS_ERR_ARGUMENT, "cancelled");
                 // eigsh: CGS with ARPACK's DGKS test; evolve: the reference's Krylov
                 // recurrence (three-term for Hermitian operators, else CGS2)
                 const int orth = q->r.kind == QS_REQ_EIGSH ? 1 : (q->op->op->hermitian ? 2 : 0);
+                q->lane = ln.id;
                 q->slot = E.add(*q->op->op, q->m, q->cv, true, q->r.kind == QS_REQ_EIGSH ? 0 : 1, orth);
                 const int comps = q->cv ? 2 : 1;
-                if (!q->v0.empty()) {
+                if (!dev_v0.empty() && dev_v0[r]) {
+                    E.load(q->slot, 0, dev_v0[r], true);
+                } else if (!q->v0.empty()) {
                     if ((int64_t)q->v0.size() != q->n * comps) throw Error(QS_ERR_DIMENSION, "v0 must have length Ns");
                     E.load(q->slot, 0, q->v0.data(), false);
                 } else {
                     E.seed(q->slot, q->r.seed ? q->r.seed : 20261203ull);
                 }
-                if (q->r.kind == QS_REQ_EIGSH) q->eig.init(q->r.k, q->r.which, q->r.tol, q->m, q->r.maxiter);
+                if (q->r.kind == QS_REQ_EIGSH) {
+                    const double tol = q->r.tol > 0 ? q->r.tol : 2.220446049250313e-16;
+                    q->eig.init(q->r.k, q->r.which, ln.id == 1 ? std::max(tol, 2e-6) : q->r.tol, q->m,
+                                q->r.maxiter);
+                }
                 norm_ids.push_back(q->slot);
                 norm_q.push_back(q);
-                live.push_back(q);
+                ln.live.push_back(q);
             } catch (const Error& e) {
                 fail(q, e.status, e.what());
             } catch (const std::exception& e) {
                 fail(q, QS_ERR_CUDA, e.what());
             }
         }
-        if (!norm_ids.empty()) {
-            std::vector<double> nrm = E.normalize(norm_ids);
-            for (size_t i = 0; i < norm_q.size(); ++i) {
-                Request& q = *norm_q[i];
-                if (q.r.kind == QS_REQ_EVOLVE) {
-                    const cd s = q.r.imag_time ? cd(-q.r.t, 0) : cd(0, -q.r.t);
-                    q.evo.init(q.m, q.n, q.op->op->hermitian, s, q.r.tol > 0 ? q.r.tol : 1e-12, nrm[i]);
-                }
-                if (q.r.kind == QS_REQ_EIGSH || !q.evo.done()) E.start(q.slot, 0);
+        if (norm_ids.empty()) return;
+        std::vector<double> nrm = E.normalize(norm_ids);
+        for (size_t i = 0; i < norm_q.size(); ++i) {
+            Request& q = *norm_q[i];
+            if (q.r.kind == QS_REQ_EVOLVE) {
+                const cd sc = q.r.imag_time ? cd(-q.r.t, 0) : cd(0, -q.r.t);
+                q.evo.init(q.m, q.n, q.op->op->hermitian, sc, q.r.tol > 0 ? q.r.tol : 1e-12, nrm[i]);
             }
-            // evolve requests with nothing to do (t = 0 or v0 = 0) finish at once:
-            // exp(0) v = v is the start vector
-            for (auto& qp : norm_q) {
-                Request& q = *qp;
-                if (q.r.kind == QS_REQ_EVOLVE && q.evo.done()) {
-                    if (q.r.want_vector) {
-                        q.vec.resize(q.n * 2);
-                        E.store(q.slot, 0, q.vec.data(), false);
-                        for (double& v : q.vec) v *= q.evo.beta;
-                    }
-                    E.remove(q.slot);
-                    q.slot = -1;
-                    finish(S, qp, QS_OK, "");
+            if (q.r.kind == QS_REQ_EIGSH || !q.evo.done()) E.start(q.slot, 0);
+        }
+        // evolve requests with nothing to do (t = 0 or v0 = 0) finish at once:
+        // exp(0) v = v is the start vector
+        for (auto& qp : norm_q) {
+            Request& q = *qp;
+            if (q.r.kind == QS_REQ_EVOLVE && q.evo.done()) {
+                if (q.r.want_vector) {
+                    q.vec.resize(q.n * 2);
+                    E.store(q.slot, 0, q.vec.data(), false);
+                    for (double& v : q.vec) v *= q.evo.beta;
                 }
+                E.remove(q.slot);
+                q.slot = -1;
+                finish(S, qp, QS_OK, "");
             }
         }
-        live.erase(std::remove_if(live.begin(), live.end(), [](const std::shared_ptr<Request>& q) { return q->slot < 0; }),
-                   live.end());
+        prune(ln);
+    };
+    // FP64 polish of a finished FP32 ground-state solve: the Rayleigh quotient
+    // of each promoted Ritz vector with the FP64 product.  Returns true when the
+    // quadratic bound meets the tolerance (values and vectors set); otherwise
+    // `promoted` holds the FP64 vectors for a refinement.
+    auto polish = [&](Request& q, PoolBuf& promoted) -> bool {
+        Engine& E = lane1->E;
+        Op& op = *q.op->op;
+        const int k = q.eig.k;
+        const int comps = q.cv ? 2 : 1;
+        const VKind k64 = q.cv ? VKind::C128 : VKind::F64;
+        promoted.alloc((size_t)k * q.n * comps * sizeof(double), s1);
+        for (int i = 0; i < k; ++i) E.store(q.slot, i, promoted.as<double>() + (size_t)i * q.n * comps, true);
+        Blas B(k64, q.n, s1);
+        PoolBuf Ax((size_t)q.n * comps * sizeof(double), s1);
+        const double tol = q.r.tol > 0 ? q.r.tol : 2.220446049250313e-16;
+        std::vector<double> th(k);
+        bool ok = true;
+        for (int i = 0; i < k; ++i) {
+            double* xq = promoted.as<double>() + (size_t)i * q.n * comps;
+            const double nx = B.norm(xq);
+            B.scale(xq, xq, cd(1.0 / nx, 0));
+            MatvecCall c;
+            c.x = xq;
+            c.y = Ax.p;
+            c.x_complex = c.y_complex = q.cv;
+            c.no_tune = true;   // the operator may be stepping on the other lane
+            op_matvec_device(op, c, s1);
+            th[i] = B.dot(xq, Ax.p).real();
+            B.axpy(Ax.p, xq, cd(-th[i], 0));
+            const double rn = B.norm(Ax.p);
+            double gap = 1e300;
+            for (int i2 = 0; i2 < k; ++i2)
+                if (i2 != i) gap = std::min(gap, std::fabs(q.eig.theta[i2] - th[i]));
+            if (gap == 1e300) gap = std::max(1e-300, std::fabs(th[i]));
+            if (rn * rn / gap > tol * std::max(1.0, std::fabs(th[i]))) ok = false;
+        }
+        QS_CUDA(cudaStreamSynchronize(s1));
+        q.matvecs += k;
+        if (!ok) return false;
+        q.values = th;
+        if (q.r.want_vector) {
+            q.vec.resize((size_t)q.n * comps * k);
+            QS_CUDA(cudaMemcpy(q.vec.data(), promoted.p, q.vec.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+        return true;
+    };
+    // One round of a lane: cancellations, a bounded chunk of steps, the events.
+    auto round = [&](Lane& ln) {
+        Engine& E = ln.E;
         // requests released while running stop here, between steps
         {
             std::vector<std::shared_ptr<Request>> cancelled;
             {
                 std::lock_guard<std::mutex> g(S.mu);
-                for (auto& q : live)
+                for (auto& q : ln.live)
                     if (q->cancel && q->slot >= 0) cancelled.push_back(q);
             }
             for (auto& q : cancelled) fail(q, QS_ERR_ARGUMENT, "cancelled");
-            if (!cancelled.empty())
-                live.erase(std::remove_if(live.begin(), live.end(),
-                                          [](const std::shared_ptr<Request>& q) { return q->slot < 0; }),
-                           live.end());
+            if (!cancelled.empty()) prune(ln);
         }
         const int steps = E.steps_to_event();
-        if (steps == 0) continue;
+        if (steps == 0) return;
         // a bounded chunk keeps admission latency low for new arrivals
         E.run(std::min(steps, S.opts.chunk_steps > 0 ? S.opts.chunk_steps : steps));
         {
@@ -507,7 +576,7 @@ void engine_loop(Server& S) {
         std::vector<RotReq> rot;
         std::vector<std::shared_ptr<Request>> eig_fin, evo_ev, holding;
         std::vector<int> hold_ids;
-        for (auto& qp : live)
+        for (auto& qp : ln.live)
             if (qp->slot >= 0 && E.slot(qp->slot).state == kSlotHold) {
                 holding.push_back(qp);
                 hold_ids.push_back(qp->slot);
@@ -537,17 +606,38 @@ void engine_loop(Server& S) {
         }
         rot.erase(std::remove_if(rot.begin(), rot.end(), [&](const RotReq& R) { return !E.alive(R.id); }), rot.end());
         E.rotate(rot);
+        std::vector<std::shared_ptr<Request>> refine;
+        std::vector<PoolBuf> refine_v0;
         for (auto& qp : eig_fin) {
             Request& q = *qp;
             q.values = q.eig.theta;
-            q.restarts = q.eig.restarts;
+            q.restarts += q.eig.restarts;
             q.err = q.eig.maxrel;
-            q.matvecs = E.matvecs(q.slot);
+            q.matvecs += E.matvecs(q.slot);
             int st = QS_OK;
             std::string e;
             if (q.eig.nconv < q.eig.k) {
                 st = QS_ERR_NOT_CONVERGED;
                 e = "eigsh did not converge within maxiter restarts";
+            } else if (q.lane == 1) {
+                PoolBuf promoted;
+                bool ok = false;
+                try {
+                    ok = polish(q, promoted);
+                } catch (const Error& ex) {
+                    st = ex.status;
+                    e = ex.what();
+                }
+                if (st == QS_OK && !ok) {
+                    // the polish missed the tolerance: a double-float solve from
+                    // the promoted ground vector finishes the job on lane 0
+                    E.remove(q.slot);
+                    q.slot = -1;
+                    q.polished = true;
+                    refine.push_back(qp);
+                    refine_v0.push_back(std::move(promoted));
+                    continue;
+                }
             } else if (q.r.want_vector) {
                 const int comps = q.cv ? 2 : 1;
                 q.vec.resize((size_t)q.n * comps * q.eig.k);
@@ -557,9 +647,15 @@ void engine_loop(Server& S) {
             q.slot = -1;
             finish(S, qp, st, e);
         }
-        for (auto& qp : live) {
+        for (auto& qp : ln.live) {
             Request& q = *qp;
             if (q.slot >= 0 && q.r.kind == QS_REQ_EIGSH && E.slot(q.slot).state == kSlotHold) E.start(q.slot, q.eig.p);
+        }
+        if (!refine.empty()) {
+            std::vector<const double*> v0s;
+            for (auto& b : refine_v0) v0s.push_back(b.as<double>());
+            QS_CUDA(cudaStreamSynchronize(s1));
+            admit(lane0, refine, v0s);
         }
         // normalise the candidates (column m of each slot, grouped by m), then
         // accept, or split and project the first half step from the same basis
@@ -622,14 +718,36 @@ void engine_loop(Server& S) {
             qp->matvecs = E.matvecs(qp->slot);
             E.start(qp->slot, 0);
         }
-        live.erase(std::remove_if(live.begin(), live.end(), [](const std::shared_ptr<Request>& q) { return q->slot < 0; }),
-                   live.end());
+        prune(ln);
+    };
+    while (true) {
+        std::vector<std::shared_ptr<Request>> fresh;
+        {
+            std::unique_lock<std::mutex> g(S.mu);
+            if (S.stop) break;
+            const bool idle = lane0.E.steps_to_event() == 0 && (!lane1 || lane1->E.steps_to_event() == 0);
+            if (S.ready.empty() && idle) S.cv_engine.wait_for(g, std::chrono::milliseconds(20));
+            if (S.stop) break;
+            while (!S.ready.empty()) {
+                fresh.push_back(S.ready.front());
+                S.ready.pop_front();
+            }
+        }
+        // new slots join between steps, whatever the phase of the others
+        std::vector<std::shared_ptr<Request>> to0, to1;
+        for (auto& q : fresh) (fp32 && q->r.kind == QS_REQ_EIGSH ? to1 : to0).push_back(q);
+        if (!to0.empty()) admit(lane0, to0, {});
+        if (!to1.empty()) admit(*lane1, to1, {});
+        round(lane0);
+        if (lane1) round(*lane1);
         {
             std::lock_guard<std::mutex> g(S.mu);
-            S.stats.launches = E.launches();
+            S.stats.launches = lane0.E.launches() + (lane1 ? lane1->E.launches() : 0);
         }
     }
-    note_launches(E.launches());
+    note_launches(lane0.E.launches() + (lane1 ? lane1->E.launches() : 0));
+    lane1.reset();
+    if (s1) cudaStreamDestroy(s1);
 }
 
 }  // namespace

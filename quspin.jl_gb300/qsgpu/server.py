@@ -30,7 +30,10 @@ class Server:
     def __init__(self, hbm_budget_gb=150.0, max_slots=64, precision="fp64df", op_cache=True, chunk_steps=8,
                  builders=4, policy="fifo", max_wait_s=10.0):
         """policy "fifo" admits in arrival order; "sjf" admits the smallest
-        estimated work first, except a request waiting longer than max_wait_s."""
+        estimated work first, except a request waiting longer than max_wait_s.
+        precision "fp64" or "fp64df" sets the Krylov storage of every solve;
+        "fp32" runs eigsh in FP32 with an FP64 polish of each eigenpair (FP64
+        eigenvalues, FP32-level eigenvector residuals) and evolve in fp64df."""
         if policy not in ("fifo", "sjf"):
             raise ArgumentError("policy must be fifo or sjf")
         opts = _lib.ServerOpts(float(hbm_budget_gb) * 1e9, int(max_slots), _precision_code(precision),

@@ -26,7 +26,7 @@ def dense(ora, L, nup, sym, sp):
     return H
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp64df"])
+@pytest.mark.parametrize("precision", ["fp64", "fp64df", "fp32"])
 def test_served_results_match_dense(qs, ora, precision):
     L = 12
     sp = models.j1j2(L, 1.0, 0.3)   # away from J2 = 0.5, where sector ground states are degenerate
@@ -47,7 +47,10 @@ def test_served_results_match_dense(qs, ora, precision):
                 w = np.linalg.eigvalsh(D)[:2]
                 assert np.allclose(res["values"], w, rtol=1e-10, atol=1e-10), (sym, res["values"], w)
                 vec = srv.vector(t)
-                assert np.abs(D @ vec - vec * np.array(res["values"])).max() < 1e-8
+                # the FP32 form's eigenvalues are polished to FP64 accuracy; its
+                # vectors keep FP32-level residuals
+                res_tol = 1e-6 if precision == "fp32" else 1e-8
+                assert np.abs(D @ vec - vec * np.array(res["values"])).max() < res_tol
             else:
                 want = sla.expm(-1j * 1.7 * D) @ item[4]
                 got = srv.vector(t)
@@ -73,7 +76,7 @@ def test_same_result_alone_and_in_the_mix(qs):
             return srv.submit_eigsh(basis, tm, k=1, tol=1e-10, seed=seed, want_vector=True)
         return srv.submit_evolve(basis, tm, 2.3, seed=seed, tol=1e-9)
 
-    for precision in ("fp64", "fp64df"):
+    for precision in ("fp64", "fp64df", "fp32"):
         with qs.Server(precision=precision) as srv:
             alone = []
             for i, (kind, basis) in enumerate(probe):
