@@ -258,6 +258,55 @@ QS_API int qs_expm_multiply(qs_op *op, const double *a, const double *v, double 
 QS_API int qs_evolve(qs_op *op, const double *v0, double t0, const double *times, int32_t nt, int32_t imag_time,
               double tol, int32_t krylov_dim, int32_t precision, double *out);
 
+/* ------------------------------------------------------------ Krylov tools */
+
+/* Lanczos bases held on the device: the recurrences of tools.jl's
+ * lanczos_full / lanczos_iter for one Hermitian operator from nstart start
+ * vectors, run together on the batched engine (one FP64 slot per start). */
+typedef struct qs_lanczos qs_lanczos;
+
+typedef struct {
+    int32_t m;                /* Lanczos dimension, 1 <= m < Ns and m <= 256 */
+    int32_t full_ortho;       /* 1: re-orthogonalise against every kept vector */
+    double eps;               /* a basis stops where beta <= eps; 0 = machine epsilon */
+    int32_t complex_vectors;  /* 1: complex start vectors for a real operator */
+    int32_t mem;              /* QS_MEM_HOST or QS_MEM_DEVICE for v0 */
+} qs_lanczos_opts;
+
+/* lanczos_full(A, v0, m; full_ortho, eps) (tools.jl:2742-2805) and
+ * _lanczos_coefficients (2807-2843) for nstart start vectors at once: v0 is
+ * Ns x nstart column-major (real for a real operator unless
+ * opts->complex_vectors, else interleaved complex).  ArgumentError codes:
+ * m outside 1:Ns-1 or above 256, a zero start vector, a non-Hermitian operator. */
+QS_API int qs_lanczos_run(qs_op *op, const qs_lanczos_opts *opts, int32_t nstart, const double *v0,
+                          qs_lanczos **out);
+QS_API void qs_lanczos_destroy(qs_lanczos *lanczos);
+/* The recurrence of start s: alphas (m doubles, `used` valid), betas (m - 1
+ * doubles, used - 1 valid) and the number of Lanczos vectors kept (m, or
+ * fewer where beta fell to eps). */
+QS_API int qs_lanczos_coefficients(const qs_lanczos *lanczos, int32_t s, double *alphas, double *betas,
+                                   int32_t *used);
+/* 1 when the Lanczos vectors are complex. */
+QS_API int qs_lanczos_complex(const qs_lanczos *lanczos);
+/* The rows Q_T of start s: used x Ns, each Lanczos vector contiguous (real or
+ * interleaved complex per qs_lanczos_complex); host or device per mem. */
+QS_API int qs_lanczos_rows(qs_lanczos *lanczos, int32_t s, double *out, int32_t mem);
+/* lin_comb_Q_T(coeff, Q_T) (tools.jl:2909-2945), also expm_lanczos
+ * (2947-2952) and the Ritz vectors of ltlm_static_iteration: out[:, c] =
+ * sum_i coeff[i + c * used] q_i for c < ncoef; coeff complex (used x ncoef,
+ * column-major, interleaved), out complex Ns x ncoef (host or device per mem). */
+QS_API int qs_lanczos_combine(qs_lanczos *lanczos, int32_t s, const double *coeff, int32_t ncoef, double *out,
+                              int32_t mem);
+/* The overlaps of ftlm_static_iteration (tools.jl:2966-3013): out[s * m + i] =
+ * <q_i, O q_0> of every start s (complex, nstart x m, rows past `used` zero),
+ * for an observable on a basis of the same size. */
+QS_API int qs_lanczos_overlaps(qs_lanczos *lanczos, qs_op *observable, double *out);
+/* The projected observable of ltlm_static_iteration (tools.jl:3015-3068):
+ * out = R^* O R with R = sum_i q_i Y[i, :] (Y real, used x nv column-major);
+ * out complex nv x nv column-major (host). */
+QS_API int qs_lanczos_ritz_matrix(qs_lanczos *lanczos, int32_t s, qs_op *observable, const double *Y, int32_t nv,
+                                  double *out);
+
 /* ---------------------------------------------------------------- serving */
 
 /* A request loop for ground-state and time-evolution solves of mixed sizes and

@@ -436,3 +436,134 @@ def eigsh_arpack(matvec, n, k, dtype, v0=None, tol=0.0, ncv=None, maxiter=None):
     vals, vecs = spla.eigsh(op, k=k, which="SA", v0=v0, tol=tol, ncv=ncv, maxiter=maxiter)
     order = np.argsort(vals)
     return vals[order], vecs[:, order]
+
+
+# ----------------------------------------------------------------- Krylov tools
+def lanczos_coefficients(matvec, v0, m, eps=None, full_ortho=False, keep=False):
+    """Restates the recurrence of ``lanczos_full`` (src/tools.jl:2742-2805) and
+    ``_lanczos_coefficients`` (src/tools.jl:2807-2843): m steps of the
+    three-term Lanczos recurrence from v0 / ||v0||, with an optional
+    modified Gram-Schmidt pass over every kept vector (``full_ortho``),
+    stopping early when beta <= eps.  Returns (alphas, betas, rows) with rows
+    the Lanczos vectors (used x n) when ``keep``."""
+    v0 = np.asarray(v0)
+    n = v0.size
+    if not 1 <= m < n:
+        raise OracleError("Lanczos dimension m must satisfy 1 <= m < length(v0)")
+    nrm = np.linalg.norm(v0)
+    if not nrm > 0:
+        raise OracleError("initial Lanczos vector must be nonzero")
+    first = np.asarray(matvec(v0))
+    dt = np.result_type(v0.dtype, first.dtype, np.float64)
+    tol = np.finfo(np.float64).eps if eps is None else float(eps)
+    q = v0.astype(dt) / nrm
+    q_prev = np.zeros(n, dtype=dt)
+    r = first.astype(dt) / nrm
+    beta_prev = 0.0
+    alphas, betas, rows = [], [], []
+    for index in range(1, m + 1):
+        if keep or full_ortho:
+            rows.append(q.copy())
+        if index > 1:
+            r = np.asarray(matvec(q)).astype(dt)
+            r = r - beta_prev * q_prev
+        a = float(np.real(np.vdot(q, r)))
+        r = r - a * q
+        if full_ortho:
+            for b in rows:
+                r = r - np.vdot(b, r) * b
+        alphas.append(a)
+        if index == m:
+            break
+        beta = float(np.linalg.norm(r))
+        if beta <= tol:
+            break
+        betas.append(beta)
+        q_prev = q
+        q = r / beta
+        beta_prev = beta
+    return np.array(alphas), np.array(betas), (np.array(rows) if (keep or full_ortho) else None)
+
+
+def lanczos_full(matvec, v0, m, full_ortho=False, eps=None):
+    """Restates ``lanczos_full`` (src/tools.jl:2742-2805): (E, V, Q_T) with Q_T
+    the Lanczos vectors in rows and (E, V) the eigenpairs of the tridiagonal."""
+    import scipy.linalg as sla
+    a, b, rows = lanczos_coefficients(matvec, v0, m, eps, full_ortho, keep=True)
+    E, V = sla.eigh_tridiagonal(a, b) if a.size > 1 else (a.copy(), np.ones((1, 1)))
+    return E, V, rows
+
+
+def lanczos_vectors(matvec, v0, alphas, betas):
+    """Restates ``_LanczosVectorIterator`` (src/tools.jl:2845-2882): the Lanczos
+    vectors regenerated from v0 and the recurrence coefficients."""
+    q = np.asarray(v0, dtype=np.result_type(np.asarray(v0).dtype, np.float64))
+    q = q / np.linalg.norm(q)
+    q_prev = np.zeros_like(q)
+    yield q.copy()
+    for index in range(1, len(alphas)):
+        r = np.asarray(matvec(q)).astype(q.dtype)
+        if index > 1:
+            r = r - betas[index - 2] * q_prev
+        r = r - alphas[index - 1] * q
+        q_prev, q = q, r / betas[index - 1]
+        yield q.copy()
+
+
+def lin_comb_Q_T(coeff, rows):
+    """Restates ``lin_comb_Q_T`` (src/tools.jl:2909-2945) for rows held as a
+    matrix (Lanczos vectors in rows)."""
+    coeff = np.asarray(coeff)
+    if coeff.size != rows.shape[0]:
+        raise OracleError("one coefficient is required per Lanczos vector")
+    return rows.T @ coeff
+
+
+def expm_lanczos(E, V, rows, a=1.0):
+    """Restates ``expm_lanczos`` (src/tools.jl:2947-2952)."""
+    return lin_comb_Q_T(V @ (np.exp(a * np.asarray(E)) * V[0, :]), rows)
+
+
+def ftlm_static_iteration(observables, E, V, rows, beta=0.0):
+    """Restates ``ftlm_static_iteration`` (src/tools.jl:2966-3013):
+    results[key][b] = sum_i <q_i, O q_0> c_i(b) with
+    c = V (V[0, :] exp(-E beta)); identity = c[0, :]."""
+    scalar = np.isscalar(beta)
+    betas = np.atleast_1d(np.asarray(beta, dtype=float))
+    E = np.asarray(E)
+    c = V @ (V[0, :][:, None] * np.exp(-E[:, None] * betas[None, :]))
+    out = {}
+    for key, O in observables.items():
+        w = O(rows[0])
+        ov = np.array([np.vdot(q, w) for q in rows])
+        res = ov @ c
+        out[key] = res[0] if scalar else res
+    ident = c[0, :]
+    return out, (ident[0] if scalar else ident)
+
+
+def ltlm_static_iteration(observables, E, V, rows, beta=0.0):
+    """Restates ``ltlm_static_iteration`` (src/tools.jl:3015-3068): Ritz
+    vectors up to the Boltzmann cutoff at the smallest beta, weights
+    V[0, :nv] exp(-E beta / 2), values w^T (R^* O R) w."""
+    scalar = np.isscalar(beta)
+    betas = np.atleast_1d(np.asarray(beta, dtype=float))
+    E = np.asarray(E)
+    m = E.size
+    nv = m
+    bmin = betas.min()
+    if bmin > 0:
+        half = np.exp(-(E - E.min()) * bmin / 2)
+        idx = np.nonzero(half > np.finfo(float).eps)[0]
+        nv = int(idx[-1]) + 1 if idx.size else 1
+    En = E[:nv]
+    W = V[0, :nv][:, None] * np.exp(-En[:, None] * betas[None, :] / 2)
+    R = rows.T @ V[:, :nv]
+    out = {}
+    for key, O in observables.items():
+        OR = np.column_stack([O(R[:, c]) for c in range(nv)])
+        P = R.conj().T @ OR
+        vals = np.array([np.vdot(W[:, b], P @ W[:, b]) for b in range(betas.size)])
+        out[key] = vals[0] if scalar else vals
+    ident = np.array([np.sum(np.abs(V[0, :nv]) ** 2 * np.exp(-b * En)) for b in betas])
+    return out, (ident[0] if scalar else ident)

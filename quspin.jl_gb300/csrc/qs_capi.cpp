@@ -9,6 +9,7 @@
 #include "qs_internal.h"
 #include "qs_krylov.h"
 #include "qs_server.h"
+#include "qs_tools.h"
 
 struct qs_basis {
     qs::Basis b;
@@ -18,6 +19,9 @@ struct qs_op {
 };
 struct qs_server {
     qs::Server* s;
+};
+struct qs_lanczos {
+    std::unique_ptr<qs::LanczosSet> l;
 };
 
 namespace {
@@ -285,6 +289,61 @@ int qs_evolve(qs_op* op, const double* v0, double t0, const double* times, int32
               int32_t krylov_dim, int32_t precision, double* out) {
     return guard(
         [&] { qs::evolve(*op->op, v0, t0, times, nt, imag_time, tol, krylov_dim, precision, out); });
+}
+
+// ------------------------------------------------------------------ Krylov tools
+int qs_lanczos_run(qs_op* op, const qs_lanczos_opts* opts, int32_t nstart, const double* v0, qs_lanczos** out) {
+    return guard([&] {
+        if (!op || !opts || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        *out = nullptr;
+        auto l = qs::lanczos_run(*op->op, *opts, nstart, v0);
+        *out = new qs_lanczos{std::move(l)};
+    });
+}
+
+void qs_lanczos_destroy(qs_lanczos* lanczos) { delete lanczos; }
+
+int qs_lanczos_coefficients(const qs_lanczos* lanczos, int32_t s, double* alphas, double* betas, int32_t* used) {
+    return guard([&] {
+        if (!lanczos) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        const qs::LanczosSet& L = *lanczos->l;
+        if (s < 0 || s >= (int)L.ids.size()) throw qs::Error(QS_ERR_ARGUMENT, "start index outside the Lanczos set");
+        if (alphas) std::memcpy(alphas, L.alphas[s].data(), L.alphas[s].size() * sizeof(double));
+        if (betas) std::memcpy(betas, L.betas[s].data(), L.betas[s].size() * sizeof(double));
+        if (used) *used = L.used[s];
+    });
+}
+
+int qs_lanczos_complex(const qs_lanczos* lanczos) { return lanczos && lanczos->l->cv ? 1 : 0; }
+
+int qs_lanczos_rows(qs_lanczos* lanczos, int32_t s, double* out, int32_t mem) {
+    return guard([&] {
+        if (!lanczos || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::lanczos_rows(*lanczos->l, s, out, mem == QS_MEM_DEVICE);
+    });
+}
+
+int qs_lanczos_combine(qs_lanczos* lanczos, int32_t s, const double* coeff, int32_t ncoef, double* out,
+                       int32_t mem) {
+    return guard([&] {
+        if (!lanczos) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::lanczos_combine(*lanczos->l, s, coeff, ncoef, out, mem == QS_MEM_DEVICE);
+    });
+}
+
+int qs_lanczos_overlaps(qs_lanczos* lanczos, qs_op* observable, double* out) {
+    return guard([&] {
+        if (!lanczos || !observable || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::lanczos_overlaps(*lanczos->l, *observable->op, out);
+    });
+}
+
+int qs_lanczos_ritz_matrix(qs_lanczos* lanczos, int32_t s, qs_op* observable, const double* Y, int32_t nv,
+                           double* out) {
+    return guard([&] {
+        if (!lanczos || !observable) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::lanczos_ritz_matrix(*lanczos->l, s, *observable->op, Y, nv, out);
+    });
 }
 
 }  // extern "C"

@@ -27,7 +27,7 @@ namespace {
 
 constexpr int kT = 256;       // threads per block
 constexpr int kJT = 4;        // vectors per dots block
-constexpr int kMaxM = 64;     // largest Krylov basis of a slot
+constexpr int kMaxM = 256;    // largest Krylov basis of a slot
 
 // ------------------------------------------------------------ arithmetic
 // The same kernel source runs on FP64 values (A = double) and on
@@ -735,7 +735,7 @@ size_t Engine::slot_bytes(int64_t n, int m, bool cv, int tmp_cols, Store st) {
 int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols, int orth) {
     if (orth < 0 || orth > 2 || (orth == 2 && !op.hermitian))
         throw Error(QS_ERR_ARGUMENT, "the three-term recurrence needs a Hermitian operator");
-    if (m < 2 || m > kMaxM) throw Error(QS_ERR_ARGUMENT, "Krylov basis size must lie in 2:64");
+    if (m < 2 || m > kMaxM) throw Error(QS_ERR_ARGUMENT, "Krylov basis size must lie in 2:256");
     if (op.complex_mat && !cv) throw Error(QS_ERR_ARGUMENT, "complex operators need complex vectors");
     if (!op.assembled) op_assemble(op);
     const Assembled& M = op.asm_;

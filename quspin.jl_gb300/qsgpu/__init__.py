@@ -11,10 +11,14 @@ from .errors import ArgumentError, DimensionMismatch, ErrorException, Unsupporte
 from .operators import (ExpmMultiplyParallel, Hamiltonian, OperatorTerm, QuantumLinearOperator, apply, eigsh,
                         eigsh_batch, evolve, expm_multiply_parallel, isquantum_LinearOperator, set_a)
 from .server import Server
+from .tools import (LanczosRows, expm_lanczos, ftlm_static_iteration, lanczos_batch, lanczos_full, lanczos_iter,
+                    lin_comb_Q_T, ltlm_static_iteration)
 
 __all__ = [
     "SpinBasis1D", "states", "state_index", "state_at", "representative", "normalization", "get_amp",
     "int_to_state", "state_to_int", "OperatorTerm", "QuantumLinearOperator", "Hamiltonian", "eigsh", "eigsh_batch", "evolve",
     "ExpmMultiplyParallel", "expm_multiply_parallel", "apply", "set_a", "isquantum_LinearOperator",
     "ArgumentError", "DimensionMismatch", "ErrorException", "UnsupportedError", "Server",
+    "lanczos_full", "lanczos_iter", "lanczos_batch", "lin_comb_Q_T", "expm_lanczos", "ftlm_static_iteration",
+    "ltlm_static_iteration", "LanczosRows",
 ]

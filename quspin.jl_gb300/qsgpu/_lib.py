@@ -38,6 +38,10 @@ class EigshInfo(ctypes.Structure):
     _fields_ = [("nconv", i32), ("restarts", i32), ("matvecs", i64), ("max_rel_residual", f64), ("seconds", f64)]
 
 
+class LanczosOpts(ctypes.Structure):
+    _fields_ = [("m", i32), ("full_ortho", i32), ("eps", f64), ("complex_vectors", i32), ("mem", i32)]
+
+
 class ServerOpts(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", f64), ("max_slots", i32), ("precision", i32), ("disable_op_cache", i32),
                 ("chunk_steps", i32), ("builders", i32), ("policy", i32), ("max_wait_s", f64), ("device", i32)]
@@ -79,6 +83,8 @@ EXPORTS = (
     "qs_eigsh_batch", "qs_basis_stabilizers",
     "qs_server_create", "qs_server_destroy", "qs_server_submit", "qs_server_poll", "qs_server_wait",
     "qs_server_vector", "qs_server_release", "qs_server_stats",
+    "qs_lanczos_run", "qs_lanczos_destroy", "qs_lanczos_coefficients", "qs_lanczos_complex", "qs_lanczos_rows",
+    "qs_lanczos_combine", "qs_lanczos_overlaps", "qs_lanczos_ritz_matrix",
 )
 
 _lib = None
@@ -127,6 +133,15 @@ def load():
     L.qs_server_vector.argtypes = [P, i64, P, i64]
     L.qs_server_release.argtypes = [P, i64]
     L.qs_server_stats.argtypes = [P, ctypes.POINTER(ServerCounters)]
+    L.qs_lanczos_run.argtypes = [P, ctypes.POINTER(LanczosOpts), i32, P, ctypes.POINTER(P)]
+    L.qs_lanczos_destroy.argtypes = [P]
+    L.qs_lanczos_destroy.restype = None
+    L.qs_lanczos_coefficients.argtypes = [P, i32, P, P, ctypes.POINTER(i32)]
+    L.qs_lanczos_complex.argtypes = [P]
+    L.qs_lanczos_rows.argtypes = [P, i32, P, i32]
+    L.qs_lanczos_combine.argtypes = [P, i32, P, i32, P, i32]
+    L.qs_lanczos_overlaps.argtypes = [P, P, P]
+    L.qs_lanczos_ritz_matrix.argtypes = [P, i32, P, P, i32, P]
     L.qs_op_assemble.argtypes = [P]
     L.qs_op_nnz.argtypes = [P]
     L.qs_op_nnz.restype = i64

@@ -24,6 +24,7 @@ SOURCES = [
     "qs_assembled.cu",
     "qs_noalloc.cu",
     "qs_engine.cu",
+    "qs_tools.cu",
     "qs_dense.cpp",
     "qs_op.cpp",
     "qs_capi.cpp",

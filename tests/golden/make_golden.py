@@ -104,6 +104,36 @@ def main(root):
         "L": 4, "nup": 2, "pauli": False,
         "terms": [["zz", 1.0], ["+-", 0.5], ["-+", 0.5]], "atol": 2e-12,
     }
+    m = re.search(r'@testset "Operator algebra and Krylov tools" begin(.*?)\nend', rt, re.S)
+    block = m.group(1)
+    rows = re.search(r"A = \[\n(.*?)\n    \]", block, re.S).group(1)
+    A = [[float(x) for x in row.split()] for row in rows.strip().split("\n")]
+    B = floats(re.search(r"B = Diagonal\(\[(.*?)\]\)", block).group(1))
+    v0 = [float(x) for x in re.search(r"v0 = \[(.*?)\]", block).group(1).split(",")]
+    assert "lanczos_full(A, v0, 3)" in block and "lanczos_iter(A, v0, 3)" in block
+
+    def after(pattern):
+        t = re.search(pattern, block, re.S)
+        return floats(t.group(1)), float(t.group(2))
+    E, E_atol = after(r"@test E ≈ \[(.*?)\] atol=([0-9.e-]+)")
+    coeff = [float(x) for x in re.search(r"lin_comb_Q_T\(\[(.*?)\], Q_T\)", block).group(1).split(",")]
+    lc, lc_atol = after(r"lin_comb_Q_T\(\[.*?\], Q_T\) ≈\s*\[(.*?)\] atol=([0-9.e-]+)")
+    ea = float(re.search(r"expm_lanczos\(E, V, Q_T; a=(-?[0-9.]+)\)", block).group(1))
+    ex, ex_atol = after(r"expm_lanczos\(E, V, Q_T; a=-?[0-9.]+\) ≈\s*\[(.*?)\] atol=([0-9.e-]+)")
+    betas = floats(re.search(r"beta = \[(.*?)\]", block).group(1))
+    fi, fi_atol = after(r"@test ftlm_identity ≈ \[(.*?)\] atol=([0-9.e-]+)")
+    fb, fb_atol = after(r'@test ftlm\["B"\] ≈ \[(.*?)\] atol=([0-9.e-]+)')
+    lb, lb_atol = after(r'@test ltlm\["B"\] ≈ \[(.*?)\] atol=([0-9.e-]+)')
+    kats["krylov_tools_4x4"] = {
+        "source": "test/runtests.jl:130-172",
+        "A": A, "B_diagonal": B, "v0": v0, "m": 3,
+        "E": E, "E_atol": E_atol, "orthonormal_atol": 2e-15,
+        "lin_comb_coeff": coeff, "lin_comb": lc, "lin_comb_atol": lc_atol,
+        "expm_a": ea, "expm_lanczos": ex, "expm_atol": ex_atol,
+        "iter_atol": 1e-14,
+        "beta": betas, "ftlm_identity": fi, "ftlm_identity_atol": fi_atol,
+        "ftlm_B": fb, "ftlm_B_atol": fb_atol, "ltlm_B": lb, "ltlm_B_atol": lb_atol,
+    }
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
     with open(out, "w") as f:
         json.dump(kats, f, indent=1, sort_keys=True)

@@ -128,3 +128,31 @@ def test_two_restatements_agree(ora, L):
         terms = models.j1j2(L, 1.0, 0.5)
         x = models.seeded(ref.Ns, complex_=True)
         assert np.allclose(ref.qlo_matvec(terms, x), rep.matvec(terms, x), atol=1e-12)
+
+
+def test_krylov_tools(ora, kats):
+    """lanczos_full / lanczos_iter / lin_comb_Q_T / expm_lanczos / FTLM / LTLM
+    restatements against test/runtests.jl:130-172."""
+    k = kats["krylov_tools_4x4"]
+    A = np.array(k["A"])
+    B = np.diag(k["B_diagonal"])
+    v0 = np.array(k["v0"])
+    E, V, Q = ora.lanczos_full(lambda x: A @ x, v0, k["m"])
+    assert np.allclose(E, k["E"], atol=k["E_atol"], rtol=0)
+    assert np.allclose(Q @ Q.T, np.eye(k["m"]), atol=k["orthonormal_atol"], rtol=0)
+    assert np.allclose(ora.lin_comb_Q_T(k["lin_comb_coeff"], Q), k["lin_comb"], atol=k["lin_comb_atol"], rtol=0)
+    assert np.allclose(ora.expm_lanczos(E, V, Q, a=k["expm_a"]), k["expm_lanczos"], atol=k["expm_atol"], rtol=0)
+    a, b, _ = ora.lanczos_coefficients(lambda x: A @ x, v0, k["m"])
+    rows = np.array(list(ora.lanczos_vectors(lambda x: A @ x, v0, a, b)))
+    assert np.allclose(rows, Q, atol=k["iter_atol"], rtol=0)
+    obs = {"A": lambda x: A @ x, "B": lambda x: B @ x}
+    f, fi = ora.ftlm_static_iteration(obs, E, V, Q, beta=k["beta"])
+    lt, li = ora.ltlm_static_iteration(obs, E, V, Q, beta=k["beta"])
+    assert np.allclose(fi, k["ftlm_identity"], atol=k["ftlm_identity_atol"], rtol=0)
+    assert np.allclose(f["B"], k["ftlm_B"], atol=k["ftlm_B_atol"], rtol=0)
+    assert np.allclose(li, fi, atol=k["ftlm_identity_atol"], rtol=0)
+    assert np.allclose(lt["B"], k["ltlm_B"], atol=k["ltlm_B_atol"], rtol=0)
+    with pytest.raises(ora.OracleError):
+        ora.lanczos_full(lambda x: A @ x, v0, 4)
+    with pytest.raises(ora.OracleError):
+        ora.lanczos_full(lambda x: A @ x, np.zeros(4), 2)
