@@ -386,6 +386,73 @@ def section_c4(qs, torch):
             "ground_energy": float(np.min(vs)), "cpu_port_estimate": cpu}
 
 
+def section_ftlm(qs, torch, R=32, m=100, seq_sample=8):
+    """Finite-temperature Lanczos on the J1-J2 chain L=26, nup=13, J2=0.3,
+    k=0, p=+1: R seeded random start vectors, m Lanczos steps each, the
+    energy and nearest-neighbour zz estimates at three temperatures.  The R
+    recurrences run in one engine (lanczos_batch) against one lanczos_full
+    per vector."""
+    L = 26
+    spec = j1j2_spec(L, 1.0, 0.3)
+    zz = [("zz", [(1.0, i, i % L + 1) for i in range(1, L + 1)])]
+    basis = qs.SpinBasis1D(L, nup=13, pauli=False, kblock=0, pblock=1)
+    H = qs.Hamiltonian(basis, [qs.OperatorTerm(o, c) for o, c in spec])
+    ZZ = qs.Hamiltonian(basis, [qs.OperatorTerm(o, c) for o, c in zz])
+    n = H.Ns
+    V0 = np.random.default_rng(20261203).standard_normal((R, n)).T   # Ns x R, each start contiguous
+    beta = [0.5, 1.0, 2.0]
+    obs = {"H": H, "ZZ": ZZ}
+
+    def estimate(samples):
+        acc = {"H": 0.0, "ZZ": 0.0, "Z": 0.0}
+        for E, V, Q in samples:
+            res, ident = qs.ftlm_static_iteration(obs, E, V, Q, beta=beta)
+            acc["H"] = acc["H"] + res["H"]
+            acc["ZZ"] = acc["ZZ"] + res["ZZ"]
+            acc["Z"] = acc["Z"] + ident
+        return acc
+
+    estimate(qs.lanczos_batch(H, V0[:, :2], m))   # warm-up: tiles, graph capture
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    acc = estimate(qs.lanczos_batch(H, V0, m))
+    t_batch = time.perf_counter() - t
+    t = time.perf_counter()
+    acc_seq = estimate([qs.lanczos_full(H, V0[:, r], m) for r in range(seq_sample)])
+    t_seq = time.perf_counter() - t
+    acc_b8 = estimate(qs.lanczos_batch(H, V0[:, :seq_sample], m))
+    energy = (acc["H"] / acc["Z"]).tolist()
+    cpu = None
+    try:
+        import oracle
+        oracle.lib()
+        nthreads = os.cpu_count() or 1
+        rb = oracle.RepBasis(L, nup=13, pauli=False, nthreads=nthreads, kblock=0, pblock=1)
+        x = V0[:, 0].astype(np.complex128)
+        d = rb.diagonal(spec)
+        pk = oracle.pack_terms(spec)
+        rows, tt, blk = 0, 0.0, 4096
+        while tt < 3.0 and rows < rb.Ns:
+            r1 = min(rb.Ns, rows + blk)
+            t = time.perf_counter()
+            rb.matvec(spec, x, diag=d, rows=(rows, r1), packed=pk)
+            tt += time.perf_counter() - t
+            rows, blk = r1, blk * 2
+        per_sample = (m + 2) * n * tt / rows
+        cpu = {"cores": nthreads, "kind": "port", "estimated_samples_per_s": 1.0 / per_sample,
+               "sample": f"{rows} rows of the sector; products only (m + 2 per sample)"}
+    except Exception as exc:  # the estimate is reported, never required
+        cpu = {"error": f"{type(exc).__name__}: {exc}"}
+    return {"workload": "FTLM, J1-J2 L=26 nup=13 J2=0.3 k=0 p=+1 (%d states), %d random vectors, m=%d, "
+                        "observables H and sum zz, beta 0.5/1/2" % (n, R, m),
+            "batched_samples_per_s": R / t_batch, "sequential_samples_per_s": seq_sample / t_seq,
+            "batched_speedup": (R / t_batch) / (seq_sample / t_seq),
+            "energy_per_site": [e / L for e in energy],
+            "max_rel_diff_batched_vs_sequential": float(np.max(np.abs(
+                (acc_b8["H"] - acc_seq["H"]) / acc_seq["H"]))),
+            "cpu_port_estimate": cpu}
+
+
 def serving_requests(n_req, rate, seed=20261203):
     """The served mix: Poisson arrivals, L uniform in {18, 20, ..., 30}, nup
     uniform in [L/2-2, L/2], kblock uniform in [0, L), 70 % eigsh k=1 (tol
@@ -479,11 +546,27 @@ def profile_range(kind):
     `ncu --profile-from-start off`: a product of the default sector in FP64,
     FP32 or double-float ("product64", "product32", "productdf"), its
     matrix-free product ("matrixfree"), one Lanczos ground state of it
-    ("lanczos64", "lanczosdf"), or one batched
+    ("lanczos64", "lanczosdf"), one batched
     double-float ground-state solve of all J1-J2 sectors at L = 24 or 26
-    ("batch24", "batch26")."""
+    ("batch24", "batch26"), or the 32 batched m = 100 Lanczos recurrences of
+    the FTLM workload ("ftlm")."""
     import torch
     import qsgpu as qs
+    if kind == "ftlm":
+        L = 26
+        b = qs.SpinBasis1D(L, nup=13, pauli=False, kblock=0, pblock=1)
+        H = qs.Hamiltonian(b, [qs.OperatorTerm(o, c) for o, c in j1j2_spec(L, 1.0, 0.3)])
+        V0 = np.random.default_rng(20261203).standard_normal((32, b.Ns)).T
+        qs.lanczos_batch(H, V0[:, :2], 100)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        t = time.perf_counter()
+        out = qs.lanczos_batch(H, V0, 100)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_range": kind, "N": b.Ns, "E0": float(out[0][0][0]), "seconds": dt}))
+        return
     if kind in ("lanczos64", "lanczosdf"):
         L = 32
         b = qs.SpinBasis1D(L, nup=16, pauli=False, kblock=0, pblock=1, zblock=1)
@@ -679,6 +762,7 @@ def run_ours(args, wl, world, rank, local):
         for name, fn in (("c1_xxz_L16", lambda: section_c1(qs, torch, timed_events)),
                          ("c4_batched_sectors_L26", lambda: section_c4(qs, torch)),
                          ("c3_tfim_L30_evolve", lambda: section_c3(qs, torch)),
+                         ("ftlm_L26", lambda: section_ftlm(qs, torch)),
                          ("c5_serving", lambda: section_c5(qs, torch, n_req=args.serve_requests))):
             try:
                 sections[name] = fn()
@@ -739,7 +823,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving workload")
     ap.add_argument("--profile-range", default=None,
                     choices=["product64", "product32", "productdf", "matrixfree", "lanczos64", "lanczosdf",
-                             "batch24", "batch26"],
+                             "batch24", "batch26", "ftlm"],
                     help="run one unit inside cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     args = ap.parse_args()
     if args.profile_range:

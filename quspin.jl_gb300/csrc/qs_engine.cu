@@ -248,6 +248,37 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
     const int64_t n = S.n;
     const char* V = (const char*)S.V;
     const size_t cs = (size_t)n * vbytes<A, CV>();
+    const int64_t step = blockDim.x;
+    if (nv - i0 == 1) {
+        // one vector (a three-term step, a normalisation, the first CGS step):
+        // four rows' loads of w and the column in flight, nothing else read
+        const void* c0 = V + (size_t)i0 * cs;
+        auto acc = [&](const CA<A>& wv, const CA<A>& v) {
+            mac(re[0], v.re, wv.re);
+            if (CV) {
+                mac(re[0], v.im, wv.im);
+                mac(im[0], v.re, wv.im);
+                msub(im[0], v.im, wv.re);
+            }
+            if (want_wn) {
+                mac(wn, wv.re, wv.re);
+                if (CV) mac(wn, wv.im, wv.im);
+            }
+        };
+        int64_t r = r0 + threadIdx.x;
+        for (; r + 3 * step < r1; r += 4 * step) {
+            CA<A> wv[4], v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                wv[u] = ldv<A, CV>(w, r + u * step);
+                v[u] = ldv<A, CV>(c0, r + u * step);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc(wv[u], v[u]);
+        }
+        for (; r < r1; r += step) acc(ldv<A, CV>(w, r), ldv<A, CV>(c0, r));
+        return;
+    }
     // columns past nv repeat the last one (cached) so that every load of a row
     // is issued before the arithmetic
     const char* col[kJT];
@@ -272,7 +303,6 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
     };
     // real vectors: two rows per iteration, 2 (kJT + 1) loads issued before the
     // arithmetic; complex vectors hold twice the data per row, one row at a time
-    const int64_t step = blockDim.x;
     int64_t r = r0 + threadIdx.x;
     for (; !CV && r + step < r1; r += 2 * step) {
         const CA<A> w0 = ldv<A, CV>(w, r), w1 = ldv<A, CV>(w, r + step);
@@ -381,7 +411,7 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_do
 // mode 3: ||w''||^2 (second pass only)
 // mode 4: norm of the normalised column
 __global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl, int mmax, int mode,
-                                                 const double* __restrict__ partial) {
+                                                 const double* __restrict__ partial, int dy = 0) {
     const SlotDev& S = sl[blockIdx.x];
     int i = blockIdx.y;
     if (mode == 4) {
@@ -390,12 +420,15 @@ __global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl,
         if (S.state != kSlotStep) return;
         if ((mode == 2 || mode == 3) && S.nrm[4] == 0.0) return;
         if (mode == 0) {
+            // blocks y < dy cover the step's vectors from `first`; y = dy the
+            // DGKS norm (kept at partial index mmax)
             const int first = S.orth == 2 ? S.j : 0;
-            // blocks y = 0..j cover the vectors; y = mmax the DGKS norm
-            if (i == mmax) {
+            if (i == dy) {
                 if (S.orth != 1) return;
-            } else if (i < first || i > S.j) {
-                return;
+                i = mmax;
+            } else {
+                i += first;
+                if (i > S.j) return;
             }
         } else if (mode == 1 || mode == 3) {
             if (i) return;
@@ -481,6 +514,36 @@ __device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r
             mac(ai, v.im, h.re);
         }
     };
+    if (nv - first <= 2) {
+        // the three-term update (or a first step): two rows per iteration, all
+        // their loads issued before either row's store
+        const int two = nv - first == 2;
+        const char* va = V + (size_t)first * cs;
+        const char* vb = V + (size_t)(first + two) * cs;
+        const CA<A> ha = hs[first], hb = two ? hs[first + 1] : CA<A>{zero<A>(), zero<A>()};
+        auto one = [&](CA<A> o, const CA<A>& a, const CA<A>& b) {
+            A ar = zero<A>(), ai = zero<A>();
+            term(ar, ai, a, ha);
+            if (two) term(ar, ai, b, hb);
+            o.re = sub(o.re, ar);
+            if (CV) o.im = sub(o.im, ai);
+            mac(nacc, o.re, o.re);
+            if (CV) mac(nacc, o.im, o.im);
+            return o;
+        };
+        const int64_t step = blockDim.x;
+        int64_t r = r0 + threadIdx.x;
+        for (; r + step < r1; r += 2 * step) {
+            const CA<A> o0 = ldv<A, CV>(w, r), o1 = ldv<A, CV>(w, r + step);
+            const CA<A> a0 = ldv<A, CV>(va, r), a1 = ldv<A, CV>(va, r + step);
+            const CA<A> b0 = ldv<A, CV>(vb, r), b1 = ldv<A, CV>(vb, r + step);
+            const CA<A> n0 = one(o0, a0, b0), n1 = one(o1, a1, b1);
+            stv<A, CV>(w, r, n0);
+            stv<A, CV>(w, r + step, n1);
+        }
+        for (; r < r1; r += step) stv<A, CV>(w, r, one(ldv<A, CV>(w, r), ldv<A, CV>(va, r), ldv<A, CV>(vb, r)));
+        return nacc;
+    }
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         A ar = zero<A>(), ai = zero<A>();
         int t = first;
@@ -546,6 +609,25 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_up
 }
 
 // ------------------------------------------------------------ scale / advance
+// w[r] *= f over rows r0..r1, four rows' loads in flight before their stores
+template <class A, bool CV>
+__device__ __forceinline__ void scale_rows(void* w, int64_t r0, int64_t r1, A f) {
+    const int64_t step = blockDim.x;
+    auto sc = [&](CA<A> v) {
+        v.re = mul(v.re, f);
+        if (CV) v.im = mul(v.im, f);
+        return v;
+    };
+    int64_t r = r0 + threadIdx.x;
+    for (; r + 3 * step < r1; r += 4 * step) {
+        CA<A> v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = ldv<A, CV>(w, r + u * step);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) stv<A, CV>(w, r + u * step, sc(v[u]));
+    }
+    for (; r < r1; r += step) stv<A, CV>(w, r, sc(ldv<A, CV>(w, r)));
+}
 // mode 0: col(j+1) *= 1/beta on stepping slots; mode 1: col ncol on normalising slots
 template <class A>
 __global__ void __launch_bounds__(kT) eng_scale(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mode) {
@@ -555,18 +637,8 @@ __global__ void __launch_bounds__(kT) eng_scale(const SlotDev* __restrict__ sl, 
     void* w = colp<A>(S, mode == 0 ? S.j + 1 : S.ncol);
     const int64_t lb = blockIdx.x - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        if (S.cv) {
-            CA<A> v = ldv<A, true>(w, r);
-            v.re = mul(v.re, f);
-            v.im = mul(v.im, f);
-            stv<A, true>(w, r, v);
-        } else {
-            CA<A> v = ldv<A, false>(w, r);
-            v.re = mul(v.re, f);
-            stv<A, false>(w, r, v);
-        }
-    }
+    if (S.cv) scale_rows<A, true>(w, r0, r1, f);
+    else scale_rows<A, false>(w, r0, r1, f);
 }
 
 __global__ void eng_advance(SlotDev* sl, int nslots) {
@@ -698,26 +770,29 @@ Tiles Engine::tune(Op& op, int m, bool cv) {
     QS_CUDA(cudaEventCreate(&e1));
     Tiles best;
     float best_ms = 1e30f;
-    for (int rpb : {512, 1024, 2048})
-        for (int spb : {16, 64, 256}) {
-            E.slots_[id].d.rpb = rpb;
-            E.slots_[id].d.spb = spb;
-            E.maps_dirty_ = true;
-            E.start(id, 0);
-            E.run(2);  // captures the graph, warms up
-            E.start(id, 2);
-            QS_CUDA(cudaEventRecord(e0, s_));
-            E.run(std::min(6, mt - 2));
-            QS_CUDA(cudaEventRecord(e1, s_));
-            QS_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            QS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best_ms) {
-                best_ms = ms;
-                best.rpb = rpb;
-                best.spb = spb;
-            }
+    // only the SpMV's slices per block are timed: a row's product does not
+    // depend on them, while the BLAS row block fixes the order of every
+    // reduction and stays at its default (results repeat from run to run)
+    const int rpb = best.rpb;
+    for (int spb : {16, 64, 256}) {
+        E.slots_[id].d.rpb = rpb;
+        E.slots_[id].d.spb = spb;
+        E.maps_dirty_ = true;
+        E.start(id, 0);
+        E.run(2);  // captures the graph, warms up
+        E.start(id, 2);
+        QS_CUDA(cudaEventRecord(e0, s_));
+        E.run(std::min(6, mt - 2));
+        QS_CUDA(cudaEventRecord(e1, s_));
+        QS_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        QS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best.rpb = rpb;
+            best.spb = spb;
         }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     launches_ += E.launches();
@@ -814,7 +889,8 @@ void Engine::remove(int id) {
 
 void Engine::build_maps() {
     nrb_ = nsb_ = 0;
-    mmax_ = 1;
+    mmax_ = dmax_ = 1;
+    cgs_ = false;
     for (auto& sl : slots_) {
         SlotDev& d = sl.d;
         if (!sl.live) {
@@ -829,6 +905,8 @@ void Engine::build_maps() {
         nrb_ += d.rb_count;
         nsb_ += d.sb_count;
         mmax_ = std::max(mmax_, d.m);
+        dmax_ = std::max(dmax_, d.orth == 2 ? 1 : d.m);
+        cgs_ = cgs_ || d.orth != 2;
     }
     std::vector<int> rm(std::max(1, nrb_)), sm(std::max(1, nsb_));
     for (int i = 0; i < (int)slots_.size(); ++i) {
@@ -879,20 +957,29 @@ void Engine::sync_table() {
     dirty_ = false;
 }
 
+// One step of every stepping slot; returns the number of launches.  The dots
+// and reduce grids cover the most vectors a slot dots against (dmax), so
+// three-term slots cost one block row however large their basis; without
+// Gram-Schmidt slots the second-pass launches are left out.
 template <class A>
-static void launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const int* sm, double* pa, const void* rsq,
-                          int nrb, int nsb, int mmax, int ns, cudaStream_t s) {
-    const dim3 gd(nrb, (mmax + kJT - 1) / kJT);
+static int launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const int* sm, double* pa, const void* rsq,
+                         int nrb, int nsb, int mmax, int dmax, bool cgs, int ns, cudaStream_t s) {
+    const dim3 gd(nrb, (dmax + kJT - 1) / kJT);
     eng_spmv<A><<<nsb, kT, 0, s>>>(ds, sm, rsq);
     eng_dots<A><<<gd, kT, 0, s>>>(ds, rm, mmax, 0, pa);
-    eng_reduce<<<dim3(ns, mmax + 1), kT, 0, s>>>(ds, mmax, 0, pa);
+    eng_reduce<<<dim3(ns, dmax + 1), kT, 0, s>>>(ds, mmax, 0, pa, dmax);
     eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 0, pa);
     eng_reduce<<<dim3(ns, 1), kT, 0, s>>>(ds, mmax, 1, pa);
-    eng_reduce<<<dim3(ns, mmax), kT, 0, s>>>(ds, mmax, 2, pa);
-    eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 1, pa);
-    eng_reduce<<<dim3(ns, 1), kT, 0, s>>>(ds, mmax, 3, pa);
+    int n = 5;
+    if (cgs) {
+        eng_reduce<<<dim3(ns, mmax), kT, 0, s>>>(ds, mmax, 2, pa);
+        eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 1, pa);
+        eng_reduce<<<dim3(ns, 1), kT, 0, s>>>(ds, mmax, 3, pa);
+        n += 3;
+    }
     eng_scale<A><<<nrb, kT, 0, s>>>(ds, rm, 0);
     eng_advance<<<(ns + 127) / 128, 128, 0, s>>>(dsw, ns);
+    return n + 2;
 }
 
 void Engine::launch_step() {
@@ -900,8 +987,9 @@ void Engine::launch_step() {
     const void* rsq = st_ == Store::DF ? rsqdf_.p : (st_ == Store::F32 ? rsq32_.p : rsq64_.p);
     with_store(st_, [&](auto tag) {
         using A = decltype(tag);
-        launch_step_t<A>(dslots_.as<SlotDev>(), dslots_.as<SlotDev>(), rmap_.as<int>(), smap_.as<int>(),
-                         partial_.as<double>(), rsq, nrb_, nsb_, mmax_, ns, s_);
+        step_launches_ = launch_step_t<A>(dslots_.as<SlotDev>(), dslots_.as<SlotDev>(), rmap_.as<int>(),
+                                          smap_.as<int>(), partial_.as<double>(), rsq, nrb_, nsb_, mmax_, dmax_,
+                                          cgs_, ns, s_);
     });
 }
 
@@ -939,7 +1027,7 @@ void Engine::run(int nsteps) {
     if (nrb_ == 0) return;
     if (!exec_) capture();
     for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
-    launches_ += 10 * (int64_t)nsteps;
+    launches_ += step_launches_ * (int64_t)nsteps;
     // mirror the device step counters
     for (auto& sl : slots_) {
         if (!sl.live || sl.d.state != kSlotStep) continue;

@@ -4,7 +4,8 @@
 // One Lanczos/Arnoldi step of every stepping slot is a fixed sequence of ten
 // launches (SpMV; dots + reduce; the update with the norm and the second
 // pass's dots fused; the conditional second Gram-Schmidt update; scale;
-// advance), each covering all slots through a block -> slot map.  The step
+// advance; seven when every slot runs the three-term recurrence), each
+// covering all slots through a block -> slot map.  The step
 // counters live on the device, so the sequence is captured once in a CUDA
 // graph and replayed; the host only meets the device when a slot has filled
 // its basis (restart, convergence test, exponential).  The projected matrix of
@@ -14,9 +15,10 @@
 // Vectors are stored either in FP64 or as double-float pairs (hi + lo float,
 // arithmetic on the FP32 pipe); both take 8 bytes per real component.  Each
 // slot has its own real/complex vector flag, so a slot's arithmetic does not
-// depend on which other slots share the launches.  Tile shapes (rows per
-// BLAS block, slices per SpMV block) are per slot, chosen by a timing
-// autotuner and cached per (storage, flags, size class).
+// depend on which other slots share the launches.  The SpMV's slices per
+// block are per slot, chosen by a timing autotuner and cached per (storage,
+// flags, size class); the BLAS row block is fixed, so every reduction, and
+// with it every result, repeats from run to run.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -83,8 +85,11 @@ struct SlotDev {
 // Storage of a slot's Krylov vectors (and the arithmetic of the step kernels).
 enum class Store : int32_t { F64 = 0, DF = 1, F32 = 2 };
 
+// rpb: rows per BLAS block (4096 measured best or within 3 % on single and
+// batched solves; fixed so that reductions repeat); spb: SELL slices per SpMV
+// block (timed per operator size class)
 struct Tiles {
-    int rpb = 1024, spb = 64;
+    int rpb = 4096, spb = 64;
 };
 
 // One slot's part of a rotate() call.
@@ -160,6 +165,11 @@ class Engine {
     DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_, rsq32_, ybuf_;
     size_t cap_y_ = 0;
     int nrb_ = 0, nsb_ = 0, mmax_ = 1, cap_slots_ = 0;
+    // most vectors any slot dots against in a step (1 for three-term slots,
+    // m for Gram-Schmidt ones) and whether any slot takes a second pass
+    int dmax_ = 1;
+    bool cgs_ = false;
+    int step_launches_ = 10;
     size_t cap_partial_ = 0, cap_rmap_ = 0, cap_smap_ = 0;
     bool dirty_ = true, maps_dirty_ = true;
     cudaGraph_t graph_ = nullptr;

@@ -215,11 +215,18 @@ std::unique_ptr<LanczosSet> lanczos_run(Op& op, const qs_lanczos_opts& o, int ns
     L->E.reset(new Engine(Store::F64, op.stream));
     Engine& E = *L->E;
     const int comps = L->cv ? 2 : 1;
-    const bool dev = o.mem == QS_MEM_DEVICE;
+    // host start vectors travel in one copy, then load from device memory
+    PoolBuf staged;
+    const double* src = v0;
+    if (o.mem != QS_MEM_DEVICE) {
+        staged.alloc((size_t)nstart * n * comps * sizeof(double), op.stream);
+        QS_CUDA(cudaMemcpyAsync(staged.p, v0, staged.bytes, cudaMemcpyHostToDevice, op.stream));
+        src = staged.as<double>();
+    }
     for (int s = 0; s < nstart; ++s) {
         // three-term recurrence as the reference; full_ortho: CGS2 against every kept vector
         const int id = E.add(op, mm, L->cv, true, 1, o.full_ortho ? 0 : 2);
-        E.load(id, 0, v0 + (size_t)s * n * comps, dev);
+        E.load(id, 0, src + (size_t)s * n * comps, true);
         L->ids.push_back(id);
     }
     L->norms = E.normalize(L->ids);

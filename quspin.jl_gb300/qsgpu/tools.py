@@ -175,7 +175,9 @@ def lanczos_iter(A, v0, m, return_vec_iter=True, copy_v0=True, copy_A=False, eps
 
 def lanczos_batch(A, V0, m, full_ortho=False, eps=None):
     """lanczos_full for every column of V0 (Ns x R) at once, the R recurrences
-    stepping in the same launches: a list of (E, V, Q_T), one per column."""
+    stepping in the same launches: a list of (E, V, Q_T), one per column.  A
+    Fortran-ordered V0 (e.g. the transpose of an R x Ns array) is passed
+    without a host copy."""
     V0 = np.asarray(V0)
     if V0.ndim != 2:
         raise ArgumentError("V0 must be Ns x R")

@@ -99,3 +99,25 @@ def test_batched_mixed_real_and_complex_sizes(qs, ora):
             assert np.allclose(vals[i], dense[i], rtol=1e-10, atol=1e-10), (precision, i)
             res_tol = 1e-6 if precision == "fp32" else 1e-8
             assert np.abs(op.dot(vecs[i]) - vecs[i] * vals[i]).max() < res_tol
+
+
+def test_results_repeat_across_processes(qs):
+    """Two processes (each timing its own SpMV tiles) give the same bits: the
+    reductions' order is fixed by the BLAS row block, not by the tuner."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import json, sys; sys.path.insert(0, 'quspin.jl_gb300'); sys.path.insert(0, 'tests');"
+        "import qsgpu as qs, models;"
+        "L = 20; terms = models.to_terms(qs, models.j1j2(L, 1.0, 0.3));"
+        "ops = [qs.Hamiltonian(qs.SpinBasis1D(L, nup=10, pauli=False, kblock=k), terms) for k in (1, 2, 3)];"
+        "out = {p: qs.eigsh_batch(ops, k=1, tol=1e-10, precision=p)[:, 0].tolist() for p in ('fp64', 'fp64df')};"
+        "E, V, Q = qs.lanczos_full(ops[0], models.seeded(ops[0].Ns, complex_=True), 40);"
+        "out['lanczos'] = E.tolist(); print(json.dumps(out))")
+    runs = [subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, check=True)
+            for _ in range(2)]
+    a, b = (json.loads(r.stdout.strip().splitlines()[-1]) for r in runs)
+    assert a == b
