@@ -107,6 +107,22 @@ QS_API int qs_basis_state_index(const qs_basis *basis, const uint64_t *states, i
 QS_API int qs_basis_representative(const qs_basis *basis, const uint64_t *states, int64_t n,
                             uint64_t *reps, double *norms, double *amps, int32_t *status);
 
+/* Rows of the projection space: 2^L (pcon = 0) or the parent particle sector
+ * (pcon = 1, ascending fixed-weight states), as projection_matrix(basis;
+ * pcon) (src/basis.jl:862-880); -1 when 2^L does not fit. */
+QS_API int64_t qs_basis_projection_rows(const qs_basis *basis, int32_t pcon);
+
+/* project_from(basis, v; pcon) (src/basis.jl:889-908): out = P v with P the
+ * reference's projector (full space or parent sector), v Ns complex, out
+ * rows complex; accumulate = 1 adds P v to out.  mem: QS_MEM_HOST or
+ * QS_MEM_DEVICE for both vectors.  Bit-for-bit the reference's sparse product. */
+QS_API int qs_basis_project_from(qs_basis *basis, int32_t pcon, const double *v, double *out, int32_t accumulate,
+                                 int32_t mem);
+
+/* project_to(basis, v; pcon) (src/discrete_basis.jl:2455-2475): out = P^H v,
+ * v rows complex, out Ns complex. */
+QS_API int qs_basis_project_to(qs_basis *basis, int32_t pcon, const double *v, double *out, int32_t mem);
+
 /* --------------------------------------------------------------- operator */
 
 /* One OperatorTerm (src/operators.jl:42-63): op string over {I,z,+,-,x,y},
@@ -306,6 +322,21 @@ QS_API int qs_lanczos_overlaps(qs_lanczos *lanczos, qs_op *observable, double *o
  * out complex nv x nv column-major (host). */
 QS_API int qs_lanczos_ritz_matrix(qs_lanczos *lanczos, int32_t s, qs_op *observable, const double *Y, int32_t nv,
                                   double *out);
+
+/* ------------------------------------------------------------ block tools */
+
+/* evolve(BlockOps, psi, t0, times) and block_expm(BlockOps, psi; a, start,
+ * stop, num) (tools.jl:2445-2719) for static block Hamiltonians: ops[b] acts
+ * on block b's basis; c_b = P_b^H psi for every block (blocks whose
+ * projection has norm <= 1000 eps are left out, ArgumentError when none is
+ * left), exp(s_i H_b) c_b for the nscales complex scales s_i by the
+ * reference's _krylov_expmv_times with every block's Krylov recursions on one
+ * batched engine, out[:, i] = sum_b P_b state_b(i).  psi: rows complex (2^L,
+ * or the common parent sector with pcon); out: rows x nscales column-major
+ * complex; mem applies to both.  precision as for qs_evolve. */
+QS_API int qs_block_expm(qs_op *const *ops, int32_t nblocks, int32_t pcon, const double *psi, const double *scales,
+                         int32_t nscales, double tol, int32_t krylov_dim, int32_t precision, double *out,
+                         int32_t mem);
 
 /* ---------------------------------------------------------------- serving */
 

@@ -872,6 +872,105 @@ __global__ void query_kernel(QueryArgs a) {
     }
 }
 
+// project_from / project_to over the columns of a basis: one thread per
+// column replays the reference's projector column (states ascending) and
+// either scatters out[row(s)] += P[s, j] c_j (every parent state lies in one
+// column, so the scatter has no conflicts) or gathers c_j = sum_s
+// conj(P[s, j]) psi[row(s)] in ascending state order.  Products and sums are
+// rounded one by one (no contraction), as Julia's sparse products round them.
+struct ProjArgs {
+    ReplayCtx ctx;
+    const void* reps;      // column keys: orbit minima (or the states themselves)
+    int64_t n;
+    int symmetric;
+    int nup, pcon;
+    const uint64_t* binom;
+    int mode;              // 0: out += P in; 1: out = P^H in
+    const double2* in;
+    double2* out;
+    REnt* scratch;
+    int64_t cap, nthreads;
+};
+
+template <typename U>
+__device__ __forceinline__ int64_t proj_row(const ProjArgs& a, uint64_t s) {
+    if (a.pcon && a.nup >= 0) return combinadic_rank<U>((U)s, a.binom, 65);
+    return (int64_t)s;
+}
+
+template <typename U>
+__global__ void project_kernel(ProjArgs a) {
+    int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (tid >= a.nthreads) return;
+    REnt* buf = a.scratch + tid * 2 * a.cap;
+    REnt* tmp = buf + a.cap;
+    for (int64_t j = tid; j < a.n; j += a.nthreads) {
+        const uint64_t key = (uint64_t)((const U*)a.reps)[j];
+        int cnt = 1;
+        if (a.symmetric) {
+            cnt = replay_column(a.ctx, key, buf, tmp);
+        } else {
+            buf[0].s = key;
+            buf[0].re = 1.0;
+            buf[0].im = 0.0;
+        }
+        if (a.mode == 0) {
+            const double2 c = a.in[j];
+            for (int k = 0; k < cnt; ++k) {
+                const int64_t row = proj_row<U>(a, buf[k].s);
+                const double vr = buf[k].re, vi = buf[k].im;
+                double2 o = a.out[row];
+                o.x = __dadd_rn(o.x, __dsub_rn(__dmul_rn(vr, c.x), __dmul_rn(vi, c.y)));
+                o.y = __dadd_rn(o.y, __dadd_rn(__dmul_rn(vr, c.y), __dmul_rn(vi, c.x)));
+                a.out[row] = o;
+            }
+        } else {
+            double ar = 0.0, ai = 0.0;
+            for (int k = 0; k < cnt; ++k) {
+                const double2 x = a.in[proj_row<U>(a, buf[k].s)];
+                const double vr = buf[k].re, vi = -buf[k].im;   // conj(P[s, j])
+                ar = __dadd_rn(ar, __dsub_rn(__dmul_rn(vr, x.x), __dmul_rn(vi, x.y)));
+                ai = __dadd_rn(ai, __dadd_rn(__dmul_rn(vr, x.y), __dmul_rn(vi, x.x)));
+            }
+            a.out[j] = make_double2(ar, ai);
+        }
+    }
+}
+
+// The projector of a basis without symmetry is an embedding: row s of the
+// 2^L space holds column rank(s) when popcount(s) = nup (rank: the position
+// among the ascending fixed-weight states), column s of a full basis, and the
+// parent-sector projector (pcon) is the identity.  One thread per row.
+struct EmbedArgs {
+    int64_t rows;
+    int nup, pcon;
+    const uint64_t* binom;
+    int mode;              // 0: out += P in; 1: out = P^H in
+    const double2* in;
+    double2* out;
+};
+
+template <typename U>
+__global__ void embed_kernel(EmbedArgs a) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.rows;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        int64_t j = r;
+        if (!a.pcon && a.nup >= 0) {
+            if (__popcll((unsigned long long)r) != a.nup) continue;
+            j = combinadic_rank<U>((U)r, a.binom, 65);
+        }
+        if (a.mode == 0) {
+            double2 o = a.out[r];
+            const double2 c = a.in[j];
+            o.x = __dadd_rn(o.x, c.x);
+            o.y = __dadd_rn(o.y, c.y);
+            a.out[r] = o;
+        } else {
+            a.out[j] = a.in[r];
+        }
+    }
+}
+
 ReplayCtx make_ctx(const Basis& b, const DevBuf& lv, const DevBuf& t0) {
     ReplayCtx c{};
     c.levels = lv.as<GroupDesc>();
@@ -1024,6 +1123,73 @@ void basis_representative(Basis& b, const uint64_t* states, int64_t n, uint64_t*
     QS_CUDA(cudaMemcpyAsync(amps, damp.p, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, b.stream));
     QS_CUDA(cudaMemcpyAsync(status, dst.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, b.stream));
     QS_CUDA(cudaStreamSynchronize(b.stream));
+}
+
+int64_t basis_projection_rows(const Basis& b, bool pcon) {
+    if (pcon) return b.n_parent;
+    if (b.L > 40) throw Error(QS_ERR_UNSUPPORTED, "a full 2^L space above L=40 does not fit in device memory");
+    return (int64_t)1 << b.L;
+}
+
+void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out, bool accumulate, bool device) {
+    const int64_t rows = basis_projection_rows(b, pcon);
+    const int64_t nin = mode == 0 ? b.n : rows, nout = mode == 0 ? rows : b.n;
+    if (b.symmetric) upload_replay(b);
+    cudaStream_t s = b.stream;
+    DevBuf din, dout;
+    const double2* pin = reinterpret_cast<const double2*>(in);
+    double2* pout = reinterpret_cast<double2*>(out);
+    if (!device) {
+        din.alloc((size_t)nin * sizeof(double2));
+        dout.alloc((size_t)nout * sizeof(double2));
+        QS_CUDA(cudaMemcpyAsync(din.p, in, din.bytes, cudaMemcpyHostToDevice, s));
+        if (mode == 0 && accumulate) QS_CUDA(cudaMemcpyAsync(dout.p, out, dout.bytes, cudaMemcpyHostToDevice, s));
+        pin = din.as<double2>();
+        pout = dout.as<double2>();
+    }
+    if (mode == 0 && !accumulate) QS_CUDA(cudaMemsetAsync(pout, 0, (size_t)nout * sizeof(double2), s));
+    if (!b.symmetric) {
+        EmbedArgs e{};
+        e.rows = rows;
+        e.nup = b.nup;
+        e.pcon = pcon;
+        e.binom = b.d_binom.as<uint64_t>();
+        e.mode = mode;
+        e.in = pin;
+        e.out = pout;
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((rows + 255) / 256, 152 * 16));
+        if (b.wide) embed_kernel<uint64_t><<<grid, 256, 0, s>>>(e);
+        else embed_kernel<uint32_t><<<grid, 256, 0, s>>>(e);
+        QS_CUDA(cudaGetLastError());
+        note_launches(1);
+        if (!device) QS_CUDA(cudaMemcpyAsync(out, pout, (size_t)nout * sizeof(double2), cudaMemcpyDeviceToHost, s));
+        QS_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
+    const int64_t nt = replay_threads(b.n);
+    const int64_t cap = b.symmetric ? b.group.ng : 1;
+    DevBuf scratch((size_t)nt * 2 * cap * sizeof(REnt));
+    ProjArgs a{};
+    if (b.symmetric) a.ctx = make_ctx(b, b.d_level_groups, b.d_level0);
+    a.reps = b.d_reps.p;
+    a.n = b.n;
+    a.symmetric = b.symmetric;
+    a.nup = b.nup;
+    a.pcon = pcon;
+    a.binom = b.d_binom.as<uint64_t>();
+    a.mode = mode;
+    a.in = pin;
+    a.out = pout;
+    a.scratch = scratch.as<REnt>();
+    a.cap = cap;
+    a.nthreads = nt;
+    const unsigned grid = (unsigned)((nt + 127) / 128);
+    if (b.wide) project_kernel<uint64_t><<<grid, 128, 0, s>>>(a);
+    else project_kernel<uint32_t><<<grid, 128, 0, s>>>(a);
+    QS_CUDA(cudaGetLastError());
+    note_launches(1);
+    if (!device) QS_CUDA(cudaMemcpyAsync(out, pout, (size_t)nout * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    QS_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace qs

@@ -154,6 +154,30 @@ int qs_basis_representative(const qs_basis* basis, const uint64_t* states, int64
     });
 }
 
+int64_t qs_basis_projection_rows(const qs_basis* basis, int32_t pcon) {
+    if (!basis) return -1;
+    try {
+        return qs::basis_projection_rows(basis->b, pcon != 0);
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+int qs_basis_project_from(qs_basis* basis, int32_t pcon, const double* v, double* out, int32_t accumulate,
+                          int32_t mem) {
+    return guard([&] {
+        if (!basis || !v || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::basis_project(basis->b, pcon != 0, 0, v, out, accumulate != 0, mem == QS_MEM_DEVICE);
+    });
+}
+
+int qs_basis_project_to(qs_basis* basis, int32_t pcon, const double* v, double* out, int32_t mem) {
+    return guard([&] {
+        if (!basis || !v || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::basis_project(basis->b, pcon != 0, 1, v, out, false, mem == QS_MEM_DEVICE);
+    });
+}
+
 int qs_op_create(qs_basis* basis, const qs_term* terms, int32_t nterms, const double* diagonal, int32_t checks,
                  qs_op** out) {
     return guard([&] {
@@ -343,6 +367,20 @@ int qs_lanczos_ritz_matrix(qs_lanczos* lanczos, int32_t s, qs_op* observable, co
     return guard([&] {
         if (!lanczos || !observable) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
         qs::lanczos_ritz_matrix(*lanczos->l, s, *observable->op, Y, nv, out);
+    });
+}
+
+int qs_block_expm(qs_op* const* ops, int32_t nblocks, int32_t pcon, const double* psi, const double* scales,
+                  int32_t nscales, double tol, int32_t krylov_dim, int32_t precision, double* out, int32_t mem) {
+    return guard([&] {
+        if (!ops || nblocks < 1 || !psi || !scales || !out || nscales < 1)
+            throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        std::vector<qs::Op*> v(nblocks);
+        for (int b = 0; b < nblocks; ++b) v[b] = ops[b]->op;
+        std::vector<std::complex<double>> sc(nscales);
+        for (int i = 0; i < nscales; ++i) sc[i] = {scales[2 * i], scales[2 * i + 1]};
+        if (krylov_dim < 1) throw qs::Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
+        qs::block_expm(v, pcon != 0, psi, sc, tol > 0 ? tol : 1e-12, krylov_dim, precision, out, mem == QS_MEM_DEVICE);
     });
 }
 

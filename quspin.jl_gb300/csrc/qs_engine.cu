@@ -1534,8 +1534,11 @@ int EvoTask::after_norm(double nr, int id, RotReq& copy) {
 
 // Runs EvoTasks on their slots until all are done; out_cols[i] receives
 // beta * column 0 (host, Ns complex) of task i.
+// Runs the EvoTasks of the listed slots to completion and writes beta * the
+// accepted state of each to outs (host, or device with `device`).  Slots may
+// have different Krylov sizes (different operators).
 static void run_evo_slots(Engine& E, std::vector<int>& ids, std::vector<EvoTask>& tasks,
-                          const std::vector<double*>& outs) {
+                          const std::vector<double*>& outs, bool device = false) {
     const size_t nt = tasks.size();
     std::vector<char> fin(nt, 0);
     size_t left = 0;
@@ -1548,8 +1551,15 @@ static void run_evo_slots(Engine& E, std::vector<int>& ids, std::vector<EvoTask>
     }
     auto emit = [&](size_t i) {
         const int64_t n = tasks[i].n;
-        E.store(ids[i], 0, outs[i], false);
         const double b = tasks[i].beta;
+        if (device) {
+            E.store(ids[i], 0, outs[i], true);
+            Blas B(VKind::C128, n, E.stream());
+            B.scale(outs[i], outs[i], cd(b, 0));
+            QS_CUDA(cudaStreamSynchronize(E.stream()));
+            return;
+        }
+        E.store(ids[i], 0, outs[i], false);
         for (int64_t q = 0; q < 2 * n; ++q) outs[i][q] *= b;
     };
     for (size_t i = 0; i < nt; ++i)
@@ -1569,15 +1579,21 @@ static void run_evo_slots(Engine& E, std::vector<int>& ids, std::vector<EvoTask>
         E.records(hold_ids, H);
         std::vector<RotReq> rot(hold.size());
         for (size_t q = 0; q < hold.size(); ++q) tasks[hold[q]].on_hold(H[q], ids[hold[q]], rot[q]);
-        const int m = tasks[hold[0]].m;   // one krylov_dim per call
         std::vector<size_t> proj = hold, done_now, restart;
         // project, measure, decide; rejected slots project their half step from
         // the same basis until every slot is accepted
         while (!proj.empty()) {
             E.rotate(rot);
-            std::vector<int> pid;
-            for (size_t i : proj) pid.push_back(ids[i]);
-            std::vector<double> nr = E.normalize(pid, m);
+            // the candidates sit in column m of each slot: one normalisation per Krylov size
+            std::vector<double> nr(proj.size());
+            std::map<int, std::vector<size_t>> by_m;
+            for (size_t q = 0; q < proj.size(); ++q) by_m[tasks[proj[q]].m].push_back(q);
+            for (const auto& kv : by_m) {
+                std::vector<int> pid;
+                for (size_t q : kv.second) pid.push_back(ids[proj[q]]);
+                const std::vector<double> g = E.normalize(pid, kv.first);
+                for (size_t t = 0; t < kv.second.size(); ++t) nr[kv.second[t]] = g[t];
+            }
             std::vector<RotReq> copies, next_rot;
             std::vector<size_t> next;
             for (size_t q = 0; q < proj.size(); ++q) {
@@ -1697,6 +1713,140 @@ void evolve_engine(Op& op, const double* v0, const std::vector<cd>& scales, doub
             for (int64_t q = 0; q < 2 * n; ++q) o[q] *= inv;
         }
     QS_CUDA(cudaStreamSynchronize(E.stream()));
+    note_launches(E.launches());
+}
+
+void evolve_blocks(const std::vector<Op*>& ops, const std::vector<const double*>& v0s, const std::vector<cd>& scales,
+                   double tol, int krylov_dim, int precision, const std::vector<double*>& outs) {
+    const size_t nb = ops.size();
+    const int nt = (int)scales.size();
+    if (nb == 0 || nt == 0) return;
+    Engine E(precision == 0 ? Store::F64 : Store::DF, ops[0]->stream);
+    cudaStream_t st = E.stream();
+    std::vector<int64_t> n(nb);
+    std::vector<int> m(nb), f(nb, -1);
+    std::vector<char> herm(nb);
+    auto copy_v0 = [&](size_t b, int i) {
+        QS_CUDA(cudaMemcpyAsync(outs[b] + (size_t)i * 2 * n[b], v0s[b], (size_t)n[b] * 16, cudaMemcpyDeviceToDevice,
+                                st));
+    };
+    // phase 1: one factorisation per block from its start vector (a 1-state
+    // block still takes two columns; its second direction is zero and the
+    // breakdown test stops the projection at c = 1)
+    std::vector<int> fid;
+    for (size_t b = 0; b < nb; ++b) {
+        n[b] = ops[b]->basis->n;
+        m[b] = (int)std::max<int64_t>(2, std::min<int64_t>(std::min(krylov_dim, kMaxM), n[b]));
+        herm[b] = ops[b]->hermitian;
+        f[b] = E.add(*ops[b], m[b], true, true, 1, herm[b] ? 2 : 0);
+        E.load(f[b], 0, v0s[b], true);
+        fid.push_back(f[b]);
+    }
+    const std::vector<double> beta = E.normalize(fid);
+    std::vector<char> active(nb, 0);
+    for (size_t b = 0; b < nb; ++b) {
+        bool all_zero = true;
+        for (const cd& sc : scales) all_zero = all_zero && sc == cd(0, 0);
+        if (beta[b] == 0 || all_zero) {
+            for (int i = 0; i < nt; ++i) copy_v0(b, i);
+            E.remove(f[b]);
+        } else {
+            active[b] = 1;
+            E.start(f[b], 0);
+        }
+    }
+    for (int steps = E.steps_to_event(); steps > 0; steps = E.steps_to_event()) E.run(steps);
+    std::vector<size_t> act;
+    std::vector<int> act_ids;
+    for (size_t b = 0; b < nb; ++b)
+        if (active[b]) {
+            act.push_back(b);
+            act_ids.push_back(f[b]);
+        }
+    std::vector<std::vector<cd>> H;
+    E.records(act_ids, H);
+    // every time of every block from its shared factorisation: one rotation
+    // launch and one normalisation per Krylov size for all blocks at a time
+    std::vector<std::pair<size_t, int>> failing;
+    for (int i = 0; i < nt; ++i) {
+        std::vector<RotReq> rot;
+        std::vector<size_t> who;
+        std::vector<int> cs;
+        std::vector<double> terms;
+        for (size_t q = 0; q < act.size(); ++q) {
+            const size_t b = act[q];
+            if (scales[i] == cd(0, 0)) {
+                copy_v0(b, i);
+                continue;
+            }
+            int c;
+            std::vector<cd> coef;
+            double terminal;
+            krylov_project(H[q], m[b], herm[b], scales[i], c, coef, terminal);
+            RotReq R;
+            R.id = f[b];
+            R.nin = c;
+            R.p = 1;
+            R.out0 = m[b];
+            R.Y.resize(c);
+            for (int r = 0; r < c; ++r) R.Y[r] = coef[r] * beta[b];
+            rot.push_back(std::move(R));
+            who.push_back(b);
+            cs.push_back(c);
+            terms.push_back(std::abs(scales[i]) * terminal * beta[b] * std::abs(coef[c - 1]));
+        }
+        if (rot.empty()) continue;
+        E.rotate(rot);
+        std::map<int, std::vector<size_t>> by_m;
+        for (size_t q = 0; q < who.size(); ++q) by_m[m[who[q]]].push_back(q);
+        std::vector<double> nr(who.size());
+        for (const auto& kv : by_m) {
+            std::vector<int> ids;
+            for (size_t q : kv.second) ids.push_back(f[who[q]]);
+            const std::vector<double> g = E.normalize(ids, kv.first, false);
+            for (size_t t = 0; t < kv.second.size(); ++t) nr[kv.second[t]] = g[t];
+        }
+        for (size_t q = 0; q < who.size(); ++q) {
+            const size_t b = who[q];
+            const bool est_on = cs[q] == m[b] && m[b] < n[b];
+            const double est = est_on ? terms[q] : 0.0;
+            if (est > tol * std::max(1.0, nr[q])) failing.push_back({b, i});
+            else E.store(f[b], m[b], outs[b] + (size_t)i * 2 * n[b], true);
+        }
+    }
+    for (size_t b : act) E.remove(f[b]);
+    // phase 2: the failing (block, time) pairs run the reference's recursion
+    // from their start vectors, concurrently, in waves that fit in memory
+    size_t fr = 0, tot = 0;
+    QS_CUDA(cudaMemGetInfo(&fr, &tot));
+    for (size_t w0 = 0; w0 < failing.size();) {
+        std::vector<int> ids;
+        std::vector<EvoTask> tasks;
+        std::vector<double*> wouts;
+        std::vector<size_t> blk;
+        size_t used = 0, w1 = w0;
+        for (; w1 < failing.size(); ++w1) {
+            const size_t b = failing[w1].first;
+            const size_t per = Engine::slot_bytes(n[b], m[b], true, 1, E.store());
+            if (w1 > w0 && used + per > fr / 2) break;
+            used += per;
+            const int id = E.add(*ops[b], m[b], true, true, 1, herm[b] ? 2 : 0);
+            E.load(id, 0, v0s[b], true);
+            ids.push_back(id);
+            wouts.push_back(outs[b] + (size_t)failing[w1].second * 2 * n[b]);
+            blk.push_back(b);
+        }
+        const std::vector<double> b0 = E.normalize(ids);
+        for (size_t q = 0; q < ids.size(); ++q) {
+            EvoTask t;
+            // the recursion's first attempt is the shared factorisation, which failed
+            t.init(m[blk[q]], n[blk[q]], herm[blk[q]], scales[failing[w0 + q].second], tol, b0[q], true);
+            tasks.push_back(t);
+        }
+        run_evo_slots(E, ids, tasks, wouts, true);
+        w0 = w1;
+    }
+    QS_CUDA(cudaStreamSynchronize(st));
     note_launches(E.launches());
 }
 

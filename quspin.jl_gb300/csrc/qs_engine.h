@@ -249,5 +249,12 @@ struct EvoTask {
 // complex (host).
 void evolve_engine(Op& op, const double* v0, const std::vector<cd>& scales, double tol, int krylov_dim, int precision,
                    bool normalise, double* out);
+// The reference's _krylov_expmv_times (src/operators.jl:1805-1893) on several
+// operators at once (the blocks of tools.jl's BlockOps evolution): v0s[b]
+// and outs[b] are device complex vectors (outs[b]: n_b x nscales); the blocks'
+// factorisations step together, then the failing (block, time) pairs run
+// their recursions concurrently.
+void evolve_blocks(const std::vector<Op*>& ops, const std::vector<const double*>& v0s, const std::vector<cd>& scales,
+                   double tol, int krylov_dim, int precision, const std::vector<double*>& outs);
 
 }  // namespace qs

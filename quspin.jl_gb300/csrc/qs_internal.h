@@ -174,6 +174,11 @@ void basis_index_of(Basis& b, const uint64_t* states, int64_t n, int64_t* out);
 void basis_compute_refrep(Basis& b);
 void basis_representative(Basis& b, const uint64_t* states, int64_t n, uint64_t* reps, double* norms,
                           double* amps, int32_t* status);
+// rows of the projection space: 2^L, or the parent particle sector (pcon)
+int64_t basis_projection_rows(const Basis& b, bool pcon);
+// mode 0: out (rows) = [out +] P in (Ns); mode 1: out (Ns) = P^H in (rows);
+// complex vectors, host or device
+void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out, bool accumulate, bool device);
 
 // qs_op.cpp
 Op* op_create(Basis* basis, const qs_term* terms, int nterms, const double* diagonal, int checks);

@@ -339,4 +339,59 @@ void lanczos_ritz_matrix(LanczosSet& L, int s, Op& obs, const double* Y, int nv,
     }
 }
 
+void block_expm(const std::vector<Op*>& ops, bool pcon, const double* psi, const std::vector<cd>& scales, double tol,
+                int krylov_dim, int precision, double* out, bool device) {
+    if (ops.empty()) throw Error(QS_ERR_ARGUMENT, "at least one block is required");
+    const int64_t rows = basis_projection_rows(*ops[0]->basis, pcon);
+    for (Op* op : ops)
+        if (basis_projection_rows(*op->basis, pcon) != rows)
+            throw Error(QS_ERR_DIMENSION, "the blocks must share one projection space");
+    cudaStream_t st = ops[0]->stream;
+    const int nt = (int)scales.size();
+    PoolBuf dpsi, dout;
+    const double* p = psi;
+    double* o = out;
+    if (!device) {
+        dpsi.alloc((size_t)rows * 16, st);
+        QS_CUDA(cudaMemcpyAsync(dpsi.p, psi, dpsi.bytes, cudaMemcpyHostToDevice, st));
+        dout.alloc((size_t)rows * nt * 16, st);
+        p = dpsi.as<double>();
+        o = dout.as<double>();
+    }
+    QS_CUDA(cudaStreamSynchronize(st));
+    // c_b = P_b^H psi; blocks where it vanishes (norm <= 1000 eps) are left out,
+    // as the reference's _active_block_entries does (tools.jl:2445-2477)
+    std::vector<PoolBuf> coef(ops.size()), states(ops.size());
+    std::vector<Op*> act;
+    std::vector<const double*> v0s;
+    std::vector<double*> outs;
+    std::vector<size_t> which;
+    for (size_t b = 0; b < ops.size(); ++b) {
+        Basis& B = *ops[b]->basis;
+        coef[b].alloc((size_t)B.n * 16, B.stream);
+        basis_project(B, pcon, 1, p, coef[b].as<double>(), false, true);
+        Blas nrm(VKind::C128, B.n, B.stream);
+        if (!(nrm.norm(coef[b].p) > 1000 * 2.220446049250313e-16)) continue;
+        states[b].alloc((size_t)B.n * nt * 16, st);
+        act.push_back(ops[b]);
+        v0s.push_back(coef[b].as<double>());
+        outs.push_back(states[b].as<double>());
+        which.push_back(b);
+    }
+    if (act.empty()) throw Error(QS_ERR_ARGUMENT, "initial state has no projection onto the selected blocks");
+    evolve_blocks(act, v0s, scales, tol, krylov_dim, precision, outs);
+    // out[:, i] = sum_b P_b state_b(i), blocks in the given order
+    QS_CUDA(cudaMemsetAsync(o, 0, (size_t)rows * nt * 16, st));
+    QS_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < nt; ++i)
+        for (size_t q = 0; q < act.size(); ++q) {
+            Basis& B = *act[q]->basis;
+            basis_project(B, pcon, 0, outs[q] + (size_t)i * 2 * B.n, o + (size_t)i * 2 * rows, true, true);
+        }
+    if (!device) {
+        QS_CUDA(cudaMemcpyAsync(out, o, (size_t)rows * nt * 16, cudaMemcpyDeviceToHost, st));
+        QS_CUDA(cudaStreamSynchronize(st));
+    }
+}
+
 }  // namespace qs

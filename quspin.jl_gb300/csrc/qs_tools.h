@@ -38,4 +38,12 @@ void lanczos_overlaps(LanczosSet& L, Op& obs, double* out);
 // out = R^* O R with R = Q^T Y (Y used x nv real, column-major); complex nv x nv column-major.
 void lanczos_ritz_matrix(LanczosSet& L, int s, Op& obs, const double* Y, int nv, double* out);
 
+// evolve(BlockOps, psi, t0, times) / block_expm (src/tools.jl:2445-2719) for
+// static block operators: c_b = P_b^H psi for every block with a nonzero
+// projection, exp(s_i H_b) c_b for every scale with all blocks' Krylov
+// recursions on one engine, out[:, i] = sum_b P_b state_b(i).  psi: rows
+// complex; out: rows x nscales complex (host, or device with `device`).
+void block_expm(const std::vector<Op*>& ops, bool pcon, const double* psi, const std::vector<cd>& scales, double tol,
+                int krylov_dim, int precision, double* out, bool device);
+
 }  // namespace qs

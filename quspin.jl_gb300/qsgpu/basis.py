@@ -10,7 +10,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .errors import ArgumentError
+from .errors import ArgumentError, DimensionMismatch
 
 
 def basis_spec(L, nup=None, Nup=None, m=None, S="1/2", pauli=True, a=1, kblock=None, pblock=None, zblock=None,
@@ -179,3 +179,59 @@ def state_to_int(basis, state):
     if any(ch not in "01" for ch in compact):
         raise ArgumentError("state must be binary")
     return int(compact, 2)
+
+
+def _projection(basis, vector, pcon, mode):
+    """mode 0: P v (Ns -> rows); mode 1: P^H v (rows -> Ns); columns of a matrix one by one."""
+    lib = _lib.load()
+    rows = int(lib.qs_basis_projection_rows(basis._h, 1 if pcon else 0))
+    if rows < 0:
+        raise ArgumentError("the full Hilbert-space dimension exceeds device memory; use pcon=True")
+    v = np.asarray(vector)
+    nin, nout = (basis.Ns, rows) if mode == 0 else (rows, basis.Ns)
+    if v.shape[0] != nin:
+        raise DimensionMismatch("the first vector dimension must equal Ns" if mode == 0 else
+                                "the first vector dimension does not match the projection space")
+    if not np.iscomplexobj(v) and basis.requires_complex:
+        raise ArgumentError("this momentum sector requires a complex projection dtype")
+    cols = v.reshape(nin, -1)
+    out = np.zeros((nout, cols.shape[1]), dtype=np.complex128)
+    for c in range(cols.shape[1]):
+        x = np.ascontiguousarray(cols[:, c], dtype=np.complex128)
+        y = np.zeros(nout, dtype=np.complex128)
+        if mode == 0:
+            _lib.check(lib.qs_basis_project_from(basis._h, 1 if pcon else 0, _lib.ptr(x), _lib.ptr(y), 0,
+                                                 _lib.QS_MEM_HOST))
+        else:
+            _lib.check(lib.qs_basis_project_to(basis._h, 1 if pcon else 0, _lib.ptr(x), _lib.ptr(y),
+                                               _lib.QS_MEM_HOST))
+        out[:, c] = y
+    if not np.iscomplexobj(v):
+        out = out.real.copy()
+    return out.reshape((nout,) + v.shape[1:])
+
+
+def _maybe_sparse(a, sparse):
+    if not sparse:
+        return a
+    import scipy.sparse as sp
+    return sp.csc_matrix(a.reshape(a.shape[0], -1))
+
+
+def project_from(basis, vector, sparse=False, pcon=False):
+    """project_from(basis, vector; sparse, pcon) (src/basis.jl:889-908): P v,
+    from the sector to the full 2^L space (or the parent particle sector with
+    pcon).  Computed on the device; dense unless sparse=True (the reference's
+    default output is sparse)."""
+    return _maybe_sparse(_projection(basis, vector, pcon, 0), sparse)
+
+
+def get_vec(basis, vector, sparse=False, pcon=False):
+    """get_vec(basis, vector; kwargs...) = project_from (src/basis.jl:910-911)."""
+    return project_from(basis, vector, sparse=sparse, pcon=pcon)
+
+
+def project_to(basis, vector, sparse=False, pcon=False):
+    """project_to(basis, vector; sparse, pcon) (src/discrete_basis.jl:2455-2475):
+    P^H v, from the full space (or parent sector) to the sector."""
+    return _maybe_sparse(_projection(basis, vector, pcon, 1), sparse)

@@ -299,7 +299,12 @@ def eigsh_batch(ops, k=1, which="SA", tol=0.0, ncv=None, maxiter=None, return_ei
 
 
 def evolve(H, v0, t0, times, eom="SE", iterate=False, imag_time=False, tol=1e-12, krylov_dim=30, precision="fp64"):
-    """evolve(H, v0, t0, times; eom=:SE) for a static Hamiltonian (src/operators.jl:2073-2164)."""
+    """evolve(H, v0, t0, times; eom=:SE) for a static Hamiltonian (src/operators.jl:2073-2164).
+    A BlockOps operator evolves block by block (tools.jl:2627-2678)."""
+    from .blocks import BlockOps, evolve_blocks
+    if isinstance(H, BlockOps):
+        return evolve_blocks(H, v0, t0, times, iterate=iterate, imag_time=imag_time, tol=tol, krylov_dim=krylov_dim,
+                             precision=precision)
     if str(eom) not in ("SE", "LvNE"):
         raise ArgumentError("eom must be :SE or :LvNE")
     if str(eom) == "LvNE":

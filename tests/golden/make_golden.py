@@ -134,6 +134,25 @@ def main(root):
         "beta": betas, "ftlm_identity": fi, "ftlm_identity_atol": fi_atol,
         "ftlm_B": fb, "ftlm_B_atol": fb_atol, "ltlm_B": lb, "ltlm_B_atol": lb_atol,
     }
+    m = re.search(r'@testset "Symmetry block tools" begin(.*?)\nend', rt, re.S)
+    block = m.group(1)
+    assert 'terms = [OperatorTerm("z", [(1.0, 1), (0.5, 2)])]' in block
+    assert "blocks = [Dict(:nup => sector) for sector in 0:2]" in block
+    assert "psi = normalize(ComplexF64[1, 2, 3, 4])" in block
+    assert "times = [0.0, 0.2, 1.0]" in block
+
+    def atol_after(pattern):
+        return float(re.search(pattern + r".*?atol=([0-9.e-]+)", block, re.S).group(1))
+    kats["block_tools_L2"] = {
+        "source": "test/runtests.jl:277-325",
+        "L": 2, "pauli": False, "terms": [["z", [[1.0, 1], [0.5, 2]]]],
+        "blocks_nup": [0, 1, 2], "psi_unnormalized": [1, 2, 3, 4], "times": [0.0, 0.2, 1.0],
+        "evolve_atol": atol_after(r"@test evolve\(blocks_operator, psi, 0.0, times\) ≈"),
+        "expm_atol": atol_after(r"@test block_expm\(blocks_operator, psi\) ≈"),
+        "grid_first_atol": atol_after(r"@test grid\[:, 1\] ≈ psi"),
+        "grid_last_atol": atol_after(r"@test grid\[:, end\] ≈"),
+        "grid": {"start": 0.0, "stop": 1.0, "num": 3},
+    }
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
     with open(out, "w") as f:
         json.dump(kats, f, indent=1, sort_keys=True)
