@@ -888,6 +888,8 @@ struct ProjArgs {
     int mode;              // 0: out += P in; 1: out = P^H in
     const double2* in;
     double2* out;
+    int ncols;             // vectors, column c at in + c * in_ld, out + c * out_ld
+    int64_t in_ld, out_ld;
     REnt* scratch;
     int64_t cap, nthreads;
 };
@@ -914,25 +916,29 @@ __global__ void project_kernel(ProjArgs a) {
             buf[0].re = 1.0;
             buf[0].im = 0.0;
         }
-        if (a.mode == 0) {
-            const double2 c = a.in[j];
-            for (int k = 0; k < cnt; ++k) {
-                const int64_t row = proj_row<U>(a, buf[k].s);
-                const double vr = buf[k].re, vi = buf[k].im;
-                double2 o = a.out[row];
-                o.x = __dadd_rn(o.x, __dsub_rn(__dmul_rn(vr, c.x), __dmul_rn(vi, c.y)));
-                o.y = __dadd_rn(o.y, __dadd_rn(__dmul_rn(vr, c.y), __dmul_rn(vi, c.x)));
-                a.out[row] = o;
+        for (int col = 0; col < a.ncols; ++col) {
+            const double2* in = a.in + (size_t)col * a.in_ld;
+            double2* out = a.out + (size_t)col * a.out_ld;
+            if (a.mode == 0) {
+                const double2 c = in[j];
+                for (int k = 0; k < cnt; ++k) {
+                    const int64_t row = proj_row<U>(a, buf[k].s);
+                    const double vr = buf[k].re, vi = buf[k].im;
+                    double2 o = out[row];
+                    o.x = __dadd_rn(o.x, __dsub_rn(__dmul_rn(vr, c.x), __dmul_rn(vi, c.y)));
+                    o.y = __dadd_rn(o.y, __dadd_rn(__dmul_rn(vr, c.y), __dmul_rn(vi, c.x)));
+                    out[row] = o;
+                }
+            } else {
+                double ar = 0.0, ai = 0.0;
+                for (int k = 0; k < cnt; ++k) {
+                    const double2 x = in[proj_row<U>(a, buf[k].s)];
+                    const double vr = buf[k].re, vi = -buf[k].im;   // conj(P[s, j])
+                    ar = __dadd_rn(ar, __dsub_rn(__dmul_rn(vr, x.x), __dmul_rn(vi, x.y)));
+                    ai = __dadd_rn(ai, __dadd_rn(__dmul_rn(vr, x.y), __dmul_rn(vi, x.x)));
+                }
+                out[j] = make_double2(ar, ai);
             }
-        } else {
-            double ar = 0.0, ai = 0.0;
-            for (int k = 0; k < cnt; ++k) {
-                const double2 x = a.in[proj_row<U>(a, buf[k].s)];
-                const double vr = buf[k].re, vi = -buf[k].im;   // conj(P[s, j])
-                ar = __dadd_rn(ar, __dsub_rn(__dmul_rn(vr, x.x), __dmul_rn(vi, x.y)));
-                ai = __dadd_rn(ai, __dadd_rn(__dmul_rn(vr, x.y), __dmul_rn(vi, x.x)));
-            }
-            a.out[j] = make_double2(ar, ai);
         }
     }
 }
@@ -948,6 +954,8 @@ struct EmbedArgs {
     int mode;              // 0: out += P in; 1: out = P^H in
     const double2* in;
     double2* out;
+    int ncols;
+    int64_t in_ld, out_ld;
 };
 
 template <typename U>
@@ -959,14 +967,18 @@ __global__ void embed_kernel(EmbedArgs a) {
             if (__popcll((unsigned long long)r) != a.nup) continue;
             j = combinadic_rank<U>((U)r, a.binom, 65);
         }
-        if (a.mode == 0) {
-            double2 o = a.out[r];
-            const double2 c = a.in[j];
-            o.x = __dadd_rn(o.x, c.x);
-            o.y = __dadd_rn(o.y, c.y);
-            a.out[r] = o;
-        } else {
-            a.out[j] = a.in[r];
+        for (int col = 0; col < a.ncols; ++col) {
+            const double2* in = a.in + (size_t)col * a.in_ld;
+            double2* out = a.out + (size_t)col * a.out_ld;
+            if (a.mode == 0) {
+                double2 o = out[r];
+                const double2 c = in[j];
+                o.x = __dadd_rn(o.x, c.x);
+                o.y = __dadd_rn(o.y, c.y);
+                out[r] = o;
+            } else {
+                out[j] = in[r];
+            }
         }
     }
 }
@@ -1131,17 +1143,19 @@ int64_t basis_projection_rows(const Basis& b, bool pcon) {
     return (int64_t)1 << b.L;
 }
 
-void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out, bool accumulate, bool device) {
+void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out, bool accumulate, bool device,
+                   int ncols) {
     const int64_t rows = basis_projection_rows(b, pcon);
-    const int64_t nin = mode == 0 ? b.n : rows, nout = mode == 0 ? rows : b.n;
+    const int64_t nin1 = mode == 0 ? b.n : rows, nout1 = mode == 0 ? rows : b.n;
+    const int64_t nin = nin1 * ncols, nout = nout1 * ncols;
     if (b.symmetric) upload_replay(b);
     cudaStream_t s = b.stream;
-    DevBuf din, dout;
+    PoolBuf din, dout;
     const double2* pin = reinterpret_cast<const double2*>(in);
     double2* pout = reinterpret_cast<double2*>(out);
     if (!device) {
-        din.alloc((size_t)nin * sizeof(double2));
-        dout.alloc((size_t)nout * sizeof(double2));
+        din.alloc((size_t)nin * sizeof(double2), s);
+        dout.alloc((size_t)nout * sizeof(double2), s);
         QS_CUDA(cudaMemcpyAsync(din.p, in, din.bytes, cudaMemcpyHostToDevice, s));
         if (mode == 0 && accumulate) QS_CUDA(cudaMemcpyAsync(dout.p, out, dout.bytes, cudaMemcpyHostToDevice, s));
         pin = din.as<double2>();
@@ -1157,6 +1171,9 @@ void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out,
         e.mode = mode;
         e.in = pin;
         e.out = pout;
+        e.ncols = ncols;
+        e.in_ld = nin1;
+        e.out_ld = nout1;
         const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((rows + 255) / 256, 152 * 16));
         if (b.wide) embed_kernel<uint64_t><<<grid, 256, 0, s>>>(e);
         else embed_kernel<uint32_t><<<grid, 256, 0, s>>>(e);
@@ -1168,7 +1185,7 @@ void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out,
     }
     const int64_t nt = replay_threads(b.n);
     const int64_t cap = b.symmetric ? b.group.ng : 1;
-    DevBuf scratch((size_t)nt * 2 * cap * sizeof(REnt));
+    PoolBuf scratch((size_t)nt * 2 * cap * sizeof(REnt), s);
     ProjArgs a{};
     if (b.symmetric) a.ctx = make_ctx(b, b.d_level_groups, b.d_level0);
     a.reps = b.d_reps.p;
@@ -1180,6 +1197,9 @@ void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out,
     a.mode = mode;
     a.in = pin;
     a.out = pout;
+    a.ncols = ncols;
+    a.in_ld = nin1;
+    a.out_ld = nout1;
     a.scratch = scratch.as<REnt>();
     a.cap = cap;
     a.nthreads = nt;

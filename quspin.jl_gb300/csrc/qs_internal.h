@@ -177,8 +177,10 @@ void basis_representative(Basis& b, const uint64_t* states, int64_t n, uint64_t*
 // rows of the projection space: 2^L, or the parent particle sector (pcon)
 int64_t basis_projection_rows(const Basis& b, bool pcon);
 // mode 0: out (rows) = [out +] P in (Ns); mode 1: out (Ns) = P^H in (rows);
-// complex vectors, host or device
-void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out, bool accumulate, bool device);
+// complex vectors, host or device; ncols contiguous vectors at once (one
+// replay of each projector column for all of them)
+void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out, bool accumulate, bool device,
+                   int ncols = 1);
 
 // qs_op.cpp
 Op* op_create(Basis* basis, const qs_term* terms, int nterms, const double* diagonal, int checks);

@@ -380,14 +380,12 @@ void block_expm(const std::vector<Op*>& ops, bool pcon, const double* psi, const
     }
     if (act.empty()) throw Error(QS_ERR_ARGUMENT, "initial state has no projection onto the selected blocks");
     evolve_blocks(act, v0s, scales, tol, krylov_dim, precision, outs);
-    // out[:, i] = sum_b P_b state_b(i), blocks in the given order
+    // out[:, i] = sum_b P_b state_b(i), blocks in the given order, all times
+    // of a block in one launch
     QS_CUDA(cudaMemsetAsync(o, 0, (size_t)rows * nt * 16, st));
     QS_CUDA(cudaStreamSynchronize(st));
-    for (int i = 0; i < nt; ++i)
-        for (size_t q = 0; q < act.size(); ++q) {
-            Basis& B = *act[q]->basis;
-            basis_project(B, pcon, 0, outs[q] + (size_t)i * 2 * B.n, o + (size_t)i * 2 * rows, true, true);
-        }
+    for (size_t q = 0; q < act.size(); ++q)
+        basis_project(*act[q]->basis, pcon, 0, outs[q], o, true, true, nt);
     if (!device) {
         QS_CUDA(cudaMemcpyAsync(out, o, (size_t)rows * nt * 16, cudaMemcpyDeviceToHost, st));
         QS_CUDA(cudaStreamSynchronize(st));
