@@ -170,6 +170,11 @@ QS_API int qs_op_set_stream(qs_op *op, void *stream);
 QS_API int qs_op_assemble(qs_op *op);
 /* Stored nonzeros of the assembled form (off-diagonal), -1 if not assembled. */
 QS_API int64_t qs_op_nnz(const qs_op *op);
+/* H.data / tocsc(H) (src/operators.jl:461-576, 1347) from the device's
+ * assembled form: the off-diagonal part in CSR (rowptr Ns + 1, cols and
+ * complex values qs_op_nnz(op) each; entries of one row may repeat a column,
+ * the element is their sum) and the diagonal (Ns complex).  Host buffers. */
+QS_API int qs_op_export_csr(qs_op *op, int64_t *rowptr, int64_t *cols, double *values, double *diag);
 /* set_diagonal!(op, d) (src/operators.jl:3298-3307); d is 2*Ns doubles. */
 QS_API int qs_op_set_diagonal(qs_op *op, const double *diagonal);
 

@@ -1135,4 +1135,59 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
     note_launches(1);
 }
 
+namespace {
+
+// Element values of the assembled CSR form: value k of row r is
+// table[code_k] / sqrt(stab_r) (the row scale the products apply after the
+// sum), column col_k.
+__global__ void export_kernel(const int64_t* __restrict__ rowptr, const uint32_t* __restrict__ words,
+                              const int32_t* __restrict__ cols, const uint16_t* __restrict__ codes, int packed,
+                              int cb, uint32_t cmask, const double2* __restrict__ table,
+                              const uint16_t* __restrict__ stab, int64_t n, int64_t* __restrict__ ocol,
+                              double2* __restrict__ oval) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const double sc = stab ? 1.0 / sqrt((double)stab[r]) : 1.0;
+        for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+            uint32_t col, code;
+            if (packed) {
+                col = words[k] >> cb;
+                code = words[k] & cmask;
+            } else {
+                col = (uint32_t)cols[k];
+                code = codes[k];
+            }
+            const double2 v = table[code];
+            ocol[k] = col;
+            oval[k] = make_double2(v.x * sc, v.y * sc);
+        }
+    }
+}
+
+}  // namespace
+
+void op_export_csr(Op& op, int64_t* rowptr, int64_t* cols, double* values, double* diag) {
+    if (!op.assembled) op_assemble(op);
+    const Assembled& M = op.asm_;
+    Basis& b = *op.basis;
+    const int64_t n = b.n;
+    cudaStream_t s = op.stream;
+    PoolBuf dcol((size_t)std::max<int64_t>(1, M.nnz) * sizeof(int64_t), s),
+        dval((size_t)std::max<int64_t>(1, M.nnz) * sizeof(double2), s);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+    export_kernel<<<grid, 256, 0, s>>>(M.rowptr.as<int64_t>(), M.words.as<uint32_t>(), M.cols.as<int32_t>(),
+                                       M.codes.as<uint16_t>(), M.packed ? 1 : 0, M.code_bits,
+                                       M.code_bits >= 32 ? 0xffffffffu : ((1u << M.code_bits) - 1u),
+                                       M.table64.as<double2>(), b.symmetric ? b.d_stab.as<uint16_t>() : nullptr, n,
+                                       dcol.as<int64_t>(), dval.as<double2>());
+    QS_CUDA(cudaGetLastError());
+    note_launches(1);
+    QS_CUDA(cudaMemcpyAsync(rowptr, M.rowptr.p, (size_t)(n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    if (M.nnz) {
+        QS_CUDA(cudaMemcpyAsync(cols, dcol.p, (size_t)M.nnz * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        QS_CUDA(cudaMemcpyAsync(values, dval.p, (size_t)M.nnz * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    }
+    QS_CUDA(cudaMemcpyAsync(diag, op.d_diag.p, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    QS_CUDA(cudaStreamSynchronize(s));
+}
+
 }  // namespace qs

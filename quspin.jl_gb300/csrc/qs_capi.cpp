@@ -210,6 +210,15 @@ int qs_op_assemble(qs_op* op) {
 
 int64_t qs_op_nnz(const qs_op* op) { return op->op->assembled ? op->op->asm_.nnz : -1; }
 
+int qs_op_export_csr(qs_op* op, int64_t* rowptr, int64_t* cols, double* values, double* diag) {
+    return guard([&] {
+        if (!op || !rowptr || !diag) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        if (!op->op->assembled) throw qs::Error(QS_ERR_ARGUMENT, "assemble the operator first (qs_op_assemble)");
+        if (op->op->asm_.nnz && (!cols || !values)) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::op_export_csr(*op->op, rowptr, cols, values, diag);
+    });
+}
+
 int qs_op_dtype(const qs_op* op) { return op->op->complex_mat ? QS_C128 : QS_F64; }
 int qs_op_hermitian(const qs_op* op) { return op->op->hermitian ? 1 : 0; }
 

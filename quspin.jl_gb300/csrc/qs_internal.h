@@ -205,6 +205,9 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
 // qs_assembled.cu
 void op_assemble(Op& op);
 void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s);
+// the assembled matrix on the host: CSR off-diagonal part (rowptr n + 1,
+// cols and complex values nnz; a row may repeat a column) and the diagonal
+void op_export_csr(Op& op, int64_t* rowptr, int64_t* cols, double* values, double* diag);
 // device-wide exclusive scan of int64 (qs_basis.cu)
 void scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t s);
 // kernel launch accounting (qs_launch_count)

@@ -9,7 +9,8 @@ from .basis import (SpinBasis1D, get_amp, get_vec, int_to_state, normalization, 
                     representative, state_at, state_index, state_to_int, states)
 from .errors import ArgumentError, DimensionMismatch, ErrorException, UnsupportedError
 from .operators import (ExpmMultiplyParallel, Hamiltonian, OperatorTerm, QuantumLinearOperator, apply, eigsh,
-                        eigsh_batch, evolve, expm_multiply_parallel, isquantum_LinearOperator, set_a)
+                        eigsh_batch, evolve, expm_multiply_parallel, isquantum_LinearOperator, set_a, toarray, tocsc,
+                        tocsr)
 from .blocks import (BlockDiagHamiltonian, BlockOps, BlockProjector, block_diag_hamiltonian, block_expm,
                      evolve_blocks)
 from .server import Server
@@ -23,5 +24,5 @@ __all__ = [
     "ArgumentError", "DimensionMismatch", "ErrorException", "UnsupportedError", "Server",
     "lanczos_full", "lanczos_iter", "lanczos_batch", "lin_comb_Q_T", "expm_lanczos", "ftlm_static_iteration",
     "ltlm_static_iteration", "LanczosRows", "BlockOps", "block_diag_hamiltonian", "block_expm", "evolve_blocks",
-    "BlockProjector", "BlockDiagHamiltonian",
+    "BlockProjector", "BlockDiagHamiltonian", "tocsc", "tocsr", "toarray",
 ]

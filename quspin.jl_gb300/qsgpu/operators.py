@@ -228,6 +228,60 @@ class Hamiltonian(QuantumLinearOperator):
     def nnz(self):
         return int(_lib.load().qs_op_nnz(self._h))
 
+    def _export(self):
+        """The device's assembled matrix as a scipy CSR matrix (duplicates summed)."""
+        import scipy.sparse as sp
+        if not self.assembled:
+            raise ArgumentError("this operator has no assembled form (non-commuting terms stay matrix-free)")
+        n, nnz = self.Ns, self.nnz
+        rowptr = np.zeros(n + 1, dtype=np.int64)
+        cols = np.zeros(max(nnz, 1), dtype=np.int64)
+        vals = np.zeros(max(nnz, 1), dtype=np.complex128)
+        diag = np.zeros(n, dtype=np.complex128)
+        _lib.check(_lib.load().qs_op_export_csr(self._h, _lib.ptr(rowptr), _lib.ptr(cols), _lib.ptr(vals),
+                                                _lib.ptr(diag)))
+        real = self.dtype == np.float64
+        off = sp.csr_matrix(((vals[:nnz].real if real else vals[:nnz]), cols[:nnz], rowptr), shape=(n, n))
+        off.sum_duplicates()
+        d = diag.real if real else diag
+        nz = np.nonzero(d)[0]
+        return off + sp.csr_matrix((d[nz], (nz, nz)), shape=(n, n))
+
+    def tocsr(self, time=0):
+        """tocsr(H; time) (src/operators.jl:1348): the static matrix H.data, from the device's assembled form."""
+        return self._export()
+
+    def tocsc(self, time=0):
+        """tocsc(H; time) (src/operators.jl:1347)."""
+        return self._export().tocsc()
+
+    def toarray(self, time=0, order=None, out=None):
+        """toarray(H; time, out) (src/operators.jl:1343-1344)."""
+        a = self._export().toarray()
+        if out is None:
+            return a
+        if out.shape != a.shape:
+            raise DimensionMismatch("out must have the same axes as the result")
+        out[...] = a
+        return out
+
+    todense = toarray
+
+
+def tocsc(H, time=0):
+    """tocsc(H::Hamiltonian; time) (src/operators.jl:1347)."""
+    return H.tocsc(time)
+
+
+def tocsr(H, time=0):
+    """tocsr(H::Hamiltonian; time) (src/operators.jl:1348)."""
+    return H.tocsr(time)
+
+
+def toarray(H, time=0, order=None, out=None):
+    """toarray(H::Hamiltonian; time, out) (src/operators.jl:1343-1344)."""
+    return H.toarray(time, order, out)
+
 
 def _precision_code(precision):
     """0 = FP64, 1 = FP32 (+ FP64 polish), 2 = double-float on the FP32 pipe."""
