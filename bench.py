@@ -783,6 +783,12 @@ def run_ours(args, wl, world, rank, local):
                             restarts=info.get("restarts"))
     clk = clocks.stop()
 
+    # the FP64 roofline: one FP64 multiply-add per stored nonzero, plus the
+    # diagonal term and the row scale per row, against this GPU's measured FP64
+    # FMA throughput
+    fma_rate = ctypes.c_double(0.0)
+    _lib.check(lib.qs_fp64_fma_rate(ctypes.byref(fma_rate)))
+    fma_per_step = nnz + 2 * n
     t_step = max_over_ranks(world, float(np.mean(ms64)) / 1e3, dev)
     value = replica_value(world, asm_bytes64, t_step)
     peak, peak_kind = load_peaks()
@@ -843,6 +849,11 @@ def run_ours(args, wl, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": wl.get("traffic"), "peak_kind": peak_kind,
                      "kernel": "sell_kernel (assembled H.v, sliced ELL)"},
+        "fp64_roofline": {"bound": "fp64 pipe", "achieved": fma_per_step / (float(np.mean(ms64)) / 1e3) / 1e12,
+                          "peak": fma_rate.value / 1e12, "unit": "T FMA/s",
+                          "frac": fma_per_step / (float(np.mean(ms64)) / 1e3) / fma_rate.value,
+                          "fma_per_step": fma_per_step,
+                          "peak_kind": "measured in this run (qs_fp64_fma_rate: chained FP64 FMA kernel)"},
         "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": int(launches),
         "clocks": clk,

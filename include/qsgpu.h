@@ -429,6 +429,12 @@ QS_API int qs_server_stats(qs_server *server, qs_server_counters *out);
 /* Message of the last failure on the calling thread (empty if none). */
 QS_API const char *qs_last_error(void);
 
+/* The GPU's FP64 fused multiply-add throughput in FMA/s, measured by a short
+ * chained-FMA kernel (best of three).  No reference counterpart: the roofline
+ * for the FP64-bound kernels (GB300's FP64 rate is far below its memory
+ * bandwidth per flop). */
+QS_API int qs_fp64_fma_rate(double *fma_per_s);
+
 /* Number of kernels this library has launched in the process so far (all
  * handles).  No reference counterpart: instrumentation for benchmarks. */
 QS_API int64_t qs_launch_count(void);

@@ -379,6 +379,13 @@ int qs_lanczos_ritz_matrix(qs_lanczos* lanczos, int32_t s, qs_op* observable, co
     });
 }
 
+int qs_fp64_fma_rate(double* fma_per_s) {
+    return guard([&] {
+        if (!fma_per_s) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        *fma_per_s = qs::fp64_fma_rate();
+    });
+}
+
 int qs_block_expm(qs_op* const* ops, int32_t nblocks, int32_t pcon, const double* psi, const double* scales,
                   int32_t nscales, double tol, int32_t krylov_dim, int32_t precision, double* out, int32_t mem) {
     return guard([&] {

@@ -26,7 +26,11 @@ namespace qs {
 namespace {
 
 constexpr int kT = 256;       // threads per block
-constexpr int kJT = 4;        // vectors per dots block
+// vectors per dots block (eight measured slower than four for FP64 on GB300:
+// the dots are FP64-pipe bound, and the larger tile needs twice the
+// registers)
+template <class A>
+__host__ __device__ constexpr int jt() { return 4; }
 constexpr int kMaxM = 256;    // largest Krylov basis of a slot
 
 // ------------------------------------------------------------ arithmetic
@@ -281,12 +285,12 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
     }
     // columns past nv repeat the last one (cached) so that every load of a row
     // is issued before the arithmetic
-    const char* col[kJT];
+    const char* col[jt<A>()];
 #pragma unroll
-    for (int q = 0; q < kJT; ++q) col[q] = V + (size_t)min(i0 + q, nv - 1) * cs;
+    for (int q = 0; q < jt<A>(); ++q) col[q] = V + (size_t)min(i0 + q, nv - 1) * cs;
     auto row = [&](const CA<A>& wv, const CA<A>* v) {
 #pragma unroll
-        for (int q = 0; q < kJT; ++q) {
+        for (int q = 0; q < jt<A>(); ++q) {
             if (i0 + q < nv) {
                 mac(re[q], v[q].re, wv.re);
                 if (CV) {
@@ -301,14 +305,14 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
             if (CV) mac(wn, wv.im, wv.im);
         }
     };
-    // real vectors: two rows per iteration, 2 (kJT + 1) loads issued before the
+    // real vectors: two rows per iteration, 2 (jt<A>() + 1) loads issued before the
     // arithmetic; complex vectors hold twice the data per row, one row at a time
     int64_t r = r0 + threadIdx.x;
     for (; !CV && r + step < r1; r += 2 * step) {
         const CA<A> w0 = ldv<A, CV>(w, r), w1 = ldv<A, CV>(w, r + step);
-        CA<A> v0[kJT], v1[kJT];
+        CA<A> v0[jt<A>()], v1[jt<A>()];
 #pragma unroll
-        for (int q = 0; q < kJT; ++q) {
+        for (int q = 0; q < jt<A>(); ++q) {
             v0[q] = ldv<A, CV>(col[q], r);
             v1[q] = ldv<A, CV>(col[q], r + step);
         }
@@ -317,9 +321,9 @@ __device__ __forceinline__ void dots_rows(const SlotDev& S, int64_t r0, int64_t 
     }
     for (; r < r1; r += step) {
         const CA<A> w0 = ldv<A, CV>(w, r);
-        CA<A> v0[kJT];
+        CA<A> v0[jt<A>()];
 #pragma unroll
-        for (int q = 0; q < kJT; ++q) v0[q] = ldv<A, CV>(col[q], r);
+        for (int q = 0; q < jt<A>(); ++q) v0[q] = ldv<A, CV>(col[q], r);
         row(w0, v0);
     }
 }
@@ -336,14 +340,14 @@ __device__ __forceinline__ double block_sum(A v, double* sh) {
     return t;
 }
 
-// Block sums of the kJT accumulators into row[(base + q) * 2 + {re, im}] for
+// Block sums of the jt<A>() accumulators into row[(base + q) * 2 + {re, im}] for
 // the vectors i0 + q < nv (row: the block's slice of the partial buffer).
 template <class A>
 __device__ __forceinline__ void dots_epilogue(A* re, A* im, bool cv, int i0, int nv, int base, double* row) {
-    __shared__ double sh[kT / 32][2 * kJT];
+    __shared__ double sh[kT / 32][2 * jt<A>()];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int q = 0; q < kJT; ++q) {
+    for (int q = 0; q < jt<A>(); ++q) {
         for (int o = 16; o > 0; o >>= 1) {
             re[q] = add(re[q], shfl(re[q], o));
             if (cv) im[q] = add(im[q], shfl(im[q], o));
@@ -354,7 +358,7 @@ __device__ __forceinline__ void dots_epilogue(A* re, A* im, bool cv, int i0, int
         }
     }
     __syncthreads();
-    if (threadIdx.x < 2 * kJT) {
+    if (threadIdx.x < 2 * jt<A>()) {
         double t = 0;
         for (int q = 0; q < kT / 32; ++q) t += sh[q][threadIdx.x];
         const int q = threadIdx.x / 2;
@@ -381,14 +385,14 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_do
         nv = S.j + 1;
         w = colp<A>(S, S.j + 1);
     }
-    const int i0 = first + blockIdx.y * kJT;
+    const int i0 = first + blockIdx.y * jt<A>();
     if (i0 >= nv) return;
     const bool want_wn = mode == 0 && S.orth == 1 && blockIdx.y == 0;
     const int64_t lb = blockIdx.x - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
-    A re[kJT], im[kJT], wn = zero<A>();
+    A re[jt<A>()], im[jt<A>()], wn = zero<A>();
 #pragma unroll
-    for (int q = 0; q < kJT; ++q) re[q] = im[q] = zero<A>();
+    for (int q = 0; q < jt<A>(); ++q) re[q] = im[q] = zero<A>();
     if (S.cv) dots_rows<A, true>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
     else dots_rows<A, false>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
     dots_epilogue<A>(re, im, S.cv, i0, nv, mode == 2 ? 0 : i0, partial + (size_t)blockIdx.x * P * 2);
@@ -597,10 +601,10 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_up
         // the second pass
         const void* w = colp<A>(S, S.j + 1);
         double* row = partial + (size_t)blockIdx.x * P * 2;
-        for (int c0 = 0; c0 < nv; c0 += kJT) {
-            A re[kJT], im[kJT], dummy = zero<A>();
+        for (int c0 = 0; c0 < nv; c0 += jt<A>()) {
+            A re[jt<A>()], im[jt<A>()], dummy = zero<A>();
 #pragma unroll
-            for (int q = 0; q < kJT; ++q) re[q] = im[q] = zero<A>();
+            for (int q = 0; q < jt<A>(); ++q) re[q] = im[q] = zero<A>();
             if (S.cv) dots_rows<A, true>(S, r0, r1, c0, nv, w, re, im, false, dummy);
             else dots_rows<A, false>(S, r0, r1, c0, nv, w, re, im, false, dummy);
             dots_epilogue<A>(re, im, S.cv, c0, nv, c0, row);
@@ -689,14 +693,67 @@ __device__ __forceinline__ void rotate_rows(const SlotDev& S, int64_t r0, int64_
     }
 }
 
+// The same rotation when p <= PT: a row's p outputs stay in registers while
+// its inputs stream past once (PT multiply-adds per load), then go straight
+// into V (every input of the row has been read by then), then the carry copy.
+template <class A, bool CV, int PT>
+__device__ __forceinline__ void rotate_rows_tile(const SlotDev& S, int64_t r0, int64_t r1) {
+    char* V = (char*)S.V;
+    const size_t cs = (size_t)S.n * vbytes<A, CV>();
+    const CA<A>* __restrict__ Y = (const CA<A>*)S.y;
+    const int nin = S.rot_in, p = S.p;
+    const bool yreal = S.yreal;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        A ar[PT], ai[PT];
+#pragma unroll
+        for (int c = 0; c < PT; ++c) ar[c] = ai[c] = zero<A>();
+        auto fold = [&](const CA<A>& v, int i) {
+#pragma unroll
+            for (int c = 0; c < PT; ++c) {
+                if (c < p) {
+                    const CA<A> y = Y[(size_t)c * nin + i];
+                    mac(ar[c], v.re, y.re);
+                    if (CV) mac(ai[c], v.im, y.re);
+                    if (!yreal) {
+                        msub(ar[c], v.im, y.im);
+                        if (CV) mac(ai[c], v.re, y.im);
+                    }
+                }
+            }
+        };
+        int i = 0;
+        for (; i + 2 <= nin; i += 2) {
+            const CA<A> v0 = ldv<A, CV>(V + (size_t)i * cs, r), v1 = ldv<A, CV>(V + (size_t)(i + 1) * cs, r);
+            fold(v0, i);
+            fold(v1, i + 1);
+        }
+        if (i < nin) fold(ldv<A, CV>(V + (size_t)i * cs, r), i);
+#pragma unroll
+        for (int c = 0; c < PT; ++c)
+            if (c < p) stv<A, CV>(V + (size_t)(S.out0 + c) * cs, r, CA<A>{ar[c], ai[c]});
+        if (S.carry >= 0) stv<A, CV>(V + (size_t)S.cdst * cs, r, ldv<A, CV>(V + (size_t)S.carry * cs, r));
+    }
+}
+
 template <class A>
-__global__ void __launch_bounds__(kT, 4) eng_rotate(const SlotDev* __restrict__ sl, const int* __restrict__ rmap) {
+__global__ void __launch_bounds__(kT, 2) eng_rotate(const SlotDev* __restrict__ sl, const int* __restrict__ rmap) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
     if (S.state != kSlotRotate) return;
     const int64_t lb = blockIdx.x - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
-    if (S.cv) rotate_rows<A, true>(S, r0, r1);
-    else rotate_rows<A, false>(S, r0, r1);
+    if (S.p <= 8) {
+        if (S.cv) rotate_rows_tile<A, true, 8>(S, r0, r1);
+        else rotate_rows_tile<A, false, 8>(S, r0, r1);
+    } else if (!std::is_same<A, DF>::value && S.p <= 16) {
+        // (double-float accumulators for 16 outputs would not fit in registers)
+        if constexpr (!std::is_same<A, DF>::value) {
+            if (S.cv) rotate_rows_tile<A, true, 16>(S, r0, r1);
+            else rotate_rows_tile<A, false, 16>(S, r0, r1);
+        }
+    } else {
+        if (S.cv) rotate_rows<A, true>(S, r0, r1);
+        else rotate_rows<A, false>(S, r0, r1);
+    }
 }
 
 // Runs f with a value of the step arithmetic's type for storage st.
@@ -964,7 +1021,7 @@ void Engine::sync_table() {
 template <class A>
 static int launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const int* sm, double* pa, const void* rsq,
                          int nrb, int nsb, int mmax, int dmax, bool cgs, int ns, cudaStream_t s) {
-    const dim3 gd(nrb, (dmax + kJT - 1) / kJT);
+    const dim3 gd(nrb, (dmax + jt<A>() - 1) / jt<A>());
     eng_spmv<A><<<nsb, kT, 0, s>>>(ds, sm, rsq);
     eng_dots<A><<<gd, kT, 0, s>>>(ds, rm, mmax, 0, pa);
     eng_reduce<<<dim3(ns, dmax + 1), kT, 0, s>>>(ds, mmax, 0, pa, dmax);

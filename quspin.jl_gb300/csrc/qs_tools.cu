@@ -393,3 +393,54 @@ void block_expm(const std::vector<Op*>& ops, bool pcon, const double* psi, const
 }
 
 }  // namespace qs
+
+namespace qs {
+namespace {
+
+// Eight independent FP64 FMA chains per thread; the result is written so the
+// chains are not removed.
+__global__ void __launch_bounds__(256) fma_probe_kernel(double* __restrict__ out, double a, double b, int iters) {
+    double x[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) x[u] = threadIdx.x + u;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x[u] = fma(x[u], a, b);
+    }
+    double t = 0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) t += x[u];
+    out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = t;
+}
+
+}  // namespace
+
+double fp64_fma_rate() {
+    int dev = 0, sms = 152;
+    QS_CUDA(cudaGetDevice(&dev));
+    QS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    DevBuf out((size_t)blocks * threads * sizeof(double));
+    cudaStream_t s = nullptr;
+    QS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    QS_CUDA(cudaEventCreate(&e0));
+    QS_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+        QS_CUDA(cudaEventRecord(e0, s));
+        fma_probe_kernel<<<blocks, threads, 0, s>>>(out.as<double>(), 0.999999, 1e-7, iters);
+        QS_CUDA(cudaEventRecord(e1, s));
+        QS_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        QS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        best = std::min(best, ms);
+    }
+    note_launches(3);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    return (double)blocks * threads * 8 * iters / (best * 1e-3);
+}
+
+}  // namespace qs

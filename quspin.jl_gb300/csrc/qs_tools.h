@@ -46,4 +46,8 @@ void lanczos_ritz_matrix(LanczosSet& L, int s, Op& obs, const double* Y, int nv,
 void block_expm(const std::vector<Op*>& ops, bool pcon, const double* psi, const std::vector<cd>& scales, double tol,
                 int krylov_dim, int precision, double* out, bool device);
 
+// This GPU's FP64 fused multiply-add throughput (FMA/s): eight independent
+// chains per thread over a full grid, best of three CUDA-event timings.
+double fp64_fma_rate();
+
 }  // namespace qs
