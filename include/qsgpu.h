@@ -68,6 +68,27 @@ typedef struct {
     int32_t zBblock;
 } qs_basis_spec;
 
+/* SpinBasisGeneral(L; nup, pauli, block_order, blocks...) for spin 1/2
+ * (src/basis.jl:282-337, 455-600): nmaps symmetry blocks (map, quantum
+ * number) in intersection order.  maps[i * L + b] is the 0-based target site
+ * of source site b under map i, flips[i * L + b] = 1 where that site's spin is
+ * flipped (a negative entry of the reference's map); the map's order is the
+ * lcm of its cycle lengths (doubled for a cycle with an odd number of flips)
+ * and its eigenvalue cis(2 pi mod(q, order) / order). */
+typedef struct {
+    int32_t L;
+    int32_t nup;              /* -1: not given */
+    int32_t pauli;
+    int32_t nmaps;
+    const int32_t *maps;      /* nmaps x L */
+    const int32_t *flips;     /* nmaps x L */
+    const int32_t *qnums;     /* nmaps */
+} qs_general_spec;
+
+/* Columns are the symmetric orbit states in ascending orbit minimum, each
+ * anchored (real positive) at its minimum, which is its state label; L <= 32. */
+QS_API int qs_basis_create_general(const qs_general_spec *spec, qs_basis **out);
+
 /* Replaces SpinBasis1D(L; ...) (src/basis.jl:622-777): enumerates the sector on
  * the device, keeps one representative per symmetric orbit and orders columns
  * as the reference's projector does (ascending orbit minimum). */

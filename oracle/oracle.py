@@ -45,6 +45,9 @@ def lib():
         i64 = ctypes.c_int64
         L.ora_basis_create.argtypes = [ctypes.c_int] * 11 + [ctypes.POINTER(P), ctypes.c_char_p, ctypes.c_int]
         L.ora_basis_create.restype = ctypes.c_int
+        L.ora_basis_create_general.argtypes = [ctypes.c_int] * 4 + [P, P, P, ctypes.POINTER(P), ctypes.c_char_p,
+                                                                     ctypes.c_int]
+        L.ora_basis_create_general.restype = ctypes.c_int
         L.ora_basis_free.argtypes = [P]
         for name in ("ora_basis_size", "ora_basis_parent_size", "ora_basis_projector_nnz"):
             getattr(L, name).argtypes = [P]
@@ -166,12 +169,21 @@ class RefBasis:
     """SpinBasis1D built with the reference algorithm (explicit projector)."""
 
     def __init__(self, L, nup=None, pauli=True, a=1, kblock=None, pblock=None, zblock=None,
-                 pzblock=None, zAblock=None, zBblock=None):
+                 pzblock=None, zAblock=None, zBblock=None, _general=None):
         lb = lib()
         h = ctypes.c_void_p()
         err = ctypes.create_string_buffer(256)
-        rc = lb.ora_basis_create(*_sym_args(L, nup, pauli, a, kblock, pblock, zblock, pzblock, zAblock,
-                                            zBblock), ctypes.byref(h), err, 256)
+        if _general is not None:
+            perms, flips, qnums = _general
+            n = len(qnums)
+            pa = np.ascontiguousarray(np.asarray(perms, dtype=np.int32).reshape(-1) if n else np.zeros(1, np.int32))
+            fa = np.ascontiguousarray(np.asarray(flips, dtype=np.int32).reshape(-1) if n else np.zeros(1, np.int32))
+            qa = np.ascontiguousarray(np.asarray(qnums, dtype=np.int32) if n else np.zeros(1, np.int32))
+            rc = lb.ora_basis_create_general(int(L), -1 if nup is None else int(nup), int(bool(pauli)), n, _ptr(pa),
+                                             _ptr(fa), _ptr(qa), ctypes.byref(h), err, 256)
+        else:
+            rc = lb.ora_basis_create(*_sym_args(L, nup, pauli, a, kblock, pblock, zblock, pzblock, zAblock,
+                                                zBblock), ctypes.byref(h), err, 256)
         if rc != 0:
             raise OracleError(err.value.decode())
         self._h = h
@@ -259,6 +271,41 @@ class RefBasis:
             e[j] = 1
             out[:, j] = self.qlo_matvec(terms, e, diag=diag, extract=extract)
         return out
+
+
+def normalize_general_map(values, L):
+    """Restates _normalize_general_spin_map (src/basis.jl:282-303): a map is
+    zero-based when it holds a zero or a negative entry; a negative entry
+    flips that site's spin.  Returns (0-based targets, flip flags)."""
+    values = [int(v) for v in values]
+    if len(values) != L:
+        raise OracleError("a general symmetry map must contain one entry per site")
+    zero_based = any(v == 0 for v in values) or any(v < 0 for v in values)
+    perm, flips = [], []
+    for v in values:
+        if zero_based:
+            perm.append(v + 1 if v >= 0 else -v)
+        else:
+            if v == 0:
+                raise OracleError("one-based symmetry maps cannot contain zero")
+            perm.append(abs(v))
+        flips.append(1 if v < 0 else 0)
+    if sorted(perm) != list(range(1, L + 1)):
+        raise OracleError("a general symmetry map must be a site permutation")
+    return [p - 1 for p in perm], flips
+
+
+def general_basis(L, nup=None, pauli=True, blocks=()):
+    """SpinBasisGeneral(L; nup, pauli, blocks...) built with the reference's
+    projector algorithm (src/basis.jl:455-600): blocks is a list of
+    (map, quantum number) in intersection order."""
+    perms, flips, qnums = [], [], []
+    for m, q in blocks:
+        p, f = normalize_general_map(m, L)
+        perms.append(p)
+        flips.append(f)
+        qnums.append(int(q))
+    return RefBasis(L, nup=nup, pauli=pauli, _general=(perms, flips, qnums))
 
 
 class RepBasis:

@@ -289,9 +289,20 @@ static inline uint64_t brev_L(uint64_t s, int L) {
 
 /* Symmetry generators in the order the reference applies them
  * (basis.jl:691-735): translation first, then p, z, pz, zA, zB. */
-enum { G_T = 0, G_P, G_Z, G_PZ, G_ZA, G_ZB };
-typedef struct { int kind; int L, a; uint64_t full, odd, even; } xform_t;
+enum { G_T = 0, G_P, G_Z, G_PZ, G_ZA, G_ZB, G_GEN };
+/* G_GEN: a general site map (_general_spin_transform, src/basis.jl:325-337):
+ * source site b goes to perm[b], its spin flipped where flips has bit b. */
+typedef struct { int kind; int L, a; uint64_t full, odd, even; int perm[64]; uint64_t flips; } xform_t;
 static uint64_t xform_apply(const xform_t *x, uint64_t s) {
+    if (x->kind == G_GEN) {
+        uint64_t t = 0;
+        for (int b = 0; b < x->L; ++b) {
+            int occupied = (int)((s >> b) & 1ULL);
+            if ((x->flips >> b) & 1ULL) occupied = !occupied;
+            if (occupied) t |= 1ULL << x->perm[b];
+        }
+        return t;
+    }
     switch (x->kind) {
     case G_T: return rotl_L(s, x->L, x->a);
     case G_P: return brev_L(s, x->L);
@@ -498,6 +509,8 @@ static int cmp_state_idx(const void *x, const void *y) {
     return a < c ? -1 : (a > c);
 }
 
+static int finish_reduced(ora_basis *b, csc_t P, ora_basis **out, char *err, int errlen);
+
 /* sym[0..5] = {has_k? k : unused, p, z, pz, zA, zB} with 0 meaning "not given". */
 ORA_EXPORT int ora_basis_create(int L, int nup, int pauli, int a, int has_k, int k,
                                 int p, int z, int pz, int za, int zb,
@@ -558,6 +571,12 @@ ORA_EXPORT int ora_basis_create(int L, int nup, int pauli, int a, int has_k, int
         }
         if (rc) { if (haveP) csc_free(&P); ora_basis_free(b); return rc; }
     }
+    return finish_reduced(b, P, out, err, errlen);
+}
+
+/* The reduced basis from its projector: argmax representatives in column
+ * order and the row -> column map (src/symmetry_basis.jl:215-255). */
+static int finish_reduced(ora_basis *b, csc_t P, ora_basis **out, char *err, int errlen) {
     if (P.n == 0) { csc_free(&P); ora_basis_free(b); set_err(err, errlen, "the requested symmetry sector is empty"); return -4; }
     b->reduced = 1;
     b->P = P;
@@ -583,6 +602,61 @@ ORA_EXPORT int ora_basis_create(int L, int nup, int pauli, int a, int has_k, int
     qsort(b->sorted_idx, b->n, sizeof(int64_t), cmp_state_idx);
     *out = b;
     return 0;
+}
+
+/* SpinBasisGeneral (src/basis.jl:455-600) for spin 1/2: nmaps blocks in
+ * intersection order; perms[i * L + b] is the 0-based target of source site b,
+ * flips[i * L + b] marks a flipped spin.  Order and eigenvalue as
+ * _general_spin_map_order (src/basis.jl:305-323) and cis(2 pi mod(q, order) / order). */
+ORA_EXPORT int ora_basis_create_general(int L, int nup, int pauli, int nmaps, const int *perms, const int *flips,
+                                        const int *qnums, ora_basis **out, char *err, int errlen) {
+    *out = NULL;
+    if (L < 1 || L > 40) { set_err(err, errlen, "L outside the oracle's range"); return -1; }
+    if (nup >= 0 && nup > L) { set_err(err, errlen, "nup must lie between 0 and L"); return -1; }
+    ora_basis *b = (ora_basis *)calloc(1, sizeof(ora_basis));
+    b->L = L; b->nup = nup; b->pauli = pauli;
+    if (nup < 0 && L > 26) { free(b); set_err(err, errlen, "parent sector too large for the oracle"); return -1; }
+    if (nup >= 0 && binom_i64(L, nup) > 40000000) { free(b); set_err(err, errlen, "parent sector too large for the oracle"); return -1; }
+    if (enumerate_parent(L, nup, &b->parent, &b->n_parent)) { free(b); set_err(err, errlen, "allocation failed"); return -1; }
+    if (nmaps == 0) {
+        b->reduced = 0;
+        b->n = b->n_parent;
+        b->states = (uint64_t *)malloc(sizeof(uint64_t) * b->n);
+        memcpy(b->states, b->parent, sizeof(uint64_t) * b->n);
+        *out = b; return 0;
+    }
+    csc_t P; memset(&P, 0, sizeof(P));
+    for (int i = 0; i < nmaps; ++i) {
+        xform_t xf; memset(&xf, 0, sizeof(xf));
+        xf.kind = G_GEN; xf.L = L;
+        for (int s = 0; s < L; ++s) {
+            xf.perm[s] = perms[i * L + s];
+            if (flips[i * L + s]) xf.flips |= 1ULL << s;
+        }
+        long order = 1;
+        char seen[64] = {0};
+        for (int st = 0; st < L; ++st) {
+            if (seen[st]) continue;
+            int len = 0, par = 0, cur = st;
+            while (!seen[cur]) { seen[cur] = 1; ++len; par ^= (int)((xf.flips >> cur) & 1ULL); cur = xf.perm[cur]; }
+            long c = par ? 2L * len : (long)len, a = order, bb = c;
+            while (bb) { long t = a % bb; a = bb; bb = t; }
+            order = order / a * c;
+        }
+        long q = ((long)qnums[i] % order + order) % order;
+        double arg = 2 * M_PI * (double)q / (double)order;
+        cx eig = mkc(cos(arg), sin(arg));
+        int rc;
+        if (i == 0) {
+            rc = cyclic_projector(&P, b->parent, b->n_parent, &xf, eig, err, errlen);
+        } else {
+            csc_t Q;
+            rc = intersect_eigenspace(&Q, &P, b->parent, b->n_parent, &xf, eig, err, errlen);
+            if (!rc) { csc_free(&P); P = Q; }
+        }
+        if (rc) { csc_free(&P); ora_basis_free(b); return rc; }
+    }
+    return finish_reduced(b, P, out, err, errlen);
 }
 
 ORA_EXPORT int64_t ora_basis_size(const ora_basis *b) { return b->n; }

@@ -150,6 +150,127 @@ int64_t binom_host(int n, int k) {
 
 }  // namespace
 
+// ------------------------------------------------- general site maps
+namespace {
+
+// One element of a group of general site maps: t = perm(s) ^ mask, with its
+// character; keyed, like Elem, by the images of 0 and of every single bit.
+struct GElem {
+    std::vector<int> perm;
+    uint64_t mask = 0;
+    cplx chi = cx(1.0, 0.0);
+    std::vector<uint64_t> img;
+};
+
+uint64_t gelem_apply(const GElem& e, uint64_t s, int L) {
+    uint64_t r = 0;
+    for (int b = 0; b < L; ++b)
+        if ((s >> b) & 1ull) r |= 1ull << e.perm[b];
+    return r ^ e.mask;
+}
+
+void gelem_fill(GElem& e, int L) {
+    e.img.resize(L + 1);
+    e.img[0] = gelem_apply(e, 0, L);
+    for (int b = 0; b < L; ++b) e.img[b + 1] = gelem_apply(e, 1ull << b, L);
+}
+
+// e2 o e1 (e1 first)
+GElem gelem_compose(const GElem& e2, const GElem& e1, int L) {
+    GElem r;
+    r.perm.resize(L);
+    uint64_t pm = 0;
+    for (int b = 0; b < L; ++b) {
+        r.perm[b] = e2.perm[e1.perm[b]];
+        if ((e1.mask >> b) & 1ull) pm |= 1ull << e2.perm[b];
+    }
+    r.mask = pm ^ e2.mask;
+    r.chi = cx_mul(e1.chi, e2.chi);
+    gelem_fill(r, L);
+    return r;
+}
+
+GElem gelem_identity(int L) {
+    GElem e;
+    e.perm.resize(L);
+    for (int b = 0; b < L; ++b) e.perm[b] = b;
+    gelem_fill(e, L);
+    return e;
+}
+
+struct GClosure {
+    std::vector<GElem> elems;
+    std::map<std::vector<uint64_t>, int> index;
+};
+
+// Closure of the generators; false when the characters contradict each other
+// (the sector is then empty).
+bool close_general(const std::vector<GElem>& gens, int L, GClosure& C) {
+    GElem id = gelem_identity(L);
+    C.elems.push_back(id);
+    C.index[id.img] = 0;
+    for (size_t i = 0; i < C.elems.size(); ++i) {
+        for (const GElem& g : gens) {
+            GElem c = gelem_compose(g, C.elems[i], L);
+            auto it = C.index.find(c.img);
+            if (it != C.index.end()) {
+                const cplx a = C.elems[it->second].chi;
+                if (std::fabs(a.re - c.chi.re) > 1e-9 || std::fabs(a.im - c.chi.im) > 1e-9) return false;
+                continue;
+            }
+            if ((int)C.elems.size() >= kMaxGroup) throw Error(QS_ERR_UNSUPPORTED, "symmetry group too large");
+            C.index[c.img] = (int)C.elems.size();
+            C.elems.push_back(c);
+        }
+    }
+    return true;
+}
+
+// GroupDesc of a general group: elements grouped by permutation, one set of
+// byte tables per distinct permutation (appended to `tables`).
+void fill_desc_general(GroupDesc& d, const GClosure& C, int L, std::vector<uint64_t>& tables,
+                       std::vector<std::vector<int>>* perms = nullptr) {
+    std::memset(&d, 0, sizeof(d));
+    d.L = L;
+    d.lmask = low_mask(L);
+    d.general = 1;
+    d.nbytes = (L + 7) / 8;
+    std::vector<int> order(C.elems.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return C.elems[a].perm < C.elems[b].perm; });
+    d.ng = (int)order.size();
+    d.real_chars = 1;
+    const std::vector<int>* prev = nullptr;
+    tables.clear();
+    for (int k = 0; k < d.ng; ++k) {
+        const GElem& e = C.elems[order[k]];
+        if (!prev || *prev != e.perm) {
+            if (d.nperm >= kMaxPerm) throw Error(QS_ERR_UNSUPPORTED, "symmetry group has too many site permutations");
+            d.perm_begin[d.nperm] = (int16_t)k;
+            d.nperm++;
+            prev = &e.perm;
+            if (perms) perms->push_back(e.perm);
+            for (int byte = 0; byte < 8; ++byte)
+                for (int v = 0; v < 256; ++v) {
+                    uint64_t img = 0;
+                    for (int i = 0; i < 8; ++i) {
+                        const int b = 8 * byte + i;
+                        if (b < L && ((v >> i) & 1)) img |= 1ull << e.perm[b];
+                    }
+                    tables.push_back(img);
+                }
+        }
+        d.mask[k] = e.mask;
+        d.chi_re[k] = e.chi.re;
+        d.chi_im[k] = e.chi.im;
+        if (std::fabs(e.chi.im) > 1e-12) d.real_chars = 0;
+    }
+    d.perm_begin[d.nperm] = (int16_t)d.ng;
+}
+
+}  // namespace
+
 // ------------------------------------------------------------ enumeration
 namespace {
 
@@ -167,7 +288,8 @@ __device__ __forceinline__ int is_rep(const GroupSmem& g, const int8_t* chi_one,
     base[1] = brev_bits(s, L);
     int stab = 0;
     for (int p = 0; p < g.nperm; ++p) {
-        U r = rotl_bits<U>(base[g.refl[p]], g.shift[p], L, m);
+        U r = g.general ? (U)gperm_apply(g.gtab, p, g.nbytes, (uint64_t)s)
+                        : rotl_bits<U>(base[g.refl[p]], g.shift[p], L, m);
         const int e1 = g.begin[p + 1];
         for (int e = g.begin[p]; e < e1; ++e) {
             U c = r ^ (U)g.mask[e];
@@ -580,6 +702,178 @@ void basis_build(Basis& b) {
     else enumerate_sector<uint32_t>(b, d_chi_one);
 }
 
+// ------------------------------------------------- basis_build_general
+void basis_build_general(Basis& b, const qs_general_spec& gs) {
+    const int L = gs.L;
+    if (L < 1 || L > 32) throw Error(QS_ERR_UNSUPPORTED, "general symmetry maps are supported for L <= 32");
+    if (gs.nup < -1 || gs.nup > L) throw Error(QS_ERR_ARGUMENT, "nup must lie between 0 and L");
+    if (gs.nmaps < 0 || (gs.nmaps > 0 && (!gs.maps || !gs.flips || !gs.qnums)))
+        throw Error(QS_ERR_ARGUMENT, "general symmetry blocks must be (map, quantum_number)");
+    std::memset(&b.spec, 0, sizeof(b.spec));
+    b.spec.L = L;
+    b.spec.nup = gs.nup;
+    b.spec.pauli = gs.pauli;
+    b.spec.a = 1;
+    b.L = L;
+    b.nup = gs.nup;
+    b.wide = false;
+    b.general = true;
+    b.symmetric = gs.nmaps > 0;
+    b.n_parent = b.nup >= 0 ? binom_host(L, b.nup) : (int64_t)1 << L;
+    std::vector<GElem> gens;
+    b.gens.clear();
+    for (int i = 0; i < gs.nmaps; ++i) {
+        GElem g;
+        g.perm.resize(L);
+        std::vector<char> seen(L, 0);
+        uint64_t flips = 0;
+        for (int src = 0; src < L; ++src) {
+            const int t = gs.maps[(size_t)i * L + src];
+            if (t < 0 || t >= L || seen[t]) throw Error(QS_ERR_ARGUMENT, "a general symmetry map must be a site permutation");
+            seen[t] = 1;
+            g.perm[src] = t;
+            if (gs.flips[(size_t)i * L + src]) flips |= 1ull << src;
+        }
+        for (int src = 0; src < L; ++src)
+            if ((flips >> src) & 1ull) g.mask |= 1ull << g.perm[src];
+        if (b.nup >= 0 && flips != 0 && !(__builtin_popcountll(flips) == L && 2 * b.nup == L))
+            throw Error(QS_ERR_ARGUMENT, "symmetry transformation leaves the selected particle sector");
+        // order: lcm of the cycle lengths, a cycle with an odd number of flips counting twice
+        // (src/basis.jl:305-323)
+        int64_t order = 1;
+        std::vector<char> vis(L, 0);
+        for (int st = 0; st < L; ++st) {
+            if (vis[st]) continue;
+            int len = 0, parity = 0, cur = st;
+            while (!vis[cur]) {
+                vis[cur] = 1;
+                ++len;
+                parity ^= (int)((flips >> cur) & 1ull);
+                cur = g.perm[cur];
+            }
+            const int64_t c = parity ? 2 * len : len;
+            int64_t a = order, bb = c;
+            while (bb) {
+                const int64_t t = a % bb;
+                a = bb;
+                bb = t;
+            }
+            order = order / a * c;
+        }
+        if (order > 63) throw Error(QS_ERR_UNSUPPORTED, "symmetry map order above 63");
+        const int64_t q = ((int64_t)gs.qnums[i] % order + order) % order;
+        const double th = 2.0 * M_PI * (double)q / (double)order;
+        g.chi = cx(std::cos(th), std::sin(th));
+        gelem_fill(g, L);
+        gens.push_back(g);
+        Generator G;
+        G.kind = GEN_GENERAL;
+        G.shift = 0;
+        G.refl = 0;
+        G.mask = g.mask;
+        G.eig = g.chi;
+        G.order = (int)order;
+        G.perm = g.perm;
+        b.gens.push_back(G);
+    }
+    GClosure C;
+    if (!close_general(gens, L, C)) throw Error(QS_ERR_ARGUMENT, "the requested symmetry sector is empty");
+    // as for the 1D generators, every later map must permute the columns of
+    // the earlier ones and keep their character (the reference's
+    // permutation-like intersection, src/symmetry_basis.jl:116-198)
+    for (size_t lvl = 0; lvl + 1 < gens.size(); ++lvl) {
+        std::vector<GElem> sub(gens.begin(), gens.begin() + lvl + 1);
+        GClosure H;
+        if (!close_general(sub, L, H)) throw Error(QS_ERR_ARGUMENT, "the requested symmetry sector is empty");
+        const GElem& g = gens[lvl + 1];
+        GElem ginv = gelem_identity(L);
+        for (int k = 1; k < b.gens[lvl + 1].order; ++k) ginv = gelem_compose(g, ginv, L);
+        for (const GElem& h : H.elems) {
+            GElem c = gelem_compose(g, gelem_compose(h, ginv, L), L);
+            auto it = H.index.find(c.img);
+            bool ok = it != H.index.end();
+            if (ok) {
+                const cplx a = h.chi, bb = H.elems[it->second].chi;
+                ok = std::fabs(a.re - bb.re) < 1e-9 && std::fabs(a.im - bb.im) < 1e-9;
+            }
+            if (!ok)
+                throw Error(QS_ERR_UNSUPPORTED,
+                            "this combination of symmetry blocks needs the reference's dense nullspace "
+                            "intersection, which this engine does not implement");
+        }
+    }
+    std::vector<uint64_t> tables;
+    std::vector<std::vector<int>> perms;
+    fill_desc_general(b.group, C, L, tables, &perms);
+    b.complex_chars = !b.group.real_chars;
+    b.gen_perm_index.clear();
+    for (const GElem& g : gens) {
+        const auto it = std::find(perms.begin(), perms.end(), g.perm);
+        b.gen_perm_index.push_back((int)(it - perms.begin()));
+    }
+    // the reference-exact column replay holds at most 32 first-generator orbits
+    // per column: the later generators' cycle lengths multiply to at most that
+    int64_t leaves = 1;
+    for (size_t l = 1; l < b.gens.size(); ++l) leaves *= b.gens[l].order;
+    b.replay = b.symmetric && (int)b.gens.size() <= kMaxGens && leaves <= (1 << (kMaxGens - 1));
+    std::vector<std::vector<uint64_t>> level_tables;
+    b.level_groups.clear();
+    if (b.replay) {
+        for (size_t lvl = 0; lvl < gens.size(); ++lvl) {
+            std::vector<GElem> sub(gens.begin(), gens.begin() + lvl + 1);
+            GClosure H;
+            close_general(sub, L, H);
+            GroupDesc d;
+            std::vector<uint64_t> t;
+            fill_desc_general(d, H, L, t);
+            b.level_groups.push_back(d);
+            level_tables.push_back(std::move(t));
+        }
+        // level-0 coefficient table of the first map, as for the 1D generators
+        b.level0_table.assign(64 * 64, cx(0, 0));
+        const Generator& g0 = b.gens[0];
+        for (int n = 1; n <= std::min(g0.order, 63); ++n) {
+            if (g0.order % n) continue;
+            cplx c[64];
+            c[0] = cx(1.0, 0.0);
+            for (int j = 1; j < n; ++j) c[j] = cx_div(cx_mul(c[j - 1], cx(1.0, 0.0)), g0.eig);
+            double nrm = norm2_short(c, n);
+            for (int j = 0; j < n; ++j) b.level0_table[n * 64 + j] = cx_divr(c[j], nrm);
+        }
+    }
+    // device work
+    QS_CUDA(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
+    std::vector<uint64_t> binom(64 * 65, 0);
+    for (int n = 0; n < 64; ++n)
+        for (int k = 0; k <= 64; ++k) binom[n * 65 + k] = (uint64_t)binom_host(n, k);
+    b.d_binom.alloc(binom.size() * sizeof(uint64_t));
+    QS_CUDA(cudaMemcpy(b.d_binom.p, binom.data(), binom.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    b.d_gtab.alloc(std::max<size_t>(1, tables.size()) * sizeof(uint64_t));
+    if (!tables.empty())
+        QS_CUDA(cudaMemcpy(b.d_gtab.p, tables.data(), tables.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    b.group.gtab = b.d_gtab.as<uint64_t>();
+    b.d_level_gtab.clear();
+    for (size_t lvl = 0; lvl < level_tables.size(); ++lvl) {
+        b.d_level_gtab.emplace_back(level_tables[lvl].size() * sizeof(uint64_t));
+        QS_CUDA(cudaMemcpy(b.d_level_gtab.back().p, level_tables[lvl].data(), level_tables[lvl].size() * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice));
+        b.level_groups[lvl].gtab = b.d_level_gtab.back().as<uint64_t>();
+    }
+    b.d_group.alloc(sizeof(GroupDesc));
+    QS_CUDA(cudaMemcpy(b.d_group.p, &b.group, sizeof(GroupDesc), cudaMemcpyHostToDevice));
+    b.fast = FastGroup{};
+    if (!b.symmetric) {
+        b.n = b.n_parent;
+        return;
+    }
+    std::vector<int8_t> chi_one(kMaxGroup, 0);
+    for (int e = 0; e < b.group.ng; ++e)
+        chi_one[e] = (std::fabs(b.group.chi_re[e] - 1.0) < 1e-9 && std::fabs(b.group.chi_im[e]) < 1e-9) ? 1 : 0;
+    DevBuf d_chi_one(kMaxGroup);
+    QS_CUDA(cudaMemcpy(d_chi_one.p, chi_one.data(), kMaxGroup, cudaMemcpyHostToDevice));
+    enumerate_sector<uint32_t>(b, d_chi_one);
+}
+
 // ------------------------------------------------------------- index_of
 namespace {
 
@@ -643,6 +937,11 @@ struct ReplayCtx {
     int shift[kMaxGens];
     uint64_t mask[kMaxGens];
     double eig_re[kMaxGens];
+    double eig_im[kMaxGens];   // 0 for every 1D generator after the first
+    // general site maps: generator l is permutation gidx[l] of the group's tables
+    int general, nbytes;
+    const uint64_t* gtab;
+    int gidx[kMaxGens];
 };
 
 __host__ __device__ inline uint64_t brev_any(uint64_t x, int L) {
@@ -654,6 +953,7 @@ __host__ __device__ inline uint64_t brev_any(uint64_t x, int L) {
 }
 
 __host__ __device__ inline uint64_t gen_apply(const ReplayCtx& c, int l, uint64_t s) {
+    if (c.general) return gperm_apply(c.gtab, c.gidx[l], c.nbytes, s) ^ c.mask[l];
     uint64_t r = c.refl[l] ? brev_any(s, c.L) : s;
     return rotl_bits<uint64_t>(r, c.shift[l], c.L, low_mask(c.L)) ^ c.mask[l];
 }
@@ -662,7 +962,8 @@ __host__ __device__ inline uint64_t sub_orbit_min(const GroupDesc& g, uint64_t t
     uint64_t base[2] = {t, brev_any(t, g.L)};
     uint64_t best = ~0ull;
     for (int p = 0; p < g.nperm; ++p) {
-        uint64_t r = rotl_bits<uint64_t>(base[g.perm_refl[p]], g.perm_shift[p], g.L, g.lmask);
+        uint64_t r = g.general ? gperm_apply(g.gtab, p, g.nbytes, t)
+                               : rotl_bits<uint64_t>(base[g.perm_refl[p]], g.perm_shift[p], g.L, g.lmask);
         for (int e = g.perm_begin[p]; e < g.perm_begin[p + 1]; ++e) {
             uint64_t v = r ^ g.mask[e];
             if (v < best) best = v;
@@ -698,7 +999,7 @@ __host__ __device__ inline int find_ent(const REnt* a, int n, uint64_t s) {
 __host__ __device__ int replay_column(const ReplayCtx& c, uint64_t a, REnt* buf, REnt* tmp) {
     constexpr int kLeaves = 1 << (kMaxGens - 1);
     uint64_t anc[kMaxGens][kLeaves];
-    int8_t two[kMaxGens][kLeaves];
+    int8_t cyc[kMaxGens][kLeaves];   // cycle length of each level-l column's join (1: fixed)
     int cnt[kMaxGens];
     int off[kLeaves + 1], len[kLeaves];
     const int m = c.m;
@@ -707,11 +1008,17 @@ __host__ __device__ int replay_column(const ReplayCtx& c, uint64_t a, REnt* buf,
     for (int l = m - 1; l >= 1; --l) {
         int k = 0;
         for (int i = 0; i < cnt[l]; ++i) {
-            uint64_t x = anc[l][i];
-            anc[l - 1][k++] = x;
-            uint64_t a1 = sub_orbit_min(c.levels[l - 1], gen_apply(c, l, x));
-            two[l][i] = (a1 != x);
-            if (a1 != x) anc[l - 1][k++] = a1;
+            // the columns x, min g(x), min g(min g(x)), ... up to the return to x
+            const uint64_t x = anc[l][i];
+            uint64_t y = x;
+            int d = 0;
+            do {
+                if (k >= kLeaves) return -1;   // the host keeps trees within kLeaves
+                anc[l - 1][k++] = y;
+                ++d;
+                y = sub_orbit_min(c.levels[l - 1], gen_apply(c, l, y));
+            } while (y != x && d < 64);
+            cyc[l][i] = (int8_t)d;
         }
         cnt[l - 1] = k;
     }
@@ -723,8 +1030,7 @@ __host__ __device__ int replay_column(const ReplayCtx& c, uint64_t a, REnt* buf,
         do {
             seg[n].s = u;
             ++n;
-            uint64_t r = c.g0_refl ? brev_any(u, c.L) : u;
-            u = rotl_bits<uint64_t>(r, c.g0_shift, c.L, low_mask(c.L)) ^ c.g0_mask;
+            u = gen_apply(c, 0, u);
         } while (u != anc[0][i] && n < 64);
         for (int j = 0; j < n; ++j) {
             cplx v = c.table0[n * 64 + j];
@@ -738,55 +1044,71 @@ __host__ __device__ int replay_column(const ReplayCtx& c, uint64_t a, REnt* buf,
     }
     for (int l = 1; l < m; ++l) {
         int j = 0;
-        cplx e = cx(c.eig_re[l], 0.0);
+        const cplx e = cx(c.eig_re[l], c.eig_im[l]);
         for (int i = 0; i < cnt[l]; ++i) {
+            const int d = cyc[l][i];
             REnt* A = buf + off[j];
-            int n0 = len[j];
-            int o0 = off[j];
-            ++j;
-            if (!two[l][i]) {
+            const int n0 = len[j];
+            const int o0 = off[j];
+            if (d == 1) {
                 // fixed column: one-element orbit, coefficient 1, norm 1
                 for (int q = 0; q < n0; ++q) {
                     cplx v = cx_mul(cx(A[q].re, A[q].im), cx(1.0, 0.0));
                     A[q].re = v.re;
                     A[q].im = v.im;
                 }
+                ++j;
                 off[i] = o0;
                 len[i] = n0;
                 continue;
             }
-            REnt* B = buf + off[j];
-            int n1 = len[j];
-            ++j;
-            // phi = (P' S P)[c', c], accumulated over the rows of c in ascending order
-            cplx phi = cx(0, 0);
-            for (int q = 0; q < n0; ++q) {
-                int k = find_ent(B, n1, gen_apply(c, l, A[q].s));
-                cplx pr = k >= 0 ? cx(B[k].re, B[k].im) : cx(0, 0);
-                cplx prod = cx_mul(cx_conj(pr), cx(A[q].re, A[q].im));
-                phi = (q == 0) ? prod : cx_add(phi, prod);
-            }
-            cplx coef[2];
+            // coef_0 = 1, coef_k = coef_(k-1) ph_(k-1) / e with ph_k = (P' S P)[C_(k+1), C_k]
+            // accumulated over the rows of C_k in ascending order
+            // (src/symmetry_basis.jl:116-198, the permutation-like branch)
+            cplx coef[64];
             coef[0] = cx(1.0, 0.0);
-            coef[1] = cx_div(cx_mul(coef[0], phi), e);
-            double nu = norm2_short(coef, 2);
-            cplx r0 = cx_divr(coef[0], nu), r1 = cx_divr(coef[1], nu);
-            for (int q = 0; q < n0; ++q) {
-                cplx v = cx_mul(cx(A[q].re, A[q].im), r0);
-                A[q].re = v.re; A[q].im = v.im;
+            for (int k = 0; k + 1 < d; ++k) {
+                const REnt* Ck = buf + off[j + k];
+                const int nk = len[j + k];
+                const REnt* Cn = buf + off[j + k + 1];
+                const int nn = len[j + k + 1];
+                cplx phi = cx(0, 0);
+                for (int q = 0; q < nk; ++q) {
+                    int kk = find_ent(Cn, nn, gen_apply(c, l, Ck[q].s));
+                    cplx pr = kk >= 0 ? cx(Cn[kk].re, Cn[kk].im) : cx(0, 0);
+                    cplx prod = cx_mul(cx_conj(pr), cx(Ck[q].re, Ck[q].im));
+                    phi = (q == 0) ? prod : cx_add(phi, prod);
+                }
+                coef[k + 1] = cx_div(cx_mul(coef[k], phi), e);
             }
-            for (int q = 0; q < n1; ++q) {
-                cplx v = cx_mul(cx(B[q].re, B[q].im), r1);
-                B[q].re = v.re; B[q].im = v.im;
+            const double nu = norm2_short(coef, d);
+            int total = 0;
+            for (int k = 0; k < d; ++k) {
+                REnt* Ck = buf + off[j + k];
+                const cplx r = cx_divr(coef[k], nu);
+                for (int q = 0; q < len[j + k]; ++q) {
+                    cplx v = cx_mul(cx(Ck[q].re, Ck[q].im), r);
+                    Ck[q].re = v.re;
+                    Ck[q].im = v.im;
+                }
+                total += len[j + k];
             }
-            int x = 0, y = 0, k = 0;
-            while (x < n0 || y < n1) {
-                if (y >= n1 || (x < n0 && A[x].s < B[y].s)) tmp[k++] = A[x++];
-                else tmp[k++] = B[y++];
+            // merge the d sorted segments (contiguous from o0) by state
+            int head[64];
+            for (int k = 0; k < d; ++k) head[k] = 0;
+            for (int q = 0; q < total; ++q) {
+                int best = -1;
+                for (int k = 0; k < d; ++k) {
+                    if (head[k] >= len[j + k]) continue;
+                    if (best < 0 || buf[off[j + k] + head[k]].s < buf[off[j + best] + head[best]].s) best = k;
+                }
+                tmp[q] = buf[off[j + best] + head[best]];
+                ++head[best];
             }
-            for (int q = 0; q < k; ++q) A[q] = tmp[q];
+            for (int q = 0; q < total; ++q) A[q] = tmp[q];
+            j += d;
             off[i] = o0;
-            len[i] = k;
+            len[i] = total;
         }
     }
     return len[0];
@@ -983,6 +1305,132 @@ __global__ void embed_kernel(EmbedArgs a) {
     }
 }
 
+// Bases of general site maps carry no replay: a column is the orbit state of
+// its minimum m, P[s, col] = sqrt(stab / |G|) chi(g) for the element g taking
+// s to m (real positive at m), as the reference's cyclic projector and
+// permutation-like intersections anchor it.
+struct GenArgs {
+    const GroupDesc* group;
+    const void* reps;
+    const void* split;
+    int64_t n, nsplit, stride;
+    int L, nup, pcon;
+    const uint64_t* binom;
+    // queries
+    const uint64_t* q;
+    int64_t nq;
+    uint64_t* rep;
+    double* norm;
+    double* amp;
+    int32_t* status;
+    // projections: mode 0 out += P in (per row), mode 1 out = P^H in (per column)
+    int mode;
+    int64_t rows;
+    const double2* in;
+    double2* out;
+    int ncols;
+    int64_t in_ld, out_ld;
+};
+
+template <typename U>
+__device__ __forceinline__ bool gen_column(const GroupSmem& g, const GenArgs& a, U s, int64_t& col, double2& amp) {
+    U m;
+    int bidx, stab;
+    orbit_min<U>(g, s, m, bidx, stab);
+    col = rank_search<U>((const U*)a.reps, a.n, (const U*)a.split, (int)a.nsplit, a.stride, m);
+    if (col < 0) return false;
+    const double w = sqrt((double)stab / (double)g.ng);
+    amp = make_double2(w * a.group->chi_re[bidx], w * a.group->chi_im[bidx]);
+    return true;
+}
+
+template <typename U>
+__global__ void gen_query_kernel(GenArgs a) {
+    __shared__ GroupSmem g;
+    load_group_smem(g, a.group);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.nq; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t s64 = a.q[i];
+        a.rep[i] = 0;
+        a.norm[i] = 0;
+        a.amp[2 * i] = a.amp[2 * i + 1] = 0;
+        if ((s64 & ~low_mask(a.L)) != 0 || (a.nup >= 0 && __popcll(s64) != a.nup)) {
+            a.status[i] = 1;
+            continue;
+        }
+        U m;
+        int bidx, stab;
+        orbit_min<U>(g, (U)s64, m, bidx, stab);
+        int64_t col;
+        double2 v;
+        if (!gen_column<U>(g, a, (U)s64, col, v)) {
+            a.status[i] = 2;
+            continue;
+        }
+        a.rep[i] = (uint64_t)m;
+        a.amp[2 * i] = v.x;
+        a.amp[2 * i + 1] = v.y;
+        a.norm[i] = 1.0 / (v.x * v.x + v.y * v.y);
+        a.status[i] = 0;
+    }
+}
+
+// mode 0: one thread per row of the projection space
+template <typename U>
+__global__ void gen_from_kernel(GenArgs a) {
+    __shared__ GroupSmem g;
+    load_group_smem(g, a.group);
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.rows; r += (int64_t)gridDim.x * blockDim.x) {
+        U s;
+        if (a.pcon) {
+            s = a.nup >= 0 ? unrank_fixed<U>(r, a.L, a.nup, a.binom, 65) : (U)r;
+        } else {
+            if (a.nup >= 0 && __popcll((unsigned long long)r) != a.nup) continue;
+            s = (U)r;
+        }
+        int64_t col;
+        double2 v;
+        if (!gen_column<U>(g, a, s, col, v)) continue;
+        for (int c = 0; c < a.ncols; ++c) {
+            const double2 x = a.in[(size_t)c * a.in_ld + col];
+            double2* o = a.out + (size_t)c * a.out_ld + r;
+            double2 y = *o;
+            y.x += v.x * x.x - v.y * x.y;
+            y.y += v.x * x.y + v.y * x.x;
+            *o = y;
+        }
+    }
+}
+
+// mode 1: one thread per column, summing over every group element (each orbit
+// state is reached stab times) and dividing by stab
+template <typename U>
+__global__ void gen_to_kernel(GenArgs a, const uint16_t* __restrict__ stabs) {
+    __shared__ GroupSmem g;
+    load_group_smem(g, a.group);
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < a.n; j += (int64_t)gridDim.x * blockDim.x) {
+        const U m = ((const U*)a.reps)[j];
+        const double st = (double)stabs[j];
+        const double w = sqrt(st / (double)g.ng) / st;
+        for (int c = 0; c < a.ncols; ++c) {
+            double ar = 0, ai = 0;
+            for (int p = 0; p < g.nperm; ++p) {
+                const U rp = (U)gperm_apply(g.gtab, p, g.nbytes, (uint64_t)m);
+                for (int e = g.begin[p]; e < g.begin[p + 1]; ++e) {
+                    const U t = rp ^ (U)g.mask[e];
+                    int64_t row = (int64_t)t;
+                    if (a.pcon && a.nup >= 0) row = combinadic_rank<U>(t, a.binom, 65);
+                    const double2 x = a.in[(size_t)c * a.in_ld + row];
+                    // conj(P[t, j]) = w chi(e), e taking m to t
+                    const double cr = a.group->chi_re[e], ci = a.group->chi_im[e];
+                    ar += cr * x.x - ci * x.y;
+                    ai += cr * x.y + ci * x.x;
+                }
+            }
+            a.out[(size_t)c * a.out_ld + j] = make_double2(w * ar, w * ai);
+        }
+    }
+}
+
 ReplayCtx make_ctx(const Basis& b, const DevBuf& lv, const DevBuf& t0) {
     ReplayCtx c{};
     c.levels = lv.as<GroupDesc>();
@@ -999,6 +1447,13 @@ ReplayCtx make_ctx(const Basis& b, const DevBuf& lv, const DevBuf& t0) {
         c.shift[l] = b.gens[l].shift;
         c.mask[l] = b.gens[l].mask;
         c.eig_re[l] = b.gens[l].eig.re;
+        c.eig_im[l] = l == 0 ? 0.0 : b.gens[l].eig.im;
+    }
+    c.general = b.general;
+    if (b.general) {
+        c.nbytes = b.group.nbytes;
+        c.gtab = b.group.gtab;
+        for (int l = 0; l < c.m; ++l) c.gidx[l] = b.gen_perm_index[l];
     }
     return c;
 }
@@ -1028,6 +1483,14 @@ void basis_compute_refrep(Basis& b) {
     b.h_refrep.resize(b.n);
     if (!b.symmetric) {
         b.refrep_ready = true;  // states are computed directly by qs_basis_states
+        return;
+    }
+    if (b.general && !b.replay) {
+        // without the replay a general basis labels each column by its orbit minimum
+        std::vector<uint32_t> tmp(b.n);
+        QS_CUDA(cudaMemcpy(tmp.data(), b.d_reps.p, b.n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < b.n; ++i) b.h_refrep[i] = tmp[i];
+        b.refrep_ready = true;
         return;
     }
     upload_replay(b);
@@ -1094,6 +1557,34 @@ void basis_representative(Basis& b, const uint64_t* states, int64_t n, uint64_t*
             amps[2 * i + 1] = 0.0;
             status[i] = 0;
         }
+        return;
+    }
+    if (b.general && !b.replay) {
+        DevBuf dq(n * sizeof(uint64_t)), drep(n * sizeof(uint64_t)), dnorm(n * sizeof(double)),
+            damp(2 * n * sizeof(double)), dst(n * sizeof(int32_t));
+        QS_CUDA(cudaMemcpyAsync(dq.p, states, n * sizeof(uint64_t), cudaMemcpyHostToDevice, b.stream));
+        GenArgs a{};
+        a.group = b.d_group.as<GroupDesc>();
+        a.reps = b.d_reps.p;
+        a.split = b.d_split.p;
+        a.n = b.n;
+        a.nsplit = b.nsplit;
+        a.stride = b.split_stride;
+        a.L = b.L;
+        a.nup = b.nup;
+        a.q = dq.as<uint64_t>();
+        a.nq = n;
+        a.rep = drep.as<uint64_t>();
+        a.norm = dnorm.as<double>();
+        a.amp = damp.as<double>();
+        a.status = dst.as<int32_t>();
+        gen_query_kernel<uint32_t><<<grid_for(n, 128), 128, 0, b.stream>>>(a);
+        QS_CUDA(cudaGetLastError());
+        QS_CUDA(cudaMemcpyAsync(reps, drep.p, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, b.stream));
+        QS_CUDA(cudaMemcpyAsync(norms, dnorm.p, n * sizeof(double), cudaMemcpyDeviceToHost, b.stream));
+        QS_CUDA(cudaMemcpyAsync(amps, damp.p, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, b.stream));
+        QS_CUDA(cudaMemcpyAsync(status, dst.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, b.stream));
+        QS_CUDA(cudaStreamSynchronize(b.stream));
         return;
     }
     basis_compute_refrep(b);
@@ -1177,6 +1668,35 @@ void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out,
         const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((rows + 255) / 256, 152 * 16));
         if (b.wide) embed_kernel<uint64_t><<<grid, 256, 0, s>>>(e);
         else embed_kernel<uint32_t><<<grid, 256, 0, s>>>(e);
+        QS_CUDA(cudaGetLastError());
+        note_launches(1);
+        if (!device) QS_CUDA(cudaMemcpyAsync(out, pout, (size_t)nout * sizeof(double2), cudaMemcpyDeviceToHost, s));
+        QS_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
+    if (b.general && !b.replay) {
+        GenArgs g{};
+        g.group = b.d_group.as<GroupDesc>();
+        g.reps = b.d_reps.p;
+        g.split = b.d_split.p;
+        g.n = b.n;
+        g.nsplit = b.nsplit;
+        g.stride = b.split_stride;
+        g.L = b.L;
+        g.nup = b.nup;
+        g.pcon = pcon;
+        g.binom = b.d_binom.as<uint64_t>();
+        g.mode = mode;
+        g.rows = rows;
+        g.in = pin;
+        g.out = pout;
+        g.ncols = ncols;
+        g.in_ld = nin1;
+        g.out_ld = nout1;
+        const int64_t work = mode == 0 ? rows : b.n;
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 127) / 128, 152 * 32));
+        if (mode == 0) gen_from_kernel<uint32_t><<<grid, 128, 0, s>>>(g);
+        else gen_to_kernel<uint32_t><<<grid, 128, 0, s>>>(g, b.d_stab.as<uint16_t>());
         QS_CUDA(cudaGetLastError());
         note_launches(1);
         if (!device) QS_CUDA(cudaMemcpyAsync(out, pout, (size_t)nout * sizeof(double2), cudaMemcpyDeviceToHost, s));

@@ -85,6 +85,21 @@ void qs_basis_destroy(qs_basis* basis) { delete basis; }
 
 int64_t qs_basis_size(const qs_basis* basis) { return basis ? basis->b.n : -1; }
 
+int qs_basis_create_general(const qs_general_spec* spec, qs_basis** out) {
+    return guard([&] {
+        if (!spec || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        *out = nullptr;
+        qs_basis* h = new qs_basis();
+        try {
+            qs::basis_build_general(h->b, *spec);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
 int qs_basis_requires_complex(const qs_basis* basis) { return basis && basis->b.complex_chars ? 1 : 0; }
 
 int32_t qs_basis_group_order(const qs_basis* basis) { return basis ? basis->b.group.ng : 0; }

@@ -36,7 +36,21 @@ struct GroupDesc {
     uint64_t mask[kMaxGroup];
     double chi_re[kMaxGroup];
     double chi_im[kMaxGroup];
+    // general site permutations (SpinBasisGeneral): permutation p maps the
+    // state through gtab[(p * 8 + k) * 256 + byte k of the state], OR-ed over
+    // the nbytes bytes; perm_refl / perm_shift are unused then
+    int32_t general;
+    int32_t nbytes;
+    const uint64_t* gtab;
 };
+
+// The image of t under general permutation p (tables of a GroupDesc).
+QS_HD uint64_t gperm_apply(const uint64_t* tab, int p, int nbytes, uint64_t t) {
+    uint64_t r = 0;
+    const uint64_t* base = tab + (size_t)p * 8 * 256;
+    for (int k = 0; k < nbytes; ++k) r |= base[k * 256 + ((t >> (8 * k)) & 255u)];
+    return r;
+}
 
 // One transition program: the operator string of one coupling, ops applied in
 // array order, sites as 0-based bit positions.  When all sites are distinct the

@@ -14,6 +14,8 @@ namespace qs {
 // characters stay in global memory: only the winning element's is read).
 struct GroupSmem {
     int32_t L, ng, nperm;
+    int32_t general, nbytes;
+    const uint64_t* gtab;
     uint64_t lmask;
     int8_t refl[kMaxPerm];
     int8_t shift[kMaxPerm];
@@ -27,6 +29,9 @@ __device__ __forceinline__ void load_group_smem(GroupSmem& s, const GroupDesc* _
         s.ng = g->ng;
         s.nperm = g->nperm;
         s.lmask = g->lmask;
+        s.general = g->general;
+        s.nbytes = g->nbytes;
+        s.gtab = g->gtab;
     }
     for (int i = threadIdx.x; i < g->nperm; i += blockDim.x) {
         s.refl[i] = g->perm_refl[i];
@@ -50,7 +55,8 @@ __device__ __forceinline__ void orbit_min(const GroupSmem& g, U t, U& best, int&
     bidx = 0;
     stab = 0;
     for (int p = 0; p < g.nperm; ++p) {
-        U r = rotl_bits<U>(base[g.refl[p]], g.shift[p], L, m);
+        U r = g.general ? (U)gperm_apply(g.gtab, p, g.nbytes, (uint64_t)t)
+                        : rotl_bits<U>(base[g.refl[p]], g.shift[p], L, m);
         const int e1 = g.begin[p + 1];
         for (int e = g.begin[p]; e < e1; ++e) {
             U c = r ^ (U)g.mask[e];

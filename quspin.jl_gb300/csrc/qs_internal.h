@@ -98,13 +98,17 @@ struct PoolBuf {
 };
 
 // Symmetry generator in the reference's order (src/basis.jl:691-735).
-enum GenKind { GEN_T = 0, GEN_P, GEN_Z, GEN_PZ, GEN_ZA, GEN_ZB };
+// GEN_GENERAL: a site permutation with spin flips (SpinBasisGeneral,
+// src/basis.jl:282-337, 455-600): source site b goes to perm[b], and the
+// flips become `mask` in target coordinates (t = perm(s) ^ mask).
+enum GenKind { GEN_T = 0, GEN_P, GEN_Z, GEN_PZ, GEN_ZA, GEN_ZB, GEN_GENERAL };
 struct Generator {
     int kind;
     int shift, refl;
     uint64_t mask;
     cplx eig;       // eigenvalue exactly as the reference computes it
     int order;      // cyclic order of the map (L/a for T, 2 otherwise)
+    std::vector<int> perm;   // GEN_GENERAL only
 };
 
 struct Basis {
@@ -112,6 +116,11 @@ struct Basis {
     int L = 0;
     int nup = -1;
     bool symmetric = false;
+    bool general = false;            // general site maps (GEN_GENERAL generators)
+    DevBuf d_gtab;                   // their permutation tables (GroupDesc::gtab)
+    std::vector<int> gen_perm_index; // each generator's permutation in those tables
+    std::vector<DevBuf> d_level_gtab;// the level groups' tables
+    bool replay = true;              // the projector replay covers this basis
     bool wide = false;               // states need 64 bits (L > 32)
     bool complex_chars = false;
     int64_t n = 0;
@@ -170,6 +179,8 @@ struct Op {
 
 // qs_basis.cu
 void basis_build(Basis& b);
+// SpinBasisGeneral(L; nup, pauli, blocks...) with the blocks in intersection order
+void basis_build_general(Basis& b, const qs_general_spec& gs);
 void basis_index_of(Basis& b, const uint64_t* states, int64_t n, int64_t* out);
 void basis_compute_refrep(Basis& b);
 void basis_representative(Basis& b, const uint64_t* states, int64_t n, uint64_t* reps, double* norms,

@@ -299,7 +299,8 @@ __global__ void __launch_bounds__(kMvThreads) matvec_general_kernel(MvArgs a) {
         double acc_r = 0, acc_i = 0;
         U base[2] = {s, brev_bits(s, L)};
         for (int p = 0; p < g.nperm; ++p) {
-            U rot = rotl_bits<U>(base[g.refl[p]], g.shift[p], L, lm);
+            U rot = g.general ? (U)gperm_apply(g.gtab, p, g.nbytes, (uint64_t)s)
+                              : rotl_bits<U>(base[g.refl[p]], g.shift[p], L, lm);
             for (int e = g.begin[p]; e < g.begin[p + 1]; ++e) {
                 const U tp = rot ^ (U)g.mask[e];
                 double er = G->chi_re[e], ei = a.conj_chi ? -G->chi_im[e] : G->chi_im[e];

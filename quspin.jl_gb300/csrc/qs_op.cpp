@@ -100,7 +100,8 @@ struct Canon {
     bool operator<(const Canon& o) const { return ops < o.ops; }
 };
 
-std::map<Canon, cd> canonical_set(const std::vector<Term>& terms, int L, int refl, int shift, uint64_t mask) {
+std::map<Canon, cd> canonical_set(const std::vector<Term>& terms, int L, int refl, int shift, uint64_t mask,
+                                  const std::vector<int>* perm = nullptr) {
     std::map<Canon, cd> out;
     for (const Term& t : terms)
         for (const Coupling& c : t.couplings) {
@@ -110,6 +111,7 @@ std::map<Canon, cd> canonical_set(const std::vector<Term>& terms, int L, int ref
                 int b = c.sites[i] - 1;
                 int nb = refl ? (L - 1 - b) : b;
                 nb = ((nb + shift) % L + L) % L;
+                if (perm) nb = (*perm)[b];   // a general site map
                 char ch = t.op[i];
                 if ((mask >> nb) & 1ull) {
                     if (ch == '+') ch = '-';
@@ -144,7 +146,7 @@ bool commutes_with_group(const Basis& b, const std::vector<Term>& terms) {
     if (!b.symmetric) return true;
     auto base = canonical_set(terms, b.L, 0, 0, 0);
     for (const Generator& g : b.gens) {
-        auto img = canonical_set(terms, b.L, g.refl, g.shift, g.mask);
+        auto img = canonical_set(terms, b.L, g.refl, g.shift, g.mask, g.kind == GEN_GENERAL ? &g.perm : nullptr);
         if (!same_sets(base, img)) return false;
     }
     return true;

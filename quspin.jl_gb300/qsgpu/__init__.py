@@ -5,7 +5,7 @@ This package is the host-side mirror of the reference's Julia interface over the
 C ABI of libqsgpu (include/qsgpu.h).  Every compute call runs on the GPU; there
 is no CPU fallback.
 """
-from .basis import (SpinBasis1D, get_amp, get_vec, int_to_state, normalization, project_from, project_to,
+from .basis import (SpinBasis1D, SpinBasisGeneral, get_amp, get_vec, int_to_state, normalization, project_from, project_to,
                     representative, state_at, state_index, state_to_int, states)
 from .errors import ArgumentError, DimensionMismatch, ErrorException, UnsupportedError
 from .operators import (ExpmMultiplyParallel, Hamiltonian, OperatorTerm, QuantumLinearOperator, apply, eigsh,
@@ -18,7 +18,7 @@ from .tools import (LanczosRows, expm_lanczos, ftlm_static_iteration, lanczos_ba
                     lin_comb_Q_T, ltlm_static_iteration)
 
 __all__ = [
-    "SpinBasis1D", "states", "state_index", "state_at", "representative", "normalization", "get_amp",
+    "SpinBasis1D", "SpinBasisGeneral", "states", "state_index", "state_at", "representative", "normalization", "get_amp",
     "int_to_state", "state_to_int", "project_from", "project_to", "get_vec", "OperatorTerm", "QuantumLinearOperator", "Hamiltonian", "eigsh", "eigsh_batch", "evolve",
     "ExpmMultiplyParallel", "expm_multiply_parallel", "apply", "set_a", "isquantum_LinearOperator",
     "ArgumentError", "DimensionMismatch", "ErrorException", "UnsupportedError", "Server",

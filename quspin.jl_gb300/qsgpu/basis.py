@@ -10,7 +10,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .errors import ArgumentError, DimensionMismatch
+from .errors import ArgumentError, DimensionMismatch, UnsupportedError
 
 
 def basis_spec(L, nup=None, Nup=None, m=None, S="1/2", pauli=True, a=1, kblock=None, pblock=None, zblock=None,
@@ -235,3 +235,84 @@ def project_to(basis, vector, sparse=False, pcon=False):
     """project_to(basis, vector; sparse, pcon) (src/discrete_basis.jl:2455-2475):
     P^H v, from the full space (or parent sector) to the sector."""
     return _maybe_sparse(_projection(basis, vector, pcon, 1), sparse)
+
+
+def _normalize_general_map(values, L):
+    """_normalize_general_spin_map (src/basis.jl:282-303): a map holding a zero
+    or a negative entry is zero-based; a negative entry flips that site's spin.
+    Returns 0-based targets and flip flags."""
+    values = [int(v) for v in values]
+    if len(values) != L:
+        raise ArgumentError("a general symmetry map must contain one entry per site")
+    zero_based = any(v == 0 for v in values) or any(v < 0 for v in values)
+    perm, flips = [], []
+    for v in values:
+        if zero_based:
+            perm.append(v + 1 if v >= 0 else -v)
+        else:
+            if v == 0:
+                raise ArgumentError("one-based symmetry maps cannot contain zero")
+            perm.append(abs(v))
+        flips.append(1 if v < 0 else 0)
+    if sorted(perm) != list(range(1, L + 1)):
+        raise ArgumentError("a general symmetry map must be a site permutation")
+    return [p - 1 for p in perm], flips
+
+
+class SpinBasisGeneral(SpinBasis1D):
+    """SpinBasisGeneral(L; nup, Nup, m, S, pauli, block_order, blocks...)
+    (src/basis.jl:455-600) for spin 1/2 and L <= 32: each block is
+    (map, quantum_number) with map a site permutation (negative entries flip
+    the spin), intersected in block_order (default: keyword order).  Columns
+    are the symmetric orbit states in ascending orbit minimum, labelled by
+    that minimum (the reference's argmax representative up to ties)."""
+
+    def __init__(self, L, nup=None, Nup=None, m=None, S="1/2", pauli=True, block_order=None, make_basis=True,
+                 Ns_block_est=None, **blocks):
+        if str(S) not in ("1/2", "0.5"):
+            raise UnsupportedError("SpinBasisGeneral is implemented for spin 1/2")
+        if nup is not None and Nup is not None:
+            raise ArgumentError("specify only one of nup and Nup")
+        sel = nup if nup is not None else Nup
+        if m is not None:
+            if sel is not None:
+                raise ArgumentError("m cannot be combined with nup or Nup")
+            sel = int(round((float(m) + 0.5) * L))
+        if sel is not None and not 0 <= int(sel) <= L:
+            raise ArgumentError("nup must lie between 0 and L")
+        names = list(blocks) if block_order is None else [str(n) for n in block_order]
+        for n in blocks:
+            if n not in names:
+                names.append(n)
+        if any(n not in blocks for n in names):
+            raise ArgumentError("block_order refers to an unknown symmetry block")
+        perms, flips, qnums = [], [], []
+        for n in names:
+            spec = blocks[n]
+            if not isinstance(spec, (tuple, list)) or len(spec) < 2:
+                raise ArgumentError("general symmetry blocks must be (map, quantum_number)")
+            p, f = _normalize_general_map(spec[0], int(L))
+            perms += p
+            flips += f
+            qnums.append(int(spec[1]))
+        k = len(qnums)
+        pa = np.ascontiguousarray(perms if k else [0], dtype=np.int32)
+        fa = np.ascontiguousarray(flips if k else [0], dtype=np.int32)
+        qa = np.ascontiguousarray(qnums if k else [0], dtype=np.int32)
+        spec = _lib.GeneralSpec(int(L), -1 if sel is None else int(sel), int(bool(pauli)), k, _lib.ptr(pa),
+                                _lib.ptr(fa), _lib.ptr(qa))
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(lib.qs_basis_create_general(ctypes.byref(spec), ctypes.byref(h)))
+        self._h = h
+        self.L = int(L)
+        self.nup = None if sel is None else int(sel)
+        self.pauli = bool(pauli)
+        self.Ns = int(lib.qs_basis_size(h))
+        self.group_order = int(lib.qs_basis_group_order(h))
+        self.requires_complex = bool(lib.qs_basis_requires_complex(h))
+        self.blocks = {"nup": self.nup, "pauli": self.pauli}
+        self.blocks.update({n: (tuple(blocks[n][0]), int(blocks[n][1])) for n in names})
+        self.block_order = names
+        self.symmetric = k > 0
+        self._states = None

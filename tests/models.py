@@ -41,3 +41,34 @@ def seeded(n, seed=20261203, complex_=False):
     if complex_:
         v = v + 1j * rng.standard_normal(n)
     return v
+
+
+def torus_maps(Lx, Ly):
+    """Site maps of an Lx x Ly periodic square lattice, site = x + Lx y
+    (0-based targets, as SpinBasisGeneral's zero-based maps): translations,
+    the x reflection, and the spin flip (negative entries, -(target + 1))."""
+    def site(x, y):
+        return (x % Lx) + Lx * (y % Ly)
+    sites = [(x, y) for y in range(Ly) for x in range(Lx)]
+    Tx = [site(x + 1, y) for x, y in sites]
+    Ty = [site(x, y + 1) for x, y in sites]
+    Px = [site(Lx - 1 - x, y) for x, y in sites]
+    Z = [-(i + 1) for i in range(Lx * Ly)]
+    return Tx, Ty, Px, Z
+
+
+def torus_heisenberg(Lx, Ly, J=1.0, Jd=0.0):
+    """Nearest-neighbour Heisenberg model on the Lx x Ly torus (one-based sites),
+    with an optional diagonal coupling Jd (both diagonals)."""
+    def site(x, y):
+        return (x % Lx) + Lx * (y % Ly) + 1
+    bonds = []
+    for y in range(Ly):
+        for x in range(Lx):
+            bonds.append((J, site(x, y), site(x + 1, y)))
+            bonds.append((J, site(x, y), site(x, y + 1)))
+            if Jd:
+                bonds.append((Jd, site(x, y), site(x + 1, y + 1)))
+                bonds.append((Jd, site(x, y), site(x + 1, y - 1)))
+    return [("+-", [(j / 2, a, b) for j, a, b in bonds]), ("-+", [(j / 2, a, b) for j, a, b in bonds]),
+            ("zz", [(j, a, b) for j, a, b in bonds])]

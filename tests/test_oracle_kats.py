@@ -156,3 +156,42 @@ def test_krylov_tools(ora, kats):
         ora.lanczos_full(lambda x: A @ x, v0, 4)
     with pytest.raises(ora.OracleError):
         ora.lanczos_full(lambda x: A @ x, np.zeros(4), 2)
+
+
+def test_general_maps_restate_the_1d_blocks(ora):
+    """SpinBasisGeneral's projector algorithm over general maps (translation,
+    reflection) gives the 1D SpinBasis1D sectors: the same projector and
+    representatives (q = 0 / 1 of an order-2 map is the block +1 / -1)."""
+    L = 8
+    T = [(i + 1) % L for i in range(L)]
+    P = [L - 1 - i for i in range(L)]
+    for k in range(L):
+        g = ora.general_basis(L, nup=4, pauli=False, blocks=[(T, k)])
+        r = ora.RefBasis(L, nup=4, pauli=False, kblock=k)
+        assert np.array_equal(g.states, r.states)
+        assert np.abs(g.projector().toarray() - r.projector().toarray()).max() == 0
+    for qk, qp, kb, pb in ((0, 0, 0, 1), (0, 1, 0, -1), (4, 0, 4, 1), (4, 1, 4, -1)):
+        g = ora.general_basis(L, nup=4, pauli=False, blocks=[(T, qk), (P, qp)])
+        r = ora.RefBasis(L, nup=4, pauli=False, kblock=kb, pblock=pb)
+        assert np.array_equal(g.states, r.states)
+        assert np.abs(g.projector().toarray() - r.projector().toarray()).max() < 1e-15
+
+
+def test_general_columns_are_anchored_orbit_states(ora):
+    """On a 4 x 3 torus with (kx, ky, flip) blocks, every column of the
+    reference projector is an orbit state: uniform magnitude, real positive
+    at its orbit minimum, columns in ascending orbit minimum."""
+    import models
+    Tx, Ty, Px, Z = models.torus_maps(4, 3)
+    for qx, qy, qz in ((0, 0, 0), (1, 0, 1), (2, 1, 0), (3, 2, 1)):
+        g = ora.general_basis(12, nup=6, pauli=False, blocks=[(Tx, qx), (Ty, qy), (Z, qz)])
+        P = g.projector().tocsc()
+        P.sort_indices()
+        mins = []
+        for j in range(P.shape[1]):
+            rows = P.indices[P.indptr[j]:P.indptr[j + 1]]
+            vals = P.data[P.indptr[j]:P.indptr[j + 1]]
+            assert np.allclose(np.abs(vals), np.abs(vals[0]), rtol=1e-13, atol=0)
+            assert abs(vals[0].imag) < 1e-13 and vals[0].real > 0          # rows ascending: first = orbit minimum
+            mins.append(int(g.parent_states[rows[0]]))
+        assert mins == sorted(mins)
