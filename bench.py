@@ -513,6 +513,51 @@ def section_blocks(qs, torch, L=24, nt=10):
             "max_state_diff_batched_vs_sequential": err, "norm_drift": drift}
 
 
+def torus_blocks(Lx, Ly):
+    """Site maps of the Lx x Ly torus (site = x + Lx y, zero-based): the two
+    translations, the x reflection and the spin flip (negative entries)."""
+    site = lambda x, y: (x % Lx) + Lx * (y % Ly)  # noqa: E731
+    sites = [(x, y) for y in range(Ly) for x in range(Lx)]
+    return ([site(x + 1, y) for x, y in sites], [site(x, y + 1) for x, y in sites],
+            [site(Lx - 1 - x, y) for x, y in sites], [-(i + 1) for i in range(Lx * Ly)])
+
+
+def section_general(qs, torch, Lx=6, Ly=5, J2=0.5):
+    """SpinBasisGeneral on a 2D lattice: the J1-J2 square lattice on the 6 x 5
+    torus (L = 30, nup = 15, 155,117,520 parent states), sector k = (0, 0),
+    x reflection even, spin flip even; basis build, assembly and the Lanczos
+    ground state (k = 1, tol 1e-10) in FP64 and double-float."""
+    L = Lx * Ly
+    Tx, Ty, Px, Z = torus_blocks(Lx, Ly)
+    site = lambda x, y: (x % Lx) + Lx * (y % Ly) + 1  # noqa: E731
+    bonds = []
+    for y in range(Ly):
+        for x in range(Lx):
+            bonds += [(1.0, site(x, y), site(x + 1, y)), (1.0, site(x, y), site(x, y + 1)),
+                      (J2, site(x, y), site(x + 1, y + 1)), (J2, site(x, y), site(x + 1, y - 1))]
+    terms = [qs.OperatorTerm("+-", [(j / 2, a, b) for j, a, b in bonds]),
+             qs.OperatorTerm("-+", [(j / 2, a, b) for j, a, b in bonds]),
+             qs.OperatorTerm("zz", [(j, a, b) for j, a, b in bonds])]
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    b = qs.SpinBasisGeneral(L, nup=L // 2, pauli=False, Tx=(Tx, 0), Ty=(Ty, 0), Px=(Px, 0), Z=(Z, 0))
+    t_basis = time.perf_counter() - t
+    t = time.perf_counter()
+    H = qs.Hamiltonian(b, terms)
+    t_asm = time.perf_counter() - t
+    out = {"workload": "J1-J2 square lattice %dx%d torus (J2=%.1f), nup=%d, k=(0,0), Px=+1, Z=+1: %d states, "
+                       "nnz=%d" % (Lx, Ly, J2, L // 2, b.Ns, H.nnz),
+           "basis_build_s": t_basis, "assemble_s": t_asm, "group_order": b.group_order}
+    for prec in ("fp64", "fp64df"):
+        qs.eigsh(H, k=1, which="SA", tol=1e-10, return_eigenvectors=False, precision=prec)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        e0 = qs.eigsh(H, k=1, which="SA", tol=1e-10, return_eigenvectors=False, precision=prec)[0]
+        out["lanczos_s_" + prec] = time.perf_counter() - t
+        out["e0_per_site_" + prec] = float(e0) / L
+    return out
+
+
 def serving_requests(n_req, rate, seed=20261203):
     """The served mix: Poisson arrivals, L uniform in {18, 20, ..., 30}, nup
     uniform in [L/2-2, L/2], kblock uniform in [0, L), 70 % eigsh k=1 (tol
@@ -830,6 +875,7 @@ def run_ours(args, wl, world, rank, local):
                          ("c3_tfim_L30_evolve", lambda: section_c3(qs, torch)),
                          ("ftlm_L26", lambda: section_ftlm(qs, torch)),
                          ("blocks_L24_evolve", lambda: section_blocks(qs, torch)),
+                         ("general_6x5_torus", lambda: section_general(qs, torch)),
                          ("c5_serving", lambda: section_c5(qs, torch, n_req=args.serve_requests))):
             try:
                 sections[name] = fn()
