@@ -300,6 +300,17 @@ QS_API int qs_expm_multiply(qs_op *op, const double *a, const double *v, double 
 QS_API int qs_evolve(qs_op *op, const double *v0, double t0, const double *times, int32_t nt, int32_t imag_time,
               double tol, int32_t krylov_dim, int32_t precision, double *out);
 
+/* The Krylov exponential on a matrix: out[:, c, i] = exp(scales[i] A) V[:, c]
+ * (src/operators.jl:1895-1949 _krylov_expmv_times / _krylov_expmv on a
+ * matrix; apply(ExpmMultiplyParallel, V) and evolve(H, V0, t0, times) with a
+ * matrix of start states).  V: Ns x ncol complex column-major; scales:
+ * nscales complex; out: Ns x ncol x nscales complex.  Every column's
+ * recursion runs on one batched engine; normalise = 1 scales every state to
+ * norm 1 (evolve in imaginary time).  mem applies to V and out. */
+QS_API int qs_expm_columns(qs_op *op, const double *V, int32_t ncol, const double *scales, int32_t nscales,
+                           double tol, int32_t krylov_dim, int32_t precision, int32_t normalise, double *out,
+                           int32_t mem);
+
 /* ------------------------------------------------------------ Krylov tools */
 
 /* Lanczos bases held on the device: the recurrences of tools.jl's

@@ -394,6 +394,18 @@ int qs_lanczos_ritz_matrix(qs_lanczos* lanczos, int32_t s, qs_op* observable, co
     });
 }
 
+int qs_expm_columns(qs_op* op, const double* V, int32_t ncol, const double* scales, int32_t nscales, double tol,
+                    int32_t krylov_dim, int32_t precision, int32_t normalise, double* out, int32_t mem) {
+    return guard([&] {
+        if (!op || !V || !scales || !out) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        if (krylov_dim < 1) throw qs::Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
+        std::vector<std::complex<double>> sc(std::max(0, nscales));
+        for (int i = 0; i < nscales; ++i) sc[i] = {scales[2 * i], scales[2 * i + 1]};
+        qs::expm_columns(*op->op, V, ncol, sc, tol > 0 ? tol : 1e-12, krylov_dim, precision, normalise != 0, out,
+                         mem == QS_MEM_DEVICE);
+    });
+}
+
 int qs_fp64_fma_rate(double* fma_per_s) {
     return guard([&] {
         if (!fma_per_s) throw qs::Error(QS_ERR_ARGUMENT, "null argument");

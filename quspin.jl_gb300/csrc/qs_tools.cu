@@ -339,6 +339,54 @@ void lanczos_ritz_matrix(LanczosSet& L, int s, Op& obs, const double* Y, int nv,
     }
 }
 
+void expm_columns(Op& op, const double* V, int ncol, const std::vector<cd>& scales, double tol, int krylov_dim,
+                  int precision, bool normalise, double* out, bool device) {
+    if (ncol < 1 || scales.empty()) throw Error(QS_ERR_ARGUMENT, "at least one column and one scale are required");
+    const int64_t n = op.basis->n;
+    const int nt = (int)scales.size();
+    cudaStream_t st = op.stream;
+    const size_t col_bytes = (size_t)n * 16;
+    PoolBuf dV;
+    const double* v = V;
+    if (!device) {
+        dV.alloc(col_bytes * ncol, st);
+        QS_CUDA(cudaMemcpyAsync(dV.p, V, dV.bytes, cudaMemcpyHostToDevice, st));
+        QS_CUDA(cudaStreamSynchronize(st));
+        v = dV.as<double>();
+    }
+    // columns in waves whose Krylov slots fit in half the free memory
+    size_t fr = 0, tot = 0;
+    QS_CUDA(cudaMemGetInfo(&fr, &tot));
+    const int m = (int)std::max<int64_t>(2, std::min<int64_t>(krylov_dim, n));
+    const size_t per = Engine::slot_bytes(n, m, true, 1, precision == 0 ? Store::F64 : Store::DF) + col_bytes * nt;
+    const int wave = (int)std::max<size_t>(1, std::min<size_t>(ncol, (fr / 2) / std::max<size_t>(per, 1)));
+    for (int c0 = 0; c0 < ncol; c0 += wave) {
+        const int c1 = std::min(ncol, c0 + wave);
+        PoolBuf states(col_bytes * nt * (c1 - c0), st);
+        std::vector<Op*> ops(c1 - c0, &op);
+        std::vector<const double*> v0s;
+        std::vector<double*> outs;
+        for (int c = c0; c < c1; ++c) {
+            v0s.push_back(v + (size_t)c * n * 2);
+            outs.push_back(states.as<double>() + (size_t)(c - c0) * n * 2 * nt);
+        }
+        evolve_blocks(ops, v0s, scales, tol, krylov_dim, precision, outs);
+        Blas B(VKind::C128, n, st);
+        for (int c = c0; c < c1; ++c)
+            for (int i = 0; i < nt; ++i) {
+                double* src = outs[c - c0] + (size_t)i * n * 2;
+                if (normalise) {
+                    const double nr = B.norm(src);
+                    if (nr > 0) B.scale(src, src, cd(1.0 / nr, 0));
+                }
+                double* dst = out + ((size_t)i * ncol + c) * n * 2;   // out[:, c, i]
+                QS_CUDA(cudaMemcpyAsync(dst, src, col_bytes, device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                        st));
+            }
+        QS_CUDA(cudaStreamSynchronize(st));
+    }
+}
+
 void block_expm(const std::vector<Op*>& ops, bool pcon, const double* psi, const std::vector<cd>& scales, double tol,
                 int krylov_dim, int precision, double* out, bool device) {
     if (ops.empty()) throw Error(QS_ERR_ARGUMENT, "at least one block is required");

@@ -38,6 +38,14 @@ void lanczos_overlaps(LanczosSet& L, Op& obs, double* out);
 // out = R^* O R with R = Q^T Y (Y used x nv real, column-major); complex nv x nv column-major.
 void lanczos_ritz_matrix(LanczosSet& L, int s, Op& obs, const double* Y, int nv, double* out);
 
+// exp(s_i A) applied to every column of V (n x ncol complex): out[:, c, i]
+// (n x ncol x nscales, column-major complex), the columns' Krylov recursions
+// (_krylov_expmv_times, src/operators.jl:1805-1949) stepping together on one
+// engine, in waves that fit in memory; `normalise` scales every state to norm 1
+// (imaginary-time evolution).
+void expm_columns(Op& op, const double* V, int ncol, const std::vector<cd>& scales, double tol, int krylov_dim,
+                  int precision, bool normalise, double* out, bool device);
+
 // evolve(BlockOps, psi, t0, times) / block_expm (src/tools.jl:2445-2719) for
 // static block operators: c_b = P_b^H psi for every block with a nonzero
 // projection, exp(s_i H_b) c_b for every scale with all blocks' Krylov

@@ -365,6 +365,21 @@ def evolve(H, v0, t0, times, eom="SE", iterate=False, imag_time=False, tol=1e-12
         raise ArgumentError("LvNE evolution is not implemented on this engine")
     scalar = np.isscalar(times)
     ts = np.atleast_1d(np.asarray(times, dtype=np.float64))
+    if np.ndim(v0) == 2:
+        # a matrix of start states (src/operators.jl:2150-2164): every column's
+        # recursion on one engine, states[:, column, time]
+        V = np.asfortranarray(v0, dtype=np.complex128)
+        if V.shape[0] != H.Ns:
+            raise DimensionMismatch("operator and matrix dimensions do not match")
+        off = ts - float(t0)
+        sc = np.ascontiguousarray(-off + 0j if imag_time else -1j * off)
+        out = np.zeros((H.Ns, V.shape[1], ts.size), dtype=np.complex128, order="F")
+        _lib.check(_lib.load().qs_expm_columns(H._h, _lib.ptr(V), V.shape[1], _lib.ptr(sc), ts.size, float(tol),
+                                               int(krylov_dim), _precision_code(precision), int(bool(imag_time)),
+                                               _lib.ptr(out), _lib.QS_MEM_HOST))
+        if iterate:
+            return (out[:, :, i].copy() for i in range(ts.size))
+        return out[:, :, 0].copy() if scalar else out
     v = np.ascontiguousarray(v0, dtype=np.complex128)
     if v.shape != (H.Ns,):
         raise DimensionMismatch("operator and vector dimensions do not match")
@@ -407,14 +422,18 @@ class ExpmMultiplyParallel:
                 raise ArgumentError("work_array must have element type ComplexF64")
         tol = 1e-12 if tol is None else float(tol)
         cols = v_in.reshape(v_in.shape[0], -1)
-        res = np.zeros(cols.shape, dtype=np.complex128)
         a = np.array([self.a.real, self.a.imag])
-        for j in range(cols.shape[1]):
-            x = np.ascontiguousarray(cols[:, j], dtype=np.complex128)
-            o = np.zeros_like(x)
-            _lib.check(_lib.load().qs_expm_multiply(self.A._h, _lib.ptr(a), _lib.ptr(x), _lib.ptr(o), tol, 30,
+        if cols.shape[1] == 1:
+            x = np.ascontiguousarray(cols[:, 0], dtype=np.complex128)
+            res = np.zeros_like(x)
+            _lib.check(_lib.load().qs_expm_multiply(self.A._h, _lib.ptr(a), _lib.ptr(x), _lib.ptr(res), tol, 30,
                                                     _precision_code(precision)))
-            res[:, j] = o
+        else:
+            # every column's Krylov recursion on one engine (src/operators.jl:1922-1949)
+            X = np.asfortranarray(cols, dtype=np.complex128)
+            res = np.zeros(X.shape, dtype=np.complex128, order="F")
+            _lib.check(_lib.load().qs_expm_columns(self.A._h, _lib.ptr(X), X.shape[1], _lib.ptr(a), 1, tol, 30,
+                                                   _precision_code(precision), 0, _lib.ptr(res), _lib.QS_MEM_HOST))
         res = res.reshape(v_in.shape)
         if work_array is not None:
             work_array[:v_in.size] = v_in.reshape(-1)

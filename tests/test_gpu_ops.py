@@ -312,3 +312,35 @@ def test_expm_of_a_non_hermitian_assembled_operator(qs, ora, sym):
     got = qs.evolve(H, v, 0.0, times, tol=1e-11)
     want = np.stack([sla.expm(-1j * t * D) @ v for t in times], axis=1)
     assert np.max(np.linalg.norm(got - want, axis=0) / np.linalg.norm(want, axis=0)) < 1e-9
+
+
+def test_krylov_exponential_on_a_matrix(qs, ora):
+    """apply(ExpmMultiplyParallel(H, a), V) and evolve(H, V0, t0, times) on a
+    matrix of states (src/operators.jl:1895-1949, 2150-2164): every column's
+    recursion on one engine, equal to the column-by-column calls."""
+    import scipy.linalg as sla
+    L = 12
+    spec = models.j1j2(L, 1.0, 0.3)
+    b = qs.SpinBasis1D(L, nup=6, pauli=False, kblock=2)
+    H = qs.Hamiltonian(b, models.to_terms(qs, spec))
+    rep = ora.RepBasis(L, nup=6, pauli=False, kblock=2)
+    D = np.column_stack([rep.matvec(spec, np.eye(b.Ns, dtype=complex)[:, j]) for j in range(b.Ns)])
+    rng = np.random.default_rng(5)
+    V = rng.standard_normal((b.Ns, 4)) + 1j * rng.standard_normal((b.Ns, 4))
+    E = qs.ExpmMultiplyParallel(H, -0.6j)
+    got = E.apply(V)
+    assert got.shape == V.shape
+    want = sla.expm(-0.6j * D) @ V
+    assert np.abs(got - want).max() < 1e-10 * np.abs(V).max()
+    for j in range(4):
+        assert np.abs(got[:, j] - E.apply(V[:, j])).max() < 1e-12 * np.abs(V).max()
+    times = [0.0, 0.4, 1.5]
+    st = qs.evolve(H, V, 0.2, times)
+    assert st.shape == (b.Ns, 4, 3)
+    for i, t in enumerate(times):
+        assert np.abs(st[:, :, i] - sla.expm(-1j * (t - 0.2) * D) @ V).max() < 1e-10 * np.abs(V).max()
+    im = qs.evolve(H, V, 0.0, 1.0, imag_time=True)
+    assert im.shape == (b.Ns, 4)
+    ref = sla.expm(-1.0 * D) @ V
+    ref /= np.linalg.norm(ref, axis=0)
+    assert np.abs(im - ref).max() < 1e-10
