@@ -417,7 +417,8 @@ struct SellArgs {
     const uint16_t* stab;
     const void* diag;
     const void* diag_re;     // real diagonal (real operators)
-    int64_t nslices, n;
+    int64_t nslices, n;      // slices slice0 .. nslices - 1 are computed
+    int64_t slice0;
     double ar, ai, br, bi;
     int beta_zero;
     int conj;
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_kernel(SellArgs a) {
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const T2* __restrict__ gtab = (const T2*)a.table;
     const bool conj = a.conj;
-    for (int64_t s = warp0; s < a.nslices; s += nwarps) {
+    for (int64_t s = a.slice0 + warp0; s < a.nslices; s += nwarps) {
         const int64_t r = s * kSlice + lane;
         if (r >= a.n) continue;
         const int len = a.len[r];
@@ -532,7 +533,7 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_df_kernel(SellArgs a, con
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool conj = a.conj;
-    for (int64_t s = warp0; s < a.nslices; s += nwarps) {
+    for (int64_t s = a.slice0 + warp0; s < a.nslices; s += nwarps) {
         const int64_t r = s * kSlice + lane;
         if (r >= a.n) continue;
         const int len = a.len[r];
@@ -618,7 +619,7 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_dfio_kernel(SellArgs a, c
     const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool conj = a.conj;
-    for (int64_t s = warp0; s < a.nslices; s += nwarps) {
+    for (int64_t s = a.slice0 + warp0; s < a.nslices; s += nwarps) {
         const int64_t r = s * kSlice + lane;
         if (r >= a.n) continue;
         const int len = a.len[r];
@@ -919,7 +920,8 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
         a.code_mask = M.code_bits >= 32 ? 0xffffffffu : ((1u << M.code_bits) - 1u);
         a.ncodes = M.ncodes;
         a.stab = b.symmetric ? b.d_stab.as<uint16_t>() : nullptr;
-        a.nslices = M.nslices;
+        a.nslices = c.slice1 >= 0 ? std::min<int64_t>(c.slice1, M.nslices) : M.nslices;
+        a.slice0 = c.slice0;
         a.n = b.n;
         a.ar = c.alpha.re;
         a.ai = c.alpha.im;
@@ -931,7 +933,7 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
         a.x = c.x;
         a.y = c.y;
         const bool cm = op.complex_mat, cv = c.y_complex;
-        const int grid = grid_rows(M.nslices * kSlice);
+        const int grid = grid_rows(std::max<int64_t>(1, a.nslices - a.slice0) * kSlice);
         // variants: (gathers in flight per thread, resident blocks per SM)
 #define QS_VARIANTS(LAUNCH, v)                  \
     do {                                        \
@@ -1188,6 +1190,36 @@ void op_export_csr(Op& op, int64_t* rowptr, int64_t* cols, double* values, doubl
     }
     QS_CUDA(cudaMemcpyAsync(diag, op.d_diag.p, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, s));
     QS_CUDA(cudaStreamSynchronize(s));
+}
+
+bool op_matvec_host_overlap(Op& op, const MatvecCall& c0, void* y_host, size_t eb) {
+    const Assembled& M = op.asm_;
+    const bool T = (c0.flags & QS_TRANSPOSE) != 0;
+    if (!op.commuting || !op.assembled || !M.has_sell || (T && !op.hermitian) || c0.df || c0.df_io) return false;
+    if (!(c0.beta.re == 0.0 && c0.beta.im == 0.0)) return false;   // y is not read
+    // the first product of a kind times the kernel variants on the full range
+    if (M.sell_variant[c0.single ? 1 : 0] < 0) return false;
+    constexpr int K = 4;
+    if (M.nslices < 4 * K) return false;
+    if (!op.copy_stream) {
+        QS_CUDA(cudaStreamCreateWithFlags(&op.copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : op.range_done) QS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const int64_t n = op.basis->n;
+    for (int k = 0; k < K; ++k) {
+        MatvecCall c = c0;
+        c.slice0 = M.nslices * k / K;
+        c.slice1 = M.nslices * (k + 1) / K;
+        op_spmv_device(op, c, op.stream);
+        QS_CUDA(cudaEventRecord(op.range_done[k], op.stream));
+        QS_CUDA(cudaStreamWaitEvent(op.copy_stream, op.range_done[k], 0));
+        const int64_t r0 = c.slice0 * kSellSlice, r1 = std::min<int64_t>(n, c.slice1 * kSellSlice);
+        if (r1 > r0)
+            QS_CUDA(cudaMemcpyAsync((char*)y_host + (size_t)r0 * eb, (const char*)c0.y + (size_t)r0 * eb,
+                                    (size_t)(r1 - r0) * eb, cudaMemcpyDeviceToHost, op.copy_stream));
+    }
+    QS_CUDA(cudaStreamSynchronize(op.copy_stream));
+    return true;
 }
 
 }  // namespace qs

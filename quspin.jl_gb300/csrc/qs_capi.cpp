@@ -298,8 +298,12 @@ int qs_op_matvec(qs_op* op, int32_t flags, const double* alpha, const void* x, i
             if (!beta_zero) QS_CUDA(cudaMemcpyAsync(o.d_y.p, ys, n * yb, cudaMemcpyHostToDevice, o.stream));
             c.x = o.d_x.p;
             c.y = o.d_y.p;
-            qs::op_matvec_device(o, c, o.stream);
-            QS_CUDA(cudaMemcpyAsync(ys, o.d_y.p, n * yb, cudaMemcpyDeviceToHost, o.stream));
+            // the assembled product in row ranges, each range read back while the
+            // next computes; otherwise one product and one read-back
+            if (!qs::op_matvec_host_overlap(o, c, ys, yb)) {
+                qs::op_matvec_device(o, c, o.stream);
+                QS_CUDA(cudaMemcpyAsync(ys, o.d_y.p, n * yb, cudaMemcpyDeviceToHost, o.stream));
+            }
             QS_CUDA(cudaStreamSynchronize(o.stream));
         }
     });

@@ -174,6 +174,8 @@ struct Op {
     cudaStream_t own_stream = nullptr;  // created by the library
     Assembled asm_;                     // assembled (compiled-transition) form
     bool assembled = false;
+    cudaStream_t copy_stream = nullptr; // read-back of host products (op_matvec_host_overlap)
+    cudaEvent_t range_done[4] = {};
     ~Op();
 };
 
@@ -207,6 +209,7 @@ struct MatvecCall {
     bool df = false;                // FP64 vectors, double-float products (assembled form)
     bool df_io = false;             // double-float vectors in and out, alpha = 1, beta = 0
     bool no_tune = false;           // never time kernel variants inside this call
+    int64_t slice0 = 0, slice1 = -1; // sliced-ELL slices [slice0, slice1) only (-1: to the end)
 };
 void op_prepare_device(Op& op);
 // qs_noalloc.cu
@@ -216,6 +219,10 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
 // qs_assembled.cu
 void op_assemble(Op& op);
 void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s);
+// y = op x for one host vector with the assembled sliced-ELL product split in
+// row ranges, each range's rows of y copied back while later ranges compute;
+// false (nothing done) when the operator or the call does not allow it
+bool op_matvec_host_overlap(Op& op, const MatvecCall& c, void* y_host, size_t elem_bytes);
 // the assembled matrix on the host: CSR off-diagonal part (rowptr n + 1,
 // cols and complex values nnz; a row may repeat a column) and the diagonal
 void op_export_csr(Op& op, int64_t* rowptr, int64_t* cols, double* values, double* diag);

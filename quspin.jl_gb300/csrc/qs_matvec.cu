@@ -465,6 +465,12 @@ void note_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxe
 int64_t launches() { return g_launches.load(std::memory_order_relaxed); }
 
 Op::~Op() {
+    if (copy_stream) {
+        cudaStreamSynchronize(copy_stream);
+        cudaStreamDestroy(copy_stream);
+        for (cudaEvent_t e : range_done)
+            if (e) cudaEventDestroy(e);
+    }
     if (own_stream) cudaStreamDestroy(own_stream);
 }
 
