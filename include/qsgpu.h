@@ -86,7 +86,9 @@ typedef struct {
 } qs_general_spec;
 
 /* Columns are the symmetric orbit states in ascending orbit minimum, each
- * anchored (real positive) at its minimum, which is its state label; L <= 32. */
+ * anchored (real positive) at its minimum, labelled by the reference's own
+ * representative (its projector is replayed; trees beyond 32 first-map
+ * orbits are labelled by the orbit minimum); L <= 63. */
 QS_API int qs_basis_create_general(const qs_general_spec *spec, qs_basis **out);
 
 /* Replaces SpinBasis1D(L; ...) (src/basis.jl:622-777): enumerates the sector on

@@ -705,7 +705,7 @@ void basis_build(Basis& b) {
 // ------------------------------------------------- basis_build_general
 void basis_build_general(Basis& b, const qs_general_spec& gs) {
     const int L = gs.L;
-    if (L < 1 || L > 32) throw Error(QS_ERR_UNSUPPORTED, "general symmetry maps are supported for L <= 32");
+    if (L < 1 || L > 63) throw Error(QS_ERR_UNSUPPORTED, "general symmetry maps are supported for L <= 63");
     if (gs.nup < -1 || gs.nup > L) throw Error(QS_ERR_ARGUMENT, "nup must lie between 0 and L");
     if (gs.nmaps < 0 || (gs.nmaps > 0 && (!gs.maps || !gs.flips || !gs.qnums)))
         throw Error(QS_ERR_ARGUMENT, "general symmetry blocks must be (map, quantum_number)");
@@ -716,9 +716,10 @@ void basis_build_general(Basis& b, const qs_general_spec& gs) {
     b.spec.a = 1;
     b.L = L;
     b.nup = gs.nup;
-    b.wide = false;
+    b.wide = L > 32;
     b.general = true;
     b.symmetric = gs.nmaps > 0;
+    if (b.nup < 0 && L > 40) throw Error(QS_ERR_UNSUPPORTED, "a full 2^L space above L=40 does not fit in device memory");
     b.n_parent = b.nup >= 0 ? binom_host(L, b.nup) : (int64_t)1 << L;
     std::vector<GElem> gens;
     b.gens.clear();
@@ -871,7 +872,8 @@ void basis_build_general(Basis& b, const qs_general_spec& gs) {
         chi_one[e] = (std::fabs(b.group.chi_re[e] - 1.0) < 1e-9 && std::fabs(b.group.chi_im[e]) < 1e-9) ? 1 : 0;
     DevBuf d_chi_one(kMaxGroup);
     QS_CUDA(cudaMemcpy(d_chi_one.p, chi_one.data(), kMaxGroup, cudaMemcpyHostToDevice));
-    enumerate_sector<uint32_t>(b, d_chi_one);
+    if (b.wide) enumerate_sector<uint64_t>(b, d_chi_one);
+    else enumerate_sector<uint32_t>(b, d_chi_one);
 }
 
 // ------------------------------------------------------------- index_of
@@ -1487,9 +1489,13 @@ void basis_compute_refrep(Basis& b) {
     }
     if (b.general && !b.replay) {
         // without the replay a general basis labels each column by its orbit minimum
-        std::vector<uint32_t> tmp(b.n);
-        QS_CUDA(cudaMemcpy(tmp.data(), b.d_reps.p, b.n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-        for (int64_t i = 0; i < b.n; ++i) b.h_refrep[i] = tmp[i];
+        if (b.wide) {
+            QS_CUDA(cudaMemcpy(b.h_refrep.data(), b.d_reps.p, b.n * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<uint32_t> tmp(b.n);
+            QS_CUDA(cudaMemcpy(tmp.data(), b.d_reps.p, b.n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            for (int64_t i = 0; i < b.n; ++i) b.h_refrep[i] = tmp[i];
+        }
         b.refrep_ready = true;
         return;
     }
@@ -1578,7 +1584,8 @@ void basis_representative(Basis& b, const uint64_t* states, int64_t n, uint64_t*
         a.norm = dnorm.as<double>();
         a.amp = damp.as<double>();
         a.status = dst.as<int32_t>();
-        gen_query_kernel<uint32_t><<<grid_for(n, 128), 128, 0, b.stream>>>(a);
+        if (b.wide) gen_query_kernel<uint64_t><<<grid_for(n, 128), 128, 0, b.stream>>>(a);
+        else gen_query_kernel<uint32_t><<<grid_for(n, 128), 128, 0, b.stream>>>(a);
         QS_CUDA(cudaGetLastError());
         QS_CUDA(cudaMemcpyAsync(reps, drep.p, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, b.stream));
         QS_CUDA(cudaMemcpyAsync(norms, dnorm.p, n * sizeof(double), cudaMemcpyDeviceToHost, b.stream));
@@ -1695,8 +1702,13 @@ void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out,
         g.out_ld = nout1;
         const int64_t work = mode == 0 ? rows : b.n;
         const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 127) / 128, 152 * 32));
-        if (mode == 0) gen_from_kernel<uint32_t><<<grid, 128, 0, s>>>(g);
-        else gen_to_kernel<uint32_t><<<grid, 128, 0, s>>>(g, b.d_stab.as<uint16_t>());
+        if (b.wide) {
+            if (mode == 0) gen_from_kernel<uint64_t><<<grid, 128, 0, s>>>(g);
+            else gen_to_kernel<uint64_t><<<grid, 128, 0, s>>>(g, b.d_stab.as<uint16_t>());
+        } else {
+            if (mode == 0) gen_from_kernel<uint32_t><<<grid, 128, 0, s>>>(g);
+            else gen_to_kernel<uint32_t><<<grid, 128, 0, s>>>(g, b.d_stab.as<uint16_t>());
+        }
         QS_CUDA(cudaGetLastError());
         note_launches(1);
         if (!device) QS_CUDA(cudaMemcpyAsync(out, pout, (size_t)nout * sizeof(double2), cudaMemcpyDeviceToHost, s));

@@ -261,11 +261,11 @@ def _normalize_general_map(values, L):
 
 class SpinBasisGeneral(SpinBasis1D):
     """SpinBasisGeneral(L; nup, Nup, m, S, pauli, block_order, blocks...)
-    (src/basis.jl:455-600) for spin 1/2 and L <= 32: each block is
+    (src/basis.jl:455-600) for spin 1/2 and L <= 63: each block is
     (map, quantum_number) with map a site permutation (negative entries flip
     the spin), intersected in block_order (default: keyword order).  Columns
     are the symmetric orbit states in ascending orbit minimum, labelled by
-    that minimum (the reference's argmax representative up to ties)."""
+    the reference's own representatives (its projector is replayed)."""
 
     def __init__(self, L, nup=None, Nup=None, m=None, S="1/2", pauli=True, block_order=None, make_basis=True,
                  Ns_block_est=None, **blocks):

@@ -169,3 +169,21 @@ def test_general_argument_errors(qs):
     b = qs.SpinBasisGeneral(12, nup=6, pauli=False, Tx=(Tx, 1))
     with pytest.raises(qs.ArgumentError):
         qs.Hamiltonian(b, [qs.OperatorTerm("zz", [(1.0, 1, 2)])])
+
+
+def test_general_wide_states(qs, ora):
+    """L = 34 > 32 (64-bit states): a 17 x 2 torus at nup = 3 against the
+    oracle: sizes, representatives, the sector matrix and the ground state."""
+    Lx, Ly, nup = 17, 2, 3
+    Tx, Ty, Px, Z = models.torus_maps(Lx, Ly)
+    for qx, qy in ((0, 0), (3, 1)):
+        b = qs.SpinBasisGeneral(Lx * Ly, nup=nup, pauli=False, Tx=(Tx, qx), Ty=(Ty, qy))
+        rb = ora.general_basis(Lx * Ly, nup=nup, pauli=False, blocks=[(Tx, qx), (Ty, qy)])
+        assert b.Ns == rb.Ns
+        assert np.array_equal(qs.states(b), rb.states)
+        spec = models.torus_heisenberg(Lx, Ly, 1.0, 0.2)
+        H = qs.Hamiltonian(b, models.to_terms(qs, spec))
+        D = rb.dense(ora.consolidate_terms(spec))
+        assert np.abs(H.toarray() - D).max() < 1e-13
+        e0 = qs.eigsh(H, k=1, tol=1e-12, return_eigenvectors=False)[0]
+        assert abs(e0 - np.linalg.eigvalsh(D)[0]) < 1e-10
