@@ -546,8 +546,9 @@ def section_general(qs, torch, Lx=6, Ly=5, J2=0.5):
     t = time.perf_counter()
     H = qs.Hamiltonian(b, terms)
     t_asm = time.perf_counter() - t
-    out = {"workload": "J1-J2 square lattice %dx%d torus (J2=%.1f), nup=%d, k=(0,0), Px=+1, Z=+1: %d states, "
-                       "nnz=%d" % (Lx, Ly, J2, L // 2, b.Ns, H.nnz),
+    model = "Heisenberg model" if J2 == 0 else "J1-J2 square lattice (J2=%.2g)" % J2
+    out = {"workload": "%s on the %dx%d torus, nup=%d, k=(0,0), Px=+1, Z=+1: %d states, nnz=%d" % (
+        model, Lx, Ly, L // 2, b.Ns, H.nnz),
            "basis_build_s": t_basis, "assemble_s": t_asm, "group_order": b.group_order}
     for prec in ("fp64", "fp64df"):
         qs.eigsh(H, k=1, which="SA", tol=1e-10, return_eigenvectors=False, precision=prec)
