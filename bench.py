@@ -275,7 +275,8 @@ def section_c3(qs, torch, n_times=50):
     range(0.1, 5.0) (krylov_dim 30, tol 1e-9): one evolve call in the
     double-float form over all times (the reference's _krylov_expmv_times,
     failing times re-run concurrently), the FP64 form on the first 10 times,
-    the FP32 form on the first 5; states compared where they overlap."""
+    the FP32 form on the first 5, and all 50 times stepwise (from each time to
+    the next) in FP64 and double-float; states compared where they overlap."""
     L = 30
     b = qs.SpinBasis1D(L, pauli=True, kblock=0, pblock=1)
     t = time.perf_counter()
@@ -304,6 +305,14 @@ def section_c3(qs, torch, n_times=50):
         res[prec] = st
         out[f"norm_drift_{prec}"] = float(np.max(np.abs(np.linalg.norm(st, axis=0) - 1)))
     out["evolves_per_s_fp64df"] = 1.0 / out["evolve_s_fp64df"]
+    # the same 50 times from each to the next (evolve(..., stepwise=True)), FP64
+    # and double-float, against the reference-faithful double-float states
+    for prec in ("fp64", "fp64df"):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sw = qs.evolve(H, v0, 0.0, times, tol=1e-9, krylov_dim=30, precision=prec, stepwise=True)
+        out[f"evolve_s_{prec}_stepwise"] = time.perf_counter() - t
+        out[f"{prec}_stepwise_vs_fp64df_state_err"] = float(np.max(np.linalg.norm(sw - res["fp64df"], axis=0)))
     out["fp64df_vs_fp64_state_err"] = float(np.max(np.linalg.norm(res["fp64df"][:, :res["fp64"].shape[1]] - res["fp64"],
                                                                   axis=0)))
     out["fp32_vs_fp64_state_err"] = float(np.max(np.linalg.norm(res["fp32"] - res["fp64"][:, :res["fp32"].shape[1]],

@@ -302,6 +302,16 @@ QS_API int qs_expm_multiply(qs_op *op, const double *a, const double *v, double 
 QS_API int qs_evolve(qs_op *op, const double *v0, double t0, const double *times, int32_t nt, int32_t imag_time,
               double tol, int32_t krylov_dim, int32_t precision, double *out);
 
+/* evolve(H, v0, t0, times) computed from each time to the next (times taken
+ * in order of t - t0): every step runs the reference's Krylov recursion
+ * (_krylov_expmv_vector) from the previous state with tol / (number of
+ * steps), so the result agrees with qs_evolve to tol while late times cost a
+ * single pass over [t0, t] instead of one from v0 each.  An addition for
+ * long time series (the reference evaluates every time from v0); arguments
+ * and output as qs_evolve, assembled operators. */
+QS_API int qs_evolve_stepwise(qs_op *op, const double *v0, double t0, const double *times, int32_t nt,
+                              int32_t imag_time, double tol, int32_t krylov_dim, int32_t precision, double *out);
+
 /* The Krylov exponential on a matrix: out[:, c, i] = exp(scales[i] A) V[:, c]
  * (src/operators.jl:1895-1949 _krylov_expmv_times / _krylov_expmv on a
  * matrix; apply(ExpmMultiplyParallel, V) and evolve(H, V0, t0, times) with a

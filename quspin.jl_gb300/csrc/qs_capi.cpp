@@ -398,6 +398,17 @@ int qs_lanczos_ritz_matrix(qs_lanczos* lanczos, int32_t s, qs_op* observable, co
     });
 }
 
+int qs_evolve_stepwise(qs_op* op, const double* v0, double t0, const double* times, int32_t nt, int32_t imag_time,
+                       double tol, int32_t krylov_dim, int32_t precision, double* out) {
+    return guard([&] {
+        if (!op || !v0 || !out || (nt > 0 && !times)) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        if (krylov_dim < 1) throw qs::Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
+        std::vector<double> off(std::max(0, nt));
+        for (int i = 0; i < nt; ++i) off[i] = times[i] - t0;
+        qs::evolve_stepwise(*op->op, v0, off, imag_time != 0, tol > 0 ? tol : 1e-12, krylov_dim, precision, out);
+    });
+}
+
 int qs_expm_columns(qs_op* op, const double* V, int32_t ncol, const double* scales, int32_t nscales, double tol,
                     int32_t krylov_dim, int32_t precision, int32_t normalise, double* out, int32_t mem) {
     return guard([&] {

@@ -1773,6 +1773,62 @@ void evolve_engine(Op& op, const double* v0, const std::vector<cd>& scales, doub
     note_launches(E.launches());
 }
 
+void evolve_stepwise(Op& op, const double* v0, const std::vector<double>& offsets, bool imag_time, double tol,
+                     int krylov_dim, int precision, double* out) {
+    const int64_t n = op.basis->n;
+    const int nt = (int)offsets.size();
+    if (nt == 0) return;
+    const int m = (int)std::max<int64_t>(2, std::min<int64_t>(std::min(krylov_dim, kMaxM), n));
+    const bool herm = op.hermitian;
+    Engine E(precision == 0 ? Store::F64 : Store::DF, op.stream);
+    cudaStream_t st = E.stream();
+    const size_t bytes = (size_t)n * 16;
+    PoolBuf cur(bytes, st);
+    QS_CUDA(cudaMemcpyAsync(cur.p, v0, bytes, cudaMemcpyHostToDevice, st));
+    // the times in order of their offset from t0, propagated one from the next
+    std::vector<int> order(nt);
+    for (int i = 0; i < nt; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return offsets[a] < offsets[b]; });
+    int steps = 0;
+    double prev = 0.0;
+    for (int i : order)
+        if (offsets[i] != prev) {
+            ++steps;
+            prev = offsets[i];
+        }
+    // the steps' errors add up: each gets an equal share of the tolerance
+    const double tol_step = tol / std::max(1, steps);
+    Blas B(VKind::C128, n, st);
+    prev = 0.0;
+    for (int i : order) {
+        const double d = offsets[i] - prev;
+        if (d != 0.0) {
+            const int id = E.add(op, m, true, true, 1, herm ? 2 : 0);
+            E.load(id, 0, cur.as<double>(), true);
+            const double beta = E.normalize({id})[0];
+            if (beta > 0) {
+                std::vector<int> ids{id};
+                std::vector<EvoTask> tasks(1);
+                tasks[0].init(m, n, herm, imag_time ? cd(-d, 0) : cd(0, -d), tol_step, beta, false);
+                std::vector<double*> outs{cur.as<double>()};
+                run_evo_slots(E, ids, tasks, outs, true);
+            } else {
+                E.remove(id);
+            }
+            if (imag_time) {
+                // exp(-tau H) shrinks or grows the state: carry it at norm 1, as
+                // the reference normalises every imaginary-time state
+                const double nr = B.norm(cur.p);
+                if (nr > 0) B.scale(cur.p, cur.p, cd(1.0 / nr, 0));
+            }
+            prev = offsets[i];
+        }
+        QS_CUDA(cudaMemcpyAsync(out + (size_t)i * 2 * n, cur.p, bytes, cudaMemcpyDeviceToHost, st));
+    }
+    QS_CUDA(cudaStreamSynchronize(st));
+    note_launches(E.launches());
+}
+
 void evolve_blocks(const std::vector<Op*>& ops, const std::vector<const double*>& v0s, const std::vector<cd>& scales,
                    double tol, int krylov_dim, int precision, const std::vector<double*>& outs) {
     const size_t nb = ops.size();

@@ -249,6 +249,14 @@ struct EvoTask {
 // complex (host).
 void evolve_engine(Op& op, const double* v0, const std::vector<cd>& scales, double tol, int krylov_dim, int precision,
                    bool normalise, double* out);
+// evolve from each time to the next instead of from v0 every time: the times
+// in order of their offset from t0, each step the reference's
+// _krylov_expmv_vector recursion from the previous state with tol / steps
+// (the steps' errors add), imaginary-time states carried at norm 1.  Far fewer
+// products than _krylov_expmv_times for many late times; the results agree
+// with it to the tolerance, not bit for bit.  v0, out: host (out Ns x nt).
+void evolve_stepwise(Op& op, const double* v0, const std::vector<double>& offsets, bool imag_time, double tol,
+                     int krylov_dim, int precision, double* out);
 // The reference's _krylov_expmv_times (src/operators.jl:1805-1893) on several
 // operators at once (the blocks of tools.jl's BlockOps evolution): v0s[b]
 // and outs[b] are device complex vectors (outs[b]: n_b x nscales); the blocks'

@@ -89,7 +89,7 @@ EXPORTS = (
     "qs_server_vector", "qs_server_release", "qs_server_stats",
     "qs_lanczos_run", "qs_lanczos_destroy", "qs_lanczos_coefficients", "qs_lanczos_complex", "qs_lanczos_rows",
     "qs_lanczos_combine", "qs_lanczos_overlaps", "qs_lanczos_ritz_matrix",
-    "qs_basis_projection_rows", "qs_basis_project_from", "qs_basis_project_to", "qs_block_expm", "qs_op_export_csr", "qs_fp64_fma_rate", "qs_basis_create_general", "qs_expm_columns",
+    "qs_basis_projection_rows", "qs_basis_project_from", "qs_basis_project_to", "qs_block_expm", "qs_op_export_csr", "qs_fp64_fma_rate", "qs_basis_create_general", "qs_expm_columns", "qs_evolve_stepwise",
 )
 
 _lib = None
@@ -153,6 +153,7 @@ def load():
     L.qs_basis_project_to.argtypes = [P, i32, P, P, i32]
     L.qs_op_export_csr.argtypes = [P, P, P, P, P]
     L.qs_fp64_fma_rate.argtypes = [ctypes.POINTER(f64)]
+    L.qs_evolve_stepwise.argtypes = [P, P, f64, P, i32, i32, f64, i32, i32, P]
     L.qs_expm_columns.argtypes = [P, P, i32, P, i32, f64, i32, i32, i32, P, i32]
     L.qs_basis_create_general.argtypes = [ctypes.POINTER(GeneralSpec), ctypes.POINTER(P)]
     L.qs_block_expm.argtypes = [P, i32, i32, P, P, i32, f64, i32, i32, P, i32]

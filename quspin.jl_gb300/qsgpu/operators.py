@@ -352,9 +352,13 @@ def eigsh_batch(ops, k=1, which="SA", tol=0.0, ncv=None, maxiter=None, return_ei
     return (vals, vecs) if return_eigenvectors else vals
 
 
-def evolve(H, v0, t0, times, eom="SE", iterate=False, imag_time=False, tol=1e-12, krylov_dim=30, precision="fp64"):
+def evolve(H, v0, t0, times, eom="SE", iterate=False, imag_time=False, tol=1e-12, krylov_dim=30, precision="fp64",
+           stepwise=False):
     """evolve(H, v0, t0, times; eom=:SE) for a static Hamiltonian (src/operators.jl:2073-2164).
-    A BlockOps operator evolves block by block (tools.jl:2627-2678)."""
+    A BlockOps operator evolves block by block (tools.jl:2627-2678).
+    stepwise=True (an addition) propagates from each time to the next instead
+    of from v0 every time: the same states to tol, far fewer products for
+    long time series."""
     from .blocks import BlockOps, evolve_blocks
     if isinstance(H, BlockOps):
         return evolve_blocks(H, v0, t0, times, iterate=iterate, imag_time=imag_time, tol=tol, krylov_dim=krylov_dim,
@@ -384,8 +388,9 @@ def evolve(H, v0, t0, times, eom="SE", iterate=False, imag_time=False, tol=1e-12
     if v.shape != (H.Ns,):
         raise DimensionMismatch("operator and vector dimensions do not match")
     out = np.zeros((H.Ns, ts.size), dtype=np.complex128, order="F")
-    _lib.check(_lib.load().qs_evolve(H._h, _lib.ptr(v), float(t0), _lib.ptr(ts), ts.size, int(bool(imag_time)),
-                                     float(tol), int(krylov_dim), _precision_code(precision), _lib.ptr(out)))
+    call = _lib.load().qs_evolve_stepwise if stepwise else _lib.load().qs_evolve
+    _lib.check(call(H._h, _lib.ptr(v), float(t0), _lib.ptr(ts), ts.size, int(bool(imag_time)), float(tol),
+                    int(krylov_dim), _precision_code(precision), _lib.ptr(out)))
     if iterate:
         return (out[:, i].copy() for i in range(ts.size))
     if scalar:

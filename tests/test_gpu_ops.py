@@ -344,3 +344,30 @@ def test_krylov_exponential_on_a_matrix(qs, ora):
     ref = sla.expm(-1.0 * D) @ V
     ref /= np.linalg.norm(ref, axis=0)
     assert np.abs(im - ref).max() < 1e-10
+
+
+def test_stepwise_evolution(qs, ora):
+    """evolve(..., stepwise=True) propagates from each time to the next: the
+    states of the reference-faithful evolve to the tolerance, for times in any
+    order, repeated, and before t0, in real and imaginary time."""
+    import scipy.linalg as sla
+    L = 12
+    spec = models.xxz(L, 1.0, 0.7) + [("z", [(0.2, i) for i in range(1, L + 1)])]
+    b = qs.SpinBasis1D(L, nup=6, pauli=False, kblock=3)
+    H = qs.Hamiltonian(b, models.to_terms(qs, spec))
+    rep = ora.RepBasis(L, nup=6, pauli=False, kblock=3)
+    D = np.column_stack([rep.matvec(spec, np.eye(b.Ns, dtype=complex)[:, j]) for j in range(b.Ns)])
+    v0 = models.seeded(b.Ns, seed=8, complex_=True)
+    v0 /= np.linalg.norm(v0)
+    times = [3.0, 0.5, 7.5, 0.5, -1.0, 0.1]
+    got = qs.evolve(H, v0, 0.1, times, tol=1e-11, stepwise=True)
+    ref = qs.evolve(H, v0, 0.1, times, tol=1e-11)
+    for i, t in enumerate(times):
+        want = sla.expm(-1j * (t - 0.1) * D) @ v0
+        assert np.linalg.norm(got[:, i] - want) < 1e-9, t
+        assert np.linalg.norm(got[:, i] - ref[:, i]) < 1e-9, t
+    im = qs.evolve(H, v0, 0.0, [0.4, 1.2], imag_time=True, stepwise=True)
+    for i, tau in enumerate((0.4, 1.2)):
+        want = sla.expm(-tau * D) @ v0
+        want /= np.linalg.norm(want)
+        assert np.linalg.norm(im[:, i] - want) < 1e-9
