@@ -660,7 +660,8 @@ def section_c5(qs, torch, n_req=2000, rate=200.0, budget_gb=150.0, seq_sample=40
 def profile_range(kind):
     """One unit of work inside cudaProfilerStart/Stop, after warm-up, for
     `ncu --profile-from-start off`: a product of the default sector in FP64,
-    FP32 or double-float ("product64", "product32", "productdf"), its
+    FP32, double-float or fixed point ("product64", "product32", "productdf",
+    "productfx"), its
     matrix-free product ("matrixfree"), one Lanczos ground state of it
     ("lanczos64", "lanczosdf"), one batched
     double-float ground-state solve of all J1-J2 sectors at L = 24 or 26
@@ -706,8 +707,31 @@ def profile_range(kind):
             H = qs.QuantumLinearOperator(b, terms)
         else:
             H = qs.Hamiltonian(b, terms)
-        prec = {"product64": "fp64", "product32": "fp32", "productdf": "fp64df", "matrixfree": "fp64"}[kind]
+        prec = {"product64": "fp64", "product32": "fp32", "productdf": "fp64df", "productfx": "fp64fx",
+                "matrixfree": "fp64"}[kind]
         x = np.random.default_rng(20261203).standard_normal(b.Ns)
+        if kind == "productfx":
+            # device buffers: one full-range product (its two passes over x, then the sums)
+            import ctypes
+            from qsgpu import _lib
+            lib = _lib.load()
+            one, zero = np.array([1.0, 0.0]), np.array([0.0, 0.0])
+            xt = torch.from_numpy(x).cuda()
+            yt = torch.empty_like(xt)
+
+            def mv():
+                _lib.check(lib.qs_op_matvec(H._h, _lib.QS_FIXED_POINT, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()),
+                                            _lib.QS_F64, _lib.ptr(zero), ctypes.c_void_p(yt.data_ptr()), _lib.QS_F64,
+                                            1, _lib.QS_MEM_DEVICE))
+            for _ in range(3):
+                mv()
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
+            mv()
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
+            print(json.dumps({"profile_range": kind, "N": b.Ns, "ynorm": float(yt.norm())}))
+            return
         for _ in range(3):
             H.dot(x, precision=prec)   # the first product times the kernel variants
         torch.cuda.synchronize()
@@ -805,6 +829,11 @@ def run_ours(args, wl, world, rank, local):
     ydf = torch.empty_like(x)
     msdf, _ = timed(H, x, ydf, _lib.QS_F64, args.steps, args.warmup, _lib.QS_DOUBLE_FLOAT)
     df_err = float((ydf - y_native).norm() / y_native.norm())
+    # fixed-point row sums (FP64 vectors, integer sums per amplitude class)
+    yfx = torch.empty_like(x)
+    msfx, _ = timed(H, x, yfx, _lib.QS_F64, args.steps, args.warmup, _lib.QS_FIXED_POINT)
+    fx_err = float((yfx - y_native).norm() / y_native.norm())
+    fx_maxerr = float((yfx - y_native).abs().max() / y_native.abs().max())
     ms32, _ = timed(H, x32, y32, _lib.QS_F32, args.steps, args.warmup)
     mf_steps = max(3, min(args.steps, 10))
     ms_mf, _ = timed(op, x, y, _lib.QS_F64, mf_steps, 2)
@@ -922,6 +951,14 @@ def run_ours(args, wl, world, rank, local):
                                    "frac_of_peak": asm_bytes64 / (float(np.mean(msdf)) / 1e3) / 1e9 / peak,
                                    "rel_err_vs_native_fp64": df_err,
                                    "speedup_vs_fp64": float(np.mean(ms64)) / float(np.mean(msdf))},
+        "fp64_fixed_point_form": {"value": asm_bytes64 / (float(np.mean(msfx)) / 1e3) / 1e9, "unit": "GB/s",
+                                  "ms_per_step": float(np.mean(msfx)),
+                                  "frac_of_peak": asm_bytes64 / (float(np.mean(msfx)) / 1e3) / 1e9 / peak,
+                                  "classes": H.fixed_point_classes,
+                                  "rel_err_vs_native_fp64": fx_err, "max_err_rel_to_max_entry": fx_maxerr,
+                                  "speedup_vs_fp64": float(np.mean(ms64)) / float(np.mean(msfx)),
+                                  "note": "x sqrt(stab) scaled to int64 once per product (two passes over x, "
+                                          "included), exact integer row sums, FP64 per row"},
         "matrix_free": {"ms_per_step": float(np.mean(ms_mf)), "unit": "GB/s",
                         "value": mf_bytes64 / (float(np.mean(ms_mf)) / 1e3) / 1e9,
                         "note": "QuantumLinearOperator path: transitions regenerated every product"},
@@ -951,7 +988,7 @@ def main():
                     help="skip the side workloads (XXZ L=16, batched sectors, TFIM evolve, serving)")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving workload")
     ap.add_argument("--profile-range", default=None,
-                    choices=["product64", "product32", "productdf", "matrixfree", "lanczos64", "lanczosdf",
+                    choices=["product64", "product32", "productdf", "productfx", "matrixfree", "lanczos64", "lanczosdf",
                              "batch24", "batch26", "ftlm"],
                     help="run one unit inside cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     args = ap.parse_args()

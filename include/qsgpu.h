@@ -193,6 +193,10 @@ QS_API int qs_op_set_stream(qs_op *op, void *stream);
 QS_API int qs_op_assemble(qs_op *op);
 /* Stored nonzeros of the assembled form (off-diagonal), -1 if not assembled. */
 QS_API int64_t qs_op_nnz(const qs_op *op);
+/* Amplitude classes the QS_FIXED_POINT product sums in integers (1 to 4), or 0
+ * when the operator is not assembled or QS_FIXED_POINT falls back to the FP64
+ * product for it.  No counterpart in the reference. */
+QS_API int32_t qs_op_fixed_point_classes(const qs_op *op);
 /* H.data / tocsc(H) (src/operators.jl:461-576, 1347) from the device's
  * assembled form: the off-diagonal part in CSR (rowptr Ns + 1, cols and
  * complex values qs_op_nnz(op) each; entries of one row may repeat a column,
@@ -207,7 +211,16 @@ enum {
     /* FP64 vectors, products of an assembled operator carried in double-float
      * (pairs of FP32, ~48-bit significand) to stay off GB300's slow FP64 pipe;
      * ignored for single precision and for matrix-free operators. */
-    QS_DOUBLE_FLOAT = 4
+    QS_DOUBLE_FLOAT = 4,
+    /* FP64 vectors, row sums of an assembled operator carried exactly in 64-bit
+     * fixed point (x sqrt(stab) scaled by one power of two per product), FP64
+     * only per row: for real operators whose stored values fall in at most four
+     * amplitude classes (e.g. Heisenberg / J1-J2 / XXZ / TFIM couplings in real
+     * sectors); otherwise the FP64 product.  Each row sum is within
+     * 2^(2 ceil(log2(longest row)) - 61) max|x sqrt(stab)| of exact -- the
+     * normwise accuracy of FP64 -- but elements far below the largest do not
+     * keep FP64's relative accuracy.  Takes precedence over QS_DOUBLE_FLOAT. */
+    QS_FIXED_POINT = 8
 };
 
 /* mul!(Y, op, X, alpha, beta) (src/operators.jl:3147-3208) for nrhs column-

@@ -673,6 +673,366 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_dfio_kernel(SellArgs a, c
     }
 }
 
+// ------------------------------------------------ exact fixed-point row sums
+// When every stored value is real and, with the column's sqrt(stab) taken
+// out, one of at most four amplitudes (value = +-A_c sqrt(stab_col)), a row
+// sum needs no multiply per nonzero:
+//     sum_j value_j x_j = sum_c A_c sum_{j in c} +-x'_j,  x'_j = x_j sqrt(stab_j).
+// x' is scaled by a power of two 2^K and rounded to 64-bit integers once per
+// product (K from a bound of max |x'| within a factor of two and from the
+// longest row, so that no sum of a row can overflow), the inner sums are
+// exact integer adds on the integer pipe, and FP64 runs only per row: one
+// conversion and one multiply-add per class, the row scale and the diagonal
+// term.  Besides the FP64 product x_j sqrt(stab_j), the only rounding before
+// the row tail is that of each x'_j to a multiple of 2^-K, at most
+// 2^(len_bits - 61) max|x'|, so a row sum of at most 2^len_bits terms is
+// within 2^(2 len_bits - 61) max|x'| of exact: normwise the accuracy of an
+// FP64 row sum.  Elements far
+// below max|x'| do not keep their relative accuracy, which is why the form is
+// requested explicitly (QS_FIXED_POINT) and the FP64 product stays the default.
+
+constexpr int kFxParts = 4096;   // blocks of the max pass, at most
+// kFxCodes (256) bounds the value codes: four classes x 2 signs x the divisor
+// count of |G| (at most 24 for |G| <= 512) is 192 at most
+
+struct FxArgs {
+    const uint32_t* cls;                // per code: class << 1 | sign
+    const double* amp;                  // per class: A_c
+    const double* sq;                   // sqrt(i), i = 0 .. kMaxGroup
+    unsigned long long* part;           // per block of the max pass: max |x'_j| as its IEEE bit pattern
+    unsigned long long* maxbits;        // max |x'_j| over all of x
+    int len_bits;                       // ceil(log2(longest row))
+    void* xq;                           // round(x' 2^K): int64, or int64 pairs for complex x
+};
+
+// 2^k for -1022 <= k <= 1023, from its bit pattern
+__device__ __forceinline__ double fx_pow2(int k) { return __longlong_as_double((long long)(1023 + k) << 52); }
+
+__device__ __forceinline__ bool fx_finite(unsigned long long mb) { return mb < 0x7ff0000000000000ull; }
+
+// With max |x'| < 2^E (E from the biased exponent; subnormals count as
+// 2^-1022), |x'_j| 2^K <= 2^(62 - len_bits): a sum of at most 2^len_bits of
+// them stays within 2^62.  -978 <= K <= 1083.
+__device__ __forceinline__ int fx_shift(unsigned long long mb, int len_bits) {
+    const int e = (int)(mb >> 52);
+    return 62 - ((e > 0 ? e : 1) - 1022) - len_bits;
+}
+
+// GB300 runs FP64 at ~1/70 of its FP32 rate, so both passes over x stay on
+// the integer pipe but for one FP64 multiply x_j sqrt(stab_j) per element
+// (an integer 53 x 64-bit product in its place measured slower).
+
+// ceil(log2(sqrt(st))) for st >= 1: sqrt(st) <= 2^c
+__device__ __forceinline__ int fx_sqrt_exp(unsigned st) { return (32 - __clz(st - 1u) + 1) >> 1; }
+
+// An upper bound of |x sqrt(st)| within a factor of two, as an IEEE bit
+// pattern: |x| times 2^c added in the exponent field.  Infinities and NaNs
+// stay at or above the infinity pattern; a finite value whose bound passes
+// it is treated as non-finite (the product then runs as FP64).
+__device__ __forceinline__ unsigned long long fx_bound_bits(double v, int c) {
+    return ((unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull) + ((unsigned long long)c << 52);
+}
+
+// round(v 2^K) to the nearest integer, ties to even, from v's bit pattern;
+// |v 2^K| <= 2^62 by the choice of K
+__device__ __forceinline__ long long fx_round_scaled(double v, int K) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);
+    const unsigned long long mant = (b & 0xfffffffffffffull) | (e ? (1ull << 52) : 0ull);
+    const int t = (e ? e : 1) - 1075 + K;   // v 2^K = mant 2^t
+    unsigned long long q;
+    if (t >= 0) {
+        q = mant << t;
+    } else if (t < -63) {
+        q = 0;
+    } else {
+        const int sh = -t;
+        q = mant >> sh;
+        const unsigned long long rem = mant & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        q += (rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull;
+    }
+    return (b >> 63) ? -(long long)q : (long long)q;
+}
+
+// rows i + u st, u = 0 .. R-1: x and stab loads first (the passes are bound
+// by memory latency with one load chain per thread)
+template <bool kCV, int R>
+__device__ __forceinline__ void fx_load(const void* __restrict__ x, const uint16_t* __restrict__ stab, int64_t i,
+                                        int64_t st, double (&re)[R], double (&im)[R], unsigned (&k)[R]) {
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+        if (kCV) {
+            const double2 v = ((const double2*)x)[i + u * st];
+            re[u] = v.x;
+            im[u] = v.y;
+        } else {
+            re[u] = ((const double*)x)[i + u * st];
+            im[u] = 0.0;
+        }
+        k[u] = stab ? (unsigned)stab[i + u * st] : 1u;
+    }
+}
+
+// max of v over the block (bit patterns of non-negative doubles order as the values)
+__device__ __forceinline__ unsigned long long fx_block_max(unsigned long long m) {
+    __shared__ unsigned long long wm[kThreads / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = threadIdx.x < kThreads / 32 ? wm[threadIdx.x] : 0ull;
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+    return m;   // valid in thread 0
+}
+
+// pass 1: per block, a bound of max |x_j sqrt(stab_j)| within a factor of two
+template <bool kCV>
+__global__ void __launch_bounds__(kThreads) fx_max_kernel(const void* __restrict__ x, const uint16_t* __restrict__ stab,
+                                                          int64_t n, unsigned long long* __restrict__ part) {
+    unsigned long long m = 0;
+    const int64_t st = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    auto take = [&](double re, double im, unsigned k) {
+        const int c = fx_sqrt_exp(k);
+        m = max(m, fx_bound_bits(re, c));
+        if (kCV) m = max(m, fx_bound_bits(im, c));
+    };
+    for (; i + 3 * st < n; i += 4 * st) {
+        double re[4], im[4];
+        unsigned k[4];
+        fx_load<kCV, 4>(x, stab, i, st, re, im, k);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) take(re[u], im[u], k[u]);
+    }
+    for (; i < n; i += st) {
+        double re[1], im[1];
+        unsigned k[1];
+        fx_load<kCV, 1>(x, stab, i, st, re, im, k);
+        take(re[0], im[0], k[0]);
+    }
+    m = fx_block_max(m);
+    if (threadIdx.x == 0) part[blockIdx.x] = m;
+}
+
+// pass 2: every block reduces the partial bounds (a few KB from L2), block 0
+// publishes the total for the product kernel, and round(x_j sqrt(stab_j) 2^K)
+// is stored as int64 (one FP64 multiply, the rounding in integers)
+template <bool kCV>
+__global__ void __launch_bounds__(kThreads) fx_quant_kernel(const void* __restrict__ x, const uint16_t* __restrict__ stab,
+                                                            const double* __restrict__ sq, int64_t n,
+                                                            const unsigned long long* __restrict__ part, int nparts,
+                                                            unsigned long long* __restrict__ maxbits, int len_bits,
+                                                            void* __restrict__ xq) {
+    __shared__ double sqs[kMaxGroup + 1];
+    __shared__ unsigned long long total;
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) sqs[i] = sq[i];
+    unsigned long long m = 0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) m = max(m, part[i]);
+    m = fx_block_max(m);
+    if (threadIdx.x == 0) {
+        total = m;
+        if (blockIdx.x == 0) *maxbits = m;
+    }
+    __syncthreads();
+    const unsigned long long mb = total;
+    if (!fx_finite(mb)) return;   // the product kernel takes the FP64 path
+    const int K = fx_shift(mb, len_bits);
+    auto store = [&](int64_t r, double re, double im, unsigned k) {
+        const double s = sqs[k];
+        if (kCV) {
+            longlong2 q;
+            q.x = fx_round_scaled(stab ? re * s : re, K);
+            q.y = fx_round_scaled(stab ? im * s : im, K);
+            ((longlong2*)xq)[r] = q;
+        } else {
+            ((long long*)xq)[r] = fx_round_scaled(stab ? re * s : re, K);
+        }
+    };
+    const int64_t st = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; i + 3 * st < n; i += 4 * st) {
+        double re[4], im[4];
+        unsigned k[4];
+        fx_load<kCV, 4>(x, stab, i, st, re, im, k);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) store(i + u * st, re[u], im[u], k[u]);
+    }
+    for (; i < n; i += st) {
+        double re[1], im[1];
+        unsigned k[1];
+        fx_load<kCV, 1>(x, stab, i, st, re, im, k);
+        store(i, re[0], im[0], k[0]);
+    }
+}
+
+// y[r] = beta y[r] + alpha (d[r] x[r] + acc) for a real diagonal
+template <bool kCV>
+__device__ __forceinline__ void fx_store_row(const SellArgs& a, int64_t r, double acc_r, double acc_i) {
+    const double dr = ((const double*)a.diag_re)[r];
+    if (kCV) {
+        const double2 xv = ((const double2*)a.x)[r];
+        acc_r += dr * xv.x;
+        acc_i += dr * xv.y;
+        double2* y = (double2*)a.y;
+        double yr = 0, yi = 0;
+        if (!a.beta_zero) {
+            const double2 yo = y[r];
+            yr = a.br * yo.x - a.bi * yo.y;
+            yi = a.br * yo.y + a.bi * yo.x;
+        }
+        double2 o;
+        o.x = yr + a.ar * acc_r - a.ai * acc_i;
+        o.y = yi + a.ar * acc_i + a.ai * acc_r;
+        y[r] = o;
+    } else {
+        acc_r += dr * ((const double*)a.x)[r];
+        double* y = (double*)a.y;
+        const double yr = a.beta_zero ? 0.0 : a.br * y[r];
+        y[r] = yr + a.ar * acc_r;
+    }
+}
+
+// One thread per row: integer sums per amplitude class, FP64 per row.  NC is
+// the number of class accumulators (the operator's classes, rounded up).
+// x that holds a NaN or an infinity has no fixed-point scale: then every row
+// is computed as by the FP64 product, so non-finite values propagate alike.
+template <bool kCV, bool kPacked, int NC, int U, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) sell_fx_kernel(SellArgs a, FxArgs f) {
+    __shared__ uint32_t ccls[kFxCodes];
+    __shared__ double rsk[kMaxGroup + 1];
+    __shared__ double amp[NC];
+    const unsigned long long mb = *f.maxbits;
+    const int K = fx_shift(mb, f.len_bits);
+    // 2^-K folds into the row scale unless it leaves the normal range
+    const bool fold = K >= -900 && K <= 900;
+    for (int i = threadIdx.x; i < a.ncodes; i += blockDim.x) ccls[i] = f.cls[i];
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) {
+        const double r = i ? 1.0 / sqrt((double)i) : 0.0;
+        rsk[i] = fold ? r * fx_pow2(-K) : r;
+    }
+    if (threadIdx.x < NC) amp[threadIdx.x] = f.amp[threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    if (!fx_finite(mb)) {
+        // the FP64 product's arithmetic
+        const double2* __restrict__ tab = (const double2*)a.table;
+        for (int64_t s = a.slice0 + warp0; s < a.nslices; s += nwarps) {
+            const int64_t r = s * kSlice + lane;
+            if (r >= a.n) continue;
+            double acc_r = 0, acc_i = 0;
+            if (kCV) {
+                const double2* __restrict__ x = (const double2*)a.x;
+                sell_row<1, kPacked>(a.words, a.cols, a.codes, a.sptr[s] + lane, a.len[r], a.code_bits, a.code_mask,
+                                     [&](uint32_t c) { return __ldg(x + c); },
+                                     [&](uint32_t code, double2 xv) {
+                                         const double v = __ldg(&tab[code].x);
+                                         acc_r += v * xv.x;
+                                         acc_i += v * xv.y;
+                                     });
+            } else {
+                const double* __restrict__ x = (const double*)a.x;
+                sell_row<1, kPacked>(a.words, a.cols, a.codes, a.sptr[s] + lane, a.len[r], a.code_bits, a.code_mask,
+                                     [&](uint32_t c) { return __ldg(x + c); },
+                                     [&](uint32_t code, double xv) { acc_r += __ldg(&tab[code].x) * xv; });
+            }
+            const double sc = a.stab ? 1.0 / sqrt((double)a.stab[r]) : 1.0;
+            fx_store_row<kCV>(a, r, acc_r * sc, acc_i * sc);
+        }
+        return;
+    }
+    // rows and slices fit in 32 bits (columns are 32-bit): fewer registers
+    const int nsl = (int)a.nslices, nrows = (int)a.n, step = (int)nwarps;
+    for (int s = (int)(a.slice0 + warp0); s < nsl; s += step) {
+        const int r = s * kSlice + lane;
+        if (r >= nrows) continue;
+        const int len = a.len[r];
+        const int64_t base = a.sptr[s] + lane;
+        double acc_r = 0, acc_i = 0;
+        // all classes' signed sum (the sign applied as a mask), and the sums of
+        // classes 1 .. NC-1 by mask; class 0 is their difference (exact in two's
+        // complement)
+        if (kCV) {
+            long long tr = 0, ti = 0, sr[NC], si[NC];
+#pragma unroll
+            for (int c = 1; c < NC; ++c) sr[c] = si[c] = 0;
+            const longlong2* __restrict__ xq = (const longlong2*)f.xq;
+            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return __ldg(xq + c); },
+                                 [&](uint32_t code, longlong2 q) {
+                                     const uint32_t w = ccls[code];
+                                     const long long m = -(long long)(w & 1u);
+                                     const long long vr = (q.x ^ m) - m, vi = (q.y ^ m) - m;
+                                     tr += vr;
+                                     ti += vi;
+#pragma unroll
+                                     for (int c = 1; c < NC; ++c) {
+                                         const long long cm = -(long long)((w >> 1) == (uint32_t)c);
+                                         sr[c] += vr & cm;
+                                         si[c] += vi & cm;
+                                     }
+                                 });
+            long long r0 = tr, i0 = ti;
+#pragma unroll
+            for (int c = 1; c < NC; ++c) {
+                r0 -= sr[c];
+                i0 -= si[c];
+                acc_r = fma(amp[c], __ll2double_rn(sr[c]), acc_r);
+                acc_i = fma(amp[c], __ll2double_rn(si[c]), acc_i);
+            }
+            acc_r = fma(amp[0], __ll2double_rn(r0), acc_r);
+            acc_i = fma(amp[0], __ll2double_rn(i0), acc_i);
+        } else {
+            long long t = 0, sr[NC];
+#pragma unroll
+            for (int c = 1; c < NC; ++c) sr[c] = 0;
+            const long long* __restrict__ xq = (const long long*)f.xq;
+            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return __ldg(xq + c); },
+                                 [&](uint32_t code, long long q) {
+                                     const uint32_t w = ccls[code];
+                                     const long long m = -(long long)(w & 1u);
+                                     const long long v = (q ^ m) - m;
+                                     t += v;
+#pragma unroll
+                                     for (int c = 1; c < NC; ++c) sr[c] += v & -(long long)((w >> 1) == (uint32_t)c);
+                                 });
+            long long r0 = t;
+#pragma unroll
+            for (int c = 1; c < NC; ++c) {
+                r0 -= sr[c];
+                acc_r = fma(amp[c], __ll2double_rn(sr[c]), acc_r);
+            }
+            acc_r = fma(amp[0], __ll2double_rn(r0), acc_r);
+        }
+        const double sc = rsk[a.stab ? a.stab[r] : 1];
+        acc_r *= sc;
+        acc_i *= sc;
+        if (!fold) {
+            const int k1 = K / 2;
+            const double u1 = fx_pow2(-k1), u2 = fx_pow2(k1 - K);
+            acc_r = acc_r * u1 * u2;
+            acc_i = acc_i * u1 * u2;
+        }
+        fx_store_row<kCV>(a, r, acc_r, acc_i);
+    }
+}
+
+// the fixed-point product's variants (gathers in flight, resident blocks):
+// complex vectors and four classes hold more accumulators, so fewer blocks
+template <bool kCV, bool kPacked, int NC>
+void launch_fx(int v, int grid, cudaStream_t s, const SellArgs& a, const FxArgs& f) {
+    constexpr int B0 = kCV ? 4 : (NC <= 2 ? 8 : 6);
+    constexpr int B1 = (kCV || NC > 2) ? 4 : 6;
+    if (v == 0) sell_fx_kernel<kCV, kPacked, NC, 1, B0><<<grid, kThreads, 0, s>>>(a, f);
+    else if (v == 1) sell_fx_kernel<kCV, kPacked, NC, 2, B1><<<grid, kThreads, 0, s>>>(a, f);
+    else sell_fx_kernel<kCV, kPacked, NC, 4, 4><<<grid, kThreads, 0, s>>>(a, f);
+}
+
 int grid_rows(int64_t threads_needed) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -691,8 +1051,11 @@ void build_sell(const Basis& b, Assembled& M, cudaStream_t s) {
     const int64_t n = b.n;
     std::vector<int64_t> rp(n + 1);
     QS_CUDA(cudaMemcpy(rp.data(), M.rowptr.p, (n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
-    for (int64_t r = 0; r < n; ++r)
-        if (rp[r + 1] - rp[r] > 65535) return;  // keep the CSR path
+    int64_t maxlen = 0;
+    for (int64_t r = 0; r < n; ++r) maxlen = std::max<int64_t>(maxlen, rp[r + 1] - rp[r]);
+    if (maxlen > 65535) return;  // keep the CSR path
+    M.len_bits = 0;
+    while (((int64_t)1 << M.len_bits) < maxlen) ++M.len_bits;
     M.nslices = (n + kSlice - 1) / kSlice;
     const int64_t npos = M.nslices * kSlice;
     std::vector<int32_t> perm(npos, -1);
@@ -821,6 +1184,36 @@ void op_assemble(Op& op) {
     }
     M.table_df.alloc(ncodes * 4 * sizeof(float));
     QS_CUDA(cudaMemcpy(M.table_df.p, tdf.data(), ncodes * 4 * sizeof(float), cudaMemcpyHostToDevice));
+    {
+        // fixed-point row sums: value(code) = +-amp[class] * D[d], with class =
+        // a * nC + c real and at most four of them
+        const int ncls = nA * nC;
+        bool ok = !op.complex_mat && ncls <= 4 && ncodes <= kFxCodes;
+        std::vector<double> amp(4, 0.0);
+        for (int a = 0; ok && a < nA; ++a)
+            for (int c = 0; c < nC; ++c) {
+                const cd v = A[a] * C[c];
+                if (v.imag() != 0.0) ok = false;
+                amp[a * nC + c] = v.real();
+            }
+        M.fx_classes = 0;
+        if (ok) {
+            // per code: class << 1 | sign
+            std::vector<uint32_t> cls(ncodes);
+            for (int64_t code = 0; code < ncodes; ++code)
+                cls[code] = (uint32_t)((((code >> 1) / nD) << 1) | (code & 1));
+            std::vector<double> sq(kMaxGroup + 1);
+            for (int i = 0; i <= kMaxGroup; ++i) sq[i] = std::sqrt((double)i);
+            M.fx_cls.alloc(cls.size() * sizeof(uint32_t));
+            QS_CUDA(cudaMemcpy(M.fx_cls.p, cls.data(), cls.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+            M.fx_amp.alloc(4 * sizeof(double));
+            QS_CUDA(cudaMemcpy(M.fx_amp.p, amp.data(), 4 * sizeof(double), cudaMemcpyHostToDevice));
+            M.fx_sq.alloc(sq.size() * sizeof(double));
+            QS_CUDA(cudaMemcpy(M.fx_sq.p, sq.data(), sq.size() * sizeof(double), cudaMemcpyHostToDevice));
+            M.fx_max.alloc((1 + kFxParts) * sizeof(unsigned long long));
+            M.fx_classes = ncls;
+        }
+    }
     {
         std::vector<float> rq(2 * (kMaxGroup + 1), 0.f);
         for (int i = 1; i <= kMaxGroup; ++i) df_split_host(1.0 / std::sqrt((double)i), rq[2 * i], rq[2 * i + 1]);
@@ -964,6 +1357,44 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
 #define L_DFIO(U_, B_) QS_SHAPES(sell_dfio_kernel, U_, B_, a, td, dd, rq)
                 QS_VARIANTS(L_DFIO, v);
 #undef L_DFIO
+            };
+        } else if (c.fx && !c.single && M.fx_classes > 0) {
+            kind = 4;
+            a.table = M.table64.p;
+            a.diag = op.d_diag.p;
+            a.diag_re = op.d_diag_re.p;
+            FxArgs f{};
+            f.cls = M.fx_cls.as<uint32_t>();
+            f.amp = M.fx_amp.as<double>();
+            f.sq = M.fx_sq.as<double>();
+            f.part = M.fx_max.as<unsigned long long>() + 1;
+            f.maxbits = M.fx_max.as<unsigned long long>();
+            f.len_bits = M.len_bits;
+            f.xq = M.xsplit.p;
+            if (!c.fx_ready) {
+                // max |x sqrt(stab)| per block, then the total and the scaled integer copy
+                const int sg = std::min(grid_rows(b.n), kFxParts);
+                if (cv) {
+                    fx_max_kernel<true><<<sg, kThreads, 0, s>>>(c.x, a.stab, b.n, f.part);
+                    fx_quant_kernel<true><<<sg, kThreads, 0, s>>>(c.x, a.stab, f.sq, b.n, f.part, sg, f.maxbits,
+                                                                  f.len_bits, f.xq);
+                } else {
+                    fx_max_kernel<false><<<sg, kThreads, 0, s>>>(c.x, a.stab, b.n, f.part);
+                    fx_quant_kernel<false><<<sg, kThreads, 0, s>>>(c.x, a.stab, f.sq, b.n, f.part, sg, f.maxbits,
+                                                                   f.len_bits, f.xq);
+                }
+                QS_CUDA(cudaGetLastError());
+                note_launches(2);
+            }
+            const int nc = M.fx_classes;
+            launch = [&, f, nc](int v) {
+                if (a.packed) {
+                    if (cv) (nc <= 2 ? launch_fx<true, true, 2> : launch_fx<true, true, 4>)(v, grid, s, a, f);
+                    else (nc <= 2 ? launch_fx<false, true, 2> : launch_fx<false, true, 4>)(v, grid, s, a, f);
+                } else {
+                    if (cv) (nc <= 2 ? launch_fx<true, false, 2> : launch_fx<true, false, 4>)(v, grid, s, a, f);
+                    else (nc <= 2 ? launch_fx<false, false, 2> : launch_fx<false, false, 4>)(v, grid, s, a, f);
+                }
             };
         } else if (c.df && !c.single) {
             kind = 2;
@@ -1195,10 +1626,12 @@ void op_export_csr(Op& op, int64_t* rowptr, int64_t* cols, double* values, doubl
 bool op_matvec_host_overlap(Op& op, const MatvecCall& c0, void* y_host, size_t eb) {
     const Assembled& M = op.asm_;
     const bool T = (c0.flags & QS_TRANSPOSE) != 0;
-    if (!op.commuting || !op.assembled || !M.has_sell || (T && !op.hermitian) || c0.df || c0.df_io) return false;
+    const bool fx = c0.fx && !c0.single && M.fx_classes > 0;
+    if (!op.commuting || !op.assembled || !M.has_sell || (T && !op.hermitian) || (c0.df && !fx) || c0.df_io)
+        return false;
     if (!(c0.beta.re == 0.0 && c0.beta.im == 0.0)) return false;   // y is not read
     // the first product of a kind times the kernel variants on the full range
-    if (M.sell_variant[c0.single ? 1 : 0] < 0) return false;
+    if (M.sell_variant[fx ? 4 : (c0.single ? 1 : 0)] < 0) return false;
     constexpr int K = 4;
     if (M.nslices < 4 * K) return false;
     if (!op.copy_stream) {
@@ -1210,6 +1643,7 @@ bool op_matvec_host_overlap(Op& op, const MatvecCall& c0, void* y_host, size_t e
         MatvecCall c = c0;
         c.slice0 = M.nslices * k / K;
         c.slice1 = M.nslices * (k + 1) / K;
+        c.fx_ready = k > 0;   // the first range makes the integer copy of x for all
         op_spmv_device(op, c, op.stream);
         QS_CUDA(cudaEventRecord(op.range_done[k], op.stream));
         QS_CUDA(cudaStreamWaitEvent(op.copy_stream, op.range_done[k], 0));

@@ -6,6 +6,7 @@
 namespace qs {
 
 constexpr int kSellSlice = 32;   // rows per slice of the sliced-ELL layout
+constexpr int kFxCodes = 256;    // value codes of an operator with fixed-point row sums, at most
 
 #ifdef __CUDACC__
 // The nonzeros of one sliced-ELL row (`len` of them from `base`, stride
@@ -78,10 +79,20 @@ struct Assembled {
     DevBuf sell_len;    // uint16 length of each slice position's row
     int64_t nslices = 0;
     bool has_sell = false;
+    // exact fixed-point row sums (FP64 vectors): usable when every stored
+    // value is real and is +-A_c sqrt(stab_col) for at most four amplitude
+    // classes c; fx_classes = 0 otherwise
+    int fx_classes = 0;
+    int len_bits = 0;   // ceil(log2(longest row)), at least 0
+    DevBuf fx_cls;      // uint32 per code: class << 1 | sign
+    DevBuf fx_amp;      // double per class: A_c
+    DevBuf fx_sq;       // double sqrt(i), i = 0 .. kMaxGroup
+    DevBuf fx_max;      // uint64: max |x_j sqrt(stab_j)| of the current product (bit pattern), then per-block maxima
     // sliced-ELL kernel variant (gathers in flight x resident blocks) per
     // product kind (FP64, FP32, double-float with FP64 vectors, double-float
-    // vectors), chosen by timing on the first product that allows it (-1: not yet)
-    int sell_variant[4] = {-1, -1, -1, -1};
+    // vectors, fixed-point row sums), chosen by timing on the first product
+    // that allows it (-1: not yet)
+    int sell_variant[5] = {-1, -1, -1, -1, -1};
 };
 
 }  // namespace qs

@@ -225,6 +225,11 @@ int qs_op_assemble(qs_op* op) {
 
 int64_t qs_op_nnz(const qs_op* op) { return op->op->assembled ? op->op->asm_.nnz : -1; }
 
+int32_t qs_op_fixed_point_classes(const qs_op* op) {
+    const qs::Op& o = *op->op;
+    return o.assembled && o.asm_.has_sell ? o.asm_.fx_classes : 0;
+}
+
 int qs_op_export_csr(qs_op* op, int64_t* rowptr, int64_t* cols, double* values, double* diag) {
     return guard([&] {
         if (!op || !rowptr || !diag) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
@@ -262,6 +267,7 @@ int qs_op_matvec(qs_op* op, int32_t flags, const double* alpha, const void* x, i
         qs::MatvecCall c;
         c.flags = flags & (QS_TRANSPOSE | QS_CONJUGATE);
         c.df = (flags & QS_DOUBLE_FLOAT) != 0;
+        c.fx = (flags & QS_FIXED_POINT) != 0;
         c.alpha = qs::cx(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
         c.beta = qs::cx(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
         c.single = single;

@@ -208,6 +208,8 @@ struct MatvecCall {
     bool single = false;            // FP32 vectors and accumulation
     bool df = false;                // FP64 vectors, double-float products (assembled form)
     bool df_io = false;             // double-float vectors in and out, alpha = 1, beta = 0
+    bool fx = false;                // FP64 vectors, exact fixed-point row sums where the operator allows
+    bool fx_ready = false;          // the scaled integer copy of x is already made (later row ranges)
     bool no_tune = false;           // never time kernel variants inside this call
     int64_t slice0 = 0, slice1 = -1; // sliced-ELL slices [slice0, slice1) only (-1: to the end)
 };

@@ -75,7 +75,7 @@ QS_REQ_EIGSH, QS_REQ_EVOLVE = 0, 1
 QS_F64, QS_C128, QS_F32, QS_C64 = 0, 1, 2, 3
 QS_MEM_HOST, QS_MEM_DEVICE = 0, 1
 QS_CHECK_SYMM, QS_CHECK_HERM, QS_CHECK_PCON, QS_DIAG_COMPLEX = 1, 2, 4, 8
-QS_TRANSPOSE, QS_CONJUGATE, QS_DOUBLE_FLOAT = 1, 2, 4
+QS_TRANSPOSE, QS_CONJUGATE, QS_DOUBLE_FLOAT, QS_FIXED_POINT = 1, 2, 4, 8
 
 # every symbol declared in include/qsgpu.h
 EXPORTS = (
@@ -83,7 +83,7 @@ EXPORTS = (
     "qs_basis_states", "qs_basis_orbit_minima", "qs_basis_state_index", "qs_basis_representative",
     "qs_op_create", "qs_op_destroy", "qs_op_dtype", "qs_op_hermitian", "qs_op_set_diagonal", "qs_op_matvec",
     "qs_eigsh", "qs_expm_multiply", "qs_evolve", "qs_last_error", "qs_version", "qs_op_set_stream",
-    "qs_launch_count", "qs_op_assemble", "qs_op_nnz", "qs_op_matvec_noalloc",
+    "qs_launch_count", "qs_op_assemble", "qs_op_nnz", "qs_op_fixed_point_classes", "qs_op_matvec_noalloc",
     "qs_eigsh_batch", "qs_basis_stabilizers",
     "qs_server_create", "qs_server_destroy", "qs_server_submit", "qs_server_poll", "qs_server_wait",
     "qs_server_vector", "qs_server_release", "qs_server_stats",
@@ -160,6 +160,8 @@ def load():
     L.qs_op_assemble.argtypes = [P]
     L.qs_op_nnz.argtypes = [P]
     L.qs_op_nnz.restype = i64
+    L.qs_op_fixed_point_classes.argtypes = [P]
+    L.qs_op_fixed_point_classes.restype = ctypes.c_int32
     L.qs_launch_count.restype = i64
     L.qs_last_error.restype = ctypes.c_char_p
     L.qs_version.restype = ctypes.c_char_p

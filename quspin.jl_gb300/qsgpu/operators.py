@@ -141,10 +141,10 @@ class QuantumLinearOperator:
             raise DimensionMismatch("operator and value dimensions do not match")
         if x.ndim != out.ndim or (x.ndim == 2 and x.shape[1] != out.shape[1]):
             raise DimensionMismatch("output has the wrong dimensions")
-        if precision not in ("fp64", "fp32", "fp64df"):
-            raise ArgumentError("precision must be fp64, fp32 or fp64df")
+        if precision not in ("fp64", "fp32", "fp64df", "fp64fx"):
+            raise ArgumentError("precision must be fp64, fp32, fp64df or fp64fx")
         single = precision == "fp32"
-        flags = self._flags | (_lib.QS_DOUBLE_FLOAT if precision == "fp64df" else 0)
+        flags = self._flags | {"fp64df": _lib.QS_DOUBLE_FLOAT, "fp64fx": _lib.QS_FIXED_POINT}.get(precision, 0)
         nrhs = 1 if x.ndim == 1 else x.shape[1]
         ycx = np.iscomplexobj(out)
         if (np.iscomplexobj(x) or self.dtype == np.complex128 or complex(alpha).imag or complex(beta).imag) and not ycx:
@@ -227,6 +227,11 @@ class Hamiltonian(QuantumLinearOperator):
     @property
     def nnz(self):
         return int(_lib.load().qs_op_nnz(self._h))
+
+    @property
+    def fixed_point_classes(self):
+        """Amplitude classes of the precision="fp64fx" product (0: it runs as FP64)."""
+        return int(_lib.load().qs_op_fixed_point_classes(self._h))
 
     def _export(self):
         """The device's assembled matrix as a scipy CSR matrix (duplicates summed)."""
