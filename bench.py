@@ -522,6 +522,83 @@ def section_blocks(qs, torch, L=24, nt=10):
             "max_state_diff_batched_vs_sequential": err, "norm_drift": drift}
 
 
+def section_sweep(qs, torch, sizes=(24, 26, 28, 30), reps=10):
+    """Roofline sweep: periodic XXZ (J=1, Delta=0.5, pauli=false) at nup=L/2
+    without spatial symmetry, L = 24 .. 30 (N up to 155,117,520; the FP64
+    vector alone is 1.24 GB, ten times L2).  Per size: the assembled FP64
+    product, the fixed-point form and the matrix-free product on device
+    buffers, CUDA events on the operator's stream, a 256 MB buffer written
+    between timed products.  Algorithmic bytes of the assembled product:
+    4 per stored transition + 26 per row (row length, diagonal, x[r], y[r]);
+    the x gathers are extra DRAM traffic once x exceeds L2 (the DRAM bytes
+    of the L=28 product are in the profile summary)."""
+    import ctypes
+    from qsgpu import _lib
+    lib = _lib.load()
+    peak, _ = load_peaks()
+    one, zero = np.array([1.0, 0.0]), np.array([0.0, 0.0])
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = {"workload": "periodic XXZ J=1 Delta=0.5, nup=L/2, no spatial symmetry", "peak_gbs": peak, "sizes": {}}
+
+    def timed(o, xt, yt, flags, n):
+        _lib.check(lib.qs_op_set_stream(o._h, ctypes.c_void_p(stream.cuda_stream)))
+
+        def mv():
+            _lib.check(lib.qs_op_matvec(o._h, flags, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()), _lib.QS_F64,
+                                        _lib.ptr(zero), ctypes.c_void_p(yt.data_ptr()), _lib.QS_F64, 1,
+                                        _lib.QS_MEM_DEVICE))
+        for _ in range(3):
+            mv()
+        torch.cuda.synchronize()
+        ts = []
+        with torch.cuda.stream(stream):
+            for _ in range(n):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                mv()
+                e1.record(stream)
+                ts.append((e0, e1))
+        torch.cuda.synchronize()
+        return float(np.mean([a.elapsed_time(b) for a, b in ts]))
+
+    for L in sizes:
+        spec = xxz_spec(L)
+        terms = [qs.OperatorTerm(o, c) for o, c in spec]
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        b = qs.SpinBasis1D(L, nup=L // 2, pauli=False)
+        t_basis = time.perf_counter() - t
+        t = time.perf_counter()
+        H = qs.Hamiltonian(b, terms)
+        torch.cuda.synchronize()
+        t_asm = time.perf_counter() - t
+        n, nnz = b.Ns, H.nnz
+        x = torch.from_numpy(np.random.default_rng(20261203).standard_normal(n)).cuda()
+        y = torch.empty_like(x)
+        byts = 4 * nnz + 26 * n
+        ms64 = timed(H, x, y, 0, reps)
+        y64 = y.clone()
+        msfx = timed(H, x, y, _lib.QS_FIXED_POINT, reps)
+        fx_err = float((y - y64).norm() / y64.norm())
+        del H
+        op = qs.QuantumLinearOperator(b, terms)
+        msmf = timed(op, x, y, 0, 3)
+        mf_err = float((y - y64).norm() / y64.norm())
+        del op, x, y, y64
+        torch.cuda.empty_cache()
+        out["sizes"][str(L)] = {
+            "N": n, "nnz": nnz, "basis_s": round(t_basis, 3), "assemble_s": round(t_asm, 3),
+            "bytes_per_product": byts,
+            "fp64_ms": ms64, "fp64_gbs": byts / ms64 / 1e6, "fp64_frac": byts / ms64 / 1e6 / peak,
+            "fixed_point_ms": msfx, "fixed_point_gbs": byts / msfx / 1e6, "fixed_point_frac": byts / msfx / 1e6 / peak,
+            "fixed_point_rel_err": fx_err,
+            "matrix_free_ms": msmf, "matrix_free_rel_diff": mf_err}
+    del flush
+    return out
+
+
 def torus_blocks(Lx, Ly):
     """Site maps of the Lx x Ly torus (site = x + Lx y, zero-based): the two
     translations, the x reflection and the spin flip (negative entries)."""
@@ -698,6 +775,32 @@ def profile_range(kind):
         dt = time.perf_counter() - t
         torch.cuda.profiler.stop()
         print(json.dumps({"profile_range": kind, "e0": float(v[0]), "seconds": dt}))
+        return
+    if kind == "sweep28":
+        # one assembled FP64 product of the XXZ L=28 sector without spatial
+        # symmetry (N = 40,116,600; x 321 MB, the packed words 2.3 GB)
+        import ctypes
+        from qsgpu import _lib
+        lib = _lib.load()
+        L = 28
+        b = qs.SpinBasis1D(L, nup=L // 2, pauli=False)
+        H = qs.Hamiltonian(b, [qs.OperatorTerm(o, c) for o, c in xxz_spec(L)])
+        one, zero = np.array([1.0, 0.0]), np.array([0.0, 0.0])
+        xt = torch.from_numpy(np.random.default_rng(20261203).standard_normal(b.Ns)).cuda()
+        yt = torch.empty_like(xt)
+
+        def mv():
+            _lib.check(lib.qs_op_matvec(H._h, 0, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()), _lib.QS_F64,
+                                        _lib.ptr(zero), ctypes.c_void_p(yt.data_ptr()), _lib.QS_F64, 1,
+                                        _lib.QS_MEM_DEVICE))
+        for _ in range(3):
+            mv()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        mv()
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_range": kind, "N": b.Ns, "nnz": H.nnz, "ynorm": float(yt.norm())}))
         return
     if kind.startswith("product") or kind == "matrixfree":
         L = 32
@@ -916,7 +1019,10 @@ def run_ours(args, wl, world, rank, local):
                          ("ftlm_L26", lambda: section_ftlm(qs, torch)),
                          ("blocks_L24_evolve", lambda: section_blocks(qs, torch)),
                          ("general_6x6_heisenberg", lambda: section_general(qs, torch, Lx=6, Ly=6, J2=0.0)),
+                         ("roofline_sweep_xxz", lambda: section_sweep(qs, torch)),
                          ("c5_serving", lambda: section_c5(qs, torch, n_req=args.serve_requests))):
+            if args.only_section and name != args.only_section:
+                continue
             try:
                 sections[name] = fn()
             except Exception as exc:  # a failing side workload must not hide the headline
@@ -987,8 +1093,9 @@ def main():
     ap.add_argument("--no-sections", action="store_true",
                     help="skip the side workloads (XXZ L=16, batched sectors, TFIM evolve, serving)")
     ap.add_argument("--serve-requests", type=int, default=2000, help="requests in the serving workload")
+    ap.add_argument("--only-section", default=None, help="run this side workload only (by its JSON key)")
     ap.add_argument("--profile-range", default=None,
-                    choices=["product64", "product32", "productdf", "productfx", "matrixfree", "lanczos64", "lanczosdf",
+                    choices=["product64", "product32", "productdf", "productfx", "sweep28", "matrixfree", "lanczos64", "lanczosdf",
                              "batch24", "batch26", "ftlm"],
                     help="run one unit inside cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     args = ap.parse_args()

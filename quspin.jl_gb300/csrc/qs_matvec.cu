@@ -146,6 +146,46 @@ __device__ __forceinline__ U row_state(const MvArgs& a, int mode, int64_t r) {
     return s;
 }
 
+// The fixed-weight state of combinadic rank r (inverse of combinadic_rank32),
+// with the C(bit, p) table in shared memory.
+__device__ __forceinline__ uint32_t unrank32(int64_t r, const uint32_t* binom32, int L, int nup) {
+    uint32_t s = 0, rem = (uint32_t)r;
+    int b = L - 1;
+    for (int p = nup; p >= 1; --p) {
+        while (binom32[b * 33 + p] > rem) --b;
+        s |= 1u << b;
+        rem -= binom32[b * 33 + p];
+        --b;
+    }
+    return s;
+}
+
+// rank(t) from rank(s) = rs for fixed-weight states of equal weight that
+// differ only in bits lo .. hi: the set bits below lo and above hi keep their
+// particle numbers, so only the set bits inside the span change their terms
+// C(bit, particle).  A short span (a bond, a plaquette) costs a few table
+// reads instead of the nup of a full rank; a long one (the periodic bond of a
+// chain) takes the full rank of t.
+__device__ __forceinline__ int64_t rank_from32(uint32_t s, int64_t rs, uint32_t t, const uint32_t* binom32) {
+    const uint32_t f = s ^ t;
+    if (!f) return rs;
+    const int lo = __ffs((int)f) - 1, hi = 31 - __clz((int)f);
+    if (hi - lo > 8) return combinadic_rank32(t, binom32);
+    const uint32_t span = (hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u)) & ~((1u << lo) - 1u);
+    const int m0 = __popc(s & ((1u << lo) - 1u));
+    int64_t d = 0;
+    uint32_t bs = s & span, bt = t & span;
+    for (int p = m0 + 1; bs; ++p) {
+        d -= binom32[(__ffs((int)bs) - 1) * 33 + p];
+        bs &= bs - 1;
+    }
+    for (int p = m0 + 1; bt; ++p) {
+        d += binom32[(__ffs((int)bt) - 1) * 33 + p];
+        bt &= bt - 1;
+    }
+    return rs + d;
+}
+
 template <typename T, bool kCV>
 __device__ __forceinline__ void load_x(const MvArgs& a, int64_t i, T& xr, T& xi) {
     if (kCV) {
@@ -163,18 +203,20 @@ __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
     constexpr bool kSym = kMode >= 2;
     __shared__ GroupSmem g;
     __shared__ U spl[kMode == 2 ? kMaxSplit : 1];
-    __shared__ uint32_t binom32[kMode == 3 && sizeof(U) == 4 ? 32 * 33 : 1];
+    constexpr bool kB32 = (kMode == 3 || kMode == 1) && sizeof(U) == 4;
+    __shared__ uint32_t binom32[kB32 ? 32 * 33 : 1];
     __shared__ TermProg progs[kSmemProgs];
     __shared__ double sqrt_stab[kMaxGroup + 1];
     if (kSym) {
         load_group_smem(g, a.group);
         if (kMode == 2)
             for (int i = threadIdx.x; i < a.nsplit; i += blockDim.x) spl[i] = ((const U*)a.split)[i];
-        if (kMode == 3 && sizeof(U) == 4)
-            for (int i = threadIdx.x; i < 32 * 33; i += blockDim.x)
-                binom32[i] = (uint32_t)a.binom[(i / 33) * 65 + (i % 33)];
         for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) sqrt_stab[i] = sqrt((double)i);
     }
+    // C(bit, p) for bit < 32, p <= 32: all below 2^32
+    if (kB32 && a.nup >= 0)
+        for (int i = threadIdx.x; i < 32 * 33; i += blockDim.x)
+            binom32[i] = (uint32_t)a.binom[(i / 33) * 65 + (i % 33)];
     const int np_smem = a.nprog < kSmemProgs ? a.nprog : kSmemProgs;
     for (int i = threadIdx.x; i < np_smem; i += blockDim.x) progs[i] = a.progs[i];
     __syncthreads();
@@ -182,7 +224,7 @@ __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
     const double* chi_im = a.group->chi_im;
 
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.n; r += (int64_t)gridDim.x * blockDim.x) {
-        const U s = row_state<U>(a, kSym ? 2 : kMode, r);
+        const U s = (kB32 && kMode == 1) ? (U)unrank32(r, binom32, a.L, a.nup) : row_state<U>(a, kSym ? 2 : kMode, r);
         T inv_sr = 1;
         if (kSym) inv_sr = (T)1 / (T)sqrt_stab[a.stab[r]];
         T acc_r = 0, acc_i = 0;
@@ -229,7 +271,8 @@ __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
                 }
             } else if (kMode == 1) {
                 if (__popcll((unsigned long long)t) != a.nup) continue;
-                idx = combinadic_rank<U>(t, a.binom, 65);
+                if (kB32) idx = rank_from32((uint32_t)s, r, (uint32_t)t, binom32);
+                else idx = combinadic_rank<U>(t, a.binom, 65);
             } else {
                 idx = (int64_t)t;
             }
@@ -450,7 +493,10 @@ void launch_matvec(const Basis& b, const MvArgs& a, bool cm, bool cv, cudaStream
         if (b.wide) launch_mode<uint64_t, 2, T>(a, cm, cv, s);
         else launch_mode<uint32_t, 2, T>(a, cm, cv, s);
     } else if (b.nup >= 0) {
-        launch_mode<uint64_t, 1, T>(a, cm, cv, s);
+        // up to 32 sites: 32-bit states, the binomial table in shared memory
+        // and ranks updated from the row's own rank
+        if (b.wide) launch_mode<uint64_t, 1, T>(a, cm, cv, s);
+        else launch_mode<uint32_t, 1, T>(a, cm, cv, s);
     } else {
         launch_mode<uint64_t, 0, T>(a, cm, cv, s);
     }
