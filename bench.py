@@ -8,9 +8,13 @@ A step is one matvec y = H x over the whole sector.  `value` is the H.v
 throughput in GB/s of algorithmic traffic (bytes per row defined below) with x, y
 resident in HBM; `e2e` is the same metric through the C ABI with host buffers
 (host->device copy of x and device->host copy of y inside every timed step).
-Lanczos solves/s (eigsh k=1 :SA, tol 1e-10) and the FP32 form are reported
-beside it.  Synthetic data only (seeded N(0,1) vectors; the Hamiltonian is the
-model itself).  N > 1 runs independent replicas (the path is not sharded).
+Lanczos solves/s (eigsh k=1 :SA, tol 1e-10), the FP32, double-float and
+fixed-point forms are reported beside it, and side workloads under
+`workloads` (XXZ L=16, batched sectors, TFIM evolve, FTLM, block tools,
+SpinBasisGeneral, the XXZ roofline sweep L=24..30, serving; `--no-sections`
+skips them, `--only-section KEY` runs one).  Synthetic data only (seeded
+N(0,1) vectors; the Hamiltonian is the model itself).  N > 1 runs
+independent replicas (the path is not sharded).
 
 `--impl reference` times the CPU restatement of the reference's algorithm
 (oracle/, representative-space port, all host threads) on a bounded sample of
