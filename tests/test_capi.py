@@ -30,6 +30,32 @@ def test_library_exports_every_declared_symbol(qs):
     assert lib.qs_version().decode().startswith("qsgpu")
 
 
+def header_constants():
+    """name -> value of every QS_* enumerator of include/qsgpu.h."""
+    with open(os.path.join(ROOT, "include", "qsgpu.h")) as f:
+        src = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+    out = {}
+    for body in re.findall(r"enum\s*\{(.*?)\}", src, flags=re.S):
+        for name, val in re.findall(r"\b(QS_\w+)\s*=\s*(-?\d+)", body):
+            out[name] = int(val)
+    return out
+
+
+def test_binding_constants_match_the_header():
+    """The ctypes binding's flag, dtype, memory and status values are the
+    header's (a drift would silently select another product form)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "quspin.jl_gb300"))
+    from qsgpu import _lib
+    consts = header_constants()
+    for name in ("QS_TRANSPOSE", "QS_CONJUGATE", "QS_DOUBLE_FLOAT", "QS_FIXED_POINT", "QS_MEM_HOST",
+                 "QS_MEM_DEVICE", "QS_F64", "QS_C128", "QS_F32", "QS_C64"):
+        assert name in consts, name
+        assert getattr(_lib, name) == consts[name], name
+    flags = [consts[n] for n in ("QS_TRANSPOSE", "QS_CONJUGATE", "QS_DOUBLE_FLOAT", "QS_FIXED_POINT")]
+    assert len(set(flags)) == 4 and all(f & (f - 1) == 0 for f in flags)   # distinct single bits
+
+
 @pytest.mark.parametrize("kwargs,msg", [
     (dict(L=0), "L must be between 1 and 63"),
     (dict(L=64), "L must be between 1 and 63"),
