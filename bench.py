@@ -600,6 +600,27 @@ def section_sweep(qs, torch, sizes=(24, 26, 28, 30), reps=10):
             "fixed_point_rel_err": fx_err,
             "matrix_free_ms": msmf, "matrix_free_rel_diff": mf_err}
     del flush
+    # CPU baseline: the oracle's restatement of the reference's own algorithm
+    # (serial scatter with a lookup per generated state, 1 thread), one product
+    # of the smallest sweep size
+    try:
+        import oracle
+        L = sizes[0]
+        spec = xxz_spec(L)
+        ref = oracle.RefBasis(L, nup=L // 2, pauli=False)
+        ct = oracle.consolidate_terms(spec)
+        d = ref.extract_diagonal(ct)
+        pk = oracle.pack_terms(ct)
+        xh = np.random.default_rng(20261203).standard_normal(len(d))
+        t = time.perf_counter()
+        ref.qlo_matvec(ct, xh, total_diag=d, packed=pk)
+        cpu_ms = (time.perf_counter() - t) * 1e3
+        gpu = out["sizes"][str(L)]
+        out["cpu_reference_algorithm"] = {"L": L, "ms_per_product": cpu_ms, "cores": 1,
+                                          "vs_fp64_assembled": cpu_ms / gpu["fp64_ms"],
+                                          "vs_matrix_free": cpu_ms / gpu["matrix_free_ms"]}
+    except Exception as exc:  # the baseline must not hide the GPU figures
+        out["cpu_reference_algorithm"] = {"error": f"{type(exc).__name__}: {exc}"}
     return out
 
 
