@@ -236,16 +236,19 @@ enum {
 QS_API int qs_op_matvec(qs_op *op, int32_t flags, const double *alpha, const void *x, int32_t x_dtype,
                  const double *beta, void *y, int32_t y_dtype, int64_t nrhs, int32_t mem);
 
-/* Allocation-free form of qs_op_matvec for host buffers (x_dtype == y_dtype).
- * No counterpart in the reference: it exists for callers that cannot let a
- * library allocate device memory -- code running during CUDA graph capture,
- * hosts whose device memory belongs to their own pool allocator, loops that
- * cannot absorb cudaMalloc's synchronisation.  x and y are staged through one
- * static device array of 2 x 8 MiB (Ns times the element size must not exceed
- * 8 MiB, else QS_ERR_ARGUMENT), which every loaded device holds until the
- * process exits.  The first call on a device resolves the array's address and
- * must come before any stream capture; calls that overlap on the GPU share the
- * array and race, so the caller serialises them. */
+/* Allocation-free form of qs_op_matvec for host buffers (x_dtype == y_dtype),
+ * with the same flags (QS_TRANSPOSE, QS_CONJUGATE, QS_DOUBLE_FLOAT,
+ * QS_FIXED_POINT; other bits give QS_ERR_ARGUMENT).  No counterpart in the
+ * reference: it exists for callers that cannot let a library allocate device
+ * memory -- hosts whose device memory belongs to their own pool allocator with
+ * a hard limit (CUDA.jl, PyTorch), loops that cannot absorb cudaMalloc's
+ * synchronisation.  x and y are staged through one static device array of
+ * 2 x 8 MiB (Ns times the element size must not exceed 8 MiB, else
+ * QS_ERR_ARGUMENT), which every loaded device holds until the process exits.
+ * The device that was current when the operator was created must be current
+ * (else QS_ERR_ARGUMENT).  The first call on a device resolves the array's
+ * address and must come before any stream capture; calls that overlap on the
+ * GPU share the array and race, so the caller serialises them. */
 QS_API int qs_op_matvec_noalloc(qs_op *op, int32_t flags, const double *alpha, const void *x, int32_t x_dtype,
                                 const double *beta, void *y, int32_t y_dtype, int64_t nrhs);
 
@@ -495,6 +498,11 @@ QS_API int qs_fp64_fma_rate(double *fma_per_s);
 /* Number of kernels this library has launched in the process so far (all
  * handles).  No reference counterpart: instrumentation for benchmarks. */
 QS_API int64_t qs_launch_count(void);
+
+/* Number of device allocations (cudaMalloc calls) this library has made in the
+ * process so far, pooled blocks included.  No reference counterpart:
+ * instrumentation, e.g. to check that a call allocated nothing. */
+QS_API int64_t qs_device_alloc_count(void);
 
 /* Library version string. */
 QS_API const char *qs_version(void);

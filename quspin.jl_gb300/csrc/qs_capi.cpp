@@ -218,6 +218,7 @@ int qs_op_set_stream(qs_op* op, void* stream) {
 }
 
 int64_t qs_launch_count(void) { return qs::launches(); }
+int64_t qs_device_alloc_count(void) { return qs::device_allocs(); }
 
 int qs_op_assemble(qs_op* op) {
     return guard([&] { qs::op_assemble(*op->op); });

@@ -31,6 +31,10 @@ struct Error : std::runtime_error {
         }                                                                                    \
     } while (0)
 
+// Count of device allocations made by the library (every cudaMalloc of a
+// DevBuf or of the pool); qs_device_alloc_count reports it.
+void note_device_alloc();
+
 // Owning device buffer.
 struct DevBuf {
     void* p = nullptr;
@@ -47,7 +51,10 @@ struct DevBuf {
     ~DevBuf() { release(); }
     void alloc(size_t n) {
         release();
-        if (n) QS_CUDA(cudaMalloc(&p, n));
+        if (n) {
+            note_device_alloc();
+            QS_CUDA(cudaMalloc(&p, n));
+        }
         bytes = n;
     }
     void release() {
@@ -174,6 +181,7 @@ struct Op {
     cudaStream_t own_stream = nullptr;  // created by the library
     Assembled asm_;                     // assembled (compiled-transition) form
     bool assembled = false;
+    int device = 0;                     // device current when the operator was created
     cudaStream_t copy_stream = nullptr; // read-back of host products (op_matvec_host_overlap)
     cudaEvent_t range_done[4] = {};
     ~Op();
@@ -233,6 +241,7 @@ void scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t s);
 // kernel launch accounting (qs_launch_count)
 void note_launches(int64_t n);
 int64_t launches();
+int64_t device_allocs();
 void op_matvec_device(Op& op, const MatvecCall& c, cudaStream_t s);
 
 }  // namespace qs

@@ -506,9 +506,12 @@ void launch_matvec(const Basis& b, const MvArgs& a, bool cm, bool cv, cudaStream
 
 namespace {
 std::atomic<int64_t> g_launches{0};
+std::atomic<int64_t> g_device_allocs{0};
 }
 void note_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 int64_t launches() { return g_launches.load(std::memory_order_relaxed); }
+void note_device_alloc() { g_device_allocs.fetch_add(1, std::memory_order_relaxed); }
+int64_t device_allocs() { return g_device_allocs.load(std::memory_order_relaxed); }
 
 Op::~Op() {
     if (copy_stream) {

@@ -2,8 +2,9 @@
 //
 // qs_op_matvec with host buffers stages x and y through device buffers that it
 // allocates on first use.  Some callers cannot let a library allocate device
-// memory: code that runs while a CUDA graph is being captured, hosts whose
-// device memory is owned by their own pool allocator (CUDA.jl, PyTorch), and
+// memory: hosts whose device memory is owned by their own pool allocator with
+// a hard limit (CUDA.jl and PyTorch keep a cache of their own, and a
+// cudaMalloc behind its back can fail or force it to release its cache), and
 // latency-bound loops that must not pay for cudaMalloc's implicit
 // synchronisation.  This variant stages through one file-scope device array of
 // fixed size instead, so a call allocates nothing.
@@ -70,6 +71,13 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
     const bool ycx = (y_dtype == QS_C128 || y_dtype == QS_C64);
     if (!ycx && op.complex_mat) throw Error(QS_ERR_ARGUMENT, "the output must be complex for a complex operator");
     if (nrhs < 0) throw Error(QS_ERR_DIMENSION, "nrhs must be nonnegative");
+    if (flags & ~(QS_TRANSPOSE | QS_CONJUGATE | QS_DOUBLE_FLOAT | QS_FIXED_POINT))
+        throw Error(QS_ERR_ARGUMENT, "unknown flag bits");
+    int dev = 0;
+    QS_CUDA(cudaGetDevice(&dev));
+    if (dev != op.device)
+        throw Error(QS_ERR_ARGUMENT, "the operator lives on device " + std::to_string(op.device) +
+                                         " but device " + std::to_string(dev) + " is current");
     const size_t vb = (size_t)n * bytes_of(y_dtype);
     if (vb > kNoAllocVectorBytes)
         throw Error(QS_ERR_ARGUMENT, "the allocation-free matvec stages at most " +
@@ -78,7 +86,11 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
     unsigned char* stage = stage_address();
     MatvecCall c;
     c.no_tune = true;   // variant timing would create events
-    c.flags = flags;
+    // the same flag meaning as qs_op_matvec: double-float products and
+    // fixed-point row sums use tables and scratch that assembly allocated
+    c.flags = flags & (QS_TRANSPOSE | QS_CONJUGATE);
+    c.df = (flags & QS_DOUBLE_FLOAT) != 0;
+    c.fx = (flags & QS_FIXED_POINT) != 0;
     c.alpha = alpha;
     c.beta = beta;
     c.single = (y_dtype == QS_F32 || y_dtype == QS_C64);

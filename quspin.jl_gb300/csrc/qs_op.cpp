@@ -259,6 +259,11 @@ Op* op_create(Basis* basis, const qs_term* terms, int nterms, const double* diag
 
     Op* op = new Op();
     op->basis = basis;
+    if (cudaGetDevice(&op->device) != cudaSuccess) {
+        cudaGetLastError();
+        delete op;
+        throw Error(QS_ERR_CUDA, "no current CUDA device");
+    }
     bool has_y = false;
     for (const Term& t : checked)
         if (t.op.find('y') != std::string::npos) has_y = true;

@@ -70,6 +70,7 @@ void* pool_get(size_t bytes) {
         return b.p;
     }
     void* p = nullptr;
+    note_device_alloc();
     cudaError_t e = cudaMalloc(&p, bytes);
     if (e == cudaErrorMemoryAllocation) {
         cudaGetLastError();
@@ -77,6 +78,7 @@ void* pool_get(size_t bytes) {
             std::lock_guard<std::mutex> g(g_pool_mu);
             free_all_locked();
         }
+        note_device_alloc();
         e = cudaMalloc(&p, bytes);
     }
     if (e != cudaSuccess) {

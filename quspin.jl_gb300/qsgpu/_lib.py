@@ -90,6 +90,7 @@ EXPORTS = (
     "qs_lanczos_run", "qs_lanczos_destroy", "qs_lanczos_coefficients", "qs_lanczos_complex", "qs_lanczos_rows",
     "qs_lanczos_combine", "qs_lanczos_overlaps", "qs_lanczos_ritz_matrix",
     "qs_basis_projection_rows", "qs_basis_project_from", "qs_basis_project_to", "qs_block_expm", "qs_op_export_csr", "qs_fp64_fma_rate", "qs_basis_create_general", "qs_expm_columns", "qs_evolve_stepwise",
+    "qs_device_alloc_count",
 )
 
 _lib = None
@@ -163,6 +164,7 @@ def load():
     L.qs_op_fixed_point_classes.argtypes = [P]
     L.qs_op_fixed_point_classes.restype = ctypes.c_int32
     L.qs_launch_count.restype = i64
+    L.qs_device_alloc_count.restype = i64
     L.qs_last_error.restype = ctypes.c_char_p
     L.qs_version.restype = ctypes.c_char_p
     for name in EXPORTS:

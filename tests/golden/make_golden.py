@@ -1,8 +1,8 @@
 """Extracts the reference's own known-answer values for the hot path from its
 Julia test files (read as text) into reference_kats.json.
 
-Run from the repository root where the reference checkout is mounted:
-    python tests/golden/make_golden.py /root/reference
+Run from the repository root, giving the path of a QuSpin.jl checkout:
+    python tests/golden/make_golden.py <path-to-QuSpin.jl>
 The JSON it writes is committed; tests never read the reference at run time.
 """
 import json
@@ -160,4 +160,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path-to-QuSpin.jl>")
+    main(sys.argv[1])

@@ -72,3 +72,13 @@ def torus_heisenberg(Lx, Ly, J=1.0, Jd=0.0):
                 bonds.append((Jd, site(x, y), site(x + 1, y - 1)))
     return [("+-", [(j / 2, a, b) for j, a, b in bonds]), ("-+", [(j / 2, a, b) for j, a, b in bonds]),
             ("zz", [(j, a, b) for j, a, b in bonds])]
+
+
+def sublattice(L, J=1.0, J2=0.5, h=0.3):
+    """xx on nearest-neighbour bonds, zz on next-nearest bonds, a transverse
+    field: commutes with translations, parity and both sublattice flips (zA,
+    zB), so it lives in zA / zB sectors (no particle number)."""
+    nn = [(i, i % L + 1) for i in range(1, L + 1)]
+    nnn = [(i, (i + 1) % L + 1) for i in range(1, L + 1)]
+    return [("xx", [(J, a, b) for a, b in nn]), ("zz", [(J2, a, b) for a, b in nnn]),
+            ("x", [(h, i) for i in range(1, L + 1)])]

@@ -29,6 +29,13 @@ SECTORS = [
     (14, 7, dict(kblock=5, zblock=1)),
     (16, 8, dict(kblock=0, pblock=1, zblock=1)),
     (9, 4, dict(kblock=3, a=3)),
+    # sublattice flips (src/basis.jl:740-741): zB alone, with zA, with T(a=2)
+    (12, None, dict(zBblock=1)),
+    (12, None, dict(zBblock=-1)),
+    (12, None, dict(zAblock=1, zBblock=-1)),
+    (12, None, dict(kblock=0, zBblock=-1, a=2)),
+    (12, None, dict(kblock=0, zAblock=-1, zBblock=1, a=2)),
+    (14, None, dict(kblock=3, zAblock=1, zBblock=1, a=2)),
 ]
 
 

@@ -20,6 +20,11 @@ MV_CASES = [
     (12, None, True, dict(kblock=3), "tfim"),
     (10, None, False, dict(kblock=2), "xyz"),
     (12, None, False, dict(kblock=0, pblock=1, zblock=1), "xyz_z"),
+    # sublattice-flip sectors (zAblock / zBblock, src/basis.jl:740-741)
+    (12, None, True, dict(zBblock=1), "sub"),
+    (12, None, True, dict(kblock=0, zBblock=-1, a=2), "sub"),
+    (14, None, True, dict(kblock=3, zAblock=1, zBblock=1, a=2), "sub"),
+    (12, None, True, dict(zAblock=1, zBblock=-1), "sub"),
 ]
 
 
@@ -34,6 +39,8 @@ def spec(model, L):
         return models.xyz_field(L)
     if model == "xyz_z":
         return [t for t in models.xyz_field(L) if t[0] not in ("y", "z")]
+    if model == "sub":
+        return models.sublattice(L)
     raise ValueError(model)
 
 
