@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <functional>
 #include <cmath>
 #include <complex>
@@ -427,7 +429,7 @@ struct SellArgs {
 };
 
 // One thread per row: y[r] = beta y[r] + alpha (d[r] x[r] + rs(stab[r]) sum_j T[code_j] x[col_j])
-template <bool kCM, bool kCV, typename T, bool kPacked, int U, int MINB>
+template <bool kCM, bool kCV, typename T, bool kPacked, int U, int MINB, bool kHint>
 __global__ void __launch_bounds__(kThreads, MINB) sell_kernel(SellArgs a) {
     using T2 = typename V2<T>::t;
     __shared__ T2 tab[1024];
@@ -460,8 +462,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_kernel(SellArgs a) {
         };
         if (kCV) {
             const T2* __restrict__ x = (const T2*)a.x;
-            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
-                                 [&](uint32_t c) { return __ldg(x + c); },
+            sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return ld_gather<kHint>(x + c); },
                                  [&](uint32_t code, T2 xv) {
                                      const T2 v = value(code);
                                      if (kCM) {
@@ -474,8 +476,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_kernel(SellArgs a) {
                                  });
         } else {
             const T* __restrict__ x = (const T*)a.x;
-            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
-                                 [&](uint32_t c) { return __ldg(x + c); },
+            sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return ld_gather<kHint>(x + c); },
                                  [&](uint32_t code, T xv) { acc_r += value(code).x * xv; });
         }
         const T sc = a.stab ? rsq[a.stab[r]] : (T)1;
@@ -515,7 +517,7 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_kernel(SellArgs a) {
 
 // Double-float products, one thread per row; FP64 only in the per-row tail,
 // where all 32 lanes of a warp work on 32 rows.
-template <bool kCM, bool kCV, bool kPacked, int U, int MINB>
+template <bool kCM, bool kCV, bool kPacked, int U, int MINB, bool kHint>
 __global__ void __launch_bounds__(kThreads, MINB) sell_df_kernel(SellArgs a, const float4* __restrict__ tab_df,
                                                            const void* __restrict__ xs) {
     __shared__ float4 tab[1024];
@@ -547,8 +549,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_df_kernel(SellArgs a, con
         };
         if (kCV) {
             const float4* __restrict__ x = (const float4*)xs;
-            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
-                                 [&](uint32_t c) { return __ldg(x + c); },
+            sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return ld_gather<kHint>(x + c); },
                                  [&](uint32_t code, float4 xv) {
                                      const float4 v = value(code);
                                      df_mac(ar, v.x, v.y, xv.x, xv.y);
@@ -560,8 +562,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_df_kernel(SellArgs a, con
                                  });
         } else {
             const float2* __restrict__ x = (const float2*)xs;
-            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
-                                 [&](uint32_t c) { return __ldg(x + c); },
+            sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return ld_gather<kHint>(x + c); },
                                  [&](uint32_t code, float2 xv) {
                                      const float4 v = value(code);
                                      df_mac(ar, v.x, v.y, xv.x, xv.y);
@@ -600,7 +602,7 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_df_kernel(SellArgs a, con
 
 // Double-float storage in and out (the Krylov solvers' double-float vectors):
 // y = d .* x + rs(stab) * sum_j T[code_j] x[col_j], entirely on the FP32 pipe.
-template <bool kCM, bool kCV, bool kPacked, int U, int MINB>
+template <bool kCM, bool kCV, bool kPacked, int U, int MINB, bool kHint>
 __global__ void __launch_bounds__(kThreads, MINB) sell_dfio_kernel(SellArgs a, const float4* __restrict__ tab_df,
                                                                 const float4* __restrict__ diag_df,
                                                                 const float2* __restrict__ rsq_df) {
@@ -633,8 +635,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_dfio_kernel(SellArgs a, c
         };
         if (kCV) {
             const float4* __restrict__ x = (const float4*)a.x;
-            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
-                                 [&](uint32_t c) { return __ldg(x + c); },
+            sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return ld_gather<kHint>(x + c); },
                                  [&](uint32_t code, float4 xv) {
                                      const float4 v = value(code);
                                      df_mac(ar, v.x, v.y, xv.x, xv.y);
@@ -646,8 +648,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_dfio_kernel(SellArgs a, c
                                  });
         } else {
             const float2* __restrict__ x = (const float2*)a.x;
-            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
-                                 [&](uint32_t c) { return __ldg(x + c); },
+            sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return ld_gather<kHint>(x + c); },
                                  [&](uint32_t code, float2 xv) {
                                      const float4 v = value(code);
                                      df_mac(ar, v.x, v.y, xv.x, xv.y);
@@ -897,9 +899,11 @@ __device__ __forceinline__ void fx_store_row(const SellArgs& a, int64_t r, doubl
 
 // One thread per row: integer sums per amplitude class, FP64 per row.  NC is
 // the number of class accumulators (the operator's classes, rounded up).
+// kHint marks only the word stream here: the kernel runs at 32 registers, and
+// an x cache-policy operand on top spills.
 // x that holds a NaN or an infinity has no fixed-point scale: then every row
 // is computed as by the FP64 product, so non-finite values propagate alike.
-template <bool kCV, bool kPacked, int NC, int U, int MINB>
+template <bool kCV, bool kPacked, int NC, int U, int MINB, bool kHint>
 __global__ void __launch_bounds__(kThreads, MINB) sell_fx_kernel(SellArgs a, FxArgs f) {
     __shared__ uint32_t ccls[kFxCodes];
     __shared__ double rsk[kMaxGroup + 1];
@@ -927,8 +931,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_fx_kernel(SellArgs a, FxA
             double acc_r = 0, acc_i = 0;
             if (kCV) {
                 const double2* __restrict__ x = (const double2*)a.x;
-                sell_row<1, kPacked>(a.words, a.cols, a.codes, a.sptr[s] + lane, a.len[r], a.code_bits, a.code_mask,
-                                     [&](uint32_t c) { return __ldg(x + c); },
+                sell_row<1, kPacked, kHint>(a.words, a.cols, a.codes, a.sptr[s] + lane, a.len[r], a.code_bits, a.code_mask,
+                                     [&](uint32_t c) { return ld_gather<kHint>(x + c); },
                                      [&](uint32_t code, double2 xv) {
                                          const double v = __ldg(&tab[code].x);
                                          acc_r += v * xv.x;
@@ -936,8 +940,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_fx_kernel(SellArgs a, FxA
                                      });
             } else {
                 const double* __restrict__ x = (const double*)a.x;
-                sell_row<1, kPacked>(a.words, a.cols, a.codes, a.sptr[s] + lane, a.len[r], a.code_bits, a.code_mask,
-                                     [&](uint32_t c) { return __ldg(x + c); },
+                sell_row<1, kPacked, kHint>(a.words, a.cols, a.codes, a.sptr[s] + lane, a.len[r], a.code_bits, a.code_mask,
+                                     [&](uint32_t c) { return ld_gather<kHint>(x + c); },
                                      [&](uint32_t code, double xv) { acc_r += __ldg(&tab[code].x) * xv; });
             }
             const double sc = a.stab ? 1.0 / sqrt((double)a.stab[r]) : 1.0;
@@ -961,8 +965,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_fx_kernel(SellArgs a, FxA
 #pragma unroll
             for (int c = 1; c < NC; ++c) sr[c] = si[c] = 0;
             const longlong2* __restrict__ xq = (const longlong2*)f.xq;
-            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
-                                 [&](uint32_t c) { return __ldg(xq + c); },
+            sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return ld_gather<false>(xq + c); },
                                  [&](uint32_t code, longlong2 q) {
                                      const uint32_t w = ccls[code];
                                      const long long m = -(long long)(w & 1u);
@@ -991,8 +995,8 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_fx_kernel(SellArgs a, FxA
 #pragma unroll
             for (int c = 1; c < NC; ++c) sr[c] = 0;
             const long long* __restrict__ xq = (const long long*)f.xq;
-            sell_row<U, kPacked>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
-                                 [&](uint32_t c) { return __ldg(xq + c); },
+            sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
+                                 [&](uint32_t c) { return ld_gather<false>(xq + c); },
                                  [&](uint32_t code, long long q) {
                                      const uint32_t w = ccls[code];
                                      const long long m = -(long long)(w & 1u);
@@ -1028,9 +1032,36 @@ template <bool kCV, bool kPacked, int NC>
 void launch_fx(int v, int grid, cudaStream_t s, const SellArgs& a, const FxArgs& f) {
     constexpr int B0 = kCV ? 4 : (NC <= 2 ? 8 : 6);
     constexpr int B1 = (kCV || NC > 2) ? 4 : 6;
-    if (v == 0) sell_fx_kernel<kCV, kPacked, NC, 1, B0><<<grid, kThreads, 0, s>>>(a, f);
-    else if (v == 1) sell_fx_kernel<kCV, kPacked, NC, 2, B1><<<grid, kThreads, 0, s>>>(a, f);
-    else sell_fx_kernel<kCV, kPacked, NC, 4, 4><<<grid, kThreads, 0, s>>>(a, f);
+    switch (v) {
+        case 0: sell_fx_kernel<kCV, kPacked, NC, 1, B0, false><<<grid, kThreads, 0, s>>>(a, f); break;
+        case 1: sell_fx_kernel<kCV, kPacked, NC, 2, B1, false><<<grid, kThreads, 0, s>>>(a, f); break;
+        case 2: sell_fx_kernel<kCV, kPacked, NC, 4, 4, false><<<grid, kThreads, 0, s>>>(a, f); break;
+        case 3: sell_fx_kernel<kCV, kPacked, NC, 1, B0, true><<<grid, kThreads, 0, s>>>(a, f); break;
+        case 4: sell_fx_kernel<kCV, kPacked, NC, 2, B1, true><<<grid, kThreads, 0, s>>>(a, f); break;
+        default: sell_fx_kernel<kCV, kPacked, NC, 4, 4, true><<<grid, kThreads, 0, s>>>(a, f); break;
+    }
+}
+
+// six sliced-ELL variants: three (gathers in flight, blocks per SM) shapes,
+// each with plain loads and with the evict-first / evict-last hints
+constexpr int kSellVariants = 6;
+
+// QS_TUNE_VERBOSE=1 prints the variant timings of each tuning to stderr
+bool tune_verbose() {
+    static const bool on = [] {
+        const char* e = std::getenv("QS_TUNE_VERBOSE");
+        return e && e[0] && e[0] != '0';
+    }();
+    return on;
+}
+
+// QS_SELL_VARIANT=v (0 .. kSellVariants - 1) runs variant v instead of the
+// timed choice (read on every product; the tests run every variant with it)
+int forced_variant() {
+    const char* e = std::getenv("QS_SELL_VARIANT");
+    if (!e || !e[0]) return -1;
+    const int v = std::atoi(e);
+    return (v >= 0 && v < kSellVariants) ? v : -1;
 }
 
 int grid_rows(int64_t threads_needed) {
@@ -1327,24 +1358,30 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
         a.y = c.y;
         const bool cm = op.complex_mat, cv = c.y_complex;
         const int grid = grid_rows(std::max<int64_t>(1, a.nslices - a.slice0) * kSlice);
-        // variants: (gathers in flight per thread, resident blocks per SM)
-#define QS_VARIANTS(LAUNCH, v)                  \
-    do {                                        \
-        if ((v) == 0) LAUNCH(1, 8);             \
-        else if ((v) == 1) LAUNCH(2, 6);        \
-        else LAUNCH(4, 4);                      \
+        // variants: (gathers in flight per thread, resident blocks per SM) x
+        // (plain loads, or the word stream evict-first and x evict-last)
+#define QS_VARIANTS(LAUNCH, v)                         \
+    do {                                               \
+        switch (v) {                                   \
+            case 0: LAUNCH(1, 8, false); break;        \
+            case 1: LAUNCH(2, 6, false); break;        \
+            case 2: LAUNCH(4, 4, false); break;        \
+            case 3: LAUNCH(1, 8, true); break;         \
+            case 4: LAUNCH(2, 6, true); break;         \
+            default: LAUNCH(4, 4, true); break;        \
+        }                                              \
     } while (0)
-#define QS_SHAPES(K, U_, B_, ...)                                                        \
-    do {                                                                                 \
-        if (a.packed) {                                                                  \
-            if (cm) K<true, true, true, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);        \
-            else if (cv) K<false, true, true, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);  \
-            else K<false, false, true, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);         \
-        } else {                                                                         \
-            if (cm) K<true, true, false, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);       \
-            else if (cv) K<false, true, false, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__); \
-            else K<false, false, false, U_, B_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);        \
-        }                                                                                \
+#define QS_SHAPES(K, U_, B_, H_, ...)                                                        \
+    do {                                                                                     \
+        if (a.packed) {                                                                      \
+            if (cm) K<true, true, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);        \
+            else if (cv) K<false, true, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);  \
+            else K<false, false, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);         \
+        } else {                                                                             \
+            if (cm) K<true, true, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);       \
+            else if (cv) K<false, true, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(__VA_ARGS__); \
+            else K<false, false, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(__VA_ARGS__);        \
+        }                                                                                    \
     } while (0)
         int kind;
         std::function<void(int)> launch;
@@ -1354,7 +1391,7 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
             const float4* dd = op.d_diag_df.as<float4>();
             const float2* rq = M.rsq_df.as<float2>();
             launch = [&, td, dd, rq](int v) {
-#define L_DFIO(U_, B_) QS_SHAPES(sell_dfio_kernel, U_, B_, a, td, dd, rq)
+#define L_DFIO(U_, B_, H_) QS_SHAPES(sell_dfio_kernel, U_, B_, H_, a, td, dd, rq)
                 QS_VARIANTS(L_DFIO, v);
 #undef L_DFIO
             };
@@ -1408,7 +1445,7 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
             note_launches(1);
             const void* xs = M.xsplit.p;
             launch = [&, td, xs](int v) {
-#define L_DF(U_, B_) QS_SHAPES(sell_df_kernel, U_, B_, a, td, xs)
+#define L_DF(U_, B_, H_) QS_SHAPES(sell_df_kernel, U_, B_, H_, a, td, xs)
                 QS_VARIANTS(L_DF, v);
 #undef L_DF
             };
@@ -1418,22 +1455,20 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
             a.diag = op.d_diag32.p;
             a.diag_re = op.d_diag32_re.p;
             launch = [&](int v) {
-#define K32(CM_, CV_, P_, U_, B_) sell_kernel<CM_, CV_, float, P_, U_, B_>
-#define L_32(U_, B_)                                                                           \
-    do {                                                                                       \
-        if (a.packed) {                                                                        \
-            if (cm) sell_kernel<true, true, float, true, U_, B_><<<grid, kThreads, 0, s>>>(a);       \
-            else if (cv) sell_kernel<false, true, float, true, U_, B_><<<grid, kThreads, 0, s>>>(a); \
-            else sell_kernel<false, false, float, true, U_, B_><<<grid, kThreads, 0, s>>>(a);        \
-        } else {                                                                               \
-            if (cm) sell_kernel<true, true, float, false, U_, B_><<<grid, kThreads, 0, s>>>(a);      \
-            else if (cv) sell_kernel<false, true, float, false, U_, B_><<<grid, kThreads, 0, s>>>(a);\
-            else sell_kernel<false, false, float, false, U_, B_><<<grid, kThreads, 0, s>>>(a);       \
-        }                                                                                      \
+#define L_32(U_, B_, H_)                                                                           \
+    do {                                                                                           \
+        if (a.packed) {                                                                            \
+            if (cm) sell_kernel<true, true, float, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);       \
+            else if (cv) sell_kernel<false, true, float, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(a); \
+            else sell_kernel<false, false, float, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);        \
+        } else {                                                                                   \
+            if (cm) sell_kernel<true, true, float, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);      \
+            else if (cv) sell_kernel<false, true, float, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);\
+            else sell_kernel<false, false, float, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);       \
+        }                                                                                          \
     } while (0)
                 QS_VARIANTS(L_32, v);
 #undef L_32
-#undef K32
             };
         } else {
             kind = 0;
@@ -1441,17 +1476,17 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
             a.diag = op.d_diag.p;
             a.diag_re = op.d_diag_re.p;
             launch = [&](int v) {
-#define L_64(U_, B_)                                                                            \
-    do {                                                                                        \
-        if (a.packed) {                                                                         \
-            if (cm) sell_kernel<true, true, double, true, U_, B_><<<grid, kThreads, 0, s>>>(a);       \
-            else if (cv) sell_kernel<false, true, double, true, U_, B_><<<grid, kThreads, 0, s>>>(a); \
-            else sell_kernel<false, false, double, true, U_, B_><<<grid, kThreads, 0, s>>>(a);        \
-        } else {                                                                                \
-            if (cm) sell_kernel<true, true, double, false, U_, B_><<<grid, kThreads, 0, s>>>(a);      \
-            else if (cv) sell_kernel<false, true, double, false, U_, B_><<<grid, kThreads, 0, s>>>(a);\
-            else sell_kernel<false, false, double, false, U_, B_><<<grid, kThreads, 0, s>>>(a);       \
-        }                                                                                       \
+#define L_64(U_, B_, H_)                                                                           \
+    do {                                                                                           \
+        if (a.packed) {                                                                            \
+            if (cm) sell_kernel<true, true, double, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);       \
+            else if (cv) sell_kernel<false, true, double, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(a); \
+            else sell_kernel<false, false, double, true, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);        \
+        } else {                                                                                   \
+            if (cm) sell_kernel<true, true, double, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);      \
+            else if (cv) sell_kernel<false, true, double, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);\
+            else sell_kernel<false, false, double, false, U_, B_, H_><<<grid, kThreads, 0, s>>>(a);       \
+        }                                                                                          \
     } while (0)
                 QS_VARIANTS(L_64, v);
 #undef L_64
@@ -1460,7 +1495,7 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
 #undef QS_SHAPES
 #undef QS_VARIANTS
         int& var = op.asm_.sell_variant[kind];
-        if (var < 0 && !c.no_tune) {
+        if (var < 0 && !c.no_tune && forced_variant() < 0) {
             // choose the variant by timing, when repeating the product is harmless
             // (beta = 0) and the stream is not being captured into a graph
             cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -1471,7 +1506,8 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
                 QS_CUDA(cudaEventCreate(&e1));
                 float best = 1e30f;
                 int bv = 2;
-                for (int v = 0; v < 3; ++v) {
+                float ms_v[kSellVariants] = {};
+                for (int v = 0; v < kSellVariants; ++v) {
                     launch(v);
                     QS_CUDA(cudaGetLastError());
                     QS_CUDA(cudaEventRecord(e0, s));
@@ -1480,6 +1516,7 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
                     QS_CUDA(cudaEventSynchronize(e1));
                     float ms = 0;
                     QS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    ms_v[v] = ms / 3;
                     if (ms < best) {
                         best = ms;
                         bv = v;
@@ -1487,11 +1524,17 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
                 }
                 cudaEventDestroy(e0);
                 cudaEventDestroy(e1);
-                note_launches(12);
+                note_launches(4 * kSellVariants);
+                if (tune_verbose()) {
+                    std::fprintf(stderr, "qsgpu: sliced-ELL product kind %d, n=%lld: variant ms", kind, (long long)b.n);
+                    for (int v = 0; v < kSellVariants; ++v) std::fprintf(stderr, " %d:%.4f", v, ms_v[v]);
+                    std::fprintf(stderr, " -> %d\n", bv);
+                }
                 var = bv;
             }
         }
-        launch(var < 0 ? 2 : var);
+        const int fv = forced_variant();
+        launch(fv >= 0 ? fv : (var < 0 ? 2 : var));
         QS_CUDA(cudaGetLastError());
         note_launches(1);
         return;

@@ -9,11 +9,89 @@ constexpr int kSellSlice = 32;   // rows per slice of the sliced-ELL layout
 constexpr int kFxCodes = 256;    // value codes of an operator with fixed-point row sums, at most
 
 #ifdef __CUDACC__
+// Cache policies of the sliced-ELL walk.  kHint = false: plain read-only
+// loads (__ldg).  kHint = true: the packed words, read once per product, skip
+// L1 and leave L2 first (an L2::evict_first cache policy), and the x gathers
+// leave L2 last (L2::evict_last), so the word stream (hundreds of MB) does
+// not evict x (tens of MB) between its reuses.  Per-instruction cache-policy
+// operands only (createpolicy): no device or context setting changes.
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ unsigned long long l2_evict_last() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+template <bool kHint> __device__ __forceinline__ uint32_t ld_word(const uint32_t* p) {
+    if (!kHint) return __ldg(p);
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(l2_evict_first()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ int32_t ld_word(const int32_t* p) {
+    if (!kHint) return __ldg(p);
+    int32_t v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(l2_evict_first()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ uint16_t ld_word(const uint16_t* p) {
+    if (!kHint) return __ldg(p);
+    unsigned short v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(p), "l"(l2_evict_first()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ double ld_gather(const double* p) {
+    if (!kHint) return __ldg(p);
+    double v;
+    asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(l2_evict_last()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ double2 ld_gather(const double2* p) {
+    if (!kHint) return __ldg(p);
+    double2 v;
+    asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(l2_evict_last()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ float ld_gather(const float* p) {
+    if (!kHint) return __ldg(p);
+    float v;
+    asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(l2_evict_last()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ float2 ld_gather(const float2* p) {
+    if (!kHint) return __ldg(p);
+    float2 v;
+    asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(l2_evict_last()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ float4 ld_gather(const float4* p) {
+    if (!kHint) return __ldg(p);
+    float4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p), "l"(l2_evict_last()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ long long ld_gather(const long long* p) {
+    if (!kHint) return __ldg(p);
+    long long v;
+    asm("ld.global.nc.L2::cache_hint.s64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(l2_evict_last()));
+    return v;
+}
+template <bool kHint> __device__ __forceinline__ longlong2 ld_gather(const longlong2* p) {
+    if (!kHint) return __ldg(p);
+    longlong2 v;
+    asm("ld.global.nc.L2::cache_hint.v2.s64 {%0, %1}, [%2], %3;" : "=l"(v.x), "=l"(v.y) : "l"(p), "l"(l2_evict_last()));
+    return v;
+}
+
 // The nonzeros of one sliced-ELL row (`len` of them from `base`, stride
 // kSellSlice), fed to acc(code, x[col]) with U words and then U gathers in
 // flight before any arithmetic: the product is bound by the latency of the
 // x gathers, and this keeps U of them outstanding per thread.
-template <int U, bool kPacked, class LoadX, class Acc>
+template <int U, bool kPacked, bool kHint, class LoadX, class Acc>
 __device__ __forceinline__ void sell_row(const uint32_t* __restrict__ words, const int32_t* __restrict__ cols,
                                          const uint16_t* __restrict__ codes, int64_t base, int len, int cb,
                                          uint32_t cmask, LoadX ldx, Acc acc) {
@@ -24,12 +102,12 @@ __device__ __forceinline__ void sell_row(const uint32_t* __restrict__ words, con
         for (int u = 0; u < U; ++u) {
             const int64_t o = base + (int64_t)(j + u) * kSellSlice;
             if (kPacked) {
-                const uint32_t w = __ldg(words + o);
+                const uint32_t w = ld_word<kHint>(words + o);
                 col[u] = w >> cb;
                 code[u] = w & cmask;
             } else {
-                col[u] = (uint32_t)__ldg(cols + o);
-                code[u] = __ldg(codes + o);
+                col[u] = (uint32_t)ld_word<kHint>(cols + o);
+                code[u] = ld_word<kHint>(codes + o);
             }
         }
         decltype(ldx(0u)) xv[U];
@@ -42,12 +120,12 @@ __device__ __forceinline__ void sell_row(const uint32_t* __restrict__ words, con
         const int64_t o = base + (int64_t)j * kSellSlice;
         uint32_t col, code;
         if (kPacked) {
-            const uint32_t w = __ldg(words + o);
+            const uint32_t w = ld_word<kHint>(words + o);
             col = w >> cb;
             code = w & cmask;
         } else {
-            col = (uint32_t)__ldg(cols + o);
-            code = __ldg(codes + o);
+            col = (uint32_t)ld_word<kHint>(cols + o);
+            code = ld_word<kHint>(codes + o);
         }
         acc(code, ldx(col));
     }

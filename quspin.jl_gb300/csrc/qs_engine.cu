@@ -184,7 +184,7 @@ __device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA
         const int cnt = len[r];
         const int64_t base = S.sptr[sl] + lane;
         A ar = zero<A>(), ai = zero<A>();
-        sell_row<4, PACKED>(S.words, S.cols, S.codes, base, cnt, cb, cmask,
+        sell_row<4, PACKED, false>(S.words, S.cols, S.codes, base, cnt, cb, cmask,
                             [&](uint32_t c) { return ldv<A, CV>(x, c); },
                             [&](uint32_t code, CA<A> xv) {
                                 const CA<A> v = smem_tab ? tab[code] : ldtab<A>(S, code);
