@@ -256,7 +256,10 @@ QS_API int qs_op_matvec_noalloc(qs_op *op, int32_t flags, const double *alpha, c
 
 typedef struct {
     int32_t k;            /* number of eigenpairs */
-    int32_t which;        /* 0 = SA (smallest algebraic), 1 = LA */
+    int32_t which;        /* 0 = SA (smallest algebraic), 1 = LA (largest algebraic), 2 = LM (largest
+                             magnitude), 3 = SM (smallest magnitude), 4 = BE (half from each end);
+                             values come in the reference's order: SA ascending, LA descending,
+                             LM by decreasing and SM by increasing magnitude, BE descending */
     double tol;           /* relative Ritz tolerance, 0 = machine epsilon (ARPACK default) */
     int32_t ncv;          /* Lanczos basis size, 0 = max(20, 2k+1) (Arpack.jl default) */
     int32_t maxiter;      /* restarts, 0 = 300 */

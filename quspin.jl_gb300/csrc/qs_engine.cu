@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -16,6 +17,7 @@
 #include <type_traits>
 
 #include "qs_blas.cuh"
+#include "qs_tc.cuh"
 #include "qs_dense.h"
 #include "qs_df.cuh"
 #include "qs_engine.h"
@@ -738,7 +740,7 @@ __device__ __forceinline__ void rotate_rows_tile(const SlotDev& S, int64_t r0, i
 template <class A>
 __global__ void __launch_bounds__(kT, 2) eng_rotate(const SlotDev* __restrict__ sl, const int* __restrict__ rmap) {
     const SlotDev& S = sl[rmap[blockIdx.x]];
-    if (S.state != kSlotRotate) return;
+    if (S.state != kSlotRotate || S.rot_tc) return;
     const int64_t lb = blockIdx.x - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
     if (S.p <= 8) {
@@ -754,6 +756,189 @@ __global__ void __launch_bounds__(kT, 2) eng_rotate(const SlotDev* __restrict__ 
         if (S.cv) rotate_rows<A, true>(S, r0, r1);
         else rotate_rows<A, false>(S, r0, r1);
     }
+}
+
+
+// ------------------------------------------------------------ rotate on the tensor cores
+// The thick-restart rotation V[:, out0 + c] = sum_{i < rot_in} V[:, i] Y[i, c]
+// as an exact sliced integer product on the BF16 tensor cores (qs_tc.cuh) for
+// the FP64 and double-float storages.  A slot takes it (rot_tc) when its
+// coefficients are real with |Y| <= 1, 2 <= p <= 16 and rot_in <= 32 (the
+// restarts of eigsh, whose V columns are orthonormal); eng_rotate skips those
+// slots.  Each block keeps its row range: tiles of 128 real components (a
+// complex row is two), thread t owns component t of the tile.  One thread
+// issues the MMAs; every wait is bounded and a timeout sets *err.
+constexpr int kTcRows = 128, kTcK = 32, kTcN = 16, kTcDigits = 8, kTcGroups = 9;
+constexpr uint32_t kTcCols = 256;   // TMEM columns: nine accumulators of kTcN columns
+constexpr int kTcATile = kTcRows * kTcK * 2;   // bytes of one digit matrix of V's tile
+constexpr int kTcBTile = kTcN * kTcK * 2;      // bytes of one digit matrix of Y
+constexpr size_t kTcSmemUsed = (size_t)kTcDigits * (kTcATile + kTcBTile) + 1024;
+// requested so that at most two blocks share an SM (2 x 256 TMEM columns: an
+// allocation never has to wait for another block)
+constexpr size_t kTcSmem = 100 * 1024;
+static_assert(kTcSmemUsed <= kTcSmem, "tensor-core rotation tiles exceed their shared memory");
+constexpr long long kTcWaitCycles = 2000000000LL;   // about one second
+
+// real component e (8-byte unit: a double, or a double-float pair) as trunc(v 2^61)
+template <class A> __device__ __forceinline__ long long tc_fix(const char* col, int64_t e);
+template <> __device__ __forceinline__ long long tc_fix<double>(const char* col, int64_t e) {
+    return fix61(((const double*)col)[e]);
+}
+template <> __device__ __forceinline__ long long tc_fix<DF>(const char* col, int64_t e) {
+    const float2 v = ((const float2*)col)[e];
+    return fix61(v.x) + fix61(v.y);
+}
+// stores v 2^scale into real component e
+template <class A> __device__ __forceinline__ void tc_store(char* col, int64_t e, long long v, int scale);
+template <> __device__ __forceinline__ void tc_store<double>(char* col, int64_t e, long long v, int scale) {
+    ((double*)col)[e] = f64_of_i64(v, scale);
+}
+template <> __device__ __forceinline__ void tc_store<DF>(char* col, int64_t e, long long v, int scale) {
+    const float hi = f32_of_i64(v, scale);
+    const float lo = f32_of_i64(i64_minus_f32(v, hi, scale), scale);
+    ((float2*)col)[e] = make_float2(hi, lo);
+}
+// real part of the rotation coefficient e (column-major rot_in x p)
+template <class A> __device__ __forceinline__ long long tc_fix_y(const void* y, int e);
+template <> __device__ __forceinline__ long long tc_fix_y<double>(const void* y, int e) {
+    return fix61(((const CA<double>*)y)[e].re);
+}
+template <> __device__ __forceinline__ long long tc_fix_y<DF>(const void* y, int e) {
+    const DF v = ((const CA<DF>*)y)[e].re;
+    return fix61(v.h) + fix61(v.l);
+}
+
+template <class A>
+__global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __restrict__ sl,
+                                                           const int* __restrict__ rmap, int* __restrict__ err) {
+    const SlotDev& S = sl[rmap[blockIdx.x]];
+    if (S.state != kSlotRotate || !S.rot_tc) return;
+    extern __shared__ unsigned char tc_raw[];
+    unsigned char* sa = (unsigned char*)(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* sb = sa + kTcDigits * kTcATile;
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int nin = S.rot_in, p = S.p;
+    // zero both operand areas (the K padding beyond rot_in and the rows of Y
+    // beyond p stay zero), then the digits of Y: row c of B_b is digit b of
+    // Y[:, c] along K
+    for (int w = tid; w < kTcDigits * (kTcATile + kTcBTile) / 16; w += kTcRows)
+        ((uint4*)sa)[w] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    for (int e = tid; e < nin * p; e += kTcRows) {
+        const int i = e % nin, c = e / nin;
+        const long long X = tc_fix_y<A>(S.y, e);
+        const uint32_t sg = X < 0 ? 0x8000u : 0u;
+        const unsigned long long m = X < 0 ? (unsigned long long)(-X) : (unsigned long long)X;
+#pragma unroll
+        for (int a = 0; a < kTcDigits; ++a)
+            *(uint16_t*)(sb + a * kTcBTile + tc_off(c, i, kTcK)) =
+                (uint16_t)bf16_of_byte((uint32_t)(m >> (8 * (kTcDigits - 1 - a))) & 0xffu, sg);
+    }
+    if (warp == 0) tc_alloc(&tbase, kTcCols);
+    if (tid == 0) mbar_init(&mbar, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tbase;
+    const int comps = S.cv ? 2 : 1;
+    const int64_t lb = blockIdx.x - S.rb_begin;
+    const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
+    const int64_t e0 = r0 * comps, e1 = r1 * comps;
+    char* V = (char*)S.V;
+    const size_t cs = (size_t)S.n * comps * 8;   // bytes of one column
+    const int ksteps = (nin + 15) / 16;
+    uint32_t phase = 0;
+    for (int64_t t0 = e0; t0 < e1; t0 += kTcRows) {
+        const int64_t e = t0 + tid;
+        const bool live = e < e1;
+        // this component's inputs as fixed-point integers, eight per K core
+        // matrix, and their bytes as BF16 into the digit matrices
+        for (int kc = 0; kc * 8 < nin; ++kc) {
+            unsigned long long mag[8];
+            uint32_t sg[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = kc * 8 + u;
+                const long long X = (live && i < nin) ? tc_fix<A>(V + (size_t)i * cs, e) : 0ll;
+                sg[u] = X < 0 ? 0x8000u : 0u;
+                mag[u] = X < 0 ? (unsigned long long)(-X) : (unsigned long long)X;
+            }
+#pragma unroll
+            for (int a = 0; a < kTcDigits; ++a) {
+                const int sh = 8 * (kTcDigits - 1 - a);
+                uint32_t w[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    w[u] = bf16_of_byte((uint32_t)(mag[2 * u] >> sh) & 0xffu, sg[2 * u]) |
+                           (bf16_of_byte((uint32_t)(mag[2 * u + 1] >> sh) & 0xffu, sg[2 * u + 1]) << 16);
+                *(uint4*)(sa + a * kTcATile + tc_off(tid, kc * 8, kTcK)) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+        tc_fence_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            constexpr uint32_t idesc = tc_idesc_bf16(kTcRows, kTcN);
+            const uint32_t abase = smem_addr(sa), bbase = smem_addr(sb);
+            constexpr uint32_t sbo = (kTcK / 8) * 128;
+            // accumulator s: sum over digit pairs a + b = s of A_a B_b
+            for (int s = 0; s < kTcGroups; ++s) {
+                uint32_t acc = 0;
+                const int alo = s > kTcDigits - 1 ? s - (kTcDigits - 1) : 0, ahi = s < kTcDigits - 1 ? s : kTcDigits - 1;
+                for (int a = alo; a <= ahi; ++a)
+                    for (int kk = 0; kk < ksteps; ++kk) {
+                        const uint64_t ad = tc_sdesc(abase + a * kTcATile + kk * 256, 128, sbo);
+                        const uint64_t bd = tc_sdesc(bbase + (s - a) * kTcBTile + kk * 256, 128, sbo);
+                        tc_mma_bf16(tmem + (uint32_t)(s * kTcN), ad, bd, idesc, acc);
+                        acc = 1;
+                    }
+            }
+            tc_commit(&mbar);
+        }
+        const bool ok = __syncthreads_and(mbar_wait(&mbar, phase, kTcWaitCycles) ? 1 : 0);
+        phase ^= 1u;
+        tc_fence_after();
+        if (!ok) {
+            if (tid == 0) atomicExch(err, 1);
+            break;
+        }
+        // epilogue: row t of the tile is TMEM lane t; warp w reads lanes 32w..32w+31
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < p; c0 += 4) {
+            long long hi[4] = {0, 0, 0, 0}, lo[4] = {0, 0, 0, 0};
+#pragma unroll
+            for (int s = 0; s < kTcGroups; ++s) {
+                uint32_t v[4];
+                tc_ld4(trow + (uint32_t)(s * kTcN + c0), v);
+                tc_wait_ld();
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const long long d = (long long)__float2int_rn(__uint_as_float(v[u]));   // exact: |D_s| < 2^24
+                    if (s <= 3) hi[u] += d << (8 * (3 - s));
+                    else lo[u] += d << (8 * (8 - s));
+                }
+            }
+            if (live) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (c0 + u < p) {
+                        // sum = 2^-122 sum_s 256^(14-s) D_s = 2^-74 (hi 2^40 + lo); kept at 2^-62
+                        const long long T = (hi[u] << 28) + (lo[u] >> 12);
+                        tc_store<A>(V + (size_t)(S.out0 + c0 + u) * cs, e, T, -62);
+                    }
+            }
+        }
+        if (live && S.carry >= 0)
+            ((unsigned long long*)(V + (size_t)S.cdst * cs))[e] = ((const unsigned long long*)(V + (size_t)S.carry * cs))[e];
+        tc_fence_before();
+        __syncthreads();   // the next tile overwrites the digits and the accumulators
+        tc_fence_after();
+    }
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem, kTcCols);
 }
 
 // Runs f with a value of the step arithmetic's type for storage st.
@@ -801,6 +986,10 @@ Engine::Engine(Store st, cudaStream_t s) : st_(st), s_(s) {
     QS_CUDA(cudaMemcpy(rsq64_.p, r64.data(), r64.size() * sizeof(double), cudaMemcpyHostToDevice));
     QS_CUDA(cudaMemcpy(rsqdf_.p, rdf.data(), rdf.size() * sizeof(float), cudaMemcpyHostToDevice));
     QS_CUDA(cudaMemcpy(rsq32_.p, r32.data(), r32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    const char* tc = std::getenv("QS_TC_ROTATE");
+    tc_rotate_ = !(tc && tc[0] == '0');
+    tc_err_.alloc(sizeof(int));
+    QS_CUDA(cudaMemset(tc_err_.p, 0, sizeof(int)));
 }
 
 Engine::~Engine() {
@@ -1188,6 +1377,7 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
     else c32.resize((st_ == Store::DF ? 4 : 2) * total);
     std::vector<int> saved(reqs.size());
     size_t off = 0;
+    bool any_tc = false;
     for (size_t q = 0; q < reqs.size(); ++q) {
         const RotReq& R = reqs[q];
         Slot& sl = slots_[R.id];
@@ -1212,8 +1402,17 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
                 c64[2 * e + 1] = im;
             }
         }
+        // the tensor-core path: real coefficients |Y| <= 1 (the Ritz vectors of
+        // a thick restart), 2 <= p <= 16 outputs, at most 32 inputs, FP64 or
+        // double-float storage
+        double ymax = 0.0;
+        for (const cd& v : R.Y) ymax = std::max(ymax, std::abs(v.real()));
+        const bool tc = tc_rotate_ && st_ != Store::F32 && yreal && R.p >= 2 && R.p <= 16 && R.nin >= 1 &&
+                        R.nin <= 32 && ymax <= 1.0 + 1e-9;
+        any_tc = any_tc || tc;
         saved[q] = d.state;
         d.state = kSlotRotate;
+        d.rot_tc = tc ? 1 : 0;
         d.y = (char*)ybuf_.p + off * eb;
         d.yreal = yreal;
         d.rot_in = R.nin;
@@ -1235,12 +1434,34 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
         });
         QS_CUDA(cudaGetLastError());
         ++launches_;
+        if (any_tc) {
+            auto run_tc = [&](auto kern) {
+                static bool attr = false;   // one attribute setting per instantiation and process
+                if (!attr) {
+                    QS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+                    attr = true;
+                }
+                kern<<<nrb_, kTcRows, kTcSmem, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>(), tc_err_.as<int>());
+            };
+            if (st_ == Store::DF) run_tc(eng_rotate_tc<DF>);
+            else run_tc(eng_rotate_tc<double>);
+            QS_CUDA(cudaGetLastError());
+            ++launches_;
+            int err = 0;
+            QS_CUDA(cudaMemcpyAsync(&err, tc_err_.p, sizeof(int), cudaMemcpyDeviceToHost, s_));
+            QS_CUDA(cudaStreamSynchronize(s_));
+            if (err) {
+                QS_CUDA(cudaMemsetAsync(tc_err_.p, 0, sizeof(int), s_));
+                throw Error(QS_ERR_CUDA, "the tensor-core rotation timed out waiting for its MMAs");
+            }
+        }
     }
     for (size_t q = 0; q < reqs.size(); ++q) {
         SlotDev& d = slots_[reqs[q].id].d;
         d.state = saved[q] == kSlotRotate ? kSlotIdle : saved[q];
         d.carry = -1;
         d.p = 0;
+        d.rot_tc = 0;
     }
     dirty_ = true;
 }
@@ -1285,8 +1506,7 @@ bool EigTask::on_hold(const std::vector<cd>& H, int id, RotReq& rot) {
     }
     std::vector<double> w, Y;
     sym_eig(m, T, w, Y);
-    std::vector<int> order(m);
-    for (int q = 0; q < m; ++q) order[q] = which == 0 ? q : m - 1 - q;
+    const std::vector<int> order = ritz_order(w, which, k);
     int nc = 0;
     double mr = 0;
     for (int q = 0; q < k; ++q) {
@@ -1324,12 +1544,13 @@ bool EigTask::on_hold(const std::vector<cd>& H, int id, RotReq& rot) {
 
 // ================================================================ batched eigsh
 // Thick-restart Lanczos (the iteration of eigsh in qs_krylov.cu) on every
-// operator at once; values: nops * k, ascending per operator.
+// operator at once; values: nops * k per operator, in the order of `which`
+// (ritz_order).
 void eigsh_batch(Op** ops, int nops, const qs_eigsh_opts& o, double* values, void** vectors, qs_eigsh_info* infos) {
     auto t0 = std::chrono::steady_clock::now();
     if (nops <= 0) throw Error(QS_ERR_ARGUMENT, "no operators");
     const int k = o.k;
-    if (o.which != 0 && o.which != 1) throw Error(QS_ERR_UNSUPPORTED, "which must be SA or LA on this engine");
+    if (o.which < 0 || o.which > 4) throw Error(QS_ERR_ARGUMENT, "which must be SA, LA, SM, LM, or BE");
     int m = o.ncv > 0 ? o.ncv : std::max(20, 2 * k + 1);
     m = std::min(m, kMaxM);
     for (int i = 0; i < nops; ++i) {

@@ -76,6 +76,7 @@ struct SlotDev {
     // V[:, cdst] = V[:, carry] when carry >= 0
     int32_t rot_in, p, out0, carry, cdst;
     int32_t yreal;          // rotation coefficients are real
+    int32_t rot_tc;         // the rotation runs on the tensor cores (eng_rotate_tc)
     int32_t ncol;           // column normalised by normalize()
     // tiles
     int32_t rpb, spb;       // rows per BLAS block, slices per SpMV block
@@ -163,6 +164,8 @@ class Engine {
     cudaStream_t s_;
     std::vector<Slot> slots_;
     DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_, rsq32_, ybuf_;
+    DevBuf tc_err_;            // timeout flag of the tensor-core rotation
+    bool tc_rotate_ = true;    // QS_TC_ROTATE=0 keeps every rotation on eng_rotate
     size_t cap_y_ = 0;
     int nrb_ = 0, nsb_ = 0, mmax_ = 1, cap_slots_ = 0;
     // most vectors any slot dots against in a step (1 for three-term slots,

@@ -145,8 +145,7 @@ TRResult trlan(Ctx& c, int k, int which, double tol, int ncv, int maxiter, const
             for (int j = 0; j < m_eff; ++j) Te[(size_t)i * m_eff + j] = Tij(i, j);
         sym_eig(m_eff, Te, w, Y);
         auto yv = [&](int r, int col) { return Y[(size_t)r * m_eff + col]; };
-        std::vector<int> order(m_eff);
-        for (int i = 0; i < m_eff; ++i) order[i] = which == 0 ? i : (m_eff - 1 - i);
+        const std::vector<int> order = ritz_order(w, which, k);
         int kk = std::min(k, m_eff);
         int nconv = 0;
         double maxrel = 0.0;
@@ -204,7 +203,7 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
     const int64_t n = op.basis->n;
     const int k = o.k;
     if (k < 1 || k > n) throw Error(QS_ERR_ARGUMENT, "k must lie in 1:Ns");
-    if (o.which != 0 && o.which != 1) throw Error(QS_ERR_UNSUPPORTED, "which must be SA or LA on this engine");
+    if (o.which < 0 || o.which > 4) throw Error(QS_ERR_ARGUMENT, "which must be SA, LA, SM, LM, or BE");
     if (!op.hermitian) throw Error(QS_ERR_UNSUPPORTED, "eigsh on this engine needs a Hermitian operator");
     const bool cpx = op.complex_mat;
     const VKind k64 = cpx ? VKind::C128 : VKind::F64;
@@ -261,8 +260,11 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
                 if (best >= 0) used[best] = 1;
             }
         }
+        std::vector<double> wp(pick.size());
+        for (size_t q = 0; q < pick.size(); ++q) wp[q] = w[pick[q]];
+        const std::vector<int> rank = ritz_order(wp, o.which, k);
         std::vector<int> sel;
-        for (int q = 0; q < k; ++q) sel.push_back(o.which == 0 ? pick[q] : pick[pick.size() - 1 - q]);
+        for (int q = 0; q < k; ++q) sel.push_back(pick[rank[q]]);
         for (int q = 0; q < k; ++q) values[q] = w[sel[q]];
         if (o.want_vectors && vectors) {
             double* out = (double*)vectors;

@@ -21,6 +21,9 @@
 // shared-memory splitter stage.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+#include <cstring>
+
 #include <algorithm>
 #include <atomic>
 
@@ -321,6 +324,158 @@ __global__ void __launch_bounds__(kMvThreads) matvec_kernel(MvArgs a) {
     }
 }
 
+
+// ----------------------------------------------------- warp-cooperative rank
+// First index in [a, b) whose value is >= q (b when none), with all 32 lanes
+// of the warp probing together: each round reads 32 evenly spaced entries and
+// a ballot keeps the one stride that holds the bound, so a range shrinks
+// 32-fold per round.  q and the range are the same in every lane.
+template <typename U, class Get>
+__device__ __forceinline__ int64_t warp_lower_bound(int64_t a, int64_t b, U q, Get get) {
+    const int lane = threadIdx.x & 31;
+    while (b - a > 32) {
+        const int64_t step = (b - a + 31) / 32;
+        const int64_t idx = a + (int64_t)lane * step;
+        const unsigned below = __ballot_sync(0xffffffffu, idx < b && get(idx) < q);
+        const int c = __popc(below);   // probes are ascending, so the ones below q are a prefix
+        if (c == 0) return a;
+        const int64_t nb = a + (int64_t)c * step;
+        a = a + (int64_t)(c - 1) * step + 1;
+        b = nb < b ? nb : b;
+    }
+    const int64_t idx = a + lane;
+    return a + __popc(__ballot_sync(0xffffffffu, idx < b && get(idx) < q));
+}
+
+// Column of the representative `key` of every lane that wants one (-1: not a
+// representative), resolved for one lane after another by the whole warp: two
+// rounds over the shared-memory splitters (splitter i = reps[i * stride]),
+// then rounds over the splitter's segment of the sorted representatives in
+// global memory.  Every lane of the warp must call it.
+template <typename U>
+__device__ __forceinline__ int64_t rank_warp(const U* __restrict__ reps, int64_t n, const U* spl, int nsplit,
+                                             int64_t stride, U key, bool want) {
+    const int lane = threadIdx.x & 31;
+    int64_t out = -1;
+    unsigned pend = __ballot_sync(0xffffffffu, want);
+    while (pend) {
+        const int j = __ffs(pend) - 1;
+        pend &= pend - 1;
+        const U q = __shfl_sync(0xffffffffu, key, j);
+        const int64_t ls = warp_lower_bound<U>(0, nsplit, q, [&](int64_t i) { return spl[i]; });
+        int64_t idx = -1;
+        if (ls < nsplit && spl[ls] == q) {
+            idx = ls * stride;
+        } else if (ls > 0) {
+            const int64_t sa = (ls - 1) * stride, sb = sa + stride < n ? sa + stride : n;
+            const int64_t lb = warp_lower_bound<U>(sa, sb, q, [&](int64_t i) { return __ldg(reps + i); });
+            if (lb < sb && __ldg(reps + lb) == q) idx = lb;
+        }
+        if (lane == j) out = idx;
+    }
+    return out;
+}
+
+// The symmetric-sector product of matvec_kernel with the rank of every
+// generated state found by rank_warp (QS_RANK_MODE=warp): rows are taken a
+// warp at a time so that all 32 lanes reach every lookup together.
+template <typename U, bool kCM, bool kCV, typename T>
+__global__ void __launch_bounds__(kMvThreads) matvec_warp_rank_kernel(MvArgs a) {
+    __shared__ GroupSmem g;
+    __shared__ U spl[kMaxSplit];
+    __shared__ TermProg progs[kSmemProgs];
+    __shared__ double sqrt_stab[kMaxGroup + 1];
+    load_group_smem(g, a.group);
+    for (int i = threadIdx.x; i < a.nsplit; i += blockDim.x) spl[i] = ((const U*)a.split)[i];
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) sqrt_stab[i] = sqrt((double)i);
+    const int np_smem = a.nprog < kSmemProgs ? a.nprog : kSmemProgs;
+    for (int i = threadIdx.x; i < np_smem; i += blockDim.x) progs[i] = a.progs[i];
+    __syncthreads();
+    const double* chi_re = a.group->chi_re;
+    const double* chi_im = a.group->chi_im;
+    const int lane = threadIdx.x & 31;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < a.n; base += nthreads) {
+        const int64_t r = base + lane;
+        const bool rv = r < a.n;
+        const U s = rv ? ((const U*)a.reps)[r] : (U)0;
+        const T inv_sr = rv ? (T)1 / (T)sqrt_stab[a.stab[r]] : (T)0;
+        T acc_r = 0, acc_i = 0;
+        for (int k = 0; k < a.nprog; ++k) {
+            const TermProg& p = (k < kSmemProgs) ? progs[k] : a.progs[k];
+            U t = 0, m = 0;
+            T wr = 0, wi = 0;
+            int bi = 0, st = 0;
+            const bool alive = rv && run_prog<U, T>(p, a.pauli, s, t, wr, wi);
+            const double* chr = chi_re;
+            const double* chi = chi_im;
+            int cstride = 1;
+            if (alive) {
+                if (a.conj_amp) wi = -wi;
+                if (a.fast.enabled) {
+                    orbit_min_fast<U>(a.fast, t, m, bi, st);
+                    chr = a.fast_chi;
+                    chi = a.fast_chi + 1;
+                    cstride = 2;
+                } else {
+                    orbit_min<U>(g, t, m, bi, st);
+                }
+            }
+            const int64_t idx = rank_warp<U>((const U*)a.reps, a.n, spl, (int)a.nsplit, a.stride, m, alive);
+            if (!alive || idx < 0) continue;
+            const T f = (T)sqrt_stab[st] * inv_sr;
+            if (kCM) {
+                T cr = (T)__ldg(chr + bi * cstride), ci = (T)__ldg(chi + bi * cstride);
+                if (a.conj_chi) ci = -ci;
+                const T nr = wr * cr - wi * ci, ni = wr * ci + wi * cr;
+                wr = nr * f;
+                wi = ni * f;
+            } else {
+                wr *= (T)__ldg(chr + bi * cstride) * f;
+            }
+            T xr, xi;
+            load_x<T, kCV>(a, idx, xr, xi);
+            if (kCM) {
+                acc_r += wr * xr - wi * xi;
+                acc_i += wr * xi + wi * xr;
+            } else if (kCV) {
+                acc_r += wr * xr;
+                acc_i += wr * xi;
+            } else {
+                acc_r += wr * xr;
+            }
+        }
+        if (!rv) continue;
+        typename V2<T>::t d = ((const typename V2<T>::t*)a.diag)[r];
+        const T dr = d.x, di = a.conj_amp ? -d.y : d.y;
+        T xr, xi;
+        load_x<T, kCV>(a, r, xr, xi);
+        if (kCV) {
+            acc_r += dr * xr - di * xi;
+            acc_i += dr * xi + di * xr;
+        } else {
+            acc_r += dr * xr;
+        }
+        if (kCV) {
+            typename V2<T>::t* y = (typename V2<T>::t*)a.y;
+            T yr = 0, yi = 0;
+            if (!a.beta_zero) {
+                typename V2<T>::t yo = y[r];
+                yr = (T)a.br * yo.x - (T)a.bi * yo.y;
+                yi = (T)a.br * yo.y + (T)a.bi * yo.x;
+            }
+            typename V2<T>::t o;
+            o.x = yr + (T)a.ar * acc_r - (T)a.ai * acc_i;
+            o.y = yi + (T)a.ar * acc_i + (T)a.ai * acc_r;
+            y[r] = o;
+        } else {
+            T* y = (T*)a.y;
+            const T yr = a.beta_zero ? (T)0 : (T)a.br * y[r];
+            y[r] = yr + (T)a.ar * acc_r;
+        }
+    }
+}
+
 // General path for operators that do not commute with the group (reference:
 // check_symm=false on a symmetric basis, src/operators.jl:2500-2506): the full
 // P' A P with both projector sides expanded over the group,
@@ -484,8 +639,40 @@ void launch_mode(const MvArgs& a, bool cm, bool cv, cudaStream_t s) {
     else matvec_kernel<U, kMode, false, false, T><<<grid, kMvThreads, 0, s>>>(a);
 }
 
+// QS_RANK_MODE picks the rank lookup of a symmetric sector's generated states
+// (read on every product): "direct" (the rank -> column table, when built),
+// "search" (per-thread binary search behind shared-memory splitters) or
+// "warp" (the warp-cooperative search); default: direct when built, else search.
+int rank_mode_env() {
+    const char* e = std::getenv("QS_RANK_MODE");
+    if (!e || !e[0]) return -1;
+    if (!std::strcmp(e, "direct")) return 3;
+    if (!std::strcmp(e, "search")) return 2;
+    if (!std::strcmp(e, "warp")) return 4;
+    return -1;
+}
+
 template <typename T>
 void launch_matvec(const Basis& b, const MvArgs& a, bool cm, bool cv, cudaStream_t s) {
+    const int rm = b.symmetric ? rank_mode_env() : -1;
+    if (rm == 4) {
+        const int grid = mv_grid(a.n);
+        if (b.wide) {
+            if (cm) matvec_warp_rank_kernel<uint64_t, true, true, T><<<grid, kMvThreads, 0, s>>>(a);
+            else if (cv) matvec_warp_rank_kernel<uint64_t, false, true, T><<<grid, kMvThreads, 0, s>>>(a);
+            else matvec_warp_rank_kernel<uint64_t, false, false, T><<<grid, kMvThreads, 0, s>>>(a);
+        } else {
+            if (cm) matvec_warp_rank_kernel<uint32_t, true, true, T><<<grid, kMvThreads, 0, s>>>(a);
+            else if (cv) matvec_warp_rank_kernel<uint32_t, false, true, T><<<grid, kMvThreads, 0, s>>>(a);
+            else matvec_warp_rank_kernel<uint32_t, false, false, T><<<grid, kMvThreads, 0, s>>>(a);
+        }
+        return;
+    }
+    if (b.symmetric && rm == 2) {
+        if (b.wide) launch_mode<uint64_t, 2, T>(a, cm, cv, s);
+        else launch_mode<uint32_t, 2, T>(a, cm, cv, s);
+        return;
+    }
     if (b.symmetric && b.has_index) {
         if (b.wide) launch_mode<uint64_t, 3, T>(a, cm, cv, s);
         else launch_mode<uint32_t, 3, T>(a, cm, cv, s);

@@ -793,8 +793,8 @@ int64_t server_submit(Server* S, const qs_request* r) {
     if (!r) throw Error(QS_ERR_ARGUMENT, "null request");
     if (r->kind != QS_REQ_EIGSH && r->kind != QS_REQ_EVOLVE) throw Error(QS_ERR_ARGUMENT, "unknown request kind");
     if (r->nterms < 0 || (r->nterms > 0 && !r->terms)) throw Error(QS_ERR_ARGUMENT, "terms missing");
-    if (r->kind == QS_REQ_EIGSH && r->which != 0 && r->which != 1)
-        throw Error(QS_ERR_UNSUPPORTED, "which must be SA or LA on this engine");
+    if (r->kind == QS_REQ_EIGSH && (r->which < 0 || r->which > 4))
+        throw Error(QS_ERR_ARGUMENT, "which must be SA, LA, SM, LM, or BE");
     auto q = std::make_shared<Request>();
     q->r = *r;
     q->r.terms = nullptr;

@@ -296,6 +296,18 @@ def _precision_code(precision):
     return codes[precision]
 
 
+_WHICH = {"SA": 0, "LA": 1, "LM": 2, "SM": 3, "BE": 4}
+
+
+def _which_code(which):
+    """eigsh's `which` (src/operators.jl:3376-3378): SA and LA by algebraic
+    value, LM and SM by magnitude, BE half from each end."""
+    w = str(which).upper()
+    if w not in _WHICH:
+        raise ArgumentError("which must be SA, LA, SM, LM, or BE")
+    return _WHICH[w]
+
+
 def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, ncv=None, maxiter=None,
           precision="fp64", info=None):
     """eigsh(op; k, which=:SA, v0, tol, ncv, maxiter): k extremal eigenpairs."""
@@ -303,17 +315,13 @@ def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, nc
     k = min(6, n) if k is None else int(k)
     if not (1 <= k <= n):
         raise ArgumentError("k must lie in 1:Ns")
-    w = str(which).upper()
-    if w not in ("SA", "LA", "SM", "LM", "BE"):
-        raise ArgumentError("which must be SA, LA, SM, LM, or BE")
-    if w not in ("SA", "LA"):
-        raise ArgumentError(f"which={w} is not implemented on this engine")
+    code = _which_code(which)
     vv = None
     if v0 is not None:
         vv = np.ascontiguousarray(v0, dtype=op.dtype)
         if vv.shape != (n,):
             raise DimensionMismatch("v0 must have length Ns")
-    opts = _lib.EigshOpts(k, 0 if w == "SA" else 1, float(tol), int(ncv or 0), int(maxiter or 0),
+    opts = _lib.EigshOpts(k, code, float(tol), int(ncv or 0), int(maxiter or 0),
                           _precision_code(precision), int(bool(return_eigenvectors)),
                           _lib.ptr(vv) if vv is not None else None, _lib.QS_MEM_HOST)
     vals = np.zeros(k)
@@ -336,12 +344,10 @@ def eigsh_batch(ops, k=1, which="SA", tol=0.0, ncv=None, maxiter=None, return_ei
     Rayleigh-quotient polish (and a double-float refinement where the polish
     misses the tolerance).  Returns an (len(ops), k) array of eigenvalues and,
     when asked, one Ns_i x k vector block per operator."""
-    w = str(which).upper()
-    if w not in ("SA", "LA"):
-        raise ArgumentError("which must be SA or LA on this engine")
+    code = _which_code(which)
     n = len(ops)
     arr = (ctypes.c_void_p * n)(*[o._h for o in ops])
-    opts = _lib.EigshOpts(int(k), 0 if w == "SA" else 1, float(tol), int(ncv or 0), int(maxiter or 0),
+    opts = _lib.EigshOpts(int(k), code, float(tol), int(ncv or 0), int(maxiter or 0),
                           _precision_code(precision), 0, None, _lib.QS_MEM_HOST)
     vals = np.zeros((n, int(k)))
     vecs = None

@@ -378,3 +378,70 @@ def test_stepwise_evolution(qs, ora):
         want = sla.expm(-tau * D) @ v0
         want /= np.linalg.norm(want)
         assert np.linalg.norm(im[:, i] - want) < 1e-9
+
+
+def _dense_from_oracle(ora, L, nup, pauli, sym, sp):
+    rep = ora.RepBasis(L, nup=nup, pauli=pauli, **sym)
+    n = rep.Ns
+    D = np.zeros((n, n), dtype=np.complex128)
+    e = np.zeros(n, dtype=np.complex128)
+    for j in range(n):
+        e[:] = 0
+        e[j] = 1
+        D[:, j] = rep.matvec(sp, e)
+    return D
+
+
+def _expected(w, which, k):
+    """The reference's selection and order (src/operators.jl:1587-1596, 3393-3401)."""
+    if which == "SA":
+        return np.sort(w)[:k]
+    if which == "LA":
+        return np.sort(w)[::-1][:k]
+    if which == "LM":
+        return w[np.argsort(-np.abs(w), kind="stable")][:k]
+    if which == "SM":
+        return w[np.argsort(np.abs(w), kind="stable")][:k]
+    ws = np.sort(w)
+    return np.sort(np.concatenate([ws[:k // 2], ws[len(ws) - (k - k // 2):]]))[::-1]
+
+
+@pytest.mark.parametrize("which", ["SA", "LA", "LM", "SM", "BE"])
+def test_eigsh_which_matches_dense(qs, ora, which):
+    """which = SA / LA / LM / SM / BE on the matrix-free, assembled (FP64 and
+    double-float engines) and FP32 + polish paths, and on the dense branch."""
+    L, nup, sym = 14, 7, dict(kblock=0, pblock=1, zblock=1)
+    sp = models.j1j2(L, 1.0, 0.5)
+    b = qs.SpinBasis1D(L, nup=nup, pauli=False, **sym)
+    D = _dense_from_oracle(ora, L, nup, False, sym, sp)
+    w = np.linalg.eigvalsh(D)
+    k = 4
+    want = _expected(w, which, k)
+    scale = float(np.abs(w).max())
+    Q = qs.QuantumLinearOperator(b, models.to_terms(qs, sp))
+    H = qs.Hamiltonian(b, models.to_terms(qs, sp))
+    for op, prec in ((Q, "fp64"), (H, "fp64"), (H, "fp64df"), (H, "fp32")):
+        vals, vecs = qs.eigsh(op, k=k, which=which, tol=1e-12, ncv=40, maxiter=3000, precision=prec)
+        assert np.allclose(vals, want, rtol=1e-10, atol=1e-10 * scale), (prec, vals, want)
+        assert np.max(np.abs(D @ vecs - vecs * vals)) < 1e-7 * scale, prec
+    # k >= Ns - 1 takes the dense branch
+    small = qs.SpinBasis1D(8, nup=4, pauli=False, kblock=0, pblock=1)
+    sps = models.j1j2(8, 1.0, 0.5)
+    Ds = _dense_from_oracle(ora, 8, 4, False, dict(kblock=0, pblock=1), sps)
+    ws = np.linalg.eigvalsh(Ds)
+    ks = small.Ns - 1
+    got = qs.eigsh(qs.QuantumLinearOperator(small, models.to_terms(qs, sps)), k=ks, which=which,
+                   return_eigenvectors=False)
+    assert np.allclose(got, _expected(ws, which, ks), atol=1e-10 * max(1.0, np.abs(ws).max()))
+
+
+def test_eigsh_batch_which(qs, ora):
+    L = 12
+    sp = models.j1j2(L, 1.0, 0.5)
+    syms = [dict(kblock=0, pblock=1), dict(kblock=3), dict(kblock=6, pblock=-1)]
+    ops = [qs.Hamiltonian(qs.SpinBasis1D(L, nup=6, pauli=False, **sy), models.to_terms(qs, sp)) for sy in syms]
+    for which in ("LM", "BE"):
+        got = qs.eigsh_batch(ops, k=3, which=which, tol=1e-12, ncv=30, maxiter=3000)
+        for i, sy in enumerate(syms):
+            w = np.linalg.eigvalsh(_dense_from_oracle(ora, L, 6, False, sy, sp))
+            assert np.allclose(got[i], _expected(w, which, 3), rtol=1e-10, atol=1e-10 * np.abs(w).max()), (which, i)
