@@ -952,36 +952,28 @@ def profile_range(kind):
         prec = {"product64": "fp64", "product32": "fp32", "productdf": "fp64df", "productfx": "fp64fx",
                 "matrixfree": "fp64"}[kind]
         x = np.random.default_rng(20261203).standard_normal(b.Ns)
-        if kind == "productfx":
-            # device buffers: one full-range product (its two passes over x, then the sums)
-            import ctypes
-            from qsgpu import _lib
-            lib = _lib.load()
-            one, zero = np.array([1.0, 0.0]), np.array([0.0, 0.0])
-            xt = torch.from_numpy(x).cuda()
-            yt = torch.empty_like(xt)
+        # device buffers (what the bench times): one launch is one full-range
+        # product; the warm-up products time the kernel variants first
+        import ctypes
+        from qsgpu import _lib
+        lib = _lib.load()
+        one, zero = np.array([1.0, 0.0]), np.array([0.0, 0.0])
+        code = _lib.QS_F32 if prec == "fp32" else _lib.QS_F64
+        xt = torch.from_numpy(x.astype(np.float32) if prec == "fp32" else x).cuda()
+        yt = torch.empty_like(xt)
+        flags = {"fp64df": _lib.QS_DOUBLE_FLOAT, "fp64fx": _lib.QS_FIXED_POINT}.get(prec, 0)
 
-            def mv():
-                _lib.check(lib.qs_op_matvec(H._h, _lib.QS_FIXED_POINT, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()),
-                                            _lib.QS_F64, _lib.ptr(zero), ctypes.c_void_p(yt.data_ptr()), _lib.QS_F64,
-                                            1, _lib.QS_MEM_DEVICE))
-            for _ in range(3):
-                mv()
-            torch.cuda.synchronize()
-            torch.cuda.profiler.start()
-            mv()
-            torch.cuda.synchronize()
-            torch.cuda.profiler.stop()
-            print(json.dumps({"profile_range": kind, "N": b.Ns, "ynorm": float(yt.norm())}))
-            return
+        def mv():
+            _lib.check(lib.qs_op_matvec(H._h, flags, _lib.ptr(one), ctypes.c_void_p(xt.data_ptr()), code,
+                                        _lib.ptr(zero), ctypes.c_void_p(yt.data_ptr()), code, 1, _lib.QS_MEM_DEVICE))
         for _ in range(3):
-            H.dot(x, precision=prec)   # the first product times the kernel variants
+            mv()
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
-        y = H.dot(x, precision=prec)
+        mv()
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
-        print(json.dumps({"profile_range": kind, "N": b.Ns, "ynorm": float(np.linalg.norm(y))}))
+        print(json.dumps({"profile_range": kind, "N": b.Ns, "ynorm": float(yt.double().norm())}))
         return
     L = int(kind[len("batch"):])
     terms = [qs.OperatorTerm(o, c) for o, c in j1j2_spec(L, 1.0, 0.3)]

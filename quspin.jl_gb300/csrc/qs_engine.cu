@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(kT, 2) eng_rotate(const SlotDev* __restrict__ 
 // ------------------------------------------------------------ rotate on the tensor cores
 // The thick-restart rotation V[:, out0 + c] = sum_{i < rot_in} V[:, i] Y[i, c]
 // as an exact sliced integer product on the BF16 tensor cores (qs_tc.cuh) for
-// the FP64 and double-float storages.  A slot takes it (rot_tc) when its
+// the FP64 storage.  A slot takes it (rot_tc) when its
 // coefficients are real with |Y| <= 1, 2 <= p <= 16 and rot_in <= 32 (the
 // restarts of eigsh, whose V columns are orthonormal); eng_rotate skips those
 // slots.  Each block keeps its row range: tiles of 128 real components (a
@@ -779,33 +779,20 @@ constexpr size_t kTcSmem = 100 * 1024;
 static_assert(kTcSmemUsed <= kTcSmem, "tensor-core rotation tiles exceed their shared memory");
 constexpr long long kTcWaitCycles = 2000000000LL;   // about one second
 
-// real component e (8-byte unit: a double, or a double-float pair) as trunc(v 2^61)
-template <class A> __device__ __forceinline__ long long tc_fix(const char* col, int64_t e);
-template <> __device__ __forceinline__ long long tc_fix<double>(const char* col, int64_t e) {
-    return fix61(((const double*)col)[e]);
-}
-template <> __device__ __forceinline__ long long tc_fix<DF>(const char* col, int64_t e) {
-    const float2 v = ((const float2*)col)[e];
-    return fix61(v.x) + fix61(v.y);
+// real component (8 bytes) as trunc(v 2^61), from its raw bits
+template <class A> __device__ __forceinline__ long long tc_fix_bits(unsigned long long b);
+template <> __device__ __forceinline__ long long tc_fix_bits<double>(unsigned long long b) {
+    return fix61(__longlong_as_double((long long)b));
 }
 // stores v 2^scale into real component e
 template <class A> __device__ __forceinline__ void tc_store(char* col, int64_t e, long long v, int scale);
 template <> __device__ __forceinline__ void tc_store<double>(char* col, int64_t e, long long v, int scale) {
     ((double*)col)[e] = f64_of_i64(v, scale);
 }
-template <> __device__ __forceinline__ void tc_store<DF>(char* col, int64_t e, long long v, int scale) {
-    const float hi = f32_of_i64(v, scale);
-    const float lo = f32_of_i64(i64_minus_f32(v, hi, scale), scale);
-    ((float2*)col)[e] = make_float2(hi, lo);
-}
 // real part of the rotation coefficient e (column-major rot_in x p)
 template <class A> __device__ __forceinline__ long long tc_fix_y(const void* y, int e);
 template <> __device__ __forceinline__ long long tc_fix_y<double>(const void* y, int e) {
     return fix61(((const CA<double>*)y)[e].re);
-}
-template <> __device__ __forceinline__ long long tc_fix_y<DF>(const void* y, int e) {
-    const DF v = ((const CA<DF>*)y)[e].re;
-    return fix61(v.h) + fix61(v.l);
 }
 
 template <class A>
@@ -850,18 +837,30 @@ __global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __res
     const size_t cs = (size_t)S.n * comps * 8;   // bytes of one column
     const int ksteps = (nin + 15) / 16;
     uint32_t phase = 0;
+    // raw inputs of this thread's component, the next tile's loaded while the
+    // tensor cores work on the current one
+    unsigned long long raw[kTcK];
+    auto load_tile = [&](int64_t t0) {
+        const int64_t e = t0 + tid;
+        const bool live = e < e1;
+#pragma unroll
+        for (int i = 0; i < kTcK; ++i)
+            raw[i] = (live && i < nin) ? ((const unsigned long long*)(V + (size_t)i * cs))[e] : 0ull;
+    };
+    if (e0 < e1) load_tile(e0);
     for (int64_t t0 = e0; t0 < e1; t0 += kTcRows) {
         const int64_t e = t0 + tid;
         const bool live = e < e1;
-        // this component's inputs as fixed-point integers, eight per K core
-        // matrix, and their bytes as BF16 into the digit matrices
-        for (int kc = 0; kc * 8 < nin; ++kc) {
+        // the inputs as fixed-point integers, eight per K core matrix, and
+        // their bytes as BF16 into the digit matrices
+#pragma unroll
+        for (int kc = 0; kc < kTcK / 8; ++kc) {
+            if (kc * 8 >= nin) break;
             unsigned long long mag[8];
             uint32_t sg[8];
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
-                const int i = kc * 8 + u;
-                const long long X = (live && i < nin) ? tc_fix<A>(V + (size_t)i * cs, e) : 0ll;
+                const long long X = tc_fix_bits<A>(raw[kc * 8 + u]);
                 sg[u] = X < 0 ? 0x8000u : 0u;
                 mag[u] = X < 0 ? (unsigned long long)(-X) : (unsigned long long)X;
             }
@@ -898,6 +897,8 @@ __global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __res
             }
             tc_commit(&mbar);
         }
+        // the digits are in shared memory: fetch the next tile meanwhile
+        if (t0 + kTcRows < e1) load_tile(t0 + kTcRows);
         const bool ok = __syncthreads_and(mbar_wait(&mbar, phase, kTcWaitCycles) ? 1 : 0);
         phase ^= 1u;
         tc_fence_after();
@@ -908,15 +909,19 @@ __global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __res
         // epilogue: row t of the tile is TMEM lane t; warp w reads lanes 32w..32w+31
         const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
         for (int c0 = 0; c0 < p; c0 += 4) {
+            uint32_t v[kTcGroups][4];
+#pragma unroll
+            for (int s = 0; s < kTcGroups; ++s) tc_ld4(trow + (uint32_t)(s * kTcN + c0), v[s]);
+            tc_wait_ld();
             long long hi[4] = {0, 0, 0, 0}, lo[4] = {0, 0, 0, 0};
 #pragma unroll
             for (int s = 0; s < kTcGroups; ++s) {
-                uint32_t v[4];
-                tc_ld4(trow + (uint32_t)(s * kTcN + c0), v);
-                tc_wait_ld();
+                // a new definition after the wait: no use of the loaded
+                // registers can move above it
+                asm volatile("" : "+r"(v[s][0]), "+r"(v[s][1]), "+r"(v[s][2]), "+r"(v[s][3]));
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
-                    const long long d = (long long)__float2int_rn(__uint_as_float(v[u]));   // exact: |D_s| < 2^24
+                    const long long d = (long long)__float2int_rn(__uint_as_float(v[s][u]));   // exact: |D_s| < 2^24
                     if (s <= 3) hi[u] += d << (8 * (3 - s));
                     else lo[u] += d << (8 * (8 - s));
                 }
@@ -1403,11 +1408,13 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
             }
         }
         // the tensor-core path: real coefficients |Y| <= 1 (the Ritz vectors of
-        // a thick restart), 2 <= p <= 16 outputs, at most 32 inputs, FP64 or
-        // double-float storage
+        // a thick restart), 2 <= p <= 16 outputs, at most 32 inputs
         double ymax = 0.0;
         for (const cd& v : R.Y) ymax = std::max(ymax, std::abs(v.real()));
-        const bool tc = tc_rotate_ && st_ != Store::F32 && yreal && R.p >= 2 && R.p <= 16 && R.nin >= 1 &&
+        // (the double-float rotation runs on the FP32 pipe near its memory
+        // bound, and measured no slower than the tensor-core form: only the
+        // FP64 storage takes it)
+        const bool tc = tc_rotate_ && st_ == Store::F64 && yreal && R.p >= 2 && R.p <= 16 && R.nin >= 1 &&
                         R.nin <= 32 && ymax <= 1.0 + 1e-9;
         any_tc = any_tc || tc;
         saved[q] = d.state;
@@ -1435,16 +1442,17 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
         QS_CUDA(cudaGetLastError());
         ++launches_;
         if (any_tc) {
-            auto run_tc = [&](auto kern) {
-                static bool attr = false;   // one attribute setting per instantiation and process
-                if (!attr) {
-                    QS_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
-                    attr = true;
-                }
-                kern<<<nrb_, kTcRows, kTcSmem, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>(), tc_err_.as<int>());
-            };
-            if (st_ == Store::DF) run_tc(eng_rotate_tc<DF>);
-            else run_tc(eng_rotate_tc<double>);
+            // the shared-memory size, once per device
+            static thread_local int attr_dev = -1;
+            int dev = 0;
+            QS_CUDA(cudaGetDevice(&dev));
+            if (attr_dev != dev) {
+                QS_CUDA(cudaFuncSetAttribute(eng_rotate_tc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kTcSmem));
+                attr_dev = dev;
+            }
+            eng_rotate_tc<double><<<nrb_, kTcRows, kTcSmem, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>(),
+                                                                   tc_err_.as<int>());
             QS_CUDA(cudaGetLastError());
             ++launches_;
             int err = 0;

@@ -3,8 +3,8 @@
 //
 // The Krylov restart rotation V[:, 0:p] = V[:, 0:m] Y is the one dense
 // contraction of the solvers (N x m by m x p, m <= 32).  GB300 has no fast
-// FP64 tensor path, so the FP64 and double-float engines run it as an exact
-// integer product on the BF16 tensor cores, after Ozaki et al. ("Error-free
+// FP64 tensor path, so the FP64 engine runs it as an exact integer product on
+// the BF16 tensor cores, after Ozaki et al. ("Error-free
 // transformations of matrix multiplication by using fast routines of matrix
 // multiplication and its applications", Numer. Algorithms 2012): every entry
 // (|v| <= 2) is scaled to a 61-bit fixed-point integer X = trunc(v 2^61),
@@ -118,17 +118,6 @@ __device__ __forceinline__ long long fix61(double v) {
     if (e != 0) q = sh >= 0 ? mant << (sh > 9 ? 9 : sh) : (sh > -64 ? mant >> -sh : 0ull);
     return (b >> 63) ? -(long long)q : (long long)q;
 }
-// the same for a float (exact: a float has 24 significant bits)
-__device__ __forceinline__ long long fix61(float v) {
-    const unsigned b = __float_as_uint(v);
-    const int e = (int)((b >> 23) & 0xff);
-    const unsigned long long mant = (unsigned long long)((b & 0x7fffffu) | (1u << 23));
-    const int sh = e - 127 - 23 + 61;
-    unsigned long long q = 0;
-    if (e != 0) q = sh >= 0 ? mant << (sh > 38 ? 38 : sh) : (sh > -64 ? mant >> -sh : 0ull);
-    return (b >> 31) ? -(long long)q : (long long)q;
-}
-
 // BF16 bits of sign * byte (byte <= 255 is exact in BF16's 8 significant bits)
 __device__ __forceinline__ uint32_t bf16_of_byte(uint32_t byte, uint32_t sign) {
     const float f = __uint_as_float(0x4B000000u | byte) - 8388608.0f;
@@ -156,39 +145,6 @@ __device__ __forceinline__ double f64_of_i64(long long v, int scale) {
     return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + scale + 1023) << 52) |
                                             (mant & 0xfffffffffffffull)));
 }
-// the same to a float
-__device__ __forceinline__ float f32_of_i64(long long v, int scale) {
-    if (v == 0) return 0.f;
-    const unsigned sgn = v < 0 ? 0x80000000u : 0u;
-    unsigned long long m = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
-    const int lz = __clzll((long long)m);
-    int e = 63 - lz;
-    m <<= lz;
-    unsigned long long mant = m >> 40;
-    const unsigned long long rem = m & 0xffffffffffull;
-    const unsigned long long half = 1ull << 39;
-    if (rem > half || (rem == half && (mant & 1ull))) {
-        mant += 1;
-        if (mant >> 24) {
-            mant >>= 1;
-            e += 1;
-        }
-    }
-    const int be = e + scale + 127;
-    if (be <= 0) return 0.f;   // below the float range: a double-float's low part of a tiny value
-    return __uint_as_float(sgn | ((unsigned)be << 23) | (unsigned)(mant & 0x7fffffull));
-}
-// the float nearest v 2^scale, and v minus its integer value (in units of
-// 2^scale) for the low part of a double-float
-__device__ __forceinline__ long long i64_minus_f32(long long v, float hi, int scale) {
-    if (hi == 0.f) return v;
-    const unsigned b = __float_as_uint(hi);
-    const int e = (int)((b >> 23) & 0xff) - 127 - 23 - scale;   // hi 2^-scale = mant 2^e
-    const long long mant = (long long)((b & 0x7fffffu) | (1u << 23));
-    const long long hv = e >= 0 ? (mant << e) : (mant >> -e);   // exact: hi is v rounded to 24 bits
-    return v - ((b >> 31) ? -hv : hv);
-}
-
 #endif
 
 }  // namespace qs

@@ -406,42 +406,50 @@ def _expected(w, which, k):
     return np.sort(np.concatenate([ws[:k // 2], ws[len(ws) - (k - k // 2):]]))[::-1]
 
 
+def _check_which(vals, w, which, k, tol):
+    """Same values as the reference selects (as a set: magnitudes that tie to
+    rounding may come in either order) and the reference's order."""
+    want = _expected(w, which, k)
+    assert np.allclose(np.sort(vals), np.sort(want), rtol=tol, atol=tol * np.abs(w).max()), (which, vals, want)
+    key = {"SA": vals, "LA": -vals, "LM": -np.abs(vals), "SM": np.abs(vals), "BE": -vals}[which]
+    assert np.all(np.diff(key) >= -tol * np.abs(w).max()), (which, vals)
+
+
 @pytest.mark.parametrize("which", ["SA", "LA", "LM", "SM", "BE"])
 def test_eigsh_which_matches_dense(qs, ora, which):
     """which = SA / LA / LM / SM / BE on the matrix-free, assembled (FP64 and
     double-float engines) and FP32 + polish paths, and on the dense branch."""
     L, nup, sym = 14, 7, dict(kblock=0, pblock=1, zblock=1)
-    sp = models.j1j2(L, 1.0, 0.5)
+    sp = models.j1j2(L, 1.0, 0.37)   # no exact degeneracies (J2 = 0.5 has some)
     b = qs.SpinBasis1D(L, nup=nup, pauli=False, **sym)
     D = _dense_from_oracle(ora, L, nup, False, sym, sp)
     w = np.linalg.eigvalsh(D)
     k = 4
-    want = _expected(w, which, k)
     scale = float(np.abs(w).max())
     Q = qs.QuantumLinearOperator(b, models.to_terms(qs, sp))
     H = qs.Hamiltonian(b, models.to_terms(qs, sp))
     for op, prec in ((Q, "fp64"), (H, "fp64"), (H, "fp64df"), (H, "fp32")):
         vals, vecs = qs.eigsh(op, k=k, which=which, tol=1e-12, ncv=40, maxiter=3000, precision=prec)
-        assert np.allclose(vals, want, rtol=1e-10, atol=1e-10 * scale), (prec, vals, want)
+        _check_which(vals, w, which, k, 1e-10)
         assert np.max(np.abs(D @ vecs - vecs * vals)) < 1e-7 * scale, prec
     # k >= Ns - 1 takes the dense branch
     small = qs.SpinBasis1D(8, nup=4, pauli=False, kblock=0, pblock=1)
-    sps = models.j1j2(8, 1.0, 0.5)
+    sps = models.j1j2(8, 1.0, 0.37)
     Ds = _dense_from_oracle(ora, 8, 4, False, dict(kblock=0, pblock=1), sps)
     ws = np.linalg.eigvalsh(Ds)
     ks = small.Ns - 1
     got = qs.eigsh(qs.QuantumLinearOperator(small, models.to_terms(qs, sps)), k=ks, which=which,
                    return_eigenvectors=False)
-    assert np.allclose(got, _expected(ws, which, ks), atol=1e-10 * max(1.0, np.abs(ws).max()))
+    _check_which(got, ws, which, ks, 1e-10)
 
 
 def test_eigsh_batch_which(qs, ora):
     L = 12
-    sp = models.j1j2(L, 1.0, 0.5)
+    sp = models.j1j2(L, 1.0, 0.37)
     syms = [dict(kblock=0, pblock=1), dict(kblock=3), dict(kblock=6, pblock=-1)]
     ops = [qs.Hamiltonian(qs.SpinBasis1D(L, nup=6, pauli=False, **sy), models.to_terms(qs, sp)) for sy in syms]
     for which in ("LM", "BE"):
         got = qs.eigsh_batch(ops, k=3, which=which, tol=1e-12, ncv=30, maxiter=3000)
         for i, sy in enumerate(syms):
             w = np.linalg.eigvalsh(_dense_from_oracle(ora, L, 6, False, sy, sp))
-            assert np.allclose(got[i], _expected(w, which, 3), rtol=1e-10, atol=1e-10 * np.abs(w).max()), (which, i)
+            _check_which(got[i], w, which, 3, 1e-10)
