@@ -281,13 +281,22 @@ typedef struct {
 } qs_eigsh_info;
 
 /* eigsh(op; k, which=:SA, v0, tol, ncv, maxiter) (src/operators.jl:3367-3408):
- * values ascending (k doubles); vectors Ns x k column-major in the op dtype
+ * values (k doubles) in the order of opts->which; vectors Ns x k column-major in the op dtype
  * (host, or device with opts->mem).  A thick-restart Lanczos with full
  * reorthogonalisation replaces the ARPACK implicitly restarted Lanczos;
  * convergence is ARPACK's test ||r_i|| <= tol * max(eps^(2/3), |theta_i|).
  * Assembled operators (qs_op_assemble) run on the batched engine with one
  * operator (as qs_eigsh_batch). */
 QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *vectors, qs_eigsh_info *info);
+
+/* eigsh(op; k, which, v0, tol, ncv, maxiter) for a non-Hermitian operator
+ * (src/operators.jl:3367-3408, where ARPACK's nonsymmetric driver returns
+ * complex values, 3402-3404): which = SA / LA select by real part (the
+ * reference's :SR / :LR), LM / SM by magnitude (BE is rejected), in the
+ * reference's output order.  values: 2k doubles (complex); vectors: Ns x k
+ * ComplexF64 column-major (host, or device with opts->mem); v0 in the
+ * operator's dtype.  Krylov-Schur restarted Arnoldi on the device. */
+QS_API int qs_eigs(qs_op *op, const qs_eigsh_opts *opts, double *values, void *vectors, qs_eigsh_info *info);
 
 /* eigsh on nops Hermitian operators at once (e.g. every momentum / parity
  * sector of one model): the Lanczos iterations of all operators run in

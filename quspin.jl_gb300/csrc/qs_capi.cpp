@@ -328,6 +328,13 @@ int qs_eigsh(qs_op* op, const qs_eigsh_opts* opts, double* values, void* vectors
     return guard([&] { qs::eigsh(*op->op, *opts, values, vectors, info); });
 }
 
+int qs_eigs(qs_op* op, const qs_eigsh_opts* opts, double* values, void* vectors, qs_eigsh_info* info) {
+    return guard([&] {
+        if (!op || !opts || !values) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        qs::eigs_general(*op->op, *opts, values, vectors, info);
+    });
+}
+
 int qs_eigsh_batch(qs_op* const* ops, int32_t nops, const qs_eigsh_opts* opts, double* values, void** vectors,
                    qs_eigsh_info* infos) {
     return guard([&] {

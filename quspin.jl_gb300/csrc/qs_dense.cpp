@@ -4,7 +4,12 @@
 //     a Wilkinson shift (Golub & Van Loan, Matrix Computations, 4th ed.,
 //     section 8.3);
 //   * scaling and squaring with the [13/13] Pade approximant for exp(A)
-//     (Higham, SIAM J. Matrix Anal. Appl. 26 (2005) 1179-1193).
+//     (Higham, SIAM J. Matrix Anal. Appl. 26 (2005) 1179-1193);
+//   * the complex Schur form: Householder reduction to Hessenberg form, then
+//     the implicit single-shift QR iteration with Wilkinson shifts and
+//     deflation, reordering of the Schur form by adjacent Givens swaps, and
+//     eigenvectors of the triangular factor by back substitution (Golub &
+//     Van Loan, sections 7.4-7.7).
 #include "qs_dense.h"
 
 #include <algorithm>
@@ -214,6 +219,167 @@ void expm_complex(int n, const std::vector<std::complex<double>>& A_in, std::vec
     CMat R = csolve(n, P, Q);
     for (int s = 0; s < sq; ++s) R = cmatmul(n, R, R);
     E.swap(R);
+}
+
+
+// ------------------------------------------------------------- complex Schur
+namespace {
+
+using cx = std::complex<double>;
+
+// Givens rotation [c s; -conj(s) c] with c real that maps (x, y) to (r, 0)
+void cgivens(cx x, cx y, double& c, cx& s) {
+    const double ax = std::abs(x), ay = std::abs(y);
+    if (ay == 0.0) {
+        c = 1.0;
+        s = 0.0;
+        return;
+    }
+    if (ax == 0.0) {
+        c = 0.0;
+        s = std::conj(y) / ay;
+        return;
+    }
+    const double nr = std::hypot(ax, ay);
+    c = ax / nr;
+    s = (x / ax) * std::conj(y) / nr;
+}
+
+// rows k, k+1 of A (columns c0 .. n-1) <- G rows; columns k, k+1 of A (rows
+// 0 .. r1-1) and of Q <- times G^H
+void rot_rows(std::vector<cx>& A, int n, int k, int c0, double c, cx s) {
+    for (int j = c0; j < n; ++j) {
+        const cx a = A[(size_t)k * n + j], b = A[(size_t)(k + 1) * n + j];
+        A[(size_t)k * n + j] = c * a + s * b;
+        A[(size_t)(k + 1) * n + j] = -std::conj(s) * a + c * b;
+    }
+}
+void rot_cols(std::vector<cx>& A, int n, int k, int r1, double c, cx s) {
+    for (int i = 0; i < r1; ++i) {
+        const cx a = A[(size_t)i * n + k], b = A[(size_t)i * n + k + 1];
+        A[(size_t)i * n + k] = c * a + std::conj(s) * b;
+        A[(size_t)i * n + k + 1] = -s * a + c * b;
+    }
+}
+
+}  // namespace
+
+void complex_schur(int n, std::vector<cx>& A, std::vector<cx>& Q) {
+    Q.assign((size_t)n * n, cx(0, 0));
+    for (int i = 0; i < n; ++i) Q[(size_t)i * n + i] = 1.0;
+    // Householder reduction to upper Hessenberg form, A <- P^H A P, Q <- Q P
+    for (int k = 0; k + 2 < n; ++k) {
+        double alpha2 = 0.0;
+        for (int i = k + 1; i < n; ++i) alpha2 += std::norm(A[(size_t)i * n + k]);
+        const double alpha = std::sqrt(alpha2);
+        if (alpha == 0.0) continue;
+        const cx x0 = A[(size_t)(k + 1) * n + k];
+        const cx ph = std::abs(x0) > 0 ? x0 / std::abs(x0) : cx(1, 0);
+        std::vector<cx> v(n, cx(0, 0));
+        v[k + 1] = x0 + ph * alpha;
+        for (int i = k + 2; i < n; ++i) v[i] = A[(size_t)i * n + k];
+        double vn = 0.0;
+        for (int i = k + 1; i < n; ++i) vn += std::norm(v[i]);
+        if (vn == 0.0) continue;
+        // A <- (I - 2 v v^H / vn) A (I - 2 v v^H / vn)
+        for (int j = 0; j < n; ++j) {
+            cx t = 0;
+            for (int i = k + 1; i < n; ++i) t += std::conj(v[i]) * A[(size_t)i * n + j];
+            t *= 2.0 / vn;
+            for (int i = k + 1; i < n; ++i) A[(size_t)i * n + j] -= v[i] * t;
+        }
+        for (int i = 0; i < n; ++i) {
+            cx t = 0;
+            for (int j = k + 1; j < n; ++j) t += A[(size_t)i * n + j] * v[j];
+            t *= 2.0 / vn;
+            for (int j = k + 1; j < n; ++j) A[(size_t)i * n + j] -= t * std::conj(v[j]);
+            cx u = 0;
+            for (int j = k + 1; j < n; ++j) u += Q[(size_t)i * n + j] * v[j];
+            u *= 2.0 / vn;
+            for (int j = k + 1; j < n; ++j) Q[(size_t)i * n + j] -= u * std::conj(v[j]);
+        }
+        for (int i = k + 2; i < n; ++i) A[(size_t)i * n + k] = 0.0;
+    }
+    // implicit single-shift QR on the active window [lo, hi]
+    const double eps = 2.220446049250313e-16;
+    int hi = n - 1, iter = 0;
+    while (hi > 0) {
+        int lo = hi;
+        while (lo > 0) {
+            const double sub = std::abs(A[(size_t)lo * n + lo - 1]);
+            const double dn = std::abs(A[(size_t)lo * n + lo]) + std::abs(A[(size_t)(lo - 1) * n + lo - 1]);
+            if (sub <= eps * (dn > 0 ? dn : 1.0)) {
+                A[(size_t)lo * n + lo - 1] = 0.0;
+                break;
+            }
+            --lo;
+        }
+        if (lo == hi) {
+            --hi;
+            iter = 0;
+            continue;
+        }
+        if (++iter > 60 * n) throw std::runtime_error("complex Schur iteration did not converge");
+        // Wilkinson shift from the trailing 2 x 2 block (exceptional shift now and then)
+        const cx a = A[(size_t)(hi - 1) * n + hi - 1], b = A[(size_t)(hi - 1) * n + hi];
+        const cx c2 = A[(size_t)hi * n + hi - 1], d = A[(size_t)hi * n + hi];
+        cx mu;
+        if (iter % 11 == 10) {
+            mu = d + std::abs(A[(size_t)hi * n + hi - 1]) * 0.75;
+        } else {
+            const cx tr = 0.5 * (a + d), det = a * d - b * c2;
+            const cx disc = std::sqrt(tr * tr - det);
+            const cx l1 = tr + disc, l2 = tr - disc;
+            mu = std::abs(l1 - d) < std::abs(l2 - d) ? l1 : l2;
+        }
+        cx x = A[(size_t)lo * n + lo] - mu, y = A[(size_t)(lo + 1) * n + lo];
+        for (int k = lo; k < hi; ++k) {
+            double c;
+            cx sn;
+            cgivens(x, y, c, sn);
+            rot_rows(A, n, k, k > lo ? k - 1 : k, c, sn);
+            rot_cols(A, n, k, std::min(k + 3, hi + 1), c, sn);
+            rot_cols(Q, n, k, n, c, sn);
+            if (k > lo) A[(size_t)(k + 1) * n + k - 1] = 0.0;
+            if (k + 1 < hi) {
+                x = A[(size_t)(k + 1) * n + k];
+                y = A[(size_t)(k + 2) * n + k];
+            }
+        }
+    }
+}
+
+void schur_swap(int n, std::vector<cx>& T, std::vector<cx>& Q, int k) {
+    const cx a = T[(size_t)k * n + k], b = T[(size_t)k * n + k + 1], d = T[(size_t)(k + 1) * n + k + 1];
+    double c;
+    cx s;
+    cgivens(b, d - a, c, s);   // rotates the eigenvector (b, d - a) of d onto e_1
+    rot_rows(T, n, k, k, c, s);
+    rot_cols(T, n, k, n, c, s);
+    rot_cols(Q, n, k, n, c, s);
+    T[(size_t)(k + 1) * n + k] = 0.0;
+    T[(size_t)k * n + k] = d;
+    T[(size_t)(k + 1) * n + k + 1] = a;
+}
+
+void schur_vector(int n, const std::vector<cx>& T, int i, std::vector<cx>& y) {
+    y.assign(n, cx(0, 0));
+    y[i] = 1.0;
+    const cx lam = T[(size_t)i * n + i];
+    double tn = 0.0;
+    for (const cx& v : T) tn = std::max(tn, std::abs(v));
+    const double small = 2.220446049250313e-16 * std::max(tn, 1e-300);
+    for (int j = i - 1; j >= 0; --j) {
+        cx sacc = 0;
+        for (int l = j + 1; l <= i; ++l) sacc += T[(size_t)j * n + l] * y[l];
+        cx den = T[(size_t)j * n + j] - lam;
+        if (std::abs(den) < small) den = small;
+        y[j] = -sacc / den;
+    }
+    double nr = 0.0;
+    for (const cx& v : y) nr += std::norm(v);
+    nr = std::sqrt(nr);
+    for (cx& v : y) v /= nr;
 }
 
 }  // namespace qs

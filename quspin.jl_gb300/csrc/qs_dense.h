@@ -50,6 +50,15 @@ inline std::vector<int> ritz_order(const std::vector<double>& w, int which, int 
     return o;
 }
 
+// Complex Schur form of a general n x n matrix (row-major): on return A holds
+// the upper-triangular T and Q the unitary factor, A_in = Q T Q^H.
+void complex_schur(int n, std::vector<std::complex<double>>& A, std::vector<std::complex<double>>& Q);
+// Swaps the diagonal entries k and k + 1 of the Schur form (T, Q), keeping
+// A_in = Q T Q^H.
+void schur_swap(int n, std::vector<std::complex<double>>& T, std::vector<std::complex<double>>& Q, int k);
+// Unit eigenvector y of the upper-triangular T for its diagonal entry i.
+void schur_vector(int n, const std::vector<std::complex<double>>& T, int i, std::vector<std::complex<double>>& y);
+
 // exp(A) for a complex n x n matrix (row-major).
 void expm_complex(int n, const std::vector<std::complex<double>>& A, std::vector<std::complex<double>>& E);
 

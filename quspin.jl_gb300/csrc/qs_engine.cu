@@ -761,7 +761,7 @@ __global__ void __launch_bounds__(kT, 2) eng_rotate(const SlotDev* __restrict__ 
 
 // ------------------------------------------------------------ rotate on the tensor cores
 // The thick-restart rotation V[:, out0 + c] = sum_{i < rot_in} V[:, i] Y[i, c]
-// as an exact sliced integer product on the BF16 tensor cores (qs_tc.cuh) for
+// as an exact sliced integer product on the FP16 tensor cores (qs_tc.cuh) for
 // the FP64 storage.  A slot takes it (rot_tc) when its
 // coefficients are real with |Y| <= 1, 2 <= p <= 16 and rot_in <= 32 (the
 // restarts of eigsh, whose V columns are orthonormal); eng_rotate skips those
@@ -821,7 +821,7 @@ __global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __res
 #pragma unroll
         for (int a = 0; a < kTcDigits; ++a)
             *(uint16_t*)(sb + a * kTcBTile + tc_off(c, i, kTcK)) =
-                (uint16_t)bf16_of_byte((uint32_t)(m >> (8 * (kTcDigits - 1 - a))) & 0xffu, sg);
+                (uint16_t)f16_of_byte((uint32_t)(m >> (8 * (kTcDigits - 1 - a))) & 0xffu, sg);
     }
     if (warp == 0) tc_alloc(&tbase, kTcCols);
     if (tid == 0) mbar_init(&mbar, 1);
@@ -852,7 +852,7 @@ __global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __res
         const int64_t e = t0 + tid;
         const bool live = e < e1;
         // the inputs as fixed-point integers, eight per K core matrix, and
-        // their bytes as BF16 into the digit matrices
+        // their bytes as FP16 into the digit matrices
 #pragma unroll
         for (int kc = 0; kc < kTcK / 8; ++kc) {
             if (kc * 8 >= nin) break;
@@ -864,23 +864,41 @@ __global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __res
                 sg[u] = X < 0 ? 0x8000u : 0u;
                 mag[u] = X < 0 ? (unsigned long long)(-X) : (unsigned long long)X;
             }
+            uint32_t sg2[4], lo[8], hi[8];
 #pragma unroll
-            for (int a = 0; a < kTcDigits; ++a) {
-                const int sh = 8 * (kTcDigits - 1 - a);
-                uint32_t w[4];
+            for (int u = 0; u < 4; ++u) sg2[u] = sg[2 * u] | (sg[2 * u + 1] << 16);
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    w[u] = bf16_of_byte((uint32_t)(mag[2 * u] >> sh) & 0xffu, sg[2 * u]) |
-                           (bf16_of_byte((uint32_t)(mag[2 * u + 1] >> sh) & 0xffu, sg[2 * u + 1]) << 16);
-                *(uint4*)(sa + a * kTcATile + tc_off(tid, kc * 8, kTcK)) = make_uint4(w[0], w[1], w[2], w[3]);
+            for (int u = 0; u < 8; ++u) {
+                lo[u] = (uint32_t)mag[u];
+                hi[u] = (uint32_t)(mag[u] >> 32);
             }
+            // digit a is byte 7 - a of the magnitude
+            auto put = [&](int a, const uint32_t (&w)[4]) {
+                *(uint4*)(sa + a * kTcATile + tc_off(tid, kc * 8, kTcK)) = make_uint4(w[0], w[1], w[2], w[3]);
+            };
+#define QS_TC_DIGIT(A_, WORD_, BB_)                                                                  \
+            {                                                                                       \
+                uint32_t w[4];                                                                      \
+                _Pragma("unroll") for (int u = 0; u < 4; ++u)                                       \
+                    w[u] = f16x2_of_bytes<BB_>(WORD_[2 * u], WORD_[2 * u + 1], sg2[u]);             \
+                put(A_, w);                                                                         \
+            }
+            QS_TC_DIGIT(0, hi, 3)
+            QS_TC_DIGIT(1, hi, 2)
+            QS_TC_DIGIT(2, hi, 1)
+            QS_TC_DIGIT(3, hi, 0)
+            QS_TC_DIGIT(4, lo, 3)
+            QS_TC_DIGIT(5, lo, 2)
+            QS_TC_DIGIT(6, lo, 1)
+            QS_TC_DIGIT(7, lo, 0)
+#undef QS_TC_DIGIT
         }
         tc_fence_smem();
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
         if (tid == 0) {
-            constexpr uint32_t idesc = tc_idesc_bf16(kTcRows, kTcN);
+            constexpr uint32_t idesc = tc_idesc_f16(kTcRows, kTcN);
             const uint32_t abase = smem_addr(sa), bbase = smem_addr(sb);
             constexpr uint32_t sbo = (kTcK / 8) * 128;
             // accumulator s: sum over digit pairs a + b = s of A_a B_b
@@ -891,7 +909,7 @@ __global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __res
                     for (int kk = 0; kk < ksteps; ++kk) {
                         const uint64_t ad = tc_sdesc(abase + a * kTcATile + kk * 256, 128, sbo);
                         const uint64_t bd = tc_sdesc(bbase + (s - a) * kTcBTile + kk * 256, 128, sbo);
-                        tc_mma_bf16(tmem + (uint32_t)(s * kTcN), ad, bd, idesc, acc);
+                        tc_mma_f16(tmem + (uint32_t)(s * kTcN), ad, bd, idesc, acc);
                         acc = 1;
                     }
             }

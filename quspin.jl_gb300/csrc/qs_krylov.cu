@@ -195,7 +195,235 @@ TRResult trlan(Ctx& c, int k, int which, double tol, int ncv, int maxiter, const
     return R;
 }
 
+
+// Ranking of complex Ritz values for a non-Hermitian eigsh: SA / LA by real
+// part (the reference asks ARPACK for :SR / :LR, src/operators.jl:3383),
+// LM / SM by magnitude; stable, wanted values first in output order.
+std::vector<int> ritz_order_complex(const std::vector<cd>& w, int which) {
+    std::vector<int> o(w.size());
+    for (size_t i = 0; i < o.size(); ++i) o[i] = (int)i;
+    auto key = [&](int i) -> double {
+        switch (which) {
+            case 0: return w[i].real();
+            case 1: return -w[i].real();
+            case 2: return -std::abs(w[i]);
+            default: return std::abs(w[i]);
+        }
+    };
+    std::stable_sort(o.begin(), o.end(), [&](int a, int b) { return key(a) < key(b); });
+    return o;
+}
+
+struct KSResult {
+    std::vector<cd> theta;
+    int nconv = 0;
+    int restarts = 0;
+    double max_rel = 0.0;
+};
+
+// Krylov-Schur restarted Arnoldi (Stewart, SIAM J. Matrix Anal. Appl. 23
+// (2001) 601-614) for a non-Hermitian operator, in place of the reference's
+// ARPACK znaupd / dnaupd run (src/operators.jl:3384-3390): Arnoldi steps with
+// CGS2, the complex Schur form of the projected matrix reordered so that the
+// wanted Ritz values lead, truncation to p of them (V <- V Q_p, the residual
+// direction follows), ARPACK's Ritz bound |beta (Q y)_m| <= tol max(eps^(2/3),
+// |theta|) as the convergence test.  Complex vectors (C128) throughout.
+KSResult krylov_schur(Ctx& c, int k, int which, double tol, int ncv, int maxiter, const void* v0, void* X) {
+    const int64_t n = c.n;
+    const int m = (int)std::min<int64_t>(ncv, n);
+    DevBuf V((size_t)n * (m + 1) * 16), tmp((size_t)n * m * 16);
+    c.blas.copy(V.p, v0);
+    const double nv0 = c.blas.norm(V.p);
+    if (!(nv0 > 0)) throw Error(QS_ERR_ARGUMENT, "starting vector must be nonzero");
+    c.blas.scale(V.p, V.p, cd(1.0 / nv0, 0));
+    std::vector<cd> H((size_t)(m + 1) * m, cd(0, 0));
+    auto Hij = [&](int i, int j) -> cd& { return H[(size_t)i * m + j]; };
+    const double e23 = std::pow(kEps, 2.0 / 3.0);
+    int j0 = 0;
+    KSResult R;
+    for (int iter = 0; iter < maxiter; ++iter) {
+        R.restarts = iter;
+        int me = m;
+        double beta = 0.0;
+        for (int j = j0; j < m; ++j) {
+            void* wv = c.col(V, j + 1);
+            c.matvec(c.col(V, j), wv);
+            const std::vector<cd> h = orthogonalize(c, V, j + 1, wv);
+            for (int i = 0; i <= j; ++i) Hij(i, j) += h[i];
+            beta = c.blas.norm(wv);
+            double hn = 0.0;
+            for (int i = 0; i <= j; ++i) hn = std::max(hn, std::abs(Hij(i, j)));
+            if (beta <= 1e-13 * std::max(1.0, hn)) {
+                me = j + 1;   // an invariant subspace: its Ritz values are exact
+                beta = 0.0;
+                break;
+            }
+            c.blas.scale(wv, wv, cd(1.0 / beta, 0));
+            Hij(j + 1, j) = beta;
+        }
+        std::vector<cd> T((size_t)me * me), Q;
+        for (int i = 0; i < me; ++i)
+            for (int j = 0; j < me; ++j) T[(size_t)i * me + j] = Hij(i, j);
+        complex_schur(me, T, Q);
+        // bring the wanted values to the front, in ranking order
+        const int kk = std::min(k, me);
+        int p = std::max(kk, std::min(me - 2, kk + (me - kk) / 2));
+        if (me < m) p = me;
+        std::vector<cd> diag(me);
+        for (int i = 0; i < me; ++i) diag[i] = T[(size_t)i * me + i];
+        const std::vector<int> order = ritz_order_complex(diag, which);
+        std::vector<int> at(me);   // at[pos] = original index now at pos
+        for (int i = 0; i < me; ++i) at[i] = i;
+        for (int q = 0; q < p; ++q) {
+            int pos = q;
+            while (at[pos] != order[q]) ++pos;
+            for (int s2 = pos - 1; s2 >= q; --s2) {
+                schur_swap(me, T, Q, s2);
+                std::swap(at[s2], at[s2 + 1]);
+            }
+        }
+        int nconv = 0;
+        double maxrel = 0.0;
+        std::vector<std::vector<cd>> Y(kk);
+        for (int q = 0; q < kk; ++q) {
+            schur_vector(me, T, q, Y[q]);
+            cd last = 0;
+            for (int l = 0; l <= q; ++l) last += Q[(size_t)(me - 1) * me + l] * Y[q][l];
+            const double th = std::abs(T[(size_t)q * me + q]);
+            const double bound = beta * std::abs(last);
+            maxrel = std::max(maxrel, bound / std::max(e23, th));
+            if (bound <= tol * std::max(e23, th)) ++nconv;
+        }
+        R.nconv = nconv;
+        R.max_rel = maxrel;
+        if (nconv >= kk || me < m || iter == maxiter - 1) {
+            R.theta.resize(kk);
+            for (int q = 0; q < kk; ++q) {
+                R.theta[q] = T[(size_t)q * me + q];
+                std::vector<cd> z(me, cd(0, 0));
+                for (int r = 0; r < me; ++r)
+                    for (int l = 0; l <= q; ++l) z[r] += Q[(size_t)r * me + l] * Y[q][l];
+                c.blas.combine((char*)X + (size_t)q * n * 16, V.p, n, me, z);
+            }
+            if (me < m) R.nconv = kk;
+            QS_CUDA(cudaStreamSynchronize(c.s));
+            return R;
+        }
+        // truncate to the p leading Schur vectors; the residual direction follows
+        for (int q = 0; q < p; ++q) {
+            std::vector<cd> z(me);
+            for (int r = 0; r < me; ++r) z[r] = Q[(size_t)r * me + q];
+            c.blas.combine(c.col(tmp, q), V.p, n, me, z);
+        }
+        QS_CUDA(cudaMemcpyAsync(V.p, tmp.p, (size_t)n * p * 16, cudaMemcpyDeviceToDevice, c.s));
+        c.blas.copy(c.col(V, p), c.col(V, m));
+        std::fill(H.begin(), H.end(), cd(0, 0));
+        for (int i = 0; i < p; ++i)
+            for (int j = i; j < p; ++j) Hij(i, j) = T[(size_t)i * me + j];
+        for (int j = 0; j < p; ++j) Hij(p, j) = beta * Q[(size_t)(me - 1) * me + j];
+        j0 = p;
+    }
+    return R;
+}
+
 }  // namespace
+
+// ----------------------------------------------------- non-Hermitian eigsh
+void eigs_general(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eigsh_info* info) {
+    auto t0 = std::chrono::steady_clock::now();
+    const int64_t n = op.basis->n;
+    const int k = o.k;
+    if (k < 1 || k > n) throw Error(QS_ERR_ARGUMENT, "k must lie in 1:Ns");
+    if (o.which < 0 || o.which > 3)
+        throw Error(QS_ERR_ARGUMENT, "which must be SA, LA, SM or LM for a non-Hermitian operator");
+    const bool dev = o.mem == QS_MEM_DEVICE;
+    const size_t esz = op.complex_mat ? 16 : 8;   // dtype of v0
+    Ctx c(op, VKind::C128);
+    std::vector<cd> theta;
+    DevBuf X((size_t)n * k * 16);
+    int64_t mv = 0;
+    int nconv = k, restarts = 0;
+    double maxrel = 0.0;
+    if (k >= n - 1) {
+        // dense branch: the matrix column by column, its complex Schur form
+        const int N = (int)n;
+        std::vector<cd> A((size_t)N * N), hcol(N);
+        DevBuf e(n * 16), col(n * 16);
+        for (int j = 0; j < N; ++j) {
+            std::vector<cd> h(N, cd(0, 0));
+            h[j] = 1.0;
+            QS_CUDA(cudaMemcpyAsync(e.p, h.data(), n * 16, cudaMemcpyHostToDevice, op.stream));
+            c.matvec(e.p, col.p);
+            QS_CUDA(cudaMemcpyAsync(hcol.data(), col.p, n * 16, cudaMemcpyDeviceToHost, op.stream));
+            QS_CUDA(cudaStreamSynchronize(op.stream));
+            for (int i = 0; i < N; ++i) A[(size_t)i * N + j] = hcol[i];
+        }
+        std::vector<cd> Q;
+        complex_schur(N, A, Q);
+        std::vector<cd> diag(N);
+        for (int i = 0; i < N; ++i) diag[i] = A[(size_t)i * N + i];
+        const std::vector<int> order = ritz_order_complex(diag, o.which);
+        std::vector<cd> out((size_t)N * k);
+        for (int q = 0; q < k; ++q) {
+            std::vector<cd> y;
+            schur_vector(N, A, order[q], y);
+            for (int r = 0; r < N; ++r) {
+                cd z = 0;
+                for (int l = 0; l < N; ++l) z += Q[(size_t)r * N + l] * y[l];
+                out[(size_t)q * N + r] = z;
+            }
+            theta.push_back(diag[order[q]]);
+        }
+        QS_CUDA(cudaMemcpyAsync(X.p, out.data(), out.size() * 16, cudaMemcpyHostToDevice, op.stream));
+        mv = n;
+    } else {
+        int ncv = o.ncv > 0 ? o.ncv : std::max(20, 2 * k + 1);
+        ncv = std::min(ncv, 128);
+        if (ncv <= k) ncv = (int)std::min<int64_t>(n, k + 2);
+        const double tol = o.tol > 0 ? o.tol : kEps;
+        const int maxiter = o.maxiter > 0 ? o.maxiter : 300;
+        DevBuf v0((size_t)n * 16);
+        if (o.v0) {
+            std::vector<cd> h(n);
+            if (dev) {
+                std::vector<char> raw(n * esz);
+                QS_CUDA(cudaMemcpyAsync(raw.data(), o.v0, n * esz, cudaMemcpyDeviceToHost, op.stream));
+                QS_CUDA(cudaStreamSynchronize(op.stream));
+                for (int64_t i = 0; i < n; ++i)
+                    h[i] = esz == 16 ? ((const cd*)raw.data())[i] : cd(((const double*)raw.data())[i], 0.0);
+            } else {
+                for (int64_t i = 0; i < n; ++i) h[i] = esz == 16 ? ((const cd*)o.v0)[i] : cd(o.v0[i], 0.0);
+            }
+            QS_CUDA(cudaMemcpyAsync(v0.p, h.data(), n * 16, cudaMemcpyHostToDevice, op.stream));
+            QS_CUDA(cudaStreamSynchronize(op.stream));
+        } else {
+            random_vector(c, v0.p, 20261203ull);
+        }
+        KSResult R = krylov_schur(c, k, o.which, tol, ncv, maxiter, v0.p, X.p);
+        if (R.nconv < k) throw Error(QS_ERR_NOT_CONVERGED, "eigsh did not converge within maxiter restarts");
+        theta = R.theta;
+        nconv = R.nconv;
+        restarts = R.restarts;
+        maxrel = R.max_rel;
+        mv = c.matvecs;
+    }
+    for (int q = 0; q < k; ++q) {
+        values[2 * q] = theta[q].real();
+        values[2 * q + 1] = theta[q].imag();
+    }
+    if (o.want_vectors && vectors) {
+        QS_CUDA(cudaMemcpyAsync(vectors, X.p, (size_t)n * k * 16, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                op.stream));
+    }
+    QS_CUDA(cudaStreamSynchronize(op.stream));
+    if (info) {
+        info->nconv = nconv;
+        info->restarts = restarts;
+        info->matvecs = mv;
+        info->max_rel_residual = maxrel;
+        info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+}
 
 // --------------------------------------------------------------------- eigsh
 void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eigsh_info* info) {
@@ -204,7 +432,8 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
     const int k = o.k;
     if (k < 1 || k > n) throw Error(QS_ERR_ARGUMENT, "k must lie in 1:Ns");
     if (o.which < 0 || o.which > 4) throw Error(QS_ERR_ARGUMENT, "which must be SA, LA, SM, LM, or BE");
-    if (!op.hermitian) throw Error(QS_ERR_UNSUPPORTED, "eigsh on this engine needs a Hermitian operator");
+    if (!op.hermitian)
+        throw Error(QS_ERR_ARGUMENT, "a non-Hermitian operator returns complex eigenvalues: use qs_eigs");
     const bool cpx = op.complex_mat;
     const VKind k64 = cpx ? VKind::C128 : VKind::F64;
     const size_t esz = cpx ? 16 : 8;

@@ -4,12 +4,12 @@
 // The Krylov restart rotation V[:, 0:p] = V[:, 0:m] Y is the one dense
 // contraction of the solvers (N x m by m x p, m <= 32).  GB300 has no fast
 // FP64 tensor path, so the FP64 engine runs it as an exact integer product on
-// the BF16 tensor cores, after Ozaki et al. ("Error-free
+// the FP16 tensor cores, after Ozaki et al. ("Error-free
 // transformations of matrix multiplication by using fast routines of matrix
 // multiplication and its applications", Numer. Algorithms 2012): every entry
 // (|v| <= 2) is scaled to a 61-bit fixed-point integer X = trunc(v 2^61),
 // whose magnitude splits into eight bytes d_0 (most significant) .. d_7, each
-// exact in BF16 with the entry's sign.  A product of two digits is below 2^16,
+// exact in FP16 with the entry's sign.  A product of two digits is below 2^16,
 // so the sum over the m <= 32 terms of every digit pair (a, b) with the same
 // a + b = s (at most nine pairs) stays below 2^24 and accumulates exactly in
 // the FP32 tensor accumulator; the nine sums D_s (s = 0 .. 8) are combined in
@@ -41,10 +41,10 @@ __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint3
     return d;
 }
 
-// Instruction descriptor of kind::f16 with BF16 A and B (both K-major) and
+// Instruction descriptor of kind::f16 with FP16 A and B (both K-major) and
 // an FP32 accumulator, M x N.
-__host__ __device__ constexpr uint32_t tc_idesc_bf16(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+__host__ __device__ constexpr uint32_t tc_idesc_f16(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 // Byte offset of element (row, k) of a K-major no-swizzle tile whose rows
@@ -61,7 +61,7 @@ __device__ __forceinline__ void tc_alloc(uint32_t* dst_smem, uint32_t ncols) {
 __device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols));
 }
-__device__ __forceinline__ void tc_mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+__device__ __forceinline__ void tc_mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                             uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -118,10 +118,24 @@ __device__ __forceinline__ long long fix61(double v) {
     if (e != 0) q = sh >= 0 ? mant << (sh > 9 ? 9 : sh) : (sh > -64 ? mant >> -sh : 0ull);
     return (b >> 63) ? -(long long)q : (long long)q;
 }
-// BF16 bits of sign * byte (byte <= 255 is exact in BF16's 8 significant bits)
-__device__ __forceinline__ uint32_t bf16_of_byte(uint32_t byte, uint32_t sign) {
-    const float f = __uint_as_float(0x4B000000u | byte) - 8388608.0f;
-    return (__float_as_uint(f) >> 16) | sign;
+// Two FP16 digits at once: byte bb (0..3) of x and of y, each below 256 and
+// exact in FP16, with the signs sg (0x8000 in either half), as one f16x2
+// word: a byte permutation puts each byte under the exponent of 1024
+// (FP16 0x6400 + b is 1024 + b exactly), one packed subtraction removes the
+// 1024.
+template <int bb>
+__device__ __forceinline__ uint32_t f16x2_of_bytes(uint32_t x, uint32_t y, uint32_t sg) {
+    constexpr uint32_t sel = (uint32_t)bb | ((uint32_t)(4 + bb) << 8);
+    const uint32_t t = (__byte_perm(x, y, sel) & 0x00FF00FFu) | 0x64006400u;
+    uint32_t r;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(t), "r"(0x64006400u));
+    return r | sg;
+}
+// FP16 bits of sign * byte
+__device__ __forceinline__ uint32_t f16_of_byte(uint32_t byte, uint32_t sign) {
+    uint32_t r;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(0x6400u | byte), "r"(0x6400u));
+    return (r & 0xffffu) | sign;
 }
 
 // v 2^scale rounded to the nearest double (ties to even); v 2^scale in the

@@ -324,6 +324,21 @@ def eigsh(op, k=None, which="SA", return_eigenvectors=True, v0=None, tol=0.0, nc
     opts = _lib.EigshOpts(k, code, float(tol), int(ncv or 0), int(maxiter or 0),
                           _precision_code(precision), int(bool(return_eigenvectors)),
                           _lib.ptr(vv) if vv is not None else None, _lib.QS_MEM_HOST)
+    if not getattr(op, "hermitian", True):
+        # complex eigenvalues and vectors, as the reference returns for a
+        # non-Hermitian operator (src/operators.jl:3402-3404)
+        if code == 4:
+            raise ArgumentError("which must be SA, LA, SM or LM for a non-Hermitian operator")
+        cvals = np.zeros(2 * k)
+        cvecs = np.zeros((n, k), dtype=np.complex128, order="F") if return_eigenvectors else None
+        inf = _lib.EigshInfo()
+        _lib.check(_lib.load().qs_eigs(op._h, ctypes.byref(opts), _lib.ptr(cvals),
+                                       _lib.ptr(cvecs) if cvecs is not None else None, ctypes.byref(inf)))
+        if info is not None:
+            info.update(nconv=inf.nconv, restarts=inf.restarts, matvecs=inf.matvecs,
+                        max_rel_residual=inf.max_rel_residual, seconds=inf.seconds)
+        vals = cvals[0::2] + 1j * cvals[1::2]
+        return (vals, cvecs) if return_eigenvectors else vals
     vals = np.zeros(k)
     vecs = np.zeros((n, k), dtype=op.dtype, order="F") if return_eigenvectors else None
     inf = _lib.EigshInfo()

@@ -453,3 +453,55 @@ def test_eigsh_batch_which(qs, ora):
         for i, sy in enumerate(syms):
             w = np.linalg.eigvalsh(_dense_from_oracle(ora, L, 6, False, sy, sp))
             _check_which(got[i], w, which, 3, 1e-10)
+
+
+def _expected_complex(w, which, k):
+    """The reference's ARPACK selection for a non-Hermitian operator (:SR / :LR
+    for SA / LA, magnitude for LM / SM) in its output order."""
+    key = {"SA": w.real, "LA": -w.real, "LM": -np.abs(w), "SM": np.abs(w)}[which]
+    return w[np.argsort(key, kind="stable")][:k]
+
+
+@pytest.mark.parametrize("which", ["SA", "LA", "LM", "SM"])
+@pytest.mark.parametrize("cplx", [True, False])
+def test_eigsh_non_hermitian(qs, ora, which, cplx):
+    """eigsh of a non-Hermitian operator returns complex eigenvalues and
+    vectors (src/operators.jl:3402-3404): Krylov-Schur against the dense
+    spectrum, and the dense branch for k >= Ns - 1."""
+    L = 12
+    bonds = [(i, i % L + 1) for i in range(1, L + 1)]
+    a = 0.7 + 0.25j if cplx else 0.7
+    sp = [("+-", [(a, i, j) for i, j in bonds]), ("-+", [(0.3, i, j) for i, j in bonds]),
+          ("zz", [(0.45, i, j) for i, j in bonds]), ("z", [(0.1 * (i % 3), i) for i in range(1, L + 1)])]
+    b = qs.SpinBasis1D(L, nup=6, pauli=False)
+    # SM without a shift-invert wants interior eigenvalues (a degenerate
+    # cluster near zero here): a diagonal shift makes them the left edge
+    shift = np.full(b.Ns, 3.0) if which == "SM" else None
+    op = qs.QuantumLinearOperator(b, models.to_terms(qs, sp), diagonal=shift, check_herm=False)
+    assert not op.hermitian
+    M = ora.RefBasis(L, nup=6, pauli=False).dense(ora.consolidate_terms(sp))
+    if shift is not None:
+        M = M + np.diag(shift)
+    w = np.linalg.eigvals(M)
+    k = 4
+    vals, vecs = qs.eigsh(op, k=k, which=which, tol=1e-12, ncv=40, maxiter=3000)
+    assert vals.dtype == np.complex128 and vecs.dtype == np.complex128
+    want = _expected_complex(w, which, k)
+    scale = float(np.abs(w).max())
+    # the same values (near-ties in the ranking may swap), then each pair's residual
+    for v in want:
+        assert np.min(np.abs(vals - v)) <= 1e-9 * scale, (which, vals, want)
+    assert np.max(np.linalg.norm(M @ vecs - vecs * vals, axis=0)) <= 1e-8 * scale
+    assert np.allclose(np.linalg.norm(vecs, axis=0), 1.0, atol=1e-10)
+    # dense branch
+    bs = qs.SpinBasis1D(6, nup=3, pauli=False)
+    bonds6 = [(i, i % 6 + 1) for i in range(1, 7)]
+    sp6 = [("+-", [(a, i, j) for i, j in bonds6]), ("-+", [(0.3, i, j) for i, j in bonds6]),
+           ("zz", [(0.45, i, j) for i, j in bonds6])]
+    ops = qs.QuantumLinearOperator(bs, models.to_terms(qs, sp6), check_herm=False)
+    Ms = ora.RefBasis(6, nup=3, pauli=False).dense(ora.consolidate_terms(sp6))
+    ws = np.linalg.eigvals(Ms)
+    ks = bs.Ns - 1
+    got = qs.eigsh(ops, k=ks, which=which, return_eigenvectors=False)
+    for v in _expected_complex(ws, which, ks):
+        assert np.min(np.abs(got - v)) <= 1e-10 * max(1.0, np.abs(ws).max())

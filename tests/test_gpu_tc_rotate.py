@@ -1,7 +1,7 @@
 """The thick-restart rotation on the tensor cores against the FP64 rotation.
 
 eigsh's restarts rotate the Krylov basis by the Ritz vectors (V[:, :p] = V Y),
-which the FP64 engine runs as an exact sliced integer product on the BF16
+which the FP64 engine runs as an exact sliced integer product on the FP16
 tensor cores (tcgen05).  QS_TC_ROTATE=0 keeps the rotation on the FP64
 arithmetic kernel; both must give the same eigenpairs, and those must match the
 dense spectrum (1e-10 relative) with FP64-class residuals.  The double-float
