@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <functional>
 #include <cmath>
 #include <complex>
@@ -404,6 +405,60 @@ __global__ void sell_fill_kernel(const int64_t* rowptr, const uint32_t* words, c
     }
 }
 
+// Explicitly rounded multiply-adds: the single product and the several-column
+// product run the same operations in the same order, whatever the compiler
+// would have contracted.
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double mul_t(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_t(float a, float b) { return __fmul_rn(a, b); }
+
+// acc += value * x (complex value when kCM, complex x when kCV)
+template <bool kCM, bool kCV, typename T, typename T2>
+__device__ __forceinline__ void sell_mac(T& acc_r, T& acc_i, T2 v, T xr, T xi) {
+    if (kCM) {
+        acc_r = fma_t(v.x, xr, acc_r);
+        acc_r = fma_t(-v.y, xi, acc_r);
+        acc_i = fma_t(v.x, xi, acc_i);
+        acc_i = fma_t(v.y, xr, acc_i);
+    } else {
+        acc_r = fma_t(v.x, xr, acc_r);
+        if (kCV) acc_i = fma_t(v.x, xi, acc_i);
+    }
+}
+
+// y[r] = beta y[r] + alpha (d[r] x[r] + sc acc) for one row of one column
+template <bool kCV, typename T, typename T2>
+__device__ __forceinline__ void sell_tail(T acc_r, T acc_i, T sc, T dr, T di, T xr, T xi, T2* y2, T* y1, int64_t r,
+                                          double br, double bi, double ar, double ai, bool beta_zero) {
+    acc_r = mul_t(acc_r, sc);
+    acc_i = mul_t(acc_i, sc);
+    if (kCV) {
+        acc_r = fma_t(dr, xr, acc_r);
+        acc_r = fma_t(-di, xi, acc_r);
+        acc_i = fma_t(dr, xi, acc_i);
+        acc_i = fma_t(di, xr, acc_i);
+        T yr = 0, yi = 0;
+        if (!beta_zero) {
+            const T2 yo = y2[r];
+            yr = mul_t((T)br, yo.x);
+            yr = fma_t(-(T)bi, yo.y, yr);
+            yi = mul_t((T)br, yo.y);
+            yi = fma_t((T)bi, yo.x, yi);
+        }
+        T2 o;
+        o.x = fma_t((T)ar, acc_r, yr);
+        o.x = fma_t(-(T)ai, acc_i, o.x);
+        o.y = fma_t((T)ar, acc_i, yi);
+        o.y = fma_t((T)ai, acc_r, o.y);
+        y2[r] = o;
+    } else {
+        acc_r = fma_t(dr, xr, acc_r);
+        const T yr = beta_zero ? (T)0 : mul_t((T)br, y1[r]);
+        y1[r] = fma_t((T)ar, acc_r, yr);
+    }
+}
+
 struct SellArgs {
     const int64_t* sptr;
     const int32_t* perm;
@@ -464,25 +519,14 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_kernel(SellArgs a) {
             const T2* __restrict__ x = (const T2*)a.x;
             sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
                                  [&](uint32_t c) { return ld_gather<kHint>(x + c); },
-                                 [&](uint32_t code, T2 xv) {
-                                     const T2 v = value(code);
-                                     if (kCM) {
-                                         acc_r += v.x * xv.x - v.y * xv.y;
-                                         acc_i += v.x * xv.y + v.y * xv.x;
-                                     } else {
-                                         acc_r += v.x * xv.x;
-                                         acc_i += v.x * xv.y;
-                                     }
-                                 });
+                                 [&](uint32_t code, T2 xv) { sell_mac<kCM, true>(acc_r, acc_i, value(code), xv.x, xv.y); });
         } else {
             const T* __restrict__ x = (const T*)a.x;
             sell_row<U, kPacked, kHint>(a.words, a.cols, a.codes, base, len, a.code_bits, a.code_mask,
                                  [&](uint32_t c) { return ld_gather<kHint>(x + c); },
-                                 [&](uint32_t code, T xv) { acc_r += value(code).x * xv; });
+                                 [&](uint32_t code, T xv) { sell_mac<false, false>(acc_r, acc_i, value(code), xv, (T)0); });
         }
         const T sc = a.stab ? rsq[a.stab[r]] : (T)1;
-        acc_r *= sc;
-        acc_i *= sc;
         T dr, di = 0;
         if (kCM) {
             const T2 d = ((const T2*)a.diag)[r];
@@ -491,26 +535,132 @@ __global__ void __launch_bounds__(kThreads, MINB) sell_kernel(SellArgs a) {
         } else {
             dr = ((const T*)a.diag_re)[r];
         }
+        T xr, xi = 0;
         if (kCV) {
             const T2 xv = ((const T2*)a.x)[r];
-            acc_r += dr * xv.x - di * xv.y;
-            acc_i += dr * xv.y + di * xv.x;
-            T2* y = (T2*)a.y;
-            T yr = 0, yi = 0;
-            if (!a.beta_zero) {
-                const T2 yo = y[r];
-                yr = (T)a.br * yo.x - (T)a.bi * yo.y;
-                yi = (T)a.br * yo.y + (T)a.bi * yo.x;
-            }
-            T2 o;
-            o.x = yr + (T)a.ar * acc_r - (T)a.ai * acc_i;
-            o.y = yi + (T)a.ar * acc_i + (T)a.ai * acc_r;
-            y[r] = o;
+            xr = xv.x;
+            xi = xv.y;
         } else {
-            acc_r += dr * ((const T*)a.x)[r];
-            T* y = (T*)a.y;
-            const T yr = a.beta_zero ? (T)0 : (T)a.br * y[r];
-            y[r] = yr + (T)a.ar * acc_r;
+            xr = ((const T*)a.x)[r];
+        }
+        sell_tail<kCV>(acc_r, acc_i, sc, dr, di, xr, xi, (T2*)a.y, (T*)a.y, r, a.br, a.bi, a.ar, a.ai, a.beta_zero);
+    }
+}
+
+// ------------------------------------------------ several right-hand sides
+// mul!(Y, op, X) with X and Y column-major n x ncols (src/operators.jl:
+// 3185-3208, a column loop in the reference), up to R = 8 columns per launch.
+// X is first interleaved into Xt (row r holds its R values contiguously, the
+// unused columns zero), so that one gather brings every column's x[col]
+// (64 bytes in FP64) where separate products would gather R times; one
+// thread per row walks the row's packed words once.  Per column the sum runs
+// over the row's nonzeros in the order of sell_kernel and the row tail is the
+// same, so each column of Y is bit-identical to a single product.
+template <typename E, int R>
+__global__ void interleave_kernel(const E* __restrict__ X, E* __restrict__ Xt, int64_t n, int ncols) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        E v[R];
+#pragma unroll
+        for (int c = 0; c < R; ++c) {
+            if (c < ncols) v[c] = X[(int64_t)c * n + r];
+            else memset(&v[c], 0, sizeof(E));
+        }
+#pragma unroll
+        for (int c = 0; c < R; ++c) Xt[r * R + c] = v[c];
+    }
+}
+
+// R values of type T starting at p (16-byte aligned), read 16 bytes at a time
+template <typename T, int R>
+__device__ __forceinline__ void ld_row(const T* p, T (&v)[R]) {
+    static_assert((R * sizeof(T)) % 16 == 0, "rows of whole 16-byte units");
+    if (sizeof(T) == 8) {
+#pragma unroll
+        for (int c = 0; c < R; c += 2) {
+            const double2 d = ld_gather<true>((const double2*)(p + c));
+            memcpy(&v[c], &d, 16);
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < R; c += 4) {
+            const float4 f = ld_gather<true>((const float4*)(p + c));
+            memcpy(&v[c], &f, 16);
+        }
+    }
+}
+
+template <bool kCM, bool kCV, typename T, bool kPacked, int R>
+__global__ void __launch_bounds__(kThreads, 2) sell_mm_kernel(SellArgs a, int ncols, int64_t ldy) {
+    using T2 = typename V2<T>::t;
+    __shared__ T2 tab[1024];
+    __shared__ T rsq[kMaxGroup + 1];
+    const bool smem_tab = a.ncodes <= 1024;
+    if (smem_tab)
+        for (int i = threadIdx.x; i < a.ncodes; i += blockDim.x) {
+            T2 v = ((const T2*)a.table)[i];
+            if (a.conj) v.y = -v.y;
+            tab[i] = v;
+        }
+    for (int i = threadIdx.x; i <= kMaxGroup; i += blockDim.x) rsq[i] = i ? (T)(1.0 / sqrt((double)i)) : (T)0;
+    __syncthreads();
+    constexpr int W = kCV ? 2 * R : R;   // reals per interleaved row
+    const T* __restrict__ Xt = (const T*)a.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const T2* __restrict__ gtab = (const T2*)a.table;
+    const bool conj = a.conj;
+    for (int64_t s = a.slice0 + warp0; s < a.nslices; s += nwarps) {
+        const int64_t r = s * kSlice + lane;
+        if (r >= a.n) continue;
+        const int len = a.len[r];
+        const int64_t base = a.sptr[s] + lane;
+        T acc_r[R], acc_i[R];
+#pragma unroll
+        for (int c = 0; c < R; ++c) acc_r[c] = acc_i[c] = 0;
+        for (int j = 0; j < len; ++j) {
+            const int64_t o = base + (int64_t)j * kSellSlice;
+            uint32_t col, code;
+            if (kPacked) {
+                const uint32_t w = ld_word<true>(a.words + o);
+                col = w >> a.code_bits;
+                code = w & a.code_mask;
+            } else {
+                col = (uint32_t)ld_word<true>(a.cols + o);
+                code = ld_word<true>(a.codes + o);
+            }
+            T xv[W];
+            ld_row<T, W>(Xt + (int64_t)col * W, xv);
+            T2 v;
+            if (smem_tab) {
+                v = tab[code];
+            } else {
+                v = gtab[code];
+                if (conj) v.y = -v.y;
+            }
+#pragma unroll
+            for (int c = 0; c < R; ++c) {
+                if (kCV) sell_mac<kCM, true>(acc_r[c], acc_i[c], v, xv[2 * c], xv[2 * c + 1]);
+                else sell_mac<false, false>(acc_r[c], acc_i[c], v, xv[c], (T)0);
+            }
+        }
+        const T sc = a.stab ? rsq[a.stab[r]] : (T)1;
+        T dr, di = 0;
+        if (kCM) {
+            const T2 d = ((const T2*)a.diag)[r];
+            dr = d.x;
+            di = a.conj ? -d.y : d.y;
+        } else {
+            dr = ((const T*)a.diag_re)[r];
+        }
+        T xr_row[W];
+        ld_row<T, W>(Xt + r * W, xr_row);
+#pragma unroll
+        for (int c = 0; c < R; ++c) {
+            if (c >= ncols) break;
+            const T xr = kCV ? xr_row[2 * c] : xr_row[c], xi = kCV ? xr_row[2 * c + 1] : (T)0;
+            sell_tail<kCV>(acc_r[c], acc_i[c], sc, dr, di, xr, xi, (T2*)a.y + c * ldy, (T*)a.y + c * ldy, r, a.br,
+                           a.bi, a.ar, a.ai, a.beta_zero);
         }
     }
 }
@@ -1609,6 +1759,79 @@ void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s) {
 #undef QS_SPMV
     QS_CUDA(cudaGetLastError());
     note_launches(1);
+}
+
+
+bool op_spmm_device(Op& op, const MatvecCall& c, int64_t nrhs, cudaStream_t s) {
+    const Basis& b = *op.basis;
+    const Assembled& M = op.asm_;
+    const bool T = (c.flags & QS_TRANSPOSE) != 0, C = (c.flags & QS_CONJUGATE) != 0;
+    if (nrhs < 2 || !op.commuting || !op.assembled || !M.has_sell || (T && !op.hermitian) || c.df || c.fx ||
+        c.df_io || c.slice1 >= 0 || c.slice0 != 0)
+        return false;
+    SellArgs a{};
+    a.sptr = M.sell_ptr.as<int64_t>();
+    a.perm = M.sell_perm.as<int32_t>();
+    a.len = M.sell_len.as<uint16_t>();
+    a.words = M.sell_words.as<uint32_t>();
+    a.cols = M.sell_cols.as<int32_t>();
+    a.codes = M.sell_codes.as<uint16_t>();
+    a.packed = M.packed;
+    a.code_bits = M.code_bits;
+    a.code_mask = M.code_bits >= 32 ? 0xffffffffu : ((1u << M.code_bits) - 1u);
+    a.ncodes = M.ncodes;
+    a.stab = b.symmetric ? b.d_stab.as<uint16_t>() : nullptr;
+    a.nslices = M.nslices;
+    a.slice0 = 0;
+    a.n = b.n;
+    a.ar = c.alpha.re;
+    a.ai = c.alpha.im;
+    a.br = c.beta.re;
+    a.bi = c.beta.im;
+    a.beta_zero = (c.beta.re == 0.0 && c.beta.im == 0.0);
+    a.conj = T != C;
+    const bool cm = op.complex_mat, cv = c.y_complex;
+    if (c.single) {
+        a.table = M.table32.p;
+        a.diag = op.d_diag32.p;
+        a.diag_re = op.d_diag32_re.p;
+    } else {
+        a.table = M.table64.p;
+        a.diag = op.d_diag.p;
+        a.diag_re = op.d_diag_re.p;
+    }
+    constexpr int R = 8;
+    const size_t eb = (c.single ? 4 : 8) * (cv ? 2 : 1);
+    const int grid = grid_rows(std::max<int64_t>(1, a.nslices) * kSlice);
+    PoolBuf xt((size_t)b.n * R * eb, s);   // the interleaved columns
+    const int ig = grid_rows(b.n);
+    for (int64_t j0 = 0; j0 < nrhs; j0 += R) {
+        const int nc = (int)std::min<int64_t>(R, nrhs - j0);
+        const void* xs = (const char*)c.x + (size_t)j0 * b.n * eb;
+        if (eb == 4) interleave_kernel<float, R><<<ig, kThreads, 0, s>>>((const float*)xs, xt.as<float>(), b.n, nc);
+        else if (eb == 8) interleave_kernel<double, R><<<ig, kThreads, 0, s>>>((const double*)xs, xt.as<double>(), b.n, nc);
+        else interleave_kernel<double2, R><<<ig, kThreads, 0, s>>>((const double2*)xs, xt.as<double2>(), b.n, nc);
+        a.x = xt.p;
+        a.y = (char*)c.y + (size_t)j0 * b.n * eb;
+#define QS_MM(TT)                                                                                        \
+        do {                                                                                             \
+            if (a.packed) {                                                                              \
+                if (cm) sell_mm_kernel<true, true, TT, true, R><<<grid, kThreads, 0, s>>>(a, nc, b.n);      \
+                else if (cv) sell_mm_kernel<false, true, TT, true, R><<<grid, kThreads, 0, s>>>(a, nc, b.n); \
+                else sell_mm_kernel<false, false, TT, true, R><<<grid, kThreads, 0, s>>>(a, nc, b.n);        \
+            } else {                                                                                     \
+                if (cm) sell_mm_kernel<true, true, TT, false, R><<<grid, kThreads, 0, s>>>(a, nc, b.n);     \
+                else if (cv) sell_mm_kernel<false, true, TT, false, R><<<grid, kThreads, 0, s>>>(a, nc, b.n); \
+                else sell_mm_kernel<false, false, TT, false, R><<<grid, kThreads, 0, s>>>(a, nc, b.n);       \
+            }                                                                                            \
+        } while (0)
+        if (c.single) QS_MM(float);
+        else QS_MM(double);
+#undef QS_MM
+        QS_CUDA(cudaGetLastError());
+        note_launches(2);
+    }
+    return true;
 }
 
 namespace {

@@ -278,6 +278,10 @@ int qs_op_matvec(qs_op* op, int32_t flags, const double* alpha, const void* x, i
         if (mem == QS_MEM_DEVICE) {
             if (is_complex(x_dtype) != ycx)
                 throw qs::Error(QS_ERR_UNSUPPORTED, "device buffers must share the output dtype");
+            c.x = x;
+            c.y = y;
+            // several columns at once on the sliced-ELL form (one pass over its words)
+            if (nrhs > 1 && qs::op_spmm_device(o, c, nrhs, o.stream)) return;
             for (int64_t j = 0; j < nrhs; ++j) {
                 c.x = (const char*)x + (size_t)j * n * xb;
                 c.y = (char*)y + (size_t)j * n * yb;

@@ -229,6 +229,10 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
 // qs_assembled.cu
 void op_assemble(Op& op);
 void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s);
+// y = op x for nrhs column-major vectors (n apart) with one pass over the
+// sliced-ELL words per 8 columns; false (nothing done) when the operator or
+// the call does not allow it (then the caller loops over the columns)
+bool op_spmm_device(Op& op, const MatvecCall& c, int64_t nrhs, cudaStream_t s);
 // y = op x for one host vector with the assembled sliced-ELL product split in
 // row ranges, each range's rows of y copied back while later ranges compute;
 // false (nothing done) when the operator or the call does not allow it
