@@ -65,7 +65,7 @@ WORKLOADS = {
     # timed run; traffic_source names the summary it comes from)
     "j1j2_L32_k0_p1_z1": dict(L=32, nup=16, sym=dict(kblock=0, pblock=1, zblock=1), J2=0.5,
                               desc="Heisenberg J1-J2 chain L=32, nup=16, kblock=0, pblock=+1, zblock=+1, "
-                                   "J1=1.0, J2=0.5", traffic=801.39e6 + 36.99e6,
+                                   "J1=1.0, J2=0.5", traffic=788.81e6 + 27.69e6,
                               traffic_source="ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
                                              "profiles/sell_fp64_j1j2_L32_k0p1z1.md (not measured in this run)"),
     "j1j2_L24_k0_p1_z1": dict(L=24, nup=12, sym=dict(kblock=0, pblock=1, zblock=1), J2=0.5,
