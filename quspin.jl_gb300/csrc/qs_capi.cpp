@@ -306,8 +306,17 @@ int qs_op_matvec(qs_op* op, int32_t flags, const double* alpha, const void* x, i
                 QS_CUDA(cudaMemcpyAsync(o.d_x.p, widen.data(), n * yb, cudaMemcpyHostToDevice, o.stream));
             }
             char* ys = (char*)y + (size_t)j * n * yb;
-            if (!beta_zero) QS_CUDA(cudaMemcpyAsync(o.d_y.p, ys, n * yb, cudaMemcpyHostToDevice, o.stream));
             c.x = o.d_x.p;
+            // page-locked y and nothing to read from it: the product writes it
+            // through its mapped address, with no device copy and no read-back
+            void* y_mapped = beta_zero ? qs::mapped_host_address(ys) : nullptr;
+            if (y_mapped) {
+                c.y = y_mapped;
+                qs::op_matvec_device(o, c, o.stream);
+                QS_CUDA(cudaStreamSynchronize(o.stream));
+                continue;
+            }
+            if (!beta_zero) QS_CUDA(cudaMemcpyAsync(o.d_y.p, ys, n * yb, cudaMemcpyHostToDevice, o.stream));
             c.y = o.d_y.p;
             // the assembled product in row ranges, each range read back while the
             // next computes; otherwise one product and one read-back

@@ -75,6 +75,9 @@ struct DevBuf {
 void* pool_get(size_t bytes);
 void pool_put(void* p, size_t bytes, cudaStream_t last_use);
 void pool_trim();
+// Device address of page-locked host memory (cudaHostAlloc / cudaHostRegister,
+// mapped under unified addressing), or null for any other pointer.
+void* mapped_host_address(void* p);
 
 struct PoolBuf {
     void* p = nullptr;

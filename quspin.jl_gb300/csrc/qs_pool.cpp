@@ -116,6 +116,15 @@ void pool_put(void* p, size_t bytes, cudaStream_t last_use) {
     }
 }
 
+void* mapped_host_address(void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 void pool_trim() {
     std::lock_guard<std::mutex> g(g_pool_mu);
     free_all_locked();

@@ -505,3 +505,35 @@ def test_eigsh_non_hermitian(qs, ora, which, cplx):
     got = qs.eigsh(ops, k=ks, which=which, return_eigenvectors=False)
     for v in _expected_complex(ws, which, ks):
         assert np.min(np.abs(got - v)) <= 1e-10 * max(1.0, np.abs(ws).max())
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp64fx"])
+def test_page_locked_output_written_in_place(qs, ora, prec):
+    """With a page-locked output and beta = 0 the product writes y through its
+    mapped address (no device copy of y): the same values as pageable output."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from qsgpu import _lib
+    lib = _lib.load()
+    L = 16
+    b = qs.SpinBasis1D(L, nup=8, pauli=False, kblock=0, pblock=1, zblock=1)
+    for op in (qs.Hamiltonian(b, models.to_terms(qs, models.j1j2(L, 1.0, 0.5))),
+               qs.QuantumLinearOperator(b, models.to_terms(qs, models.j1j2(L, 1.0, 0.5)))):
+        if prec == "fp64fx" and not getattr(op, "fixed_point_classes", 0):
+            continue
+        dt = torch.float32 if prec == "fp32" else torch.float64
+        code = _lib.QS_F32 if prec == "fp32" else _lib.QS_F64
+        flags = _lib.QS_FIXED_POINT if prec == "fp64fx" else 0
+        x = torch.from_numpy(models.seeded(b.Ns)).to(dt)
+        xp = torch.empty(b.Ns, dtype=dt, pin_memory=True)
+        xp.copy_(x)
+        yp = torch.full((b.Ns,), float("nan"), dtype=dt, pin_memory=True)
+        ypage = np.full(b.Ns, np.nan, dtype=np.float32 if prec == "fp32" else np.float64)
+        one, zero = np.array([1.0, 0.0]), np.array([0.0, 0.0])
+        for y, ptr in ((yp, ctypes.c_void_p(yp.data_ptr())), (ypage, _lib.ptr(ypage))):
+            _lib.check(lib.qs_op_matvec(op._h, flags, _lib.ptr(one), ctypes.c_void_p(xp.data_ptr()), code,
+                                        _lib.ptr(zero), ptr, code, 1, _lib.QS_MEM_HOST))
+        assert np.array_equal(yp.numpy(), ypage)
+        want = op.dot(models.seeded(b.Ns))
+        tol = 2e-5 if prec == "fp32" else 1e-13
+        assert np.max(np.abs(yp.numpy() - want)) <= tol * max(1.0, np.abs(want).max())
