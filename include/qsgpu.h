@@ -286,7 +286,10 @@ typedef struct {
  * reorthogonalisation replaces the ARPACK implicitly restarted Lanczos;
  * convergence is ARPACK's test ||r_i|| <= tol * max(eps^(2/3), |theta_i|).
  * Assembled operators (qs_op_assemble) run on the batched engine with one
- * operator (as qs_eigsh_batch). */
+ * operator (as qs_eigsh_batch).  A matrix-free operator whose assembled form
+ * fits in a quarter of free device memory is assembled for the length of the
+ * call and runs there too (the form is dropped on return; environment
+ * QS_TRANSIENT_ASSEMBLY=0 keeps the call matrix-free). */
 QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *vectors, qs_eigsh_info *info);
 
 /* eigsh(op; k, which, v0, tol, ncv, maxiter) for a non-Hermitian operator
@@ -319,7 +322,8 @@ QS_API int qs_eigsh_batch(qs_op *const *ops, int32_t nops, const qs_eigsh_opts *
  * Krylov exponential action _krylov_expmv_vector (src/operators.jl:1758-1803):
  * out = exp(a * A) v with complex a.  v, out: Ns complex (host).
  * precision: 0 FP64, 1 FP32 Krylov vectors, 2 double-float Krylov vectors
- * (assembled operators; otherwise FP64). */
+ * (assembled operators; otherwise FP64).  A matrix-free operator is assembled
+ * for the length of the call as in qs_eigsh. */
 QS_API int qs_expm_multiply(qs_op *op, const double *a, const double *v, double *out, double tol,
                      int32_t krylov_dim, int32_t precision);
 

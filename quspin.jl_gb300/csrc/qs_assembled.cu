@@ -1889,6 +1889,43 @@ void op_export_csr(Op& op, int64_t* rowptr, int64_t* cols, double* values, doubl
     QS_CUDA(cudaStreamSynchronize(s));
 }
 
+
+void op_release_assembly(Op& op) {
+    if (!op.assembled) return;
+    QS_CUDA(cudaStreamSynchronize(op.stream));
+    op.asm_ = Assembled();
+    op.assembled = false;
+}
+
+TransientAssembly::TransientAssembly(Op& o) : op(o) {
+    if (op.assembled || !op.commuting) return;
+    const char* e = std::getenv("QS_TRANSIENT_ASSEMBLY");
+    if (e && e[0] == '0') return;
+    // an upper bound of the assembled form (both layouts): a packed word per
+    // program and row, twice, with the row tables; a quarter of free memory at most
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    const double bound = (double)op.basis->n * ((double)op.progs.size() / 2 * 4.0 * 2 + 64);
+    if (bound > 0.25 * (double)free_b) return;
+    try {
+        op_assemble(op);
+        made = true;
+    } catch (const Error& err) {
+        if (err.status != QS_ERR_UNSUPPORTED) throw;   // programs that cannot be assembled stay matrix-free
+    }
+}
+
+TransientAssembly::~TransientAssembly() {
+    if (!made) return;
+    try {
+        op_release_assembly(op);
+    } catch (...) {
+    }
+}
+
 bool op_matvec_host_overlap(Op& op, const MatvecCall& c0, void* y_host, size_t eb) {
     const Assembled& M = op.asm_;
     const bool T = (c0.flags & QS_TRANSPOSE) != 0;

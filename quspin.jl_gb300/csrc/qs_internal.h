@@ -231,6 +231,21 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
                        int64_t nrhs);
 // qs_assembled.cu
 void op_assemble(Op& op);
+// drops the assembled form (the operator runs matrix-free again)
+void op_release_assembly(Op& op);
+// The Krylov solvers of a matrix-free operator run on its assembled form for
+// the length of one call when the form fits in a quarter of free memory:
+// assembly is one pass of the product kernel, and each product after it is an
+// order of magnitude cheaper than the matrix-free one.  The form is dropped
+// when the call returns (QS_TRANSIENT_ASSEMBLY=0 keeps the solvers matrix-free).
+struct TransientAssembly {
+    Op& op;
+    bool made = false;
+    explicit TransientAssembly(Op& o);
+    ~TransientAssembly();
+    TransientAssembly(const TransientAssembly&) = delete;
+    TransientAssembly& operator=(const TransientAssembly&) = delete;
+};
 void op_spmv_device(Op& op, const MatvecCall& c, cudaStream_t s);
 // y = op x for nrhs column-major vectors (n apart) with one pass over the
 // sliced-ELL words per 8 columns; false (nothing done) when the operator or

@@ -377,6 +377,7 @@ void eigs_general(Op& op, const qs_eigsh_opts& o, double* values, void* vectors,
         QS_CUDA(cudaMemcpyAsync(X.p, out.data(), out.size() * 16, cudaMemcpyHostToDevice, op.stream));
         mv = n;
     } else {
+        TransientAssembly ta(op);
         int ncv = o.ncv > 0 ? o.ncv : std::max(20, 2 * k + 1);
         ncv = std::min(ncv, 128);
         if (ncv <= k) ncv = (int)std::min<int64_t>(n, k + 2);
@@ -524,6 +525,7 @@ void eigsh(Op& op, const qs_eigsh_opts& o, double* values, void* vectors, qs_eig
         }
         return;
     }
+    TransientAssembly ta(op);
     if (op.assembled && op.asm_.has_sell && k < n - 1) {
         // assembled operators: the batched engine with one slot (graph-replayed
         // steps, device-resident Lanczos coefficients, ARPACK's DGKS test)
@@ -737,6 +739,7 @@ void expm_multiply(Op& op, cd a, const double* v, double* out, double tol, int k
     const int64_t n = op.basis->n;
     if (tol <= 0) throw Error(QS_ERR_ARGUMENT, "tol must be positive");
     if (krylov_dim <= 0) throw Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
+    TransientAssembly ta(op);
     if (op.assembled && op.asm_.has_sell && precision != 1 && krylov_dim <= 64 && n >= 2) {
         evolve_engine(op, v, {a}, tol, krylov_dim, precision, false, out);
         return;
@@ -758,6 +761,7 @@ void evolve(Op& op, const double* v0, double t0, const double* times, int nt, in
     const int64_t n = op.basis->n;
     if (tol <= 0) throw Error(QS_ERR_ARGUMENT, "tol must be positive");
     if (krylov_dim <= 0) throw Error(QS_ERR_ARGUMENT, "krylov_dim must be positive");
+    TransientAssembly ta(op);
     if (op.assembled && op.asm_.has_sell && precision != 1 && krylov_dim <= 64 && n >= 2) {
         std::vector<cd> sc(nt);
         for (int i = 0; i < nt; ++i) {

@@ -537,3 +537,30 @@ def test_page_locked_output_written_in_place(qs, ora, prec):
         want = op.dot(models.seeded(b.Ns))
         tol = 2e-5 if prec == "fp32" else 1e-13
         assert np.max(np.abs(yp.numpy() - want)) <= tol * max(1.0, np.abs(want).max())
+
+
+def test_transient_assembly_of_matrix_free_solvers(qs, ora, monkeypatch):
+    """eigsh / evolve / expm on a matrix-free operator run on an assembled form
+    built for the call and dropped after it: the same results as the
+    matrix-free solve (QS_TRANSIENT_ASSEMBLY=0) and the operator left
+    matrix-free (no stored nonzeros)."""
+    L = 16
+    sym = dict(kblock=0, pblock=1, zblock=1)
+    sp = models.j1j2(L, 1.0, 0.37)
+    b = qs.SpinBasis1D(L, nup=8, pauli=False, **sym)
+    Q = qs.QuantumLinearOperator(b, models.to_terms(qs, sp))
+    v0 = models.seeded(b.Ns, seed=5)
+    v = models.seeded(b.Ns, seed=6, complex_=True)
+    v /= np.linalg.norm(v)
+    got = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("QS_TRANSIENT_ASSEMBLY", mode)
+        e = qs.eigsh(Q, k=3, which="SA", tol=1e-12, v0=v0, return_eigenvectors=False)
+        st = qs.evolve(Q, v, 0.0, [0.5, 1.5], tol=1e-10)
+        got[mode] = (e, st)
+        assert Q.nnz < 0
+    M = ora.RefBasis(L, nup=8, pauli=False, **sym).dense(ora.consolidate_terms(sp))
+    w = np.linalg.eigvalsh(M)[:3]
+    assert np.max(np.abs(got["1"][0] - w)) <= 1e-10 * np.abs(w).max()
+    assert np.max(np.abs(got["1"][0] - got["0"][0])) <= 1e-10 * np.abs(got["0"][0]).max()
+    assert np.max(np.linalg.norm(got["1"][1] - got["0"][1], axis=0)) <= 1e-9
