@@ -881,7 +881,7 @@ def profile_range(kind):
     matrix-free product ("matrixfree"), one Lanczos ground state of it
     ("lanczos64", "lanczosdf"), one batched
     double-float ground-state solve of all J1-J2 sectors at L = 24 or 26
-    ("batch24", "batch26"), or the 32 batched m = 100 Lanczos recurrences of
+    ("batch24", "batch26"; "batch26_fp64" in FP64), or the 32 batched m = 100 Lanczos recurrences of
     the FTLM workload ("ftlm")."""
     import torch
     import qsgpu as qs
@@ -975,17 +975,19 @@ def profile_range(kind):
         torch.cuda.profiler.stop()
         print(json.dumps({"profile_range": kind, "N": b.Ns, "ynorm": float(yt.double().norm())}))
         return
-    L = int(kind[len("batch"):])
+    spec = kind[len("batch"):].split("_")
+    L = int(spec[0])
+    prec = spec[1] if len(spec) > 1 else "fp64df"
     terms = [qs.OperatorTerm(o, c) for o, c in j1j2_spec(L, 1.0, 0.3)]
     syms = []
     for k in range(L):
         syms += [dict(kblock=k, pblock=1), dict(kblock=k, pblock=-1)] if k in (0, L // 2) else [dict(kblock=k)]
     ops = [qs.Hamiltonian(qs.SpinBasis1D(L, nup=L // 2, pauli=False, **sy), terms) for sy in syms]
-    qs.eigsh_batch(ops, k=1, tol=1e-10, precision="fp64df")
+    qs.eigsh_batch(ops, k=1, tol=1e-10, precision=prec)
     torch.cuda.synchronize()
     torch.cuda.profiler.start()
     t = time.perf_counter()
-    qs.eigsh_batch(ops, k=1, tol=1e-10, precision="fp64df")
+    qs.eigsh_batch(ops, k=1, tol=1e-10, precision=prec)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t
     torch.cuda.profiler.stop()
@@ -1263,7 +1265,7 @@ def main():
     ap.add_argument("--only-section", default=None, help="run this side workload only (by its JSON key)")
     ap.add_argument("--profile-range", default=None,
                     choices=["product64", "product32", "productdf", "productfx", "sweep28", "matrixfree", "lanczos64", "lanczosdf",
-                             "batch24", "batch26", "ftlm"],
+                             "batch24", "batch26", "batch26_fp64", "ftlm"],
                     help="run one unit inside cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     args = ap.parse_args()
     if args.profile_range:

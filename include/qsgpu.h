@@ -511,6 +511,15 @@ QS_API const char *qs_last_error(void);
  * bandwidth per flop). */
 QS_API int qs_fp64_fma_rate(double *fma_per_s);
 
+/* Check of the bounded grid barrier that separates the phases of the
+ * persistent Lanczos step: `blocks` co-resident blocks pass eight barriers
+ * that expect `phantom` more blocks than run.  phantom = 0: QS_OK.  phantom > 0:
+ * the barriers cannot complete, every wait gives up after limit_ms (at most
+ * 2000) of device time and the call returns QS_ERR_TIMEOUT with the device
+ * still usable.  No reference counterpart: the failure path of the device
+ * waits, exercised without a fault. */
+QS_API int qs_grid_barrier_check(int32_t phantom, double limit_ms, int32_t blocks);
+
 /* Number of kernels this library has launched in the process so far (all
  * handles).  No reference counterpart: instrumentation for benchmarks. */
 QS_API int64_t qs_launch_count(void);

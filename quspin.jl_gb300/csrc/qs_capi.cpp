@@ -448,6 +448,10 @@ int qs_expm_columns(qs_op* op, const double* V, int32_t ncol, const double* scal
     });
 }
 
+int qs_grid_barrier_check(int32_t phantom, double limit_ms, int32_t blocks) {
+    return guard([&] { qs::grid_barrier_check(phantom, limit_ms, blocks); });
+}
+
 int qs_fp64_fma_rate(double* fma_per_s) {
     return guard([&] {
         if (!fma_per_s) throw qs::Error(QS_ERR_ARGUMENT, "null argument");

@@ -216,11 +216,11 @@ __device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT) eng_spmv(const SlotDev* __restrict__ sl, const int* __restrict__ smap,
-                                               const void* __restrict__ rsqt) {
+__device__ __forceinline__ void spmv_block(const SlotDev* sl, const int* __restrict__ smap,
+                                           const void* __restrict__ rsqt, int bx) {
     __shared__ CA<A> tab[1024];
     __shared__ A rsq[kMaxGroup + 1];
-    const SlotDev& S = sl[smap[blockIdx.x]];
+    const SlotDev& S = sl[smap[bx]];
     if (S.state != kSlotStep) return;
     const bool smem_tab = S.ncodes <= 1024;
     if (smem_tab)
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(kT) eng_spmv(const SlotDev* __restrict__ sl, c
     if (S.stab)
         for (int i = threadIdx.x; i <= S.max_stab; i += blockDim.x) rsq[i] = ldrsq<A>(rsqt, i);
     __syncthreads();
-    const int64_t lb = blockIdx.x - S.sb_begin;
+    const int64_t lb = bx - S.sb_begin;
     if (S.packed) {
         if (!S.cv) spmv_rows<A, false, false, true>(S, lb, tab, smem_tab, rsq);
         else if (!S.cm) spmv_rows<A, true, false, true>(S, lb, tab, smem_tab, rsq);
@@ -238,6 +238,12 @@ __global__ void __launch_bounds__(kT) eng_spmv(const SlotDev* __restrict__ sl, c
         else if (!S.cm) spmv_rows<A, true, false, false>(S, lb, tab, smem_tab, rsq);
         else spmv_rows<A, true, true, false>(S, lb, tab, smem_tab, rsq);
     }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT) eng_spmv(const SlotDev* __restrict__ sl, const int* __restrict__ smap,
+                                               const void* __restrict__ rsqt) {
+    spmv_block<A>(sl, smap, rsqt, blockIdx.x);
 }
 
 // ------------------------------------------------------------ dots
@@ -370,9 +376,9 @@ __device__ __forceinline__ void dots_epilogue(A* re, A* im, bool cv, int i0, int
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
-                                               int mode, double* __restrict__ partial) {
-    const SlotDev& S = sl[rmap[blockIdx.x]];
+__device__ __forceinline__ void dots_block(const SlotDev* sl, const int* __restrict__ rmap, int mmax, int mode,
+                                           double* partial, int bx, int by) {
+    const SlotDev& S = sl[rmap[bx]];
     if (S.state != (mode == 2 ? kSlotNormalize : kSlotStep)) return;
     if (mode == 1 && S.nrm[4] == 0.0) return;
     const int P = mmax + 1;
@@ -387,25 +393,102 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_do
         nv = S.j + 1;
         w = colp<A>(S, S.j + 1);
     }
-    const int i0 = first + blockIdx.y * jt<A>();
+    const int i0 = first + by * jt<A>();
     if (i0 >= nv) return;
-    const bool want_wn = mode == 0 && S.orth == 1 && blockIdx.y == 0;
-    const int64_t lb = blockIdx.x - S.rb_begin;
+    const bool want_wn = mode == 0 && S.orth == 1 && by == 0;
+    const int64_t lb = bx - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
     A re[jt<A>()], im[jt<A>()], wn = zero<A>();
 #pragma unroll
     for (int q = 0; q < jt<A>(); ++q) re[q] = im[q] = zero<A>();
     if (S.cv) dots_rows<A, true>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
     else dots_rows<A, false>(S, r0, r1, i0, nv, w, re, im, want_wn, wn);
-    dots_epilogue<A>(re, im, S.cv, i0, nv, mode == 2 ? 0 : i0, partial + (size_t)blockIdx.x * P * 2);
+    dots_epilogue<A>(re, im, S.cv, i0, nv, mode == 2 ? 0 : i0, partial + (size_t)bx * P * 2);
     if (want_wn) {
         __shared__ double sw[kT / 32];
         const double t = block_sum(wn, sw);
         if (threadIdx.x == 0) {
-            partial[((size_t)blockIdx.x * P + mmax) * 2] = t;
-            partial[((size_t)blockIdx.x * P + mmax) * 2 + 1] = 0.0;
+            partial[((size_t)bx * P + mmax) * 2] = t;
+            partial[((size_t)bx * P + mmax) * 2 + 1] = 0.0;
         }
     }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_dots(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+                                               int mode, double* __restrict__ partial) {
+    dots_block<A>(sl, rmap, mmax, mode, partial, blockIdx.x, blockIdx.y);
+}
+
+// First-pass dots of a real Gram-Schmidt slot with 2 <= nv <= 20 vectors in
+// one block per row block: each row's w and nv vector entries are loaded once
+// (all loads before the arithmetic) and every column's sum advances, where
+// eng_dots reads w once per tile of jt columns.  Per thread the rows and the
+// multiply-add order of each column's sum and of ||w||^2 are those of
+// dots_rows, and the block sums go through dots_epilogue / block_sum, so the
+// partials are bit-identical to dots_block's.
+template <class A, int NV>
+__device__ __forceinline__ void dots_fused_rows(const SlotDev& S, int64_t r0, int64_t r1, int nv, const void* w,
+                                                bool want_wn, int mmax, double* partial, int bx) {
+    const char* V = (const char*)S.V;
+    const size_t cs = (size_t)S.n * vbytes<A, false>();
+    A acc[NV];
+#pragma unroll
+    for (int t = 0; t < NV; ++t) acc[t] = zero<A>();
+    A wn = zero<A>();
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        A v[NV];
+#pragma unroll
+        for (int t = 0; t < NV; ++t)
+            if (t < nv) v[t] = ldv<A, false>(V + (size_t)t * cs, r).re;
+        const A wr = ldv<A, false>(w, r).re;
+#pragma unroll
+        for (int t = 0; t < NV; ++t)
+            if (t < nv) mac(acc[t], v[t], wr);
+        if (want_wn) mac(wn, wr, wr);
+    }
+    const int P = mmax + 1;
+    double* row = partial + (size_t)bx * P * 2;
+#pragma unroll
+    for (int c0 = 0; c0 < NV; c0 += jt<A>()) {
+        if (c0 < nv) {
+            A re[jt<A>()], im[jt<A>()];
+#pragma unroll
+            for (int q = 0; q < jt<A>(); ++q) {
+                re[q] = c0 + q < NV ? acc[c0 + q < NV ? c0 + q : 0] : zero<A>();
+                im[q] = zero<A>();
+            }
+            dots_epilogue<A>(re, im, false, c0, nv, c0, row);
+        }
+    }
+    if (want_wn) {
+        __shared__ double sw[kT / 32];
+        const double t = block_sum(wn, sw);
+        if (threadIdx.x == 0) {
+            partial[((size_t)bx * P + mmax) * 2] = t;
+            partial[((size_t)bx * P + mmax) * 2 + 1] = 0.0;
+        }
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT, 2) eng_dots_fused(const SlotDev* __restrict__ sl, const int* __restrict__ rmap,
+                                                        int mmax, double* __restrict__ partial) {
+    const int bx = blockIdx.x, by = blockIdx.y;
+    const SlotDev& S = sl[rmap[bx]];
+    if (S.state != kSlotStep) return;
+    const int nv = S.j + 1;
+    if (S.cv || S.orth == 2 || nv < 2 || nv > 20) {
+        dots_block<A>(sl, rmap, mmax, 0, partial, bx, by);
+        return;
+    }
+    if (by) return;
+    const int64_t lb = bx - S.rb_begin;
+    const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
+    const void* w = colp<A>(S, S.j + 1);
+    const bool want_wn = S.orth == 1;
+    if (nv <= 12) dots_fused_rows<A, 12>(S, r0, r1, nv, w, want_wn, mmax, partial, bx);
+    else dots_fused_rows<A, 20>(S, r0, r1, nv, w, want_wn, mmax, partial, bx);
 }
 
 // ------------------------------------------------------------ reduce
@@ -416,10 +499,10 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_do
 // mode 2: h2 and the record column h1 + h2 (second pass only)
 // mode 3: ||w''||^2 (second pass only)
 // mode 4: norm of the normalised column
-__global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl, int mmax, int mode,
-                                                 const double* __restrict__ partial, int dy = 0) {
-    const SlotDev& S = sl[blockIdx.x];
-    int i = blockIdx.y;
+__device__ __forceinline__ void reduce_block(const SlotDev* sl, int mmax, int mode, const double* partial, int dy,
+                                             int bx, int by) {
+    const SlotDev& S = sl[bx];
+    int i = by;
     if (mode == 4) {
         if (S.state != kSlotNormalize || i) return;
     } else {
@@ -501,6 +584,11 @@ __global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl,
     }
 }
 
+__global__ void __launch_bounds__(kT) eng_reduce(const SlotDev* __restrict__ sl, int mmax, int mode,
+                                                 const double* __restrict__ partial, int dy = 0) {
+    reduce_block(sl, mmax, mode, partial, dy, blockIdx.x, blockIdx.y);
+}
+
 // ------------------------------------------------------------ update
 // col(j+1) -= sum_i col(i) h_i over the pass's vectors (pass 0: h1 from
 // `first`, pass 1: h2 over 0..j, only where the step's flag asks), leaving the
@@ -573,9 +661,9 @@ __device__ __forceinline__ A update_rows(const SlotDev& S, int64_t r0, int64_t r
 }
 
 template <class A>
-__global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_update(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
-                                                 int pass, double* __restrict__ partial) {
-    const SlotDev& S = sl[rmap[blockIdx.x]];
+__device__ __forceinline__ void update_block(const SlotDev* sl, const int* __restrict__ rmap, int mmax, int pass,
+                                             double* partial, int bx) {
+    const SlotDev& S = sl[rmap[bx]];
     if (S.state != kSlotStep) return;
     if (pass == 1 && S.nrm[4] == 0.0) return;
     __shared__ CA<A> hs[kMaxM];
@@ -587,22 +675,22 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_up
         hs[t] = CA<A>{from_d<A>(v.x), from_d<A>(v.y)};
     }
     __syncthreads();
-    const int64_t lb = blockIdx.x - S.rb_begin;
+    const int64_t lb = bx - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
     A nacc = S.cv ? update_rows<A, true>(S, r0, r1, first, nv, hs) : update_rows<A, false>(S, r0, r1, first, nv, hs);
     __shared__ double sh[kT / 32];
     const double t = block_sum(nacc, sh);
     const int P = mmax + 1;
     if (threadIdx.x == 0) {
-        partial[((size_t)blockIdx.x * P + mmax) * 2] = t;
-        partial[((size_t)blockIdx.x * P + mmax) * 2 + 1] = 0.0;
+        partial[((size_t)bx * P + mmax) * 2] = t;
+        partial[((size_t)bx * P + mmax) * 2 + 1] = 0.0;
     }
     if (pass == 0 && S.orth != 2) {
         // the Gram-Schmidt slots' second-pass dots V^* w' over this block's rows,
         // while V and w' are still in cache; used when the DGKS test asks for
         // the second pass
         const void* w = colp<A>(S, S.j + 1);
-        double* row = partial + (size_t)blockIdx.x * P * 2;
+        double* row = partial + (size_t)bx * P * 2;
         for (int c0 = 0; c0 < nv; c0 += jt<A>()) {
             A re[jt<A>()], im[jt<A>()], dummy = zero<A>();
 #pragma unroll
@@ -612,6 +700,98 @@ __global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_up
             dots_epilogue<A>(re, im, S.cv, c0, nv, c0, row);
         }
     }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3) eng_update(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mmax,
+                                                 int pass, double* __restrict__ partial) {
+    update_block<A>(sl, rmap, mmax, pass, partial, blockIdx.x);
+}
+
+// Pass 0 of a real Gram-Schmidt slot with nv <= NV vectors, each row's nv
+// vector entries held in registers: w'[r] = w[r] - sum_t V[r, t] h_t, then
+// the second-pass dots acc[t] += V[r, t] w'[r] from the same registers (no
+// second read of V).  Per thread the rows, the terms and the argument order
+// of every multiply-add are those of update_rows followed by dots_rows, and
+// the block sums go through the same dots_epilogue, so the results are
+// bit-identical to update_block's.
+__device__ __forceinline__ double ld_volatile(const volatile double* p) { return *p; }
+__device__ __forceinline__ float ld_volatile(const volatile float* p) { return *p; }
+__device__ __forceinline__ DF ld_volatile(const volatile DF* p) { return DF{p->h, p->l}; }
+
+template <class A, int NV>
+__device__ __forceinline__ void update_fused_rows(const SlotDev& S, int64_t r0, int64_t r1, int nv, const CA<A>* hs,
+                                                  int mmax, double* partial, int bx) {
+    const char* V = (const char*)S.V;
+    const size_t cs = (size_t)S.n * vbytes<A, false>();
+    void* w = (void*)(V + (size_t)(S.j + 1) * cs);
+    A acc[NV];
+#pragma unroll
+    for (int t = 0; t < NV; ++t) acc[t] = zero<A>();
+    A nacc = zero<A>();
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        A v[NV];
+#pragma unroll
+        for (int t = 0; t < NV; ++t)
+            if (t < nv) v[t] = ldv<A, false>(V + (size_t)t * cs, r).re;
+        A ar = zero<A>();
+        // h from shared memory at each use (held in registers across the row
+        // loop it would take NV more of them)
+        const volatile A* hv = (const volatile A*)hs;
+#pragma unroll
+        for (int t = 0; t < NV; ++t)
+            if (t < nv) mac(ar, v[t], ld_volatile(hv + 2 * t));
+        A o = ldv<A, false>(w, r).re;
+        o = sub(o, ar);
+        stv<A, false>(w, r, CA<A>{o, zero<A>()});
+        mac(nacc, o, o);
+#pragma unroll
+        for (int t = 0; t < NV; ++t)
+            if (t < nv) mac(acc[t], v[t], o);
+    }
+    __shared__ double sh[kT / 32];
+    const double tn = block_sum(nacc, sh);
+    const int P = mmax + 1;
+    if (threadIdx.x == 0) {
+        partial[((size_t)bx * P + mmax) * 2] = tn;
+        partial[((size_t)bx * P + mmax) * 2 + 1] = 0.0;
+    }
+    double* row = partial + (size_t)bx * P * 2;
+#pragma unroll
+    for (int c0 = 0; c0 < NV; c0 += jt<A>()) {
+        if (c0 < nv) {
+            A re[jt<A>()], im[jt<A>()];
+#pragma unroll
+            for (int q = 0; q < jt<A>(); ++q) {
+                re[q] = c0 + q < NV ? acc[c0 + q < NV ? c0 + q : 0] : zero<A>();
+                im[q] = zero<A>();
+            }
+            dots_epilogue<A>(re, im, false, c0, nv, c0, row);
+        }
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT, 2) eng_update_fused(const SlotDev* __restrict__ sl, const int* __restrict__ rmap,
+                                                          int mmax, double* __restrict__ partial) {
+    const int bx = blockIdx.x;
+    const SlotDev& S = sl[rmap[bx]];
+    if (S.state != kSlotStep) return;
+    const int nv = S.j + 1;
+    if (S.cv || S.orth == 2 || nv < 3 || nv > 20) {
+        update_block<A>(sl, rmap, mmax, 0, partial, bx);
+        return;
+    }
+    __shared__ CA<A> hs[20];
+    for (int t = threadIdx.x; t < nv; t += blockDim.x) {
+        const double2 v = S.h1[t];
+        hs[t] = CA<A>{from_d<A>(v.x), from_d<A>(v.y)};
+    }
+    __syncthreads();
+    const int64_t lb = bx - S.rb_begin;
+    const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
+    if (nv <= 12) update_fused_rows<A, 12>(S, r0, r1, nv, hs, mmax, partial, bx);
+    else update_fused_rows<A, 20>(S, r0, r1, nv, hs, mmax, partial, bx);
 }
 
 // ------------------------------------------------------------ scale / advance
@@ -636,15 +816,20 @@ __device__ __forceinline__ void scale_rows(void* w, int64_t r0, int64_t r1, A f)
 }
 // mode 0: col(j+1) *= 1/beta on stepping slots; mode 1: col ncol on normalising slots
 template <class A>
-__global__ void __launch_bounds__(kT) eng_scale(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mode) {
-    const SlotDev& S = sl[rmap[blockIdx.x]];
+__device__ __forceinline__ void scale_block(const SlotDev* sl, const int* __restrict__ rmap, int mode, int bx) {
+    const SlotDev& S = sl[rmap[bx]];
     if (S.state != (mode == 0 ? kSlotStep : kSlotNormalize)) return;
     const A f = from_d<A>(S.nrm[1]);
     void* w = colp<A>(S, mode == 0 ? S.j + 1 : S.ncol);
-    const int64_t lb = blockIdx.x - S.rb_begin;
+    const int64_t lb = bx - S.rb_begin;
     const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
     if (S.cv) scale_rows<A, true>(w, r0, r1, f);
     else scale_rows<A, false>(w, r0, r1, f);
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT) eng_scale(const SlotDev* __restrict__ sl, const int* __restrict__ rmap, int mode) {
+    scale_block<A>(sl, rmap, mode, blockIdx.x);
 }
 
 __global__ void eng_advance(SlotDev* sl, int nslots) {
@@ -1230,14 +1415,24 @@ void Engine::sync_table() {
 // and reduce grids cover the most vectors a slot dots against (dmax), so
 // three-term slots cost one block row however large their basis; without
 // Gram-Schmidt slots the second-pass launches are left out.
+// QS_FUSED_UPDATE=0 keeps the first-pass dots on eng_dots and pass 0 on
+// eng_update (the fused kernels give the same bits; the switch exists to time
+// the two)
+static bool fused_update_on() {
+    const char* e = std::getenv("QS_FUSED_UPDATE");
+    return !(e && e[0] == '0');
+}
+
 template <class A>
 static int launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const int* sm, double* pa, const void* rsq,
                          int nrb, int nsb, int mmax, int dmax, bool cgs, int ns, cudaStream_t s) {
     const dim3 gd(nrb, (dmax + jt<A>() - 1) / jt<A>());
     eng_spmv<A><<<nsb, kT, 0, s>>>(ds, sm, rsq);
-    eng_dots<A><<<gd, kT, 0, s>>>(ds, rm, mmax, 0, pa);
+    if (fused_update_on()) eng_dots_fused<A><<<gd, kT, 0, s>>>(ds, rm, mmax, pa);
+    else eng_dots<A><<<gd, kT, 0, s>>>(ds, rm, mmax, 0, pa);
     eng_reduce<<<dim3(ns, dmax + 1), kT, 0, s>>>(ds, mmax, 0, pa, dmax);
-    eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 0, pa);
+    if (fused_update_on()) eng_update_fused<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, pa);
+    else eng_update<A><<<nrb, kT, 0, s>>>(ds, rm, mmax, 0, pa);
     eng_reduce<<<dim3(ns, 1), kT, 0, s>>>(ds, mmax, 1, pa);
     int n = 5;
     if (cgs) {
@@ -1249,6 +1444,136 @@ static int launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const i
     eng_scale<A><<<nrb, kT, 0, s>>>(ds, rm, 0);
     eng_advance<<<(ns + 127) / 128, 128, 0, s>>>(dsw, ns);
     return n + 2;
+}
+
+// ------------------------------------------------------------ persistent step
+// The same step as launch_step_t in one cooperative launch: every phase runs
+// the kernels' block bodies over the same virtual block indices (so each
+// slot's arithmetic, and its result, is the one of the graph replay), and a
+// grid-wide barrier separates the phases.  The launch runs nsteps steps.
+//
+// Barrier: arrival counter + generation word.  Thread 0 of each block
+// releases the block's writes, arrives, and the last arrival resets the
+// counter and publishes the next generation; the others wait for it with an
+// acquire load (which also drops stale L1 lines of other blocks' data).  Each
+// wait gives up after limit_ns of global time: it then sets the shared error
+// word and returns false, every block leaves the kernel at its next barrier,
+// and the host reads the word (QS_ERR_TIMEOUT).
+// Two levels: a block arrives at its group's counter (block index mod
+// kBarGroups, one 128-byte line each); the last arrival of a group arrives at
+// the top counter, and the last group publishes the next generation.  At most
+// ceil(blocks / kBarGroups) atomics meet on one address.
+constexpr int kBarGroups = 16;
+struct GridBar {
+    unsigned group[kBarGroups][32];
+    unsigned top, gen;
+    int err, pad[29];
+};
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// `expected` blocks with indices 0..expected-1 take part (blockIdx.x is one);
+// group g holds the indices i with i mod kBarGroups == g.
+__device__ __noinline__ bool grid_barrier(GridBar* b, unsigned expected, unsigned long long limit_ns) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int good = 1;
+        const unsigned g = ld_acquire_gpu(&b->gen);
+        const unsigned grp = blockIdx.x % kBarGroups;
+        const unsigned ngroups = expected < (unsigned)kBarGroups ? expected : (unsigned)kBarGroups;
+        const unsigned in_grp = expected / kBarGroups + (grp < expected % kBarGroups ? 1u : 0u);
+        __threadfence();
+        bool last = false;
+        if (atomicAdd(&b->group[grp][0], 1u) == in_grp - 1) {
+            atomicExch(&b->group[grp][0], 0u);
+            __threadfence();
+            last = atomicAdd(&b->top, 1u) == ngroups - 1;
+        }
+        if (last) {
+            atomicExch(&b->top, 0u);
+            __threadfence();
+            st_release_gpu(&b->gen, g + 1);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (ld_acquire_gpu(&b->gen) == g) {
+                if (*(volatile int*)&b->err) {
+                    good = 0;
+                    break;
+                }
+                if (global_ns() - t0 > limit_ns) {
+                    atomicExch(&b->err, 1);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        ok = good && *(volatile int*)&b->err == 0;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;   // 2 s of global time
+
+template <class A>
+__global__ void __launch_bounds__(kT, std::is_same<A, DF>::value ? 4 : 3)
+    eng_persist(SlotDev* sl, const int* __restrict__ rm, const int* __restrict__ sm, double* pa, const void* rsq,
+                int nrb, int nsb, int mmax, int dmax, int cgs, int ns, int nsteps, GridBar* bar,
+                unsigned long long limit_ns) {
+    const int nb = gridDim.x;
+    const unsigned expected = gridDim.x;
+    const int ydots = (dmax + jt<A>() - 1) / jt<A>();
+#define QS_PHASE(count, body)                                 \
+    for (int v = blockIdx.x; v < (count); v += nb) {          \
+        body;                                                 \
+        __syncthreads();                                      \
+    }                                                         \
+    if (!grid_barrier(bar, expected, limit_ns)) return;
+    for (int step = 0; step < nsteps; ++step) {
+        QS_PHASE(nsb, spmv_block<A>(sl, sm, rsq, v));
+        QS_PHASE(nrb * ydots, dots_block<A>(sl, rm, mmax, 0, pa, v % nrb, v / nrb));
+        QS_PHASE(ns * (dmax + 1), reduce_block(sl, mmax, 0, pa, dmax, v % ns, v / ns));
+        QS_PHASE(nrb, update_block<A>(sl, rm, mmax, 0, pa, v));
+        QS_PHASE(ns, reduce_block(sl, mmax, 1, pa, 0, v, 0));
+        if (cgs) {
+            QS_PHASE(ns * mmax, reduce_block(sl, mmax, 2, pa, 0, v % ns, v / ns));
+            QS_PHASE(nrb, update_block<A>(sl, rm, mmax, 1, pa, v));
+            QS_PHASE(ns, reduce_block(sl, mmax, 3, pa, 0, v, 0));
+        }
+        QS_PHASE(nrb, scale_block<A>(sl, rm, 0, v));
+        if (blockIdx.x == 0)
+            for (int id = threadIdx.x; id < ns; id += blockDim.x) {
+                SlotDev& S = sl[id];
+                if (S.state != kSlotStep) continue;
+                S.j += 1;
+                if (S.j >= S.m) S.state = kSlotHold;
+            }
+        if (!grid_barrier(bar, expected, limit_ns)) return;
+    }
+#undef QS_PHASE
+}
+
+// A few barriers of a cooperative grid that expects `phantom` more blocks
+// than it has: with phantom > 0 the first barrier can never complete, so
+// every wait runs into its limit (the bounded-wait check of the barrier).
+__global__ void eng_barrier_check(GridBar* bar, int phantom, unsigned long long limit_ns, int rounds) {
+    for (int r = 0; r < rounds; ++r)
+        if (!grid_barrier(bar, gridDim.x + (unsigned)phantom, limit_ns)) return;
 }
 
 void Engine::launch_step() {
@@ -1290,13 +1615,110 @@ int Engine::steps_to_event() const {
     return best;
 }
 
+// Resident blocks of the persistent step (cooperative grid), once per device
+// and storage; 0 when the device cannot run it.
+static int persist_capacity(Store st) {
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, int> cap;
+    int dev = 0;
+    QS_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    const auto key = std::make_pair(dev, (int)st);
+    auto it = cap.find(key);
+    if (it != cap.end()) return it->second;
+    int coop = 0, nsm = 0, per_sm = 0;
+    QS_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    QS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    with_store(st, [&](auto tag) {
+        using A = decltype(tag);
+        QS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eng_persist<A>, kT, 0));
+    });
+    const int c = coop ? per_sm * nsm : 0;
+    cap[key] = c;
+    return c;
+}
+
+bool Engine::persistent_wanted() const {
+    const char* e = std::getenv("QS_PERSISTENT_STEP");
+    if (e && e[0] == '0') return false;
+    const int cap = persist_capacity(st_);
+    if (cap <= 0) return false;
+    if (e && e[0] == '1') return true;
+    // off unless asked for: on GB300 the graph replay measured faster at every
+    // size (the launch gaps between graph nodes cost less than the barriers)
+    return false;
+}
+
+void Engine::run_persistent(int nsteps) {
+    const int ns = (int)slots_.size();
+    const int ydots = (dmax_ + jt<double>() - 1) / jt<double>();
+    // as many blocks as the widest product / vector phase has virtual blocks,
+    // at most the resident capacity (fewer blocks make cheaper barriers; the
+    // reductions' small virtual blocks loop)
+    int widest = std::max(nsb_, nrb_ * ydots);
+    const int grid = std::max(1, std::min(persist_capacity(st_), widest));
+    if (!bar_.p) bar_.alloc(sizeof(GridBar));
+    QS_CUDA(cudaMemsetAsync(bar_.p, 0, sizeof(GridBar), s_));
+    const void* rsq = st_ == Store::DF ? rsqdf_.p : (st_ == Store::F32 ? rsq32_.p : rsq64_.p);
+    SlotDev* ds = dslots_.as<SlotDev>();
+    const int* rm = rmap_.as<int>();
+    const int* sm = smap_.as<int>();
+    double* pa = partial_.as<double>();
+    GridBar* bar = bar_.as<GridBar>();
+    int cgs = cgs_ ? 1 : 0;
+    unsigned long long limit = kBarrierLimitNs;
+    void* args[] = {&ds, &rm, &sm, &pa, &rsq, &nrb_, &nsb_, &mmax_, &dmax_, &cgs, (void*)&ns, &nsteps, &bar, &limit};
+    with_store(st_, [&](auto tag) {
+        using A = decltype(tag);
+        QS_CUDA(cudaLaunchCooperativeKernel((const void*)eng_persist<A>, dim3(grid), dim3(kT), args, 0, s_));
+    });
+    ++launches_;
+    GridBar h{};
+    QS_CUDA(cudaMemcpyAsync(&h, bar_.p, sizeof(GridBar), cudaMemcpyDeviceToHost, s_));
+    QS_CUDA(cudaStreamSynchronize(s_));
+    if (h.err) throw Error(QS_ERR_TIMEOUT, "a grid barrier of the persistent Lanczos step timed out");
+}
+
+void grid_barrier_check(int phantom, double limit_ms, int blocks) {
+    if (phantom < 0 || blocks < 1 || !(limit_ms > 0) || limit_ms > 2000)
+        throw Error(QS_ERR_ARGUMENT, "phantom >= 0, blocks >= 1 and 0 < limit_ms <= 2000 required");
+    int dev = 0, coop = 0, nsm = 0, per_sm = 0;
+    QS_CUDA(cudaGetDevice(&dev));
+    QS_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    QS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    QS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eng_barrier_check, kT, 0));
+    if (!coop || blocks > per_sm * nsm) throw Error(QS_ERR_UNSUPPORTED, "cooperative grid too large for this device");
+    cudaStream_t s = nullptr;
+    QS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    DevBuf bar(sizeof(GridBar));
+    GridBar h{};
+    cudaError_t e = cudaMemsetAsync(bar.p, 0, sizeof(GridBar), s);
+    GridBar* b = bar.as<GridBar>();
+    unsigned long long limit = (unsigned long long)(limit_ms * 1e6);
+    int rounds = 8;
+    void* args[] = {&b, &phantom, &limit, &rounds};
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void*)eng_barrier_check, dim3(blocks), dim3(kT), args, 0, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, bar.p, sizeof(GridBar), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) throw Error(QS_ERR_CUDA, cudaGetErrorString(e));
+    note_launches(1);
+    if (h.err) throw Error(QS_ERR_TIMEOUT, "grid barrier wait ran out");
+    if (h.gen != (unsigned)rounds) throw Error(QS_ERR_CUDA, "grid barrier completed a wrong number of rounds");
+}
+
 void Engine::run(int nsteps) {
     if (nsteps <= 0) return;
     sync_table();
     if (nrb_ == 0) return;
-    if (!exec_) capture();
-    for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
-    launches_ += step_launches_ * (int64_t)nsteps;
+    if (persistent_wanted()) {
+        run_persistent(nsteps);
+    } else {
+        if (!exec_) capture();
+        for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
+        launches_ += step_launches_ * (int64_t)nsteps;
+    }
     // mirror the device step counters
     for (auto& sl : slots_) {
         if (!sl.live || sl.d.state != kSlotStep) continue;
@@ -1478,7 +1900,7 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
             QS_CUDA(cudaStreamSynchronize(s_));
             if (err) {
                 QS_CUDA(cudaMemsetAsync(tc_err_.p, 0, sizeof(int), s_));
-                throw Error(QS_ERR_CUDA, "the tensor-core rotation timed out waiting for its MMAs");
+                throw Error(QS_ERR_TIMEOUT, "the tensor-core rotation timed out waiting for its MMAs");
             }
         }
     }

@@ -159,12 +159,18 @@ class Engine {
     void build_maps();
     void capture();
     void launch_step();
+    // The step as one cooperative launch of nsteps steps (eng_persist):
+    // chosen when every phase fits in one wave of resident blocks, forced by
+    // QS_PERSISTENT_STEP=1 and disabled by QS_PERSISTENT_STEP=0
+    bool persistent_wanted() const;
+    void run_persistent(int nsteps);
     Tiles tune(Op& op, int m, bool cv);
     Store st_;
     cudaStream_t s_;
     std::vector<Slot> slots_;
     DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_, rsq32_, ybuf_;
     DevBuf tc_err_;            // timeout flag of the tensor-core rotation
+    DevBuf bar_;               // grid barrier of the persistent step
     bool tc_rotate_ = true;    // QS_TC_ROTATE=0 keeps every rotation on eng_rotate
     size_t cap_y_ = 0;
     int nrb_ = 0, nsb_ = 0, mmax_ = 1, cap_slots_ = 0;
@@ -180,6 +186,12 @@ class Engine {
     int64_t launches_ = 0;
     friend struct EngineTuner;
 };
+
+// Runs `blocks` cooperative blocks through eight grid barriers (the persistent
+// step's barrier) that expect `phantom` blocks more than run: with phantom 0
+// they complete, otherwise every wait runs out after limit_ms and this throws
+// QS_ERR_TIMEOUT.
+void grid_barrier_check(int phantom, double limit_ms, int blocks);
 
 // Thick-restart Lanczos (Wu-Simon) on one slot, ARPACK's convergence test:
 // the state kept on the host between the slot's Hold events.

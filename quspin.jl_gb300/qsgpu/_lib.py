@@ -90,7 +90,7 @@ EXPORTS = (
     "qs_lanczos_run", "qs_lanczos_destroy", "qs_lanczos_coefficients", "qs_lanczos_complex", "qs_lanczos_rows",
     "qs_lanczos_combine", "qs_lanczos_overlaps", "qs_lanczos_ritz_matrix",
     "qs_basis_projection_rows", "qs_basis_project_from", "qs_basis_project_to", "qs_block_expm", "qs_op_export_csr", "qs_fp64_fma_rate", "qs_basis_create_general", "qs_expm_columns", "qs_evolve_stepwise",
-    "qs_device_alloc_count", "qs_eigs",
+    "qs_device_alloc_count", "qs_eigs", "qs_grid_barrier_check",
 )
 
 _lib = None
@@ -125,6 +125,8 @@ def load():
     L.qs_op_matvec.argtypes = [P, i32, P, P, i32, P, P, i32, i64, i32]
     L.qs_eigsh.argtypes = [P, ctypes.POINTER(EigshOpts), P, P, ctypes.POINTER(EigshInfo)]
     L.qs_eigs.argtypes = [P, ctypes.POINTER(EigshOpts), P, P, ctypes.POINTER(EigshInfo)]
+    L.qs_grid_barrier_check.argtypes = [i32, ctypes.c_double, i32]
+    L.qs_grid_barrier_check.restype = ctypes.c_int
     L.qs_expm_multiply.argtypes = [P, P, P, P, f64, i32, i32]
     L.qs_evolve.argtypes = [P, P, f64, P, i32, i32, f64, i32, i32, P]
     L.qs_op_set_stream.argtypes = [P, P]

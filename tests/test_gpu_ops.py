@@ -544,6 +544,7 @@ def test_transient_assembly_of_matrix_free_solvers(qs, ora, monkeypatch):
     built for the call and dropped after it: the same results as the
     matrix-free solve (QS_TRANSIENT_ASSEMBLY=0) and the operator left
     matrix-free (no stored nonzeros)."""
+    from qsgpu import _lib
     L = 16
     sym = dict(kblock=0, pblock=1, zblock=1)
     sp = models.j1j2(L, 1.0, 0.37)
@@ -558,7 +559,7 @@ def test_transient_assembly_of_matrix_free_solvers(qs, ora, monkeypatch):
         e = qs.eigsh(Q, k=3, which="SA", tol=1e-12, v0=v0, return_eigenvectors=False)
         st = qs.evolve(Q, v, 0.0, [0.5, 1.5], tol=1e-10)
         got[mode] = (e, st)
-        assert Q.nnz < 0
+        assert _lib.load().qs_op_nnz(Q._h) < 0   # not assembled after the calls
     M = ora.RefBasis(L, nup=8, pauli=False, **sym).dense(ora.consolidate_terms(sp))
     w = np.linalg.eigvalsh(M)[:3]
     assert np.max(np.abs(got["1"][0] - w)) <= 1e-10 * np.abs(w).max()
