@@ -93,7 +93,14 @@ QS_API int qs_basis_create_general(const qs_general_spec *spec, qs_basis **out);
 
 /* Replaces SpinBasis1D(L; ...) (src/basis.jl:622-777): enumerates the sector on
  * the device, keeps one representative per symmetric orbit and orders columns
- * as the reference's projector does (ascending orbit minimum). */
+ * as the reference's projector does (ascending orbit minimum).  When a later
+ * block's generator does not map the earlier blocks' eigenvectors onto one
+ * another (e.g. zAblock after a one-site translation), the sector comes from
+ * the reference's dense nullspace intersection (src/symmetry_basis.jl:199-212,
+ * at most 512 reduced columns, else QS_ERR_ARGUMENT with its message): columns
+ * are then nullspace vectors over the parent sector, operators on it are
+ * P^H A P, and the orbit queries below return QS_ERR_UNSUPPORTED.  The same
+ * holds for qs_basis_create_general. */
 QS_API int qs_basis_create(const qs_basis_spec *spec, qs_basis **out);
 QS_API void qs_basis_destroy(qs_basis *basis);
 
@@ -286,9 +293,9 @@ typedef struct {
  * reorthogonalisation replaces the ARPACK implicitly restarted Lanczos;
  * convergence is ARPACK's test ||r_i|| <= tol * max(eps^(2/3), |theta_i|).
  * Assembled operators (qs_op_assemble) run on the batched engine with one
- * operator (as qs_eigsh_batch).  A matrix-free operator whose assembled form
- * fits in a quarter of free device memory is assembled for the length of the
- * call and runs there too (the form is dropped on return; environment
+ * operator (as qs_eigsh_batch).  A matrix-free operator of at least 2^16
+ * states whose assembled form fits in a quarter of free device memory is
+ * assembled for the length of the call and runs there too (the form is dropped on return; environment
  * QS_TRANSIENT_ASSEMBLY=0 keeps the call matrix-free). */
 QS_API int qs_eigsh(qs_op *op, const qs_eigsh_opts *opts, double *values, void *vectors, qs_eigsh_info *info);
 

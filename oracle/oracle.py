@@ -308,6 +308,163 @@ def general_basis(L, nup=None, pauli=True, blocks=()):
     return RefBasis(L, nup=nup, pauli=pauli, _general=(perms, flips, qnums))
 
 
+class DenseSector:
+    """SpinBasis1D sectors through the reference's level-by-level intersection
+    with its dense nullspace branch (src/symmetry_basis.jl:57-213): explicit
+    dense projectors, the cyclic projector of the first generator, then per
+    generator the represented map P^H S P (entries with abs <= 5e-12 dropped),
+    its orbit walk when it is permutation-like, else the nullspace of
+    (represented - eigenvalue I) from an SVD with atol = rtol = 2e-10
+    (LinearAlgebra.nullspace, the reference's call).  Numpy restatement for
+    small parents; the nullspace basis is LAPACK's (as the reference's is
+    Julia's LAPACK), so only basis-independent quantities (P P^H, spectra)
+    are comparable with another implementation."""
+
+    def __init__(self, L, nup=None, a=1, kblock=None, pblock=None, zblock=None, pzblock=None, zAblock=None,
+                 zBblock=None):
+        st = _parent_state_list(L, nup)
+        self.L, self.nup = L, nup
+        self.parent_states = st
+        index = {int(s): i for i, s in enumerate(st)}
+        full = (1 << L) - 1
+        odd = sum(1 << (s - 1) for s in range(1, L + 1, 2))
+        even = sum(1 << (s - 1) for s in range(2, L + 1, 2))
+
+        def perm_map(perm):
+            def f(s):
+                t = 0
+                for site in range(1, L + 1):
+                    if s >> (site - 1) & 1:
+                        t |= 1 << (perm[site - 1] - 1)
+                return t
+            return f
+
+        order = L // a
+        trans = perm_map([(site + a - 1) % L + 1 for site in range(1, L + 1)])
+        par = perm_map([L - site + 1 for site in range(1, L + 1)])
+        gens = []
+        if kblock is not None:
+            k = int(kblock) % order
+            gens.append((trans, complex(np.cos(2 * np.pi * k / order), np.sin(2 * np.pi * k / order))))
+        for v, f in ((pblock, par), (zblock, lambda s: s ^ full), (pzblock, lambda s: par(s) ^ full),
+                     (zAblock, lambda s: s ^ odd), (zBblock, lambda s: s ^ even)):
+            if v is not None:
+                gens.append((f, complex(v)))
+        n = len(st)
+        P = self._cyclic(st, index, *gens[0])
+        for f, eig in gens[1:]:
+            P = self._intersect(P, st, index, f, eig)
+        if P.shape[1] == 0:
+            raise OracleError("the requested symmetry sector is empty")
+        self.P = P
+        self.Ns = P.shape[1]
+        self.n_parent = n
+
+    @staticmethod
+    def _cyclic(st, index, f, eig):
+        n = len(st)
+        seen = np.zeros(n, bool)
+        cols = []
+        for start in range(n):
+            if seen[start]:
+                continue
+            orbit = []
+            cur = start
+            while True:
+                orbit.append(cur)
+                seen[cur] = True
+                nxt = index[f(int(st[cur]))]
+                if nxt == start:
+                    break
+                cur = nxt
+            c = np.ones(len(orbit), complex)
+            for j in range(1, len(orbit)):
+                c[j] = c[j - 1] / eig
+            if abs(c[-1] - eig * c[0]) > max(2e-10, 2e-10 * max(abs(c[-1]), abs(eig * c[0]))):
+                continue
+            col = np.zeros(n, complex)
+            col[orbit] = c / np.linalg.norm(c)
+            cols.append(col)
+        return np.array(cols).T if cols else np.zeros((n, 0), complex)
+
+    @staticmethod
+    def _intersect(P, st, index, f, eig):
+        n, rd = P.shape
+        if rd == 0:
+            return P
+        perm = np.array([index[f(int(s))] for s in st])
+        SP = np.zeros_like(P)
+        SP[perm, :] = P              # S P with S[perm[j], j] = 1
+        R = P.conj().T @ SP
+        R[np.abs(R) <= 5e-12] = 0
+        nz = [np.flatnonzero(R[:, c]) for c in range(rd)]
+        perm_like = all(len(z) == 1 for z in nz)
+        if perm_like:
+            mrow = np.array([z[0] for z in nz])
+            mph = R[mrow, np.arange(rd)]
+            perm_like = np.all(np.abs(np.abs(mph) - 1) <= 2e-10) and len(set(mrow.tolist())) == rd
+        if perm_like:
+            seen = np.zeros(rd, bool)
+            cols = []
+            for start in range(rd):
+                if seen[start]:
+                    continue
+                orbit, ph = [], []
+                cur = start
+                while True:
+                    orbit.append(cur)
+                    seen[cur] = True
+                    ph.append(mph[cur])
+                    nxt = mrow[cur]
+                    if nxt == start:
+                        break
+                    cur = nxt
+                c = np.ones(len(orbit), complex)
+                for j in range(1, len(orbit)):
+                    c[j] = c[j - 1] * ph[j - 1] / eig
+                closure = c[-1] * ph[-1]
+                if abs(closure - eig * c[0]) > max(2e-10, 2e-10 * max(abs(closure), abs(eig * c[0]))):
+                    continue
+                col = np.zeros(rd, complex)
+                col[orbit] = c / np.linalg.norm(c)
+                cols.append(col)
+            Rp = np.array(cols).T if cols else np.zeros((rd, 0), complex)
+        else:
+            if rd > 512:
+                raise OracleError(f"the requested symmetry intersection requires a dense nullspace of dimension {rd}")
+            M = R - eig * np.eye(rd)
+            _, sv, vh = np.linalg.svd(M)
+            tol = max(2e-10, sv[0] * 2e-10)
+            rank = int(np.sum(sv > tol))
+            Rp = vh[rank:].conj().T
+        out = P @ Rp
+        out[np.abs(out) <= 5e-14] = 0
+        return out
+
+    def projector_span(self):
+        """P P^H over the parent sector (basis independent)."""
+        return self.P @ self.P.conj().T
+
+
+def _parent_state_list(L, nup):
+    if nup is None:
+        return np.arange(1 << L, dtype=np.uint64)
+    from math import comb
+    n = comb(L, nup)
+    out = np.zeros(n, dtype=np.uint64)
+    if nup == 0:
+        return out
+    s = (1 << nup) - 1
+    for i in range(n):
+        out[i] = s
+        if i == n - 1:
+            break
+        low = s & -s
+        nxt = s + low
+        s = nxt | (((nxt ^ s) >> 2) // low)
+    return out
+
+
 class RepBasis:
     """Representative-space restatement (orbit minima, group by closure)."""
 

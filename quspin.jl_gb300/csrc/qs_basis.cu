@@ -650,10 +650,21 @@ void basis_build(Basis& b) {
                     cplx a = char_value(h, kmom, nT), bb = char_value(H.elems[it->second], kmom, nT);
                     ok = std::fabs(a.re - bb.re) < 1e-9 && std::fabs(a.im - bb.im) < 1e-9;
                 }
-                if (!ok)
-                    throw Error(QS_ERR_UNSUPPORTED,
-                                "this combination of symmetry blocks needs the reference's dense nullspace "
-                                "intersection, which this engine does not implement");
+                if (!ok) {
+                    // the reference's intersection of this generator is not
+                    // permutation-like on the eigenvectors of the earlier ones:
+                    // build the sector level by level with explicit projectors
+                    // (qs_projector.cu)
+                    std::vector<ProjMap> maps;
+                    std::vector<cplx> eigs;
+                    for (size_t q = 0; q < gens.size(); ++q) {
+                        const Elem e = gens[q];
+                        maps.push_back([e, L](uint64_t st) { return elem_apply(e, st, L); });
+                        eigs.push_back(b.gens[q].eig);
+                    }
+                    basis_build_projector(b, maps, eigs, (int64_t)H.elems.size());
+                    return;
+                }
             }
         }
     }
@@ -797,10 +808,18 @@ void basis_build_general(Basis& b, const qs_general_spec& gs) {
                 const cplx a = h.chi, bb = H.elems[it->second].chi;
                 ok = std::fabs(a.re - bb.re) < 1e-9 && std::fabs(a.im - bb.im) < 1e-9;
             }
-            if (!ok)
-                throw Error(QS_ERR_UNSUPPORTED,
-                            "this combination of symmetry blocks needs the reference's dense nullspace "
-                            "intersection, which this engine does not implement");
+            if (!ok) {
+                // not permutation-like: the dense nullspace intersection (qs_projector.cu)
+                std::vector<ProjMap> maps;
+                std::vector<cplx> eigs;
+                for (size_t q = 0; q < gens.size(); ++q) {
+                    const GElem e = gens[q];
+                    maps.push_back([e, L](uint64_t st) { return gelem_apply(e, st, L); });
+                    eigs.push_back(b.gens[q].eig);
+                }
+                basis_build_projector(b, maps, eigs, (int64_t)H.elems.size());
+                return;
+            }
         }
     }
     std::vector<uint64_t> tables;
@@ -1643,6 +1662,10 @@ int64_t basis_projection_rows(const Basis& b, bool pcon) {
 
 void basis_project(Basis& b, bool pcon, int mode, const double* in, double* out, bool accumulate, bool device,
                    int ncols) {
+    if (b.dense_proj) {
+        basis_project_dense(b, pcon, mode, in, out, accumulate, device, ncols);
+        return;
+    }
     const int64_t rows = basis_projection_rows(b, pcon);
     const int64_t nin1 = mode == 0 ? b.n : rows, nout1 = mode == 0 ? rows : b.n;
     const int64_t nin = nin1 * ncols, nout = nout1 * ncols;

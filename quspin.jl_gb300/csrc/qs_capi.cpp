@@ -104,9 +104,17 @@ int qs_basis_requires_complex(const qs_basis* basis) { return basis && basis->b.
 
 int32_t qs_basis_group_order(const qs_basis* basis) { return basis ? basis->b.group.ng : 0; }
 
+// a basis from the dense nullspace intersection has no orbit structure
+static void no_orbits(const qs::Basis& b) {
+    if (b.dense_proj)
+        throw qs::Error(QS_ERR_UNSUPPORTED, "a sector from the dense nullspace intersection has no orbits; its "
+                                            "columns are general combinations of parent states");
+}
+
 int qs_basis_orbit_minima(const qs_basis* basis, uint64_t* out, int64_t n) {
     return guard([&] {
         const qs::Basis& b = basis->b;
+        no_orbits(b);
         if (n != b.n) throw qs::Error(QS_ERR_DIMENSION, "output length must equal Ns");
         if (!b.symmetric) {
             if (b.nup < 0) {
@@ -138,6 +146,7 @@ int qs_basis_orbit_minima(const qs_basis* basis, uint64_t* out, int64_t n) {
 int qs_basis_stabilizers(const qs_basis* basis, uint16_t* out, int64_t n) {
     return guard([&] {
         const qs::Basis& b = basis->b;
+        no_orbits(b);
         if (n != b.n) throw qs::Error(QS_ERR_DIMENSION, "output length must equal Ns");
         if (!b.symmetric) {
             for (int64_t i = 0; i < n; ++i) out[i] = 1;
@@ -149,6 +158,11 @@ int qs_basis_stabilizers(const qs_basis* basis, uint16_t* out, int64_t n) {
 
 int qs_basis_states(const qs_basis* basis, uint64_t* out, int64_t n) {
     if (!basis) return QS_ERR_ARGUMENT;
+    if (basis->b.dense_proj)
+        return guard([&] {
+            if (n != basis->b.n) throw qs::Error(QS_ERR_DIMENSION, "output length must equal Ns");
+            std::memcpy(out, basis->b.proj_reps.data(), n * sizeof(uint64_t));
+        });
     if (!basis->b.symmetric) return qs_basis_orbit_minima(basis, out, n);
     return guard([&] {
         qs::Basis& b = const_cast<qs::Basis&>(basis->b);
@@ -159,12 +173,23 @@ int qs_basis_states(const qs_basis* basis, uint64_t* out, int64_t n) {
 }
 
 int qs_basis_state_index(const qs_basis* basis, const uint64_t* states, int64_t n, int64_t* out) {
-    return guard([&] { qs::basis_index_of(const_cast<qs::Basis&>(basis->b), states, n, out); });
+    return guard([&] {
+        const qs::Basis& b = basis->b;
+        if (b.dense_proj) {
+            for (int64_t i = 0; i < n; ++i) {
+                auto it = b.proj_index.find(states[i]);
+                out[i] = it == b.proj_index.end() ? -1 : it->second;
+            }
+            return;
+        }
+        qs::basis_index_of(const_cast<qs::Basis&>(b), states, n, out);
+    });
 }
 
 int qs_basis_representative(const qs_basis* basis, const uint64_t* states, int64_t n, uint64_t* reps, double* norms,
                             double* amps, int32_t* status) {
     return guard([&] {
+        no_orbits(basis->b);
         qs::basis_representative(const_cast<qs::Basis&>(basis->b), states, n, reps, norms, amps, status);
     });
 }
@@ -221,10 +246,20 @@ int64_t qs_launch_count(void) { return qs::launches(); }
 int64_t qs_device_alloc_count(void) { return qs::device_allocs(); }
 
 int qs_op_assemble(qs_op* op) {
-    return guard([&] { qs::op_assemble(*op->op); });
+    return guard([&] {
+        if (op->op->dense) return;   // held as the dense P^H A P from creation
+        qs::op_assemble(*op->op);
+    });
 }
 
-int64_t qs_op_nnz(const qs_op* op) { return op->op->assembled ? op->op->asm_.nnz : -1; }
+int64_t qs_op_nnz(const qs_op* op) {
+    const qs::Op& o = *op->op;
+    if (o.dense) {
+        // off-diagonal stored entries of P^H A P, as the export lists them
+        return o.dense_offdiag_nnz;
+    }
+    return o.assembled ? o.asm_.nnz : -1;
+}
 
 int32_t qs_op_fixed_point_classes(const qs_op* op) {
     const qs::Op& o = *op->op;
@@ -234,6 +269,10 @@ int32_t qs_op_fixed_point_classes(const qs_op* op) {
 int qs_op_export_csr(qs_op* op, int64_t* rowptr, int64_t* cols, double* values, double* diag) {
     return guard([&] {
         if (!op || !rowptr || !diag) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
+        if (op->op->dense) {
+            qs::op_export_dense(*op->op, rowptr, cols, values, diag);
+            return;
+        }
         if (!op->op->assembled) throw qs::Error(QS_ERR_ARGUMENT, "assemble the operator first (qs_op_assemble)");
         if (op->op->asm_.nnz && (!cols || !values)) throw qs::Error(QS_ERR_ARGUMENT, "null argument");
         qs::op_export_csr(*op->op, rowptr, cols, values, diag);
@@ -248,6 +287,10 @@ int qs_op_set_diagonal(qs_op* op, const double* diagonal) {
         qs::Op& o = *op->op;
         o.user_diag.resize(o.basis->n);
         for (int64_t i = 0; i < o.basis->n; ++i) o.user_diag[i] = {diagonal[2 * i], diagonal[2 * i + 1]};
+        if (o.dense) {
+            qs::op_dense_apply_diagonal(o);
+            return;
+        }
         qs::op_prepare_device(o);
     });
 }

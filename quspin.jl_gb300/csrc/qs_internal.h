@@ -5,8 +5,11 @@
 
 #include <complex>
 #include <cstdint>
+#include <functional>
+#include <memory>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/qsgpu.h"
@@ -156,9 +159,32 @@ struct Basis {
     std::vector<GroupDesc> level_groups;
     std::vector<cplx> level0_table;  // [len * 64 + j]
     DevBuf d_level_groups, d_level0;
+    // a sector from the dense nullspace intersection (qs_projector.cu): the
+    // projector P (parent states x n) explicitly, columns in CSC order, the
+    // argmax state of each column and the state -> column lookup
+    bool dense_proj = false;
+    std::vector<uint64_t> proj_parent;
+    std::vector<int64_t> proj_colptr, proj_row;
+    std::vector<cplx> proj_val;
+    std::vector<uint64_t> proj_reps;
+    std::unordered_map<uint64_t, int64_t> proj_index;
+    DevBuf d_proj_colptr, d_proj_row, d_proj_val;        // CSC
+    DevBuf d_proj_rowptr, d_proj_rowcol, d_proj_rowval;  // CSR over parent rows
+    DevBuf d_proj_parent;
     cudaStream_t stream = nullptr;
     ~Basis();
 };
+
+// a symmetry map on the states of a basis (state -> image state)
+using ProjMap = std::function<uint64_t(uint64_t)>;
+// Builds b as the reference does when an intersection is not permutation-like
+// (qs_projector.cu); maps and eigenvalues in the reference's intersection
+// order; group_order_before_dense bounds the parent sector it accepts.
+void basis_build_projector(Basis& b, const std::vector<ProjMap>& maps, const std::vector<cplx>& eigs,
+                           int64_t group_order_before_dense);
+// basis_project (below) for such a basis
+void basis_project_dense(Basis& b, bool pcon, int mode, const double* in, double* out, bool accumulate, bool device,
+                         int ncols);
 
 }  // namespace qs
 #include "qs_assembled.h"
@@ -187,6 +213,14 @@ struct Op {
     int device = 0;                     // device current when the operator was created
     cudaStream_t copy_stream = nullptr; // read-back of host products (op_matvec_host_overlap)
     cudaEvent_t range_done[4] = {};
+    // an operator on a dense-nullspace basis: H = P^H A P (n x n complex,
+    // column-major) without and with the user diagonal, from the operator on
+    // the parent sector
+    bool dense = false;
+    std::unique_ptr<Basis> dense_parent_basis;
+    std::unique_ptr<Op> dense_parent_op;
+    DevBuf dense_base, dense_h;
+    int64_t dense_offdiag_nnz = 0;
     ~Op();
 };
 
@@ -225,6 +259,12 @@ struct MatvecCall {
     int64_t slice0 = 0, slice1 = -1; // sliced-ELL slices [slice0, slice1) only (-1: to the end)
 };
 void op_prepare_device(Op& op);
+// qs_projector.cu: operators on a dense-nullspace basis
+void op_build_dense(Op& op, const qs_term* terms, int nterms, int checks);
+void op_dense_apply_diagonal(Op& op);
+void op_matvec_dense(Op& op, const MatvecCall& c, cudaStream_t s);
+// H.data of such an operator: off-diagonal CSR (host) and the diagonal
+void op_export_dense(Op& op, int64_t* rowptr, int64_t* cols, double* values, double* diag);
 // qs_noalloc.cu
 size_t noalloc_vector_bytes();
 void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype, cplx beta, void* y, int y_dtype,
@@ -233,8 +273,9 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
 void op_assemble(Op& op);
 // drops the assembled form (the operator runs matrix-free again)
 void op_release_assembly(Op& op);
-// The Krylov solvers of a matrix-free operator run on its assembled form for
-// the length of one call when the form fits in a quarter of free memory:
+// The Krylov solvers of a matrix-free operator with at least 2^16 rows run on
+// its assembled form for the length of one call when the form fits in a
+// quarter of free memory:
 // assembly is one pass of the product kernel, and each product after it is an
 // order of magnitude cheaper than the matrix-free one.  The form is dropped
 // when the call returns (QS_TRANSIENT_ASSEMBLY=0 keeps the solvers matrix-free).

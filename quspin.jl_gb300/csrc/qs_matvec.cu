@@ -755,6 +755,10 @@ void op_prepare_device(Op& op) {
 }
 
 void op_matvec_device(Op& op, const MatvecCall& c, cudaStream_t s) {
+    if (op.dense) {
+        op_matvec_dense(op, c, s);
+        return;
+    }
     const Basis& b = *op.basis;
     MvArgs a = base_args(op);
     a.progs = op.d_progs.as<TermProg>();

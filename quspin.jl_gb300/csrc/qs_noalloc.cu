@@ -56,6 +56,9 @@ size_t noalloc_vector_bytes() { return kNoAllocVectorBytes; }
 
 void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype, cplx beta, void* y, int y_dtype,
                        int64_t nrhs) {
+    if (op.dense)
+        throw Error(QS_ERR_UNSUPPORTED, "the allocation-free matvec covers orbit bases, not a sector from the dense "
+                                        "nullspace intersection");
     const int64_t n = op.basis->n;
     auto bytes_of = [](int dt) -> size_t {
         switch (dt) {

@@ -284,6 +284,20 @@ Op* op_create(Basis* basis, const qs_term* terms, int nterms, const double* diag
     for (int64_t i = 0; i < (int64_t)op->user_diag.size(); ++i)
         if (op->user_diag[i].imag() != 0.0) diag_real = false;
     op->hermitian = (checks & QS_CHECK_HERM) ? true : (herm && diag_real);
+    if (b.dense_proj) {
+        // P^H A P from the operator on the parent sector (qs_projector.cu)
+        try {
+            QS_CUDA(cudaStreamCreateWithFlags(&op->own_stream, cudaStreamNonBlocking));
+            op->stream = op->own_stream;
+            op->commuting = false;
+            op->extracted = false;
+            op_build_dense(*op, terms, nterms, checks);
+        } catch (...) {
+            delete op;
+            throw;
+        }
+        return op;
+    }
     std::vector<TermProg> fwd, bwd;
     for (const Term& t : checked) {
         bool diag = is_diag_op(t.op);

@@ -25,6 +25,7 @@ SOURCES = [
     "qs_noalloc.cu",
     "qs_engine.cu",
     "qs_tools.cu",
+    "qs_projector.cu",
     "qs_dense.cpp",
     "qs_op.cpp",
     "qs_capi.cpp",

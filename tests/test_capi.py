@@ -72,7 +72,12 @@ def test_basis_argument_errors(qs, kwargs, msg):
         qs.SpinBasis1D(**kwargs)
 
 
-def test_unsupported_symmetry_combination(qs):
-    # zA after a one-site translation needs the reference's dense nullspace path
-    with pytest.raises(qs.ArgumentError):
-        qs.SpinBasis1D(6, kblock=0, zAblock=1)
+def test_dense_nullspace_guard(qs, ora):
+    # zA after a one-site translation needs the reference's dense nullspace
+    # intersection, which it refuses above 512 reduced columns with this
+    # message (src/symmetry_basis.jl:199-206); the check runs before any device work
+    dim = ora.RefBasis(14, kblock=0).Ns
+    msg = (f"the requested symmetry intersection requires a dense nullspace of dimension {dim}; "
+           "the guarded limit is 512")
+    with pytest.raises(qs.ArgumentError, match=re.escape(msg)):
+        qs.SpinBasis1D(14, kblock=0, zAblock=1)

@@ -540,15 +540,16 @@ def test_page_locked_output_written_in_place(qs, ora, prec):
 
 
 def test_transient_assembly_of_matrix_free_solvers(qs, ora, monkeypatch):
-    """eigsh / evolve / expm on a matrix-free operator run on an assembled form
-    built for the call and dropped after it: the same results as the
-    matrix-free solve (QS_TRANSIENT_ASSEMBLY=0) and the operator left
-    matrix-free (no stored nonzeros)."""
+    """eigsh / evolve on a matrix-free operator of at least 2^16 states run on an
+    assembled form built for the call and dropped after it: the same results
+    as the matrix-free solve (QS_TRANSIENT_ASSEMBLY=0) and ARPACK over the
+    oracle's product, and the operator left matrix-free (no stored nonzeros)."""
     from qsgpu import _lib
-    L = 16
-    sym = dict(kblock=0, pblock=1, zblock=1)
+    L = 24
+    sym = dict(kblock=0)
     sp = models.j1j2(L, 1.0, 0.37)
-    b = qs.SpinBasis1D(L, nup=8, pauli=False, **sym)
+    b = qs.SpinBasis1D(L, nup=12, pauli=False, **sym)
+    assert b.Ns >= 1 << 16
     Q = qs.QuantumLinearOperator(b, models.to_terms(qs, sp))
     v0 = models.seeded(b.Ns, seed=5)
     v = models.seeded(b.Ns, seed=6, complex_=True)
@@ -556,12 +557,15 @@ def test_transient_assembly_of_matrix_free_solvers(qs, ora, monkeypatch):
     got = {}
     for mode in ("1", "0"):
         monkeypatch.setenv("QS_TRANSIENT_ASSEMBLY", mode)
-        e = qs.eigsh(Q, k=3, which="SA", tol=1e-12, v0=v0, return_eigenvectors=False)
+        e = qs.eigsh(Q, k=2, which="SA", tol=1e-12, v0=v0, return_eigenvectors=False)
         st = qs.evolve(Q, v, 0.0, [0.5, 1.5], tol=1e-10)
         got[mode] = (e, st)
         assert _lib.load().qs_op_nnz(Q._h) < 0   # not assembled after the calls
-    M = ora.RefBasis(L, nup=8, pauli=False, **sym).dense(ora.consolidate_terms(sp))
-    w = np.linalg.eigvalsh(M)[:3]
-    assert np.max(np.abs(got["1"][0] - w)) <= 1e-10 * np.abs(w).max()
+    rep = ora.RepBasis(L, nup=12, pauli=False, **sym)
+    pk = ora.pack_terms(sp)
+    d = rep.diagonal(sp)
+    want, _ = ora.eigsh_arpack(lambda x: rep.matvec(sp, x, diag=d, packed=pk).real, b.Ns, 2, np.float64, v0=v0,
+                               tol=1e-13)
+    assert np.max(np.abs(np.sort(got["1"][0]) - np.sort(want))) <= 1e-10 * np.abs(want).max()
     assert np.max(np.abs(got["1"][0] - got["0"][0])) <= 1e-10 * np.abs(got["0"][0]).max()
     assert np.max(np.linalg.norm(got["1"][1] - got["0"][1], axis=0)) <= 1e-9
