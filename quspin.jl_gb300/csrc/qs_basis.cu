@@ -817,6 +817,7 @@ void basis_build_general(Basis& b, const qs_general_spec& gs) {
                     maps.push_back([e, L](uint64_t st) { return gelem_apply(e, st, L); });
                     eigs.push_back(b.gens[q].eig);
                 }
+                b.group.ng = (int)C.elems.size();   // the group order the sector reports
                 basis_build_projector(b, maps, eigs, (int64_t)H.elems.size());
                 return;
             }
