@@ -108,29 +108,53 @@ def test_grid_barrier_wait_is_bounded(qs):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp64df", "fp32"])
 def test_fused_update_bit_identical(qs, precision):
-    """Pass 0 of the Gram-Schmidt update with the second-pass dots taken from
-    the registers that held V (QS_FUSED_UPDATE=1, the default) against the
-    update followed by a second read of V (QS_FUSED_UPDATE=0)."""
-    old = os.environ.get("QS_FUSED_UPDATE")
+    """The first-pass dots and the pass-0 update with each row's vector
+    entries held in registers (the second-pass dots from the values that
+    served the update; QS_FUSED_UPDATE=1, the default) against the tiled dots
+    and the update followed by a second read of V (QS_FUSED_UPDATE=0)."""
+    saved = {k: os.environ.get(k) for k in ("QS_FUSED_UPDATE", "QS_PERSISTENT_STEP")}
     L = 20
     b = qs.SpinBasis1D(L, nup=10, pauli=False, kblock=0, pblock=1, zblock=1)
     H = qs.Hamiltonian(b, models.to_terms(qs, models.j1j2(L, 1.0, 0.37)))
     ops = sector_ops(qs, 14, 7, 0.3)
     got = {}
     try:
+        os.environ["QS_PERSISTENT_STEP"] = "0"
         for m in ("0", "1"):
             os.environ["QS_FUSED_UPDATE"] = m
-            os.environ["QS_PERSISTENT_STEP"] = "0"
             got[m] = (qs.eigsh(H, k=3, which="SA", tol=1e-12, v0=models.seeded(b.Ns, seed=4), precision=precision),
                       qs.eigsh_batch(ops, k=2, tol=1e-12, return_eigenvectors=True, precision=precision))
     finally:
-        os.environ.pop("QS_PERSISTENT_STEP", None)
-        if old is None:
-            os.environ.pop("QS_FUSED_UPDATE", None)
-        else:
-            os.environ["QS_FUSED_UPDATE"] = old
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     (a0, a1), (b0, b1) = got["0"], got["1"]
     assert np.array_equal(a0[0], b0[0]) and np.array_equal(a0[1], b0[1])
     assert np.array_equal(a1[0], b1[0])
     for x, y in zip(a1[1], b1[1]):
         assert np.array_equal(x, y)
+
+
+def test_fused_update_at_config_size(qs):
+    """The fused kernels on the 4.7 M-state sector (1150 row blocks): the same
+    eigenvalue bits as the unfused ones in the three precision forms."""
+    saved = os.environ.get("QS_FUSED_UPDATE")
+    L = 32
+    b = qs.SpinBasis1D(L, nup=16, pauli=False, kblock=0, pblock=1, zblock=1)
+    H = qs.Hamiltonian(b, models.to_terms(qs, models.j1j2(L, 1.0, 0.5)))
+    v0 = models.seeded(b.Ns, seed=2)
+    out = {}
+    try:
+        for m in ("0", "1"):
+            os.environ["QS_FUSED_UPDATE"] = m
+            out[m] = [qs.eigsh(H, k=1, which="SA", tol=1e-10, v0=v0, return_eigenvectors=False, precision=p)[0]
+                      for p in ("fp64", "fp64df", "fp32")]
+    finally:
+        if saved is None:
+            os.environ.pop("QS_FUSED_UPDATE", None)
+        else:
+            os.environ["QS_FUSED_UPDATE"] = saved
+    assert out["0"] == out["1"]
+    assert abs(out["1"][0] + 12.0) < 1e-10 * 12   # the Majumdar-Ghosh energy -3L/8 = -12
