@@ -351,6 +351,8 @@ class DenseSector:
             if v is not None:
                 gens.append((f, complex(v)))
         n = len(st)
+        self._gens = gens
+        self._index = index
         P = self._cyclic(st, index, *gens[0])
         for f, eig in gens[1:]:
             P = self._intersect(P, st, index, f, eig)
@@ -444,6 +446,12 @@ class DenseSector:
     def projector_span(self):
         """P P^H over the parent sector (basis independent)."""
         return self.P @ self.P.conj().T
+
+    def generators(self):
+        """[(perm, eigenvalue)] of the requested generators in intersection
+        order: perm[i] is the parent index of the image of parent state i."""
+        st = self.parent_states
+        return [(np.array([self._index[f(int(s))] for s in st]), eig) for f, eig in self._gens]
 
 
 def _parent_state_list(L, nup):

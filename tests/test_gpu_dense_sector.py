@@ -55,6 +55,11 @@ def test_dense_sector_against_oracle(qs, ora, sym):
     # orthonormal columns spanning the oracle's sector
     assert np.max(np.abs(P.conj().T @ P - np.eye(b.Ns))) < 1e-12
     assert np.max(np.abs(P @ P.conj().T - ref.projector_span())) < 1e-10
+    # every column is an eigenvector of every requested generator (G P = lambda P)
+    for perm, lam in ref.generators():
+        GP = np.zeros_like(P)
+        GP[perm, :] = P
+        assert np.max(np.abs(GP - lam * P)) < 1e-10
     # the states are the argmax rows of the columns (first wins)
     states = b.states
     for c in range(b.Ns):
