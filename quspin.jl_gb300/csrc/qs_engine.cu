@@ -169,11 +169,10 @@ template <class A> __device__ __forceinline__ char* colp(const SlotDev& S, int c
 // y = col(j + 1) = H col(j) on every stepping slot: sliced ELL, one thread per
 // row, the slot's value table staged in shared memory.
 template <class A, bool CV, bool CM, bool PACKED>
-__device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA<A>* tab, bool smem_tab,
+__device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t s0, int64_t s1, const CA<A>* tab, bool smem_tab,
                                           const A* rsq) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     const int64_t n = S.n;
-    const int64_t s0 = lb * S.spb, s1 = min(S.nslices, s0 + S.spb);
     const void* x = colp<A>(S, S.j);
     void* y = colp<A>(S, S.j + 1);
     const int cb = S.code_bits;
@@ -215,6 +214,21 @@ __device__ __forceinline__ void spmv_rows(const SlotDev& S, int64_t lb, const CA
     }
 }
 
+// the slot's slices [s0, s1) of y = col(j + 1) = H col(j)
+template <class A>
+__device__ __forceinline__ void spmv_slices(const SlotDev& S, int64_t s0, int64_t s1, const CA<A>* tab, bool smem_tab,
+                                            const A* rsq) {
+    if (S.packed) {
+        if (!S.cv) spmv_rows<A, false, false, true>(S, s0, s1, tab, smem_tab, rsq);
+        else if (!S.cm) spmv_rows<A, true, false, true>(S, s0, s1, tab, smem_tab, rsq);
+        else spmv_rows<A, true, true, true>(S, s0, s1, tab, smem_tab, rsq);
+    } else {
+        if (!S.cv) spmv_rows<A, false, false, false>(S, s0, s1, tab, smem_tab, rsq);
+        else if (!S.cm) spmv_rows<A, true, false, false>(S, s0, s1, tab, smem_tab, rsq);
+        else spmv_rows<A, true, true, false>(S, s0, s1, tab, smem_tab, rsq);
+    }
+}
+
 template <class A>
 __device__ __forceinline__ void spmv_block(const SlotDev* sl, const int* __restrict__ smap,
                                            const void* __restrict__ rsqt, int bx) {
@@ -229,15 +243,7 @@ __device__ __forceinline__ void spmv_block(const SlotDev* sl, const int* __restr
         for (int i = threadIdx.x; i <= S.max_stab; i += blockDim.x) rsq[i] = ldrsq<A>(rsqt, i);
     __syncthreads();
     const int64_t lb = bx - S.sb_begin;
-    if (S.packed) {
-        if (!S.cv) spmv_rows<A, false, false, true>(S, lb, tab, smem_tab, rsq);
-        else if (!S.cm) spmv_rows<A, true, false, true>(S, lb, tab, smem_tab, rsq);
-        else spmv_rows<A, true, true, true>(S, lb, tab, smem_tab, rsq);
-    } else {
-        if (!S.cv) spmv_rows<A, false, false, false>(S, lb, tab, smem_tab, rsq);
-        else if (!S.cm) spmv_rows<A, true, false, false>(S, lb, tab, smem_tab, rsq);
-        else spmv_rows<A, true, true, false>(S, lb, tab, smem_tab, rsq);
-    }
+    spmv_slices<A>(S, lb * S.spb, min(S.nslices, lb * S.spb + S.spb), tab, smem_tab, rsq);
 }
 
 template <class A>
@@ -1446,6 +1452,209 @@ static int launch_step_t(const SlotDev* ds, SlotDev* dsw, const int* rm, const i
     return n + 2;
 }
 
+// ------------------------------------------------------------ cluster step
+// The Lanczos steps of every stepping slot, one thread-block cluster per
+// slot, in one launch that runs the steps up to the next Hold event: the
+// cluster's CTAs split the slot's slices (and so its rows), every phase
+// works on the CTA's own rows, and the per-step reductions (the first-pass
+// dots and ||w||^2, ||w'||^2 and the second-pass dots, ||w''||^2) cross the
+// cluster through distributed shared memory: each CTA leaves its block sums
+// in its shared memory, a cluster barrier (barrier.cluster, release /
+// acquire) separates the phases, and every CTA adds the CTAs' sums in rank
+// order, so all of them hold the same coefficients and take the same DGKS
+// decision without a broadcast.  CTA 0 writes the step's record column; the
+// slot's row range ends on a cluster barrier before the next product gathers
+// from it.  Nothing crosses clusters, so a slot's result does not depend on
+// the others; the reduction order (one partial per CTA) differs from the
+// graph replay's (one per row block), so results agree to rounding.
+__device__ __forceinline__ uint32_t cl_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cl_size() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cl_id() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cl_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// a double in CTA `rank`'s shared memory at the address of p in this CTA's
+__device__ __forceinline__ double cl_ld(const double* p, uint32_t rank) {
+    uint32_t ra;
+    double v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(smem_addr(p)), "r"(rank));
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra) : "memory");
+    return v;
+}
+
+template <class A, bool CV>
+__device__ __forceinline__ void cluster_steps(SlotDev& Ls, SlotDev* Sg, int nsteps, const CA<A>* tab, bool smem_tab,
+                                              const A* rsq, double* part1, double* part2, double* h1, double* h2,
+                                              CA<A>* hs, double* scal, double* shb) {
+    const uint32_t C = cl_size(), rank = cl_rank();
+    const int m = Ls.m, orth = Ls.orth, ld = m + 1;
+    const int64_t s0 = Ls.nslices * (int64_t)rank / C, s1 = Ls.nslices * (int64_t)(rank + 1) / C;
+    const int64_t r0 = min(Ls.n, s0 * kSellSlice), r1 = min(Ls.n, s1 * kSellSlice);
+    int j = Ls.j;
+    for (int step = 0; step < nsteps && j < m; ++step) {
+        if (threadIdx.x == 0) Ls.j = j;
+        __syncthreads();
+        // product over this CTA's slices: col(j + 1) = H col(j)
+        spmv_slices<A>(Ls, s0, s1, tab, smem_tab, rsq);
+        __syncthreads();
+        // first-pass dots over this CTA's rows (and ||w||^2 for DGKS)
+        const int nv = j + 1;
+        const int first = orth == 2 ? j : 0;
+        const bool want_wn = orth == 1;
+        const void* w = colp<A>(Ls, j + 1);
+        A wn = zero<A>();
+        for (int i0 = first; i0 < nv; i0 += jt<A>()) {
+            A re[jt<A>()], im[jt<A>()];
+#pragma unroll
+            for (int q = 0; q < jt<A>(); ++q) re[q] = im[q] = zero<A>();
+            dots_rows<A, CV>(Ls, r0, r1, i0, nv, w, re, im, want_wn && i0 == first, wn);
+            dots_epilogue<A>(re, im, CV, i0, nv, i0, part1);
+        }
+        {
+            const double t = block_sum(wn, shb);
+            if (threadIdx.x == 0) part1[m * 2] = t;
+        }
+        cl_sync();
+        // the cluster's sums, in rank order, in every CTA
+        for (int i = first + threadIdx.x; i <= j; i += blockDim.x) {
+            double re = 0, im = 0;
+            for (uint32_t r = 0; r < C; ++r) {
+                re += cl_ld(&part1[i * 2], r);
+                im += cl_ld(&part1[i * 2 + 1], r);
+            }
+            h1[i * 2] = re;
+            h1[i * 2 + 1] = im;
+        }
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (uint32_t r = 0; r < C; ++r) t += cl_ld(&part1[m * 2], r);
+            scal[0] = t;
+            // the three-term recurrence takes beta_{j-1} from the record
+            if (orth == 2 && j > 0) {
+                const double2 b = Ls.rec[(size_t)(j - 1) * ld + j];
+                h1[(j - 1) * 2] = b.x;
+                h1[(j - 1) * 2 + 1] = b.y;
+            }
+        }
+        __syncthreads();
+        // pass 0: w' = w - V h1 over this CTA's rows, ||w'||^2 and the
+        // second-pass dots V^* w'
+        const int first_u = orth == 2 ? (j > 0 ? j - 1 : 0) : 0;
+        for (int t = first_u + threadIdx.x; t < nv; t += blockDim.x)
+            hs[t] = CA<A>{from_d<A>(h1[t * 2]), from_d<A>(h1[t * 2 + 1])};
+        __syncthreads();
+        {
+            const A nacc = update_rows<A, CV>(Ls, r0, r1, first_u, nv, hs);
+            const double t = block_sum(nacc, shb);
+            if (threadIdx.x == 0) part2[m * 2] = t;
+        }
+        if (orth != 2)
+            for (int c0 = 0; c0 < nv; c0 += jt<A>()) {
+                A re[jt<A>()], im[jt<A>()], dummy = zero<A>();
+#pragma unroll
+                for (int q = 0; q < jt<A>(); ++q) re[q] = im[q] = zero<A>();
+                dots_rows<A, CV>(Ls, r0, r1, c0, nv, w, re, im, false, dummy);
+                dots_epilogue<A>(re, im, CV, c0, nv, c0, part2);
+            }
+        cl_sync();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (uint32_t r = 0; r < C; ++r) t += cl_ld(&part2[m * 2], r);
+            const double nb = sqrt(fmax(t, 0.0));
+            const bool second = orth == 0 || (orth == 1 && nb < 0.717 * sqrt(fmax(scal[0], 0.0)));
+            scal[1] = nb;
+            scal[2] = second ? 1.0 : 0.0;
+        }
+        if (orth != 2)
+            for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+                double re = 0, im = 0;
+                for (uint32_t r = 0; r < C; ++r) {
+                    re += cl_ld(&part2[i * 2], r);
+                    im += cl_ld(&part2[i * 2 + 1], r);
+                }
+                h2[i * 2] = re;
+                h2[i * 2 + 1] = im;
+            }
+        __syncthreads();
+        double2* col = Ls.rec + (size_t)j * ld;
+        double nb = scal[1];
+        if (scal[2] == 0.0) {
+            if (rank == 0 && threadIdx.x == 0) {
+                for (int q = first_u; q <= j; ++q) col[q] = make_double2(h1[q * 2], h1[q * 2 + 1]);
+                col[j + 1] = make_double2(nb, 0.0);
+            }
+        } else {
+            // second pass: w'' = w' - V h2, the record column h1 + h2
+            if (rank == 0)
+                for (int i = threadIdx.x; i <= j; i += blockDim.x)
+                    col[i] = make_double2(h1[i * 2] + h2[i * 2], h1[i * 2 + 1] + h2[i * 2 + 1]);
+            for (int t = threadIdx.x; t < nv; t += blockDim.x)
+                hs[t] = CA<A>{from_d<A>(h2[t * 2]), from_d<A>(h2[t * 2 + 1])};
+            __syncthreads();
+            const A nacc = update_rows<A, CV>(Ls, r0, r1, 0, nv, hs);
+            const double t3 = block_sum(nacc, shb);
+            if (threadIdx.x == 0) part1[m * 2] = t3;
+            cl_sync();
+            if (threadIdx.x == 0) {
+                double t = 0;
+                for (uint32_t r = 0; r < C; ++r) t += cl_ld(&part1[m * 2], r);
+                scal[1] = sqrt(fmax(t, 0.0));
+                if (rank == 0) col[j + 1] = make_double2(scal[1], 0.0);
+            }
+            __syncthreads();
+            nb = scal[1];
+        }
+        // col(j + 1) /= beta over this CTA's rows
+        const A f = from_d<A>(nb > 0 ? 1.0 / nb : 0.0);
+        scale_rows<A, CV>(colp<A>(Ls, j + 1), r0, r1, f);
+        cl_sync();
+        ++j;
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        Sg->j = j;
+        if (j >= m) Sg->state = kSlotHold;
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kT, 2) eng_cluster(SlotDev* sl, const int* __restrict__ cmap, int nsteps,
+                                                     const void* __restrict__ rsqt) {
+    __shared__ SlotDev Ls;
+    __shared__ CA<A> tab[1024];
+    __shared__ A rsq[kMaxGroup + 1];
+    __shared__ double part1[(kMaxM + 1) * 2], part2[(kMaxM + 1) * 2], h1[kMaxM * 2], h2[kMaxM * 2];
+    __shared__ CA<A> hs[kMaxM];
+    __shared__ double scal[4], shb[kT / 32];
+    SlotDev* Sg = &sl[cmap[cl_id()]];
+    if (threadIdx.x == 0) Ls = *Sg;
+    __syncthreads();
+    if (Ls.state == kSlotStepCluster) {
+        const bool smem_tab = Ls.ncodes <= 1024;
+        if (smem_tab)
+            for (int i = threadIdx.x; i < Ls.ncodes; i += blockDim.x) tab[i] = ldtab<A>(Ls, i);
+        if (Ls.stab)
+            for (int i = threadIdx.x; i <= Ls.max_stab; i += blockDim.x) rsq[i] = ldrsq<A>(rsqt, i);
+        __syncthreads();
+        if (Ls.cv)
+            cluster_steps<A, true>(Ls, Sg, nsteps, tab, smem_tab, rsq, part1, part2, h1, h2, hs, scal, shb);
+        else
+            cluster_steps<A, false>(Ls, Sg, nsteps, tab, smem_tab, rsq, part1, part2, h1, h2, hs, scal, shb);
+    }
+    cl_sync();   // no CTA leaves while another may still read its shared memory
+}
+
 // ------------------------------------------------------------ persistent step
 // The same step as launch_step_t in one cooperative launch: every phase runs
 // the kernels' block bodies over the same virtual block indices (so each
@@ -1708,24 +1917,90 @@ void grid_barrier_check(int phantom, double limit_ms, int blocks) {
     if (h.gen != (unsigned)rounds) throw Error(QS_ERR_CUDA, "grid barrier completed a wrong number of rounds");
 }
 
+// Which stepping slots take the cluster step: automatically those with at
+// most kClusterRows rows.  The cluster step gives a slot eight CTAs, which
+// suits small slots (measured on GB300: 1.3-2.2x the graph replay for slots of
+// 700 to 12,900 rows) and starves large ones (0.86x at 28,000 rows, 0.6x for
+// the 26 sectors of J1-J2 L=24 with 104,000 rows each).  The choice depends
+// on the slot alone, so a slot's result is the same in any batch.
+constexpr int64_t kClusterRows = 16384;
+
+bool Engine::cluster_wanted(const SlotDev& d) const {
+    const char* e = std::getenv("QS_CLUSTER_STEP");
+    if (e && e[0] == '0') return false;
+    if (e && e[0] == '1') return true;
+    if (persistent_wanted()) return false;
+    return d.n <= kClusterRows;
+}
+
+void Engine::run_cluster(const std::vector<int>& ids, int nsteps) {
+    if (ids.empty()) return;
+    if (ids.size() * sizeof(int) > cap_cmap_) {
+        cap_cmap_ = std::max<size_t>(64, ids.size() * sizeof(int) * 2);
+        cmap_.alloc(cap_cmap_);
+    }
+    QS_CUDA(cudaMemcpyAsync(cmap_.p, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, s_));
+    const int C = 8;   // portable cluster size
+    const void* rsq = st_ == Store::DF ? rsqdf_.p : (st_ == Store::F32 ? rsq32_.p : rsq64_.p);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(ids.size() * C));
+    cfg.blockDim = dim3(kT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s_;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SlotDev* ds = dslots_.as<SlotDev>();
+    const int* cm = cmap_.as<int>();
+    with_store(st_, [&](auto tag) {
+        using A = decltype(tag);
+        QS_CUDA(cudaLaunchKernelEx(&cfg, eng_cluster<A>, ds, cm, nsteps, rsq));
+    });
+    ++launches_;
+}
+
 void Engine::run(int nsteps) {
     if (nsteps <= 0) return;
+    // small slots step in the cluster step, marked so that the graph-replayed
+    // kernels skip them; the others in the graph replay (or the persistent step)
+    std::vector<int> cl;
+    bool rest = false;
+    for (int i = 0; i < (int)slots_.size(); ++i) {
+        Slot& sl = slots_[i];
+        if (!sl.live || sl.d.state != kSlotStep) continue;
+        if (cluster_wanted(sl.d)) {
+            sl.d.state = kSlotStepCluster;
+            cl.push_back(i);
+            dirty_ = true;
+        } else {
+            rest = true;
+        }
+    }
     sync_table();
     if (nrb_ == 0) return;
-    if (persistent_wanted()) {
-        run_persistent(nsteps);
-    } else {
-        if (!exec_) capture();
-        for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
-        launches_ += step_launches_ * (int64_t)nsteps;
+    run_cluster(cl, nsteps);
+    if (rest) {
+        if (persistent_wanted()) {
+            run_persistent(nsteps);
+        } else {
+            if (!exec_) capture();
+            for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
+            launches_ += step_launches_ * (int64_t)nsteps;
+        }
     }
-    // mirror the device step counters
+    // mirror the device step counters (the cluster step leaves its slots in
+    // kSlotStepCluster or Hold on the device; the next table upload restores Step)
     for (auto& sl : slots_) {
-        if (!sl.live || sl.d.state != kSlotStep) continue;
+        if (!sl.live || (sl.d.state != kSlotStep && sl.d.state != kSlotStepCluster)) continue;
         const int adv = std::min(nsteps, sl.d.m - sl.d.j);
         sl.d.j += adv;
         sl.matvecs += adv;
-        if (sl.d.j >= sl.d.m) sl.d.state = kSlotHold;
+        sl.d.state = sl.d.j >= sl.d.m ? kSlotHold : kSlotStep;
+        dirty_ = dirty_ || !cl.empty();
     }
 }
 

@@ -34,7 +34,10 @@ namespace qs {
 
 using cd = std::complex<double>;
 
-enum SlotState : int32_t { kSlotIdle = 0, kSlotStep = 1, kSlotRotate = 2, kSlotHold = 3, kSlotNormalize = 4 };
+// kSlotStepCluster: stepping in the cluster step (eng_cluster), which the
+// graph-replayed step kernels skip
+enum SlotState : int32_t { kSlotIdle = 0, kSlotStep = 1, kSlotRotate = 2, kSlotHold = 3, kSlotNormalize = 4,
+                           kSlotStepCluster = 5 };
 
 // Device descriptor of one slot.
 struct SlotDev {
@@ -164,6 +167,11 @@ class Engine {
     // QS_PERSISTENT_STEP=1 and disabled by QS_PERSISTENT_STEP=0
     bool persistent_wanted() const;
     void run_persistent(int nsteps);
+    // The steps of the listed slots up to their next Hold event as one launch
+    // with a thread-block cluster per slot (eng_cluster): chosen per slot for
+    // small slots, forced by QS_CLUSTER_STEP=1, disabled by =0
+    bool cluster_wanted(const SlotDev& d) const;
+    void run_cluster(const std::vector<int>& ids, int nsteps);
     Tiles tune(Op& op, int m, bool cv);
     Store st_;
     cudaStream_t s_;
@@ -171,6 +179,8 @@ class Engine {
     DevBuf dslots_, rmap_, smap_, partial_, rsq64_, rsqdf_, rsq32_, ybuf_;
     DevBuf tc_err_;            // timeout flag of the tensor-core rotation
     DevBuf bar_;               // grid barrier of the persistent step
+    DevBuf cmap_;              // stepping slot of each cluster (cluster step)
+    size_t cap_cmap_ = 0;
     bool tc_rotate_ = true;    // QS_TC_ROTATE=0 keeps every rotation on eng_rotate
     size_t cap_y_ = 0;
     int nrb_ = 0, nsb_ = 0, mmax_ = 1, cap_slots_ = 0;

@@ -22,12 +22,14 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture
 def mode_env():
-    old = os.environ.get("QS_PERSISTENT_STEP")
+    old = {k: os.environ.get(k) for k in ("QS_PERSISTENT_STEP", "QS_CLUSTER_STEP")}
+    os.environ["QS_CLUSTER_STEP"] = "0"   # the graph replay and the persistent form
     yield
-    if old is None:
-        os.environ.pop("QS_PERSISTENT_STEP", None)
-    else:
-        os.environ["QS_PERSISTENT_STEP"] = old
+    for k, v in old.items():
+        if v is None:
+            os.environ.pop(k, None)
+        else:
+            os.environ[k] = v
 
 
 def both_modes(fn):
@@ -112,7 +114,7 @@ def test_fused_update_bit_identical(qs, precision):
     entries held in registers (the second-pass dots from the values that
     served the update; QS_FUSED_UPDATE=1, the default) against the tiled dots
     and the update followed by a second read of V (QS_FUSED_UPDATE=0)."""
-    saved = {k: os.environ.get(k) for k in ("QS_FUSED_UPDATE", "QS_PERSISTENT_STEP")}
+    saved = {k: os.environ.get(k) for k in ("QS_FUSED_UPDATE", "QS_PERSISTENT_STEP", "QS_CLUSTER_STEP")}
     L = 20
     b = qs.SpinBasis1D(L, nup=10, pauli=False, kblock=0, pblock=1, zblock=1)
     H = qs.Hamiltonian(b, models.to_terms(qs, models.j1j2(L, 1.0, 0.37)))
@@ -120,6 +122,7 @@ def test_fused_update_bit_identical(qs, precision):
     got = {}
     try:
         os.environ["QS_PERSISTENT_STEP"] = "0"
+        os.environ["QS_CLUSTER_STEP"] = "0"
         for m in ("0", "1"):
             os.environ["QS_FUSED_UPDATE"] = m
             got[m] = (qs.eigsh(H, k=3, which="SA", tol=1e-12, v0=models.seeded(b.Ns, seed=4), precision=precision),
@@ -158,3 +161,38 @@ def test_fused_update_at_config_size(qs):
             os.environ["QS_FUSED_UPDATE"] = saved
     assert out["0"] == out["1"]
     assert abs(out["1"][0] + 12.0) < 1e-10 * 12   # the Majumdar-Ghosh energy -3L/8 = -12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64df", "fp32"])
+def test_cluster_step(qs, ora, precision):
+    """QS_CLUSTER_STEP=1: a thread-block cluster per slot runs the steps up to
+    each Hold event, the reductions crossing the cluster through distributed
+    shared memory.  Its reduction order differs from the graph replay's, so
+    the eigenvalues agree to rounding; a slot's result does not depend on the
+    other slots (bit-identical alone and in the batch); against the dense
+    spectrum of every sector."""
+    saved = os.environ.get("QS_CLUSTER_STEP")
+    ops = sector_ops(qs, 14, 7, 0.3)
+    try:
+        os.environ["QS_CLUSTER_STEP"] = "0"
+        g = qs.eigsh_batch(ops, k=2, tol=1e-12, precision=precision)
+        os.environ["QS_CLUSTER_STEP"] = "1"
+        c = qs.eigsh_batch(ops, k=2, tol=1e-12, precision=precision)
+        alone = [qs.eigsh_batch([op], k=2, tol=1e-12, precision=precision)[0] for op in ops[:4]]
+        L = 20
+        b = qs.SpinBasis1D(L, nup=10, pauli=False, kblock=0, pblock=1, zblock=1)
+        H = qs.Hamiltonian(b, models.to_terms(qs, models.j1j2(L, 1.0, 0.37)))
+        v0 = models.seeded(b.Ns, seed=4)
+        e1 = qs.eigsh(H, k=3, which="SA", tol=1e-12, v0=v0, precision=precision, return_eigenvectors=False)
+        os.environ["QS_CLUSTER_STEP"] = "0"
+        e0 = qs.eigsh(H, k=3, which="SA", tol=1e-12, v0=v0, precision=precision, return_eigenvectors=False)
+    finally:
+        if saved is None:
+            os.environ.pop("QS_CLUSTER_STEP", None)
+        else:
+            os.environ["QS_CLUSTER_STEP"] = saved
+    scale = np.abs(g).max()
+    assert np.max(np.abs(c - g)) <= 1e-10 * scale
+    for i, a in enumerate(alone):
+        assert np.array_equal(a, c[i])
+    assert np.max(np.abs(np.sort(e1) - np.sort(e0))) <= 1e-10 * np.abs(e0).max()
