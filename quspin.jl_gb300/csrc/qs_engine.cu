@@ -1917,30 +1917,68 @@ void grid_barrier_check(int phantom, double limit_ms, int blocks) {
     if (h.gen != (unsigned)rounds) throw Error(QS_ERR_CUDA, "grid barrier completed a wrong number of rounds");
 }
 
-// Which stepping slots take the cluster step: automatically those with at
-// most kClusterRows rows.  The cluster step gives a slot eight CTAs, which
-// suits small slots (measured on GB300: 1.3-2.2x the graph replay for slots of
-// 700 to 12,900 rows) and starves large ones (0.86x at 28,000 rows, 0.6x for
-// the 26 sectors of J1-J2 L=24 with 104,000 rows each).  The choice depends
-// on the slot alone, so a slot's result is the same in any batch.
-constexpr int64_t kClusterRows = 16384;
+// Which stepping slots take the cluster step, and with how many CTAs: by the
+// slot's own size only, so that a slot's result is the same alone and in any
+// batch.  Measured on GB300 against the graph replay: eight CTAs per slot
+// 1.3-2.2x faster for slots of 700 to 9,300 rows; sixteen CTAs for 8,400 to
+// 29,000 rows (1.9x at 8,400, 1.23x at 29,000 rows alone, even for the 22
+// sectors of J1-J2 L=22 at 32,000 rows); larger slots are faster on the graph
+// replay (0.6-0.7x for the 26 sectors of L=24 at 104,000 rows), whose kernels
+// spread a slot over the whole GPU.
+constexpr int64_t kClusterRows8 = 8192, kClusterRows16 = 32768;
 
-bool Engine::cluster_wanted(const SlotDev& d) const {
+int Engine::cluster_size_for(const SlotDev& d) const {
     const char* e = std::getenv("QS_CLUSTER_STEP");
-    if (e && e[0] == '0') return false;
-    if (e && e[0] == '1') return true;
-    if (persistent_wanted()) return false;
-    return d.n <= kClusterRows;
+    if (e && e[0] == '0') return 0;
+    if (!(e && e[0] == '1') && persistent_wanted()) return 0;
+    if (d.n <= kClusterRows8) return 8;
+    if (d.n <= kClusterRows16 || (e && e[0] == '1')) return cluster16_ok() ? 16 : 8;
+    return 0;
 }
 
-void Engine::run_cluster(const std::vector<int>& ids, int nsteps) {
+// Sixteen CTAs per cluster are a non-portable size: allowed per kernel, and
+// used where the device can place such a cluster
+bool Engine::cluster16_ok() const {
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, bool> ok;
+    int dev = 0;
+    QS_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    const auto key = std::make_pair(dev, (int)st_);
+    auto it = ok.find(key);
+    if (it != ok.end()) return it->second;
+    bool good = false;
+    with_store(st_, [&](auto tag) {
+        using A = decltype(tag);
+        if (cudaFuncSetAttribute(eng_cluster<A>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(16);
+        cfg.blockDim = dim3(kT);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 16;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, eng_cluster<A>, &cfg) == cudaSuccess) good = nclusters > 0;
+        else cudaGetLastError();
+    });
+    ok[key] = good;
+    return good;
+}
+
+void Engine::run_cluster(const std::vector<int>& ids, int nsteps, int C) {
     if (ids.empty()) return;
     if (ids.size() * sizeof(int) > cap_cmap_) {
         cap_cmap_ = std::max<size_t>(64, ids.size() * sizeof(int) * 2);
         cmap_.alloc(cap_cmap_);
     }
     QS_CUDA(cudaMemcpyAsync(cmap_.p, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, s_));
-    const int C = 8;   // portable cluster size
     const void* rsq = st_ == Store::DF ? rsqdf_.p : (st_ == Store::F32 ? rsq32_.p : rsq64_.p);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(ids.size() * C));
@@ -1967,22 +2005,25 @@ void Engine::run(int nsteps) {
     if (nsteps <= 0) return;
     // small slots step in the cluster step, marked so that the graph-replayed
     // kernels skip them; the others in the graph replay (or the persistent step)
-    std::vector<int> cl;
+    std::vector<int> cl8, cl16;
     bool rest = false;
     for (int i = 0; i < (int)slots_.size(); ++i) {
         Slot& sl = slots_[i];
         if (!sl.live || sl.d.state != kSlotStep) continue;
-        if (cluster_wanted(sl.d)) {
+        const int C = cluster_size_for(sl.d);
+        if (C) {
             sl.d.state = kSlotStepCluster;
-            cl.push_back(i);
+            (C == 16 ? cl16 : cl8).push_back(i);
             dirty_ = true;
         } else {
             rest = true;
         }
     }
+    const bool cl = !cl8.empty() || !cl16.empty();
     sync_table();
     if (nrb_ == 0) return;
-    run_cluster(cl, nsteps);
+    run_cluster(cl8, nsteps, 8);
+    run_cluster(cl16, nsteps, 16);
     if (rest) {
         if (persistent_wanted()) {
             run_persistent(nsteps);
@@ -2000,7 +2041,7 @@ void Engine::run(int nsteps) {
         sl.d.j += adv;
         sl.matvecs += adv;
         sl.d.state = sl.d.j >= sl.d.m ? kSlotHold : kSlotStep;
-        dirty_ = dirty_ || !cl.empty();
+        dirty_ = dirty_ || cl;
     }
 }
 

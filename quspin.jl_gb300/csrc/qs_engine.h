@@ -168,10 +168,11 @@ class Engine {
     bool persistent_wanted() const;
     void run_persistent(int nsteps);
     // The steps of the listed slots up to their next Hold event as one launch
-    // with a thread-block cluster per slot (eng_cluster): chosen per slot for
-    // small slots, forced by QS_CLUSTER_STEP=1, disabled by =0
-    bool cluster_wanted(const SlotDev& d) const;
-    void run_cluster(const std::vector<int>& ids, int nsteps);
+    // with a thread-block cluster of C CTAs per slot (eng_cluster): chosen per
+    // slot by its size, forced by QS_CLUSTER_STEP=1, disabled by =0
+    int cluster_size_for(const SlotDev& d) const;   // 0: not in the cluster step
+    bool cluster16_ok() const;
+    void run_cluster(const std::vector<int>& ids, int nsteps, int C);
     Tiles tune(Op& op, int m, bool cv);
     Store st_;
     cudaStream_t s_;

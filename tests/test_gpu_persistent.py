@@ -184,7 +184,14 @@ def test_cluster_step(qs, ora, precision):
         H = qs.Hamiltonian(b, models.to_terms(qs, models.j1j2(L, 1.0, 0.37)))
         v0 = models.seeded(b.Ns, seed=4)
         e1 = qs.eigsh(H, k=3, which="SA", tol=1e-12, v0=v0, precision=precision, return_eigenvectors=False)
+        # 8,359 rows: sixteen CTAs per cluster
+        b22 = qs.SpinBasis1D(22, nup=11, pauli=False, kblock=0, pblock=1, zblock=1)
+        H22 = qs.Hamiltonian(b22, models.to_terms(qs, models.j1j2(22, 1.0, 0.37)))
+        w22 = models.seeded(b22.Ns, seed=5)
+        os.environ.pop("QS_CLUSTER_STEP", None)
+        f1 = qs.eigsh(H22, k=2, which="SA", tol=1e-12, v0=w22, precision=precision, return_eigenvectors=False)
         os.environ["QS_CLUSTER_STEP"] = "0"
+        f0 = qs.eigsh(H22, k=2, which="SA", tol=1e-12, v0=w22, precision=precision, return_eigenvectors=False)
         e0 = qs.eigsh(H, k=3, which="SA", tol=1e-12, v0=v0, precision=precision, return_eigenvectors=False)
     finally:
         if saved is None:
@@ -196,3 +203,4 @@ def test_cluster_step(qs, ora, precision):
     for i, a in enumerate(alone):
         assert np.array_equal(a, c[i])
     assert np.max(np.abs(np.sort(e1) - np.sort(e0))) <= 1e-10 * np.abs(e0).max()
+    assert np.max(np.abs(np.sort(f1) - np.sort(f0))) <= 1e-10 * np.abs(f0).max()
