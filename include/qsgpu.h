@@ -293,7 +293,7 @@ typedef struct {
  * reorthogonalisation replaces the ARPACK implicitly restarted Lanczos;
  * convergence is ARPACK's test ||r_i|| <= tol * max(eps^(2/3), |theta_i|).
  * Assembled operators (qs_op_assemble) run on the batched engine with one
- * operator (as qs_eigsh_batch).  A matrix-free operator of at least 2^16
+ * operator (as qs_eigsh_batch).  A matrix-free operator of at least 4,096
  * states whose assembled form fits in a quarter of free device memory is
  * assembled for the length of the call and runs there too (the form is dropped on return; environment
  * QS_TRANSIENT_ASSEMBLY=0 keeps the call matrix-free). */

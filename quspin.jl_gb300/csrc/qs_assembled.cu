@@ -1899,11 +1899,12 @@ void op_release_assembly(Op& op) {
 
 TransientAssembly::TransientAssembly(Op& o) : op(o) {
     if (op.assembled || !op.commuting) return;
-    // below 2^16 rows a solve is dominated by per-call setup (assembly, the
-    // engine's graph capture), not by products: measured on the XXZ L=16
-    // sector (12,870 rows), eigsh k=4 took 24 ms assembled against 17 ms
+    // in small sectors a solve is dominated by per-call setup, not by
+    // products: XXZ L=16 (12,870 rows) eigsh k=4 takes 9.3 ms assembled for
+    // the call (0.8 ms of it the assembly, the steps on the cluster step)
+    // against 12.3 ms matrix-free; below 4,096 rows the operator stays
     // matrix-free
-    if (op.basis->n < ((int64_t)1 << 16)) return;
+    if (op.basis->n < 4096) return;
     const char* e = std::getenv("QS_TRANSIENT_ASSEMBLY");
     if (e && e[0] == '0') return;
     // an upper bound of the assembled form (both layouts): a packed word per

@@ -273,8 +273,8 @@ void op_matvec_noalloc(Op& op, int flags, cplx alpha, const void* x, int x_dtype
 void op_assemble(Op& op);
 // drops the assembled form (the operator runs matrix-free again)
 void op_release_assembly(Op& op);
-// The Krylov solvers of a matrix-free operator with at least 2^16 rows run on
-// its assembled form for the length of one call when the form fits in a
+// The Krylov solvers of a matrix-free operator with at least 4,096 rows run
+// on its assembled form for the length of one call when the form fits in a
 // quarter of free memory:
 // assembly is one pass of the product kernel, and each product after it is an
 // order of magnitude cheaper than the matrix-free one.  The form is dropped

@@ -540,7 +540,7 @@ def test_page_locked_output_written_in_place(qs, ora, prec):
 
 
 def test_transient_assembly_of_matrix_free_solvers(qs, ora, monkeypatch):
-    """eigsh / evolve on a matrix-free operator of at least 2^16 states run on an
+    """eigsh / evolve on a matrix-free operator of at least 4,096 states run on an
     assembled form built for the call and dropped after it: the same results
     as the matrix-free solve (QS_TRANSIENT_ASSEMBLY=0) and ARPACK over the
     oracle's product, and the operator left matrix-free (no stored nonzeros)."""
@@ -549,7 +549,7 @@ def test_transient_assembly_of_matrix_free_solvers(qs, ora, monkeypatch):
     sym = dict(kblock=0)
     sp = models.j1j2(L, 1.0, 0.37)
     b = qs.SpinBasis1D(L, nup=12, pauli=False, **sym)
-    assert b.Ns >= 1 << 16
+    assert b.Ns >= 4096
     Q = qs.QuantumLinearOperator(b, models.to_terms(qs, sp))
     v0 = models.seeded(b.Ns, seed=5)
     v = models.seeded(b.Ns, seed=6, complex_=True)
