@@ -269,7 +269,8 @@ def tfim_spec(L, J=1.0, h=0.7):
 
 def section_c1(qs, torch, timed_events):
     """Periodic XXZ L=16, nup=8 (12,870 states), no spatial symmetry, FP64:
-    one QuantumLinearOperator matvec and eigsh k=4 :SA (tol 1e-10, v0 = ones),
+    one QuantumLinearOperator matvec and eigsh k=4 :SA (tol 1e-10, v0 = ones;
+    warm, best of 3: the solver assembles the operator for each call),
     against the oracle's restatement of the reference algorithm (serial scatter
     with per-state lookups, 1 thread) and SciPy's ARPACK over it."""
     import oracle
@@ -281,9 +282,15 @@ def section_c1(qs, torch, timed_events):
     x = np.random.default_rng(20261203).standard_normal(n)
     us = timed_events(op, x, 200) * 1e3
     v0 = np.ones(n) / np.sqrt(n)
-    t = time.perf_counter()
+    # warm (the first call also builds the per-device kernel attributes), best of 3
     vals = qs.eigsh(op, k=4, which="SA", tol=1e-10, v0=v0, return_eigenvectors=False)
-    t_gpu = time.perf_counter() - t
+    t_gpu = 1e30
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        vals = qs.eigsh(op, k=4, which="SA", tol=1e-10, v0=v0, return_eigenvectors=False)
+        torch.cuda.synchronize()
+        t_gpu = min(t_gpu, time.perf_counter() - t)
     ref = oracle.RefBasis(L, nup=8, pauli=False)
     ct = oracle.consolidate_terms(spec)
     d = ref.extract_diagonal(ct)
