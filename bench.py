@@ -886,9 +886,10 @@ def profile_range(kind):
     FP32, double-float or fixed point ("product64", "product32", "productdf",
     "productfx"), its
     matrix-free product ("matrixfree"), one Lanczos ground state of it
-    ("lanczos64", "lanczosdf"), one batched
-    double-float ground-state solve of all J1-J2 sectors at L = 24 or 26
-    ("batch24", "batch26"; "batch26_fp64" in FP64), or the 32 batched m = 100 Lanczos recurrences of
+    ("lanczos64", "lanczosdf"), one batched double-float ground-state solve
+    of all J1-J2 sectors at L = 20, 24 or 26 ("batch20", "batch24",
+    "batch26"; "batch20_fp64", "batch26_fp64" in FP64; the L = 20 sectors run
+    on the cluster step), or the 32 batched m = 100 Lanczos recurrences of
     the FTLM workload ("ftlm")."""
     import torch
     import qsgpu as qs
@@ -1272,7 +1273,7 @@ def main():
     ap.add_argument("--only-section", default=None, help="run this side workload only (by its JSON key)")
     ap.add_argument("--profile-range", default=None,
                     choices=["product64", "product32", "productdf", "productfx", "sweep28", "matrixfree", "lanczos64", "lanczosdf",
-                             "batch24", "batch26", "batch26_fp64", "ftlm"],
+                             "batch20", "batch20_fp64", "batch24", "batch26", "batch26_fp64", "ftlm"],
                     help="run one unit inside cudaProfilerStart/Stop (for ncu --profile-from-start off) and exit")
     args = ap.parse_args()
     if args.profile_range:
