@@ -1022,7 +1022,11 @@ __global__ void __launch_bounds__(kTcRows, 1) eng_rotate_tc(const SlotDev* __res
     const uint32_t tmem = tbase;
     const int comps = S.cv ? 2 : 1;
     const int64_t lb = blockIdx.x - S.rb_begin;
-    const int64_t r0 = lb * S.rpb, r1 = min(S.n, r0 + S.rpb);
+    // blockIdx.y: this block's share of the row block (gridDim.y shares of
+    // whole tiles), so that a small engine still fills the GPU
+    const int64_t rb0 = lb * S.rpb, rb1 = min(S.n, rb0 + S.rpb);
+    const int64_t share = ((rb1 - rb0 + gridDim.y - 1) / gridDim.y + kTcRows - 1) / kTcRows * kTcRows;
+    const int64_t r0 = min(rb1, rb0 + (int64_t)blockIdx.y * share), r1 = min(rb1, r0 + share);
     const int64_t e0 = r0 * comps, e1 = r1 * comps;
     char* V = (char*)S.V;
     const size_t cs = (size_t)S.n * comps * 8;   // bytes of one column
@@ -2207,7 +2211,11 @@ void Engine::rotate(const std::vector<RotReq>& reqs) {
                                              (int)kTcSmem));
                 attr_dev = dev;
             }
-            eng_rotate_tc<double><<<nrb_, kTcRows, kTcSmem, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>(),
+            // at least two blocks per SM: row blocks split into shares
+            int nsm = 152;
+            QS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            const int split = std::max(1, std::min(8, (2 * nsm + nrb_ - 1) / std::max(1, nrb_)));
+            eng_rotate_tc<double><<<dim3(nrb_, split), kTcRows, kTcSmem, s_>>>(dslots_.as<SlotDev>(), rmap_.as<int>(),
                                                                    tc_err_.as<int>());
             QS_CUDA(cudaGetLastError());
             ++launches_;
