@@ -310,9 +310,11 @@ QS_API int qs_eigs(qs_op *op, const qs_eigsh_opts *opts, double *values, void *v
 
 /* eigsh on nops Hermitian operators at once (e.g. every momentum / parity
  * sector of one model): the Lanczos iterations of all operators run in
- * lockstep, each step being one launch per kernel over all operators'
- * assembled forms (assembled here if needed), replayed from a captured CUDA
- * graph; operators that converge drop out.  Replaces the per-sector loop of
+ * lockstep on their assembled forms (assembled here if needed): for
+ * operators of more than 32,768 states each step is one launch per kernel
+ * over all of them, replayed from a captured CUDA graph; smaller operators
+ * run their steps up to each restart in one launch with a thread-block
+ * cluster per operator.  Operators that converge drop out.  Replaces the per-sector loop of
  * block_diag_hamiltonian / BlockOps (tools.jl:2213-2420) followed by eigsh on
  * each block.  values: nops * k, ascending per operator; vectors: NULL or nops
  * pointers (each NULL or Ns_i x k in the operator's dtype, host); infos: NULL
