@@ -467,23 +467,28 @@ __global__ void dense_project_kernel(int mode, const int64_t* __restrict__ ptr, 
 void basis_build_projector(Basis& b, const std::vector<ProjMap>& maps, const std::vector<cplx>& eigs,
                            int64_t group_order_before_dense) {
     const int L = b.L;
-    // parent states ascending (Gosper order for a particle sector, src/basis.jl:229-250)
+    // parent states ascending (Gosper order for a particle sector, src/basis.jl:229-250).
+    // The reduced dimension before the dense level is about parent / |G|, so a
+    // parent above 8 x 512 x |G| states cannot pass the 512-column guard: it is
+    // refused before any projector is built (the reference builds them first)
     std::vector<uint64_t> st;
     const int64_t cap = (int64_t)kDenseMax * std::max<int64_t>(1, group_order_before_dense) * 8;
     if (b.nup < 0) {
         if (L > 40 || ((int64_t)1 << L) > cap)
-            throw Error(QS_ERR_ARGUMENT, "the requested symmetry intersection requires a dense nullspace of "
-                                         "dimension above the guarded limit 512. Supply permutation-like symmetry "
-                                         "maps or split the symmetry sector before intersecting it.");
+            throw Error(QS_ERR_ARGUMENT, "the requested symmetry intersection needs the dense nullspace branch on "
+                                         "a parent sector too large for its guarded limit of 512 reduced columns. "
+                                         "Supply permutation-like symmetry maps or split the symmetry sector before "
+                                         "intersecting it.");
         st.resize((size_t)1 << L);
         for (size_t i = 0; i < st.size(); ++i) st[i] = i;
     } else {
         double cnt = 1;
         for (int i = 0; i < b.nup; ++i) cnt = cnt * (L - i) / (i + 1);
         if (cnt > (double)cap)
-            throw Error(QS_ERR_ARGUMENT, "the requested symmetry intersection requires a dense nullspace of "
-                                         "dimension above the guarded limit 512. Supply permutation-like symmetry "
-                                         "maps or split the symmetry sector before intersecting it.");
+            throw Error(QS_ERR_ARGUMENT, "the requested symmetry intersection needs the dense nullspace branch on "
+                                         "a parent sector too large for its guarded limit of 512 reduced columns. "
+                                         "Supply permutation-like symmetry maps or split the symmetry sector before "
+                                         "intersecting it.");
         const int64_t n = (int64_t)std::llround(cnt);
         st.resize(n);
         if (b.nup == 0) {
