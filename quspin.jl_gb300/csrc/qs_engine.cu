@@ -1328,7 +1328,8 @@ int Engine::add(Op& op, int m, bool cv, bool tune_tiles, int tmp_cols, int orth)
     d.orth = orth;
     sl.tcols = tc;
     Tiles t;
-    if (tune_tiles && n >= 4096 && m >= 4) t = tune(op, m, cv);
+    // (a slot on the cluster step splits its slices by CTA, not by the tile)
+    if (tune_tiles && n >= 4096 && m >= 4 && cluster_size_for(d) == 0) t = tune(op, m, cv);
     d.rpb = t.rpb;
     d.spb = t.spb;
     sl.live = true;
