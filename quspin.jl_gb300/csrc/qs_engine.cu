@@ -1212,6 +1212,12 @@ Engine::Engine(Store st, cudaStream_t s) : st_(st), s_(s) {
 
 Engine::~Engine() {
     cudaStreamSynchronize(s_);
+    if (side_) {
+        cudaStreamSynchronize(side_);
+        cudaStreamDestroy(side_);
+    }
+    if (fork_) cudaEventDestroy(fork_);
+    if (join_) cudaEventDestroy(join_);
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
 }
@@ -1977,19 +1983,22 @@ bool Engine::cluster16_ok() const {
     return good;
 }
 
-void Engine::run_cluster(const std::vector<int>& ids, int nsteps, int C) {
+void Engine::run_cluster(const std::vector<int>& ids, int nsteps, int C, cudaStream_t st) {
     if (ids.empty()) return;
-    if (ids.size() * sizeof(int) > cap_cmap_) {
-        cap_cmap_ = std::max<size_t>(64, ids.size() * sizeof(int) * 2);
+    // one map per cluster size: [0, half) for eight CTAs, [half, ...) for sixteen
+    const size_t half = slots_.size();
+    if (2 * half * sizeof(int) > cap_cmap_) {
+        cap_cmap_ = std::max<size_t>(64, 2 * half * sizeof(int) * 2);
         cmap_.alloc(cap_cmap_);
     }
-    QS_CUDA(cudaMemcpyAsync(cmap_.p, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, s_));
+    int* cmd = cmap_.as<int>() + (C == 16 ? half : 0);
+    QS_CUDA(cudaMemcpyAsync(cmd, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     const void* rsq = st_ == Store::DF ? rsqdf_.p : (st_ == Store::F32 ? rsq32_.p : rsq64_.p);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(ids.size() * C));
     cfg.blockDim = dim3(kT);
     cfg.dynamicSmemBytes = 0;
-    cfg.stream = s_;
+    cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = C;
@@ -1998,7 +2007,7 @@ void Engine::run_cluster(const std::vector<int>& ids, int nsteps, int C) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     SlotDev* ds = dslots_.as<SlotDev>();
-    const int* cm = cmap_.as<int>();
+    const int* cm = cmd;
     with_store(st_, [&](auto tag) {
         using A = decltype(tag);
         QS_CUDA(cudaLaunchKernelEx(&cfg, eng_cluster<A>, ds, cm, nsteps, rsq));
@@ -2027,16 +2036,34 @@ void Engine::run(int nsteps) {
     const bool cl = !cl8.empty() || !cl16.empty();
     sync_table();
     if (nrb_ == 0) return;
-    run_cluster(cl8, nsteps, 8);
-    run_cluster(cl16, nsteps, 16);
+    // with large slots too, the cluster step runs on the side stream beside
+    // their graph replay (the two touch different slots and partial rows);
+    // never beside the cooperative step, whose blocks must all be resident
+    cudaStream_t cs = s_;
+    if (cl && rest && !persistent_wanted()) {
+        if (!side_) {
+            QS_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+            QS_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+            QS_CUDA(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming));
+        }
+        QS_CUDA(cudaEventRecord(fork_, s_));
+        QS_CUDA(cudaStreamWaitEvent(side_, fork_, 0));
+        cs = side_;
+    }
+    run_cluster(cl8, nsteps, 8, cs);
+    run_cluster(cl16, nsteps, 16, cs);
     if (rest) {
+        if (!exec_ && !persistent_wanted()) capture();
         if (persistent_wanted()) {
             run_persistent(nsteps);
         } else {
-            if (!exec_) capture();
             for (int t = 0; t < nsteps; ++t) QS_CUDA(cudaGraphLaunch(exec_, s_));
             launches_ += step_launches_ * (int64_t)nsteps;
         }
+    }
+    if (cs != s_) {
+        QS_CUDA(cudaEventRecord(join_, side_));
+        QS_CUDA(cudaStreamWaitEvent(s_, join_, 0));
     }
     // mirror the device step counters (the cluster step leaves its slots in
     // kSlotStepCluster or Hold on the device; the next table upload restores Step)

@@ -172,7 +172,7 @@ class Engine {
     // slot by its size, forced by QS_CLUSTER_STEP=1, disabled by =0
     int cluster_size_for(const SlotDev& d) const;   // 0: not in the cluster step
     bool cluster16_ok() const;
-    void run_cluster(const std::vector<int>& ids, int nsteps, int C);
+    void run_cluster(const std::vector<int>& ids, int nsteps, int C, cudaStream_t st);
     Tiles tune(Op& op, int m, bool cv);
     Store st_;
     cudaStream_t s_;
@@ -182,6 +182,10 @@ class Engine {
     DevBuf bar_;               // grid barrier of the persistent step
     DevBuf cmap_;              // stepping slot of each cluster (cluster step)
     size_t cap_cmap_ = 0;
+    // the cluster step runs on a side stream beside the graph replay of the
+    // large slots when an engine holds both (joined by events)
+    cudaStream_t side_ = nullptr;
+    cudaEvent_t fork_ = nullptr, join_ = nullptr;
     bool tc_rotate_ = true;    // QS_TC_ROTATE=0 keeps every rotation on eng_rotate
     size_t cap_y_ = 0;
     int nrb_ = 0, nsb_ = 0, mmax_ = 1, cap_slots_ = 0;

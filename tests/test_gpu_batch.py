@@ -73,6 +73,23 @@ def test_batched_result_independent_of_batch(qs):
             assert np.array_equal(vt[i], va[0]), (precision, i)
 
 
+def test_batched_cluster_beside_graph_replay(qs):
+    """A batch holding small slots (cluster step, eight and sixteen CTAs) and a
+    large one (graph replay) runs the two concurrently on two streams; every
+    sector's eigenpairs are the ones it has alone."""
+    terms = lambda L: models.to_terms(qs, models.j1j2(L, 1.0, 0.41))
+    specs = [(24, dict(kblock=0, pblock=1)), (16, dict(kblock=3)), (20, dict(kblock=3)),
+             (16, dict(kblock=0, pblock=-1))]
+    ops = [qs.Hamiltonian(qs.SpinBasis1D(L, nup=L // 2, pauli=False, **s), terms(L)) for L, s in specs]
+    assert ops[0].Ns > 32768 and 8192 < ops[2].Ns <= 32768 and ops[1].Ns <= 8192
+    for precision in ("fp64", "fp32"):
+        together, vt = qs.eigsh_batch(ops, k=2, tol=1e-12, return_eigenvectors=True, precision=precision)
+        for i, op in enumerate(ops):
+            alone, va = qs.eigsh_batch([op], k=2, tol=1e-12, return_eigenvectors=True, precision=precision)
+            assert np.array_equal(together[i], alone[0]), (precision, i)
+            assert np.array_equal(vt[i], va[0]), (precision, i)
+
+
 def test_batched_mixed_real_and_complex_sizes(qs, ora):
     """Sectors of very different sizes, real and complex, with k=3."""
     L = 12
