@@ -51,3 +51,39 @@ def test_single_process_needs_no_group():
     import bench
     assert bench.max_over_ranks(1, 0.25) == 0.25
     assert abs(bench.replica_value(1, 1e9, 0.5) - 2.0) < 1e-12
+
+
+def _reference_arm(extra_env, nproc):
+    import json
+    import subprocess
+    import sys
+    env = dict(os.environ, **extra_env)
+    cmd = [sys.executable, "bench.py", "--impl", "reference", "--workload", "j1j2_L24_k0_p1_z1",
+           "--steps", "3", "--warmup", "3"]
+    if nproc > 1:
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={nproc}",
+               "--master-addr", "127.0.0.1", f"--master-port={_free_port()}"] + cmd[1:] + ["--gpus", str(nproc)]
+    r = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+
+
+def test_reference_arm_prints_one_contract_line():
+    """`bench.py --impl reference`: the oracle's restatement of the reference
+    product on the host cores prints one JSON line with the arm's keys."""
+    lines = _reference_arm({}, 1)
+    assert len(lines) == 1
+    d = lines[0]
+    assert d["impl"] == "reference" and d["unit"] == "GB/s" and d["value"] > 0
+    assert d["higher_is_better"] is True and d["steps"] == 3 and d["warmup"] >= 3
+    assert d["config"]["N"] == 28968
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_under_two_ranks_prints_once():
+    """Launched with two ranks (gloo here), rank 0 alone runs the reference
+    arm and prints its line; the other rank exits 0 without work."""
+    lines = _reference_arm({"QS_BENCH_BACKEND": "gloo"}, 2)
+    assert len(lines) == 1 and lines[0]["impl"] == "reference" and lines[0]["n_gpus"] == 2
